@@ -1,0 +1,182 @@
+"""Python binding of the GB300 CaPS library (libcaps_gb300.so, C-ABI).
+
+The binding mirrors the reference's C API (src/include/libcaps.h): a Caps
+object wraps caps_t; logdetD, mie, M, logdetD0 and the batch/free-energy
+extensions call straight into the CUDA library.  There is no CPU path: if the
+shared library is missing, importing raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libcaps_gb300.so")
+
+DETALG_HODLR, DETALG_LU, DETALG_QR, DETALG_CHOLESKY = 0, 1, 2, 3
+PREC_FP64, PREC_MIXED = 0, 1
+HBAR_EV = 6.582119514e-16
+C_LIGHT = 299792458.0
+
+
+class _EnergyInfo(C.Structure):
+    _fields_ = [("nxi", C.c_int), ("ndet", C.c_int), ("nwasted", C.c_int), ("seconds", C.c_double),
+                ("xi", C.POINTER(C.c_double)), ("logdetD", C.POINTER(C.c_double))]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libcaps_gb300.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    d, i, vp, dp, ip = C.c_double, C.c_int, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
+    sig = {
+        "caps_init": (vp, [d, d]), "caps_free": (None, [vp]),
+        "caps_set_ldim": (i, [vp, i]), "caps_get_ldim": (i, [vp]),
+        "caps_set_detalg": (i, [vp, i]), "caps_get_detalg": (i, [vp]),
+        "caps_set_epsrel": (i, [vp, d]), "caps_get_epsrel": (d, [vp]),
+        "caps_set_epsilonm1": (None, [vp, vp, vp]),
+        "caps_set_epsilonm1_plate": (None, [vp, vp, vp]),
+        "caps_set_epsilonm1_sphere": (None, [vp, vp, vp]),
+        "caps_logdetD": (d, [vp, d, i]),
+        "caps_logdetD_batch": (i, [vp, dp, ip, i, dp, ip]),
+        "caps_mie": (None, [vp, d, i, dp, dp]), "caps_mie_perf": (None, [vp, d, i, dp, dp]),
+        "caps_lnLambda": (d, [i, i, i]),
+        "caps_fresnel": (None, [vp, d, d, dp, dp]),
+        "caps_estimate_lminmax": (i, [vp, i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+        "caps_M_init": (vp, [vp, i, d]), "caps_M_elem": (d, [vp, i, i, C.c_char, C.c_char]),
+        "caps_M_free": (None, [vp]), "caps_kernel_M": (d, [i, i, vp]),
+        "caps_logdetD0": (None, [vp, i, d, dp, dp, dp]),
+        "caps_ht_drude": (d, [vp]), "caps_ht_perf": (d, [vp, d]),
+        "caps_free_energy": (d, [vp, d, d, d, C.POINTER(_EnergyInfo)]),
+        "caps_gpu_set_precision": (i, [vp, i]),
+        "caps_gpu_last_error": (C.c_char_p, []),
+        "caps_gpu_set_stream": (None, [vp]),
+        "caps_gpu_timings": (i, [dp, i]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def last_error():
+    return lib.caps_gpu_last_error().decode()
+
+
+def set_stream(handle):
+    """Run subsequent GPU work on the given cudaStream_t handle (int) or None."""
+    lib.caps_gpu_set_stream(C.c_void_p(handle) if handle else None)
+
+
+def timings():
+    buf = (C.c_double * 6)()
+    lib.caps_gpu_timings(buf, 6)
+    return list(buf)
+
+
+class Caps:
+    """caps_t of the reference API: R and L in metres."""
+
+    def __init__(self, R, L, ldim=None, detalg=None):
+        self._h = lib.caps_init(R, L)
+        if not self._h:
+            raise ValueError("caps_init failed (R and L must be positive)")
+        self._ud = None
+        self.R, self.L = R, L
+        if ldim is not None:
+            lib.caps_set_ldim(self._h, ldim)
+        if detalg is not None:
+            lib.caps_set_detalg(self._h, detalg)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.caps_free(h)
+            self._h = None
+
+    @property
+    def ldim(self):
+        return lib.caps_get_ldim(self._h)
+
+    def set_ldim(self, ldim):
+        return lib.caps_set_ldim(self._h, ldim)
+
+    def set_detalg(self, detalg):
+        return lib.caps_set_detalg(self._h, detalg)
+
+    def set_precision(self, prec):
+        return lib.caps_gpu_set_precision(self._h, prec)
+
+    def set_drude(self, omegap_eV, gamma_eV):
+        """Drude metal (gamma=0: plasma) for plate and sphere, via caps_epsilonm1_drude."""
+        self._ud = (C.c_double * 2)(omegap_eV / HBAR_EV, gamma_eV / HBAR_EV)
+        fn = C.cast(lib.caps_epsilonm1_drude, C.c_void_p)
+        lib.caps_set_epsilonm1(self._h, fn, C.cast(self._ud, C.c_void_p))
+
+    def logdetD(self, xi_, m):
+        return lib.caps_logdetD(self._h, float(xi_), int(m))
+
+    def logdetD_batch(self, xi_, m):
+        xi_ = np.ascontiguousarray(xi_, dtype=np.float64)
+        m = np.ascontiguousarray(m, dtype=np.int32)
+        n = len(xi_)
+        out = np.empty(n)
+        st = np.empty(n, dtype=np.int32)
+        lib.caps_logdetD_batch(self._h, xi_.ctypes.data_as(C.POINTER(C.c_double)), m.ctypes.data_as(C.POINTER(C.c_int)),
+                               n, out.ctypes.data_as(C.POINTER(C.c_double)), st.ctypes.data_as(C.POINTER(C.c_int)))
+        return out, st
+
+    def mie(self, xi_, l):
+        a, b = C.c_double(), C.c_double()
+        lib.caps_mie(self._h, float(xi_), int(l), C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def mie_perf(self, xi_, l):
+        a, b = C.c_double(), C.c_double()
+        lib.caps_mie_perf(self._h, float(xi_), int(l), C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def lminmax(self, m):
+        lo, hi = C.c_size_t(), C.c_size_t()
+        lib.caps_estimate_lminmax(self._h, int(m), C.byref(lo), C.byref(hi))
+        return lo.value, hi.value
+
+    def fresnel(self, xi_, k_):
+        a, b = C.c_double(), C.c_double()
+        lib.caps_fresnel(self._h, float(xi_), float(k_), C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def M(self, xi_, m):
+        """Dense round-trip matrix (2 ldim x 2 ldim, interleaved E/M) via caps_M_init."""
+        h = lib.caps_M_init(self._h, int(m), float(xi_))
+        dim = 2 * self.ldim
+        out = np.empty((dim, dim))
+        for i in range(dim):
+            for j in range(dim):
+                out[i, j] = lib.caps_kernel_M(i, j, h)
+        lib.caps_M_free(h)
+        return out
+
+    def logdetD0(self, m, EE=True, MM=True):
+        ee, mm = C.c_double(np.nan), C.c_double(np.nan)
+        lib.caps_logdetD0(self._h, int(m), 0.0, C.byref(ee) if EE else None, C.byref(mm) if MM else None, None)
+        return ee.value, mm.value
+
+    def ht_drude(self):
+        return lib.caps_ht_drude(self._h)
+
+    def ht_perf(self, eps):
+        return lib.caps_ht_perf(self._h, eps)
+
+    def free_energy(self, T, cutoff=1e-9, epsrel=1e-6):
+        xi = (C.c_double * 4096)()
+        v = (C.c_double * 4096)()
+        info = _EnergyInfo(0, 0, 0, 0.0, C.cast(xi, C.POINTER(C.c_double)), C.cast(v, C.POINTER(C.c_double)))
+        E = lib.caps_free_energy(self._h, float(T), float(cutoff), float(epsrel), C.byref(info))
+        n = info.nxi
+        return E, dict(nxi=n, ndet=info.ndet, nwasted=info.nwasted, seconds=info.seconds,
+                       xi=list(xi[:n]), logdetD=list(v[:n]))

@@ -1,0 +1,530 @@
+// assemble.cu -- FP64 assembly of the round-trip matrices M(xi,m) of a batch.
+//
+// Phases (each one launch over the whole batch):
+//   k_setup   per task: K panel grid and the degree-recurrence coefficients
+//   k_mie     per (xi, l): log|a_l|, log|b_l|                     (libcaps.c:485-602)
+//   k_scale   per (task, l): symmetric scale factors sqrt(Lambda a_l), u(l), v(l)
+//   k_ktab    per (task, 32 quadrature nodes): all K_{nu,p} partial sums
+//   k_kred    per (task, nu): K table                             (integration.c:288-489)
+//   k_itab    per (task, l1>=l2): I_{l1 l2,p} q-sums              (integration.c:491-671)
+//   k_elem    per (task, 2x2 block): 1 - M, lower triangle        (libcaps.c:717-831,
+//                                                                   integration.c:762-888)
+//   k_stats   per task: Kahan trace, Frobenius norm, shortcut decision (matrix.c:57-119,489-505)
+#include "common.cuh"
+#include "special.cuh"
+#include "kgrid.cuh"
+#include "internal.h"
+
+namespace capsgpu {
+
+__constant__ double c_glx[GLN];
+__constant__ double c_glw[GLN];
+
+void upload_gauss_legendre(const double *x, const double *w)
+{
+    CK(cudaMemcpyToSymbol(c_glx, x, GLN * sizeof(double)));
+    CK(cudaMemcpyToSymbol(c_glw, w, GLN * sizeof(double)));
+}
+
+// ---------------------------------------------------------------------------
+// setup: quadrature grid + recurrence coefficients for every task
+// ---------------------------------------------------------------------------
+__global__ void k_setup(Task *tasks, int ntask, double *edges, int max_panels, double2 *coefAB, int nu_stride,
+                        double c_width, int *status)
+{
+    const int task = blockIdx.x;
+    if (task >= ntask) return;
+    Task &T = tasks[task];
+    if (threadIdx.x == 0) {
+        KGridParams P = kgrid_default();
+        P.c_width = c_width;
+        const int np = kgrid_build(T.alpha, T.mu, T.s, T.nu_max, P, edges + (size_t)task * (max_panels + 1), max_panels);
+        if (np < 0) { T.npanel = 0; status[task] |= ST_ERR_GRID; }
+        else T.npanel = np;
+    }
+    // A_nu = (2nu+1)/(nu-mu+1), B_nu = (nu+mu)/(nu-mu+1): P_{nu+1} = A x P_nu - B P_{nu-1}
+    const int nnu = T.nu_max - T.mu + 1;
+    for (int i = threadIdx.x; i < nnu; i += blockDim.x) {
+        const double nu = T.mu + i, d = 1.0 / (i + 1.0);
+        coefAB[(size_t)task * nu_stride + i] = make_double2((2 * nu + 1) * d, (nu + T.mu) * d);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Mie coefficients per distinct xi
+// ---------------------------------------------------------------------------
+__global__ void k_mie(const double *xi_list, const double *epsm1_list, int nxi, double LbyR, int lmax,
+                      double *lna, double *lnb)
+{
+    const int l = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int ix = blockIdx.y;
+    if (l > lmax || ix >= nxi) return;
+    double a, b;
+    mie(LbyR, xi_list[ix], l, epsm1_list[ix], &a, &b);
+    lna[(size_t)ix * (lmax + 1) + l] = a;
+    lnb[(size_t)ix * (lmax + 1) + l] = b;
+}
+
+// per task and l in [lmin, lmin+ldim-1]: Sa = exp((f(l)+log a_l)/2), Sb likewise,
+// f(l) = log(2l+1) - log l - log(l+1) + lfac(l-m) - lfac(l+m) so that
+// exp(lnLambda + (log a1 + log a2)/2) = Sa(l1) Sa(l2)   (libcaps.c:45, :787)
+__global__ void k_scale(const Task *tasks, int ntask, int ldim, const double *lna, const double *lnb, int lmax,
+                        const double *lfac_tab, sd *Sa, sd *Sb, double2 *uv)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int task = blockIdx.y;
+    if (a >= ldim + 2 || task >= ntask) return;
+    const Task &T = tasks[task];
+    const int l = T.lmin - 1 + a; // a indexes l-(lmin-1) in [0, ldim+1]
+    const size_t o = (size_t)task * (ldim + 2) + a;
+    const double m = T.m;
+    uv[o] = make_double2(l >= 0 ? (l + 1.0) * (l + m) / (2 * l + 1.0) : 0.0,
+                         l >= 0 ? (double)l * (l - m + 1.0) / (2 * l + 1.0) : 0.0);
+    if (a == 0 || a == ldim + 1) { Sa[o] = sd{0, 0}; Sb[o] = sd{0, 0}; return; }
+    const double f = log(2.0 * l + 1) - log((double)l) - log(l + 1.0) + lfac(lfac_tab, l - T.m) - lfac(lfac_tab, l + T.m);
+    const size_t mo = (size_t)T.xi_index * (lmax + 1) + l;
+    Sa[o] = sd_from_log(0.5 * (f + lna[mo]), 1);
+    Sb[o] = sd_from_log(0.5 * (f + lnb[mo]), 1);
+}
+
+// ---------------------------------------------------------------------------
+// K integrals on the shared panel grid
+// ---------------------------------------------------------------------------
+// One warp owns 32 nodes (two panels).  Each lane runs the degree recurrence of
+// P_nu^mu at its node; at every degree the warp aligns the lane values to the
+// warp-maximum binary exponent and parks them in shared memory; every 32
+// degrees lane r folds row r with the node weights (times the Fresnel
+// coefficient of each node) into the partial K sum of degree nu0+r.
+constexpr int KT_WARPS = 8;
+
+template <bool PR>
+__global__ void __launch_bounds__(KT_WARPS * 32)
+k_ktab(const Task *tasks, const double *edges, int max_panels, const double2 *coefAB, int nu_stride,
+       const double *lfac_tab, double *partM, int *partE, int max_warps)
+{
+    extern __shared__ double smem[];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *buf = smem + wib * (32 * 33);                    // [32][33]
+    double *wTM = smem + KT_WARPS * 32 * 33 + wib * 64;      // [32]
+    double *wTE = wTM + 32;                                  // [32]
+    int *rowE = (int *)(smem + KT_WARPS * (32 * 33 + 64)) + wib * 32;
+
+    const int task = blockIdx.y;
+    const Task T = tasks[task];
+    const int warp = blockIdx.x * KT_WARPS + wib;
+    const int nwarp = (T.npanel + 1) / 2;
+    if (warp >= nwarp) return;
+
+    const int panel = warp * 2 + (lane >> 4), j = lane & 15;
+    const bool valid = panel < T.npanel;
+    double x = 1.0, WTM = 0.0, WTE = 0.0;
+    int E = -(1 << 29);
+    if (valid) {
+        const double *ed = edges + (size_t)task * (max_panels + 1);
+        const double a = ed[panel], b = ed[panel + 1];
+        const double h = 0.5 * (b - a), c = 0.5 * (a + b);
+        const double t = c + h * c_glx[j], w = h * c_glw[j];
+        const double sh = sinh(t);
+        x = cosh(t);
+        // log of node weight times e^{-alpha x} sinh^{mu+1-2s} t (2mu-1)!!
+        const double ldf = lfac(lfac_tab, 2 * T.mu) - T.mu * LN2 - lfac(lfac_tab, T.mu);
+        const double lc = log(w) - T.alpha * x + (T.mu + 1 - 2 * T.s) * log(sh) + ldf;
+        const double fl = floor(lc * INV_LN2);
+        const double f = exp(lc - fl * LN2);
+        E = (int)fl;
+        double rTE = -1.0, rTM = 1.0;
+        if (!PR) { // Fresnel at k = xi_ sinh t  (libcaps.c:616)
+            const double eps = T.epsm1_plate;
+            const double y = eps / (x * x);
+            const double bm1 = y / (sqrt(1 + y) + 1);
+            rTE = -bm1 / (2 + bm1);
+            rTM = (eps - bm1) / (eps + 2 + bm1);
+        }
+        WTM = f * rTM;
+        WTE = f * rTE;
+    }
+    wTM[lane] = WTM;
+    wTE[lane] = WTE;
+
+    double pp = 0.0, pc = valid ? 1.0 : 0.0;
+    const int nnu = T.nu_max - T.mu + 1;
+    const double2 *ab = coefAB + (size_t)task * nu_stride;
+    const size_t pTM = ((size_t)(task * 2 + 1) * max_warps + warp) * nu_stride;
+    const size_t pTE = ((size_t)(task * 2 + 0) * max_warps + warp) * nu_stride;
+
+    for (int base = 0; base < nnu; base += 32) {
+        const int rows = min(32, nnu - base);
+        for (int r = 0; r < rows; r++) {
+            const int e = (pc != 0.0) ? expo(pc) + E : -(1 << 29);
+            const int emax = __reduce_max_sync(0xffffffffu, e);
+            buf[r * 33 + lane] = (pc != 0.0 && e - emax > -1000) ? shift2(pc, E - emax) : 0.0;
+            if (lane == 0) rowE[r] = emax;
+            const double2 c = __ldg(ab + base + r);
+            const double pn = fma(c.x * x, pc, -c.y * pp);
+            pp = pc;
+            pc = pn;
+            if (fabs(pc) > 0x1p600) { pc *= 0x1p-600; pp *= 0x1p-600; E += 600; }
+        }
+        __syncwarp();
+        if (lane < rows) {
+            double sTM = 0.0, sTE = 0.0;
+            const double *row = buf + lane * 33;
+#pragma unroll 8
+            for (int l = 0; l < 32; l++) {
+                const double v = row[l];
+                sTM = fma(v, wTM[l], sTM);
+                if (!PR) sTE = fma(v, wTE[l], sTE);
+            }
+            partM[pTM + base + lane] = sTM;
+            partE[pTM + base + lane] = rowE[lane];
+            if (!PR) {
+                partM[pTE + base + lane] = sTE;
+                partE[pTE + base + lane] = rowE[lane];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// fold the per-warp partials into K_{nu,p} (scaled doubles)
+__global__ void k_kred(const Task *tasks, int ntask, const double *partM, const int *partE, int max_warps, int nu_stride,
+                       sd *K, int *status)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int task = blockIdx.y;
+    if (task >= ntask) return;
+    const Task &T = tasks[task];
+    const int nnu = T.nu_max - T.mu + 1;
+    if (i >= nnu) return;
+    const int nwarp = (T.npanel + 1) / 2;
+    for (int p = 1; p >= 0; p--) {
+        sd *out = K + (size_t)(task * 2 + p) * nu_stride + i;
+        if (p == 0 && T.is_pr) { // K_TE = -K_TM for perfect reflectors (integration.c:638)
+            sd k = K[(size_t)(task * 2 + 1) * nu_stride + i];
+            *out = sd{-k.m, k.e};
+            continue;
+        }
+        const size_t base = (size_t)(task * 2 + p) * max_warps * nu_stride + i;
+        int emax = -(1 << 29);
+        for (int w = 0; w < nwarp; w++) {
+            const double m = partM[base + (size_t)w * nu_stride];
+            if (m != 0.0) emax = max(emax, partE[base + (size_t)w * nu_stride]);
+        }
+        double s = 0.0;
+        for (int w = 0; w < nwarp; w++) {
+            const double m = partM[base + (size_t)w * nu_stride];
+            const int d = partE[base + (size_t)w * nu_stride] - emax;
+            if (m != 0.0 && d > -1000) s += shift2(m, d);
+        }
+        if (s == 0.0 || !isfinite(s)) atomicOr(status + task, ST_ERR_NONFINITE);
+        *out = sd_norm(s, emax);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// I integrals: q-sum of K with the three-term a_q recurrence (integration.c:497)
+// ---------------------------------------------------------------------------
+CAPS_DEV double falpha(double p, double n, double nu)
+{
+    const double p2 = p * p;
+    return ((p2 - (n + nu + 1) * (n + nu + 1)) * (p2 - (n - nu) * (n - nu))) / (4 * p2 - 1);
+}
+
+struct QAcc {
+    double s; int e; bool on; int count; double v0;
+};
+
+CAPS_DEV void qacc_add(QAcc &A, double mant, int ex)
+{
+    if (mant == 0.0) return;
+    if (A.s == 0.0) { A.s = mant; A.e = ex; return; }
+    int d = ex - A.e;
+    if (d > 64) { A.s = (A.e - ex < -1000) ? 0.0 : shift2(A.s, A.e - ex); A.e = ex; d = 0; }
+    if (d > -1000) A.s += shift2(mant, d);
+}
+
+// the early stop of the reference: three consecutive terms 60 e-folds below the q=0 term
+CAPS_DEV void qacc_check(QAcc &A, double aq, int lscale2, sd Kv)
+{
+    const double approx = (double)(expo(aq) + lscale2 + Kv.e) * LN2; // within 2 ln2 of the log
+    double v = approx;
+    if (fabs(approx - A.v0 + 60.0) < 3.0)
+        v = log(fabs(aq)) + lscale2 * LN2 + log(fabs(Kv.m)) + Kv.e * LN2;
+    if (v - A.v0 < -60.0) { if (++A.count >= 3) A.on = false; }
+    else A.count = 0;
+}
+
+__global__ void k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lfac_tab,
+                       sd *I, int *status)
+{
+    const int L = ldim + 2;
+    const long long npair = (long long)L * (L + 1) / 2;
+    const long long pid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int task = blockIdx.y;
+    if (pid >= npair || task >= ntask) return;
+    // pair index -> (a1 >= a2)
+    int a1 = (int)((sqrt(8.0 * (double)pid + 1.0) - 1.0) * 0.5);
+    while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
+    while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
+    const int a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
+
+    const Task &T = tasks[task];
+    const int l1 = T.lmin - 1 + a1, l2 = T.lmin - 1 + a2;
+    const int mm = T.m > 0 ? T.m : 1;
+    sd *I_TM = I + (size_t)(task * 2 + 1) * L * L;
+    sd *I_TE = I + (size_t)(task * 2 + 0) * L * L;
+    const size_t o12 = (size_t)a1 * L + a2, o21 = (size_t)a2 * L + a1;
+    if (l2 < mm || l2 < T.m || l1 < 1) { // I = 0 for l < m (integration.c:631)
+        I_TM[o12] = I_TM[o21] = sd{0, 0};
+        I_TE[o12] = I_TE[o21] = sd{0, 0};
+        return;
+    }
+    const double n = l1, nu = l2, m = mm;
+    const double n4 = l1 + l2 - 2 * mm;
+    const int l12 = l1 + l2;
+    const int qmax = min(min(l1, l2), (l12 - 2 * mm) / 2);
+    const double Ap = -2 * m * (n - nu) * (n + nu + 1);
+    const double log_a0 = lfac(lfac_tab, 2 * l1) - lfac(lfac_tab, l1) + lfac(lfac_tab, 2 * l2) - lfac(lfac_tab, l2) + lfac(lfac_tab, l12)
+                        - lfac(lfac_tab, 2 * l12) + lfac(lfac_tab, l12 - 2 * mm) - lfac(lfac_tab, l1 - mm) - lfac(lfac_tab, l2 - mm);
+
+    const sd *KTM = K + (size_t)(task * 2 + 1) * nu_stride - T.mu; // indexed by nu
+    const sd *KTE = K + (size_t)(task * 2 + 0) * nu_stride - T.mu;
+    const bool both = !T.is_pr;
+
+    QAcc aT, aE;
+    {
+        const sd k0 = KTM[l12];
+        aT = QAcc{k0.m, k0.e, true, 0, log(fabs(k0.m)) + k0.e * LN2};
+        if (both) { const sd e0 = KTE[l12]; aE = QAcc{e0.m, e0.e, true, 0, log(fabs(e0.m)) + e0.e * LN2}; }
+        else aE = QAcc{0, 0, false, 0, 0};
+    }
+    double aqm2 = 0, aqm1 = 1; // a_{q-2}, a_{q-1}
+    int lscale2 = 0;
+    if (qmax >= 1) {
+        const double a1q = (n + nu - 1.5) * (1 - (2 * n + 2 * nu - 1) / (n4 * (n4 - 1)) * ((m - n) * (m - n + 1) / (2 * n - 1) + (m - nu) * (m - nu + 1) / (2 * nu - 1)));
+        const sd kt = KTM[l12 - 2];
+        qacc_add(aT, a1q * kt.m, kt.e);
+        if (both) { const sd ke = KTE[l12 - 2]; qacc_add(aE, a1q * ke.m, ke.e); }
+        aqm2 = 1; aqm1 = a1q;
+    }
+    if (qmax >= 2) {
+        const double a2q = (2 * n + 2 * nu - 1) * (2 * n + 2 * nu - 7) / 4 * ((2 * n + 2 * nu - 3) / (n4 * (n4 - 1)) * ((2 * n + 2 * nu - 5) / (2 * (n4 - 2) * (n4 - 3))
+                  * ((m - n) * (m - n + 1) * (m - n + 2) * (m - n + 3) / (2 * n - 1) / (2 * n - 3)
+                  + 2 * (m - n) * (m - n + 1) * (m - nu) * (m - nu + 1) / ((2 * n - 1) * (2 * nu - 1))
+                  + (m - nu) * (m - nu + 1) * (m - nu + 2) * (m - nu + 3) / (2 * nu - 1) / (2 * nu - 3)) - (m - n) * (m - n + 1) / (2 * n - 1)
+                  - (m - nu) * (m - nu + 1) / (2 * nu - 1)) + 0.5);
+        const sd kt = KTM[l12 - 4];
+        qacc_add(aT, a2q * kt.m, kt.e);
+        if (both) { const sd ke = KTE[l12 - 4]; qacc_add(aE, a2q * ke.m, ke.e); }
+        aqm2 = aqm1; aqm1 = a2q;
+    }
+    for (int q = 3; q <= qmax && (aT.on || aE.on); q++) {
+        const double p = n + nu - 2 * q, p1 = p - 2 * m, p2 = p + 2 * m;
+        double aq;
+        if (Ap != 0) {
+            const double c0 = (p + 2) * (p + 3) * (p1 + 1) * (p1 + 2) * Ap * falpha(p + 1, n, nu);
+            const double c1 = Ap * (Ap * Ap + (p + 1) * (p + 3) * (p1 + 2) * (p2 + 2) * falpha(p + 2, n, nu)
+                                         + (p + 2) * (p + 4) * (p1 + 3) * (p2 + 3) * falpha(p + 3, n, nu));
+            const double c2 = -(p + 2) * (p + 3) * (p2 + 3) * (p2 + 4) * Ap * falpha(p + 4, n, nu);
+            aq = (c1 * aqm1 + c2 * aqm2) / c0;
+        } else
+            aq = (p + 1) * (p2 + 2) * falpha(p + 2, n, nu) * aqm1 / ((p + 2) * (p1 + 1) * falpha(p + 1, n, nu));
+        // exact power-of-two rescaling of the recurrence (the reference rescales by |a_q| at 1e+-100)
+        if (aq != 0.0) {
+            const int k = expo(aq);
+            if (k > 300 || k < -300) { aq = shift2(aq, -k); aqm1 = shift2(aqm1, -k); lscale2 += k; }
+        }
+        const int nuq = l12 - 2 * q;
+        if (aT.on) { const sd kt = KTM[nuq]; qacc_add(aT, aq * kt.m, kt.e + lscale2); if (aq != 0.0) qacc_check(aT, aq, lscale2, kt); }
+        if (aE.on) { const sd ke = KTE[nuq]; qacc_add(aE, aq * ke.m, ke.e + lscale2); if (aq != 0.0) qacc_check(aE, aq, lscale2, ke); }
+        aqm2 = aqm1; aqm1 = aq;
+    }
+    const sd a0 = sd_from_log(log_a0, 1);
+    const sd rT = sd_mul(a0, sd_norm(aT.s, aT.e));
+    if (!isfinite(rT.m) || rT.m == 0.0) atomicOr(status + task, ST_ERR_NONFINITE);
+    I_TM[o12] = rT; I_TM[o21] = rT;
+    sd rE;
+    if (both) rE = sd_mul(a0, sd_norm(aE.s, aE.e));
+    else rE = sd{-rT.m, rT.e};
+    I_TE[o12] = rE; I_TE[o21] = rE;
+}
+
+// ---------------------------------------------------------------------------
+// elements of 1 - M (lower triangle, column-major, leading dimension lda)
+// ---------------------------------------------------------------------------
+CAPS_DEV sd sdx(double c, sd a) { return sd_norm(c * a.m, a.e); }
+CAPS_DEV sd sd_neg(sd a) { return sd{-a.m, a.e}; }
+
+__global__ void k_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv,
+                       double *A, size_t lda, size_t mat_stride, int *status)
+{
+    const int L = ldim + 2;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x; // row block
+    const int b = blockIdx.y;                            // column block
+    const int task = blockIdx.z;
+    if (a >= ldim || b > a || task >= ntask) return;
+    const Task &T = tasks[task];
+    const sd *ITM = I + (size_t)(task * 2 + 1) * L * L;
+    const sd *ITE = I + (size_t)(task * 2 + 0) * L * L;
+    const int i1 = a + 1, i2 = b + 1; // index into [lmin-1, lmin+ldim]
+    const size_t so = (size_t)task * L;
+    const sd sa1 = Sa[so + i1], sa2 = Sa[so + i2], sb1 = Sb[so + i1], sb2 = Sb[so + i2];
+    const double2 uv1 = uv[so + i1], uv2 = uv[so + i2];
+    const double m = T.m;
+    auto Iv = [&](const sd *t, int x, int y) { return t[(size_t)x * L + y]; };
+
+    sd EE, MM, EM = sd{0, 0}, ME = sd{0, 0};
+    if (T.m == 0) {
+        EE = sd_mul(sd_mul(sa1, sa2), Iv(ITM, i1, i2));          // B_TM, A = 0
+        MM = sd_neg(sd_mul(sd_mul(sb1, sb2), Iv(ITE, i1, i2)));  // -B_TE
+    } else {
+        const double m2 = m * m;
+        auto Bv = [&](const sd *t) {
+            sd r = sdx(uv1.x * uv2.x, Iv(t, i1 - 1, i2 - 1));
+            r = sd_add(r, sdx(-uv1.y * uv2.x, Iv(t, i1 + 1, i2 - 1)));
+            r = sd_add(r, sdx(-uv1.x * uv2.y, Iv(t, i1 - 1, i2 + 1)));
+            r = sd_add(r, sdx(uv1.y * uv2.y, Iv(t, i1 + 1, i2 + 1)));
+            return r;
+        };
+        // C_p(l1,l2) = m (v(l2) I(l1,l2+1) - u(l2) I(l1,l2-1)); D_p(l1,l2) = C_p(l2,l1)
+        auto Cv = [&](const sd *t) { return sdx(m, sd_add(sdx(uv2.y, Iv(t, i1, i2 + 1)), sdx(-uv2.x, Iv(t, i1, i2 - 1)))); };
+        auto Dv = [&](const sd *t) { return sdx(m, sd_add(sdx(uv1.y, Iv(t, i2, i1 + 1)), sdx(-uv1.x, Iv(t, i2, i1 - 1)))); };
+        EE = sd_mul(sd_mul(sa1, sa2), sd_add(Bv(ITM), sdx(-m2, Iv(ITE, i1, i2))));
+        MM = sd_mul(sd_mul(sb1, sb2), sd_add(sdx(m2, Iv(ITM, i1, i2)), sd_neg(Bv(ITE))));
+        EM = sd_mul(sd_mul(sa1, sb2), sd_add(Dv(ITM), sd_neg(Cv(ITE))));
+        ME = sd_mul(sd_mul(sb1, sa2), sd_add(Cv(ITM), sd_neg(Dv(ITE))));
+    }
+    double *Am = A + (size_t)task * mat_stride;
+    const int r0 = 2 * a, c0 = 2 * b;
+    const double ee = sd_to_double(EE), mm = sd_to_double(MM), me = sd_to_double(ME), em = sd_to_double(EM);
+    if (!isfinite(ee) || !isfinite(mm) || !isfinite(me) || !isfinite(em)) atomicOr(status + task, ST_ERR_NONFINITE);
+    Am[(size_t)c0 * lda + r0] = (a == b ? 1.0 : 0.0) - ee;
+    Am[(size_t)c0 * lda + r0 + 1] = -me;
+    Am[(size_t)(c0 + 1) * lda + r0 + 1] = (a == b ? 1.0 : 0.0) - mm;
+    if (a != b) Am[(size_t)(c0 + 1) * lda + r0] = -em;
+}
+
+// ---------------------------------------------------------------------------
+// trace / Frobenius norm / shortcut decision (one block per task)
+// ---------------------------------------------------------------------------
+// mode: 0 = dense semantics (trace + Mercator shortcut), 1 = HODLR semantics
+// (trace shortcut only; |tr| > |logdet| checked after the factorisation).
+__global__ void k_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode,
+                        double *trace_out, double *result, int *status)
+{
+    const int task = blockIdx.x;
+    if (task >= ntask) return;
+    const double *Am = A + (size_t)task * mat_stride;
+    __shared__ double red[256];
+    double s = 0.0;
+    // sum of squares of M: diagonal once, strict lower twice (M is symmetric)
+    for (int j = 0; j < n; j++) {
+        const double *col = Am + (size_t)j * lda;
+        for (int i = j + threadIdx.x; i < n; i += blockDim.x) {
+            const double v = (i == j) ? 1.0 - col[i] : -col[i];
+            s += (i == j ? 1.0 : 2.0) * v * v;
+        }
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    // Kahan trace in index order (misc.c:26)
+    double tr = 0.0, c = 0.0;
+    for (int i = 0; i < n; i++) {
+        const double y = (1.0 - Am[(size_t)i * lda + i]) - c;
+        const double t = tr + y;
+        c = (t - tr) - y;
+        tr = t;
+    }
+    trace_out[task] = tr;
+    if (status[task] & ~0xF) { result[task] = NAN; return; }
+    if (fabs(tr) < 1e-8) { result[task] = -tr; status[task] = ST_TRACE; return; }
+    const double fro2 = red[0], fro = sqrt(fro2);
+    if (mode == 0 && fro < 1) {
+        const double merc = -tr - fro2 / 2;
+        const double err = fabs(fro2 / 2 + fro + log1p(-fro));
+        if (fabs(err / merc) < 1e-8) { result[task] = merc; status[task] = ST_MERCATOR; return; }
+    }
+    status[task] = ST_FACTOR;
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+void launch_setup(Task *tasks, int ntask, double *edges, int max_panels, double2 *coefAB, int nu_stride, double c_width,
+                  int *status, cudaStream_t st)
+{
+    k_setup<<<ntask, 256, 0, st>>>(tasks, ntask, edges, max_panels, coefAB, nu_stride, c_width, status);
+    CK(cudaGetLastError());
+}
+
+void launch_mie(const double *xi, const double *epsm1, int nxi, double LbyR, int lmax, double *lna, double *lnb, cudaStream_t st)
+{
+    dim3 g((lmax + 127) / 128, nxi);
+    k_mie<<<g, 128, 0, st>>>(xi, epsm1, nxi, LbyR, lmax, lna, lnb);
+    CK(cudaGetLastError());
+}
+
+void launch_scale(const Task *tasks, int ntask, int ldim, const double *lna, const double *lnb, int lmax, const double *lfac_tab,
+                  sd *Sa, sd *Sb, double2 *uv, cudaStream_t st)
+{
+    dim3 g((ldim + 2 + 127) / 128, ntask);
+    k_scale<<<g, 128, 0, st>>>(tasks, ntask, ldim, lna, lnb, lmax, lfac_tab, Sa, Sb, uv);
+    CK(cudaGetLastError());
+}
+
+size_t ktab_smem_bytes() { return (size_t)KT_WARPS * (32 * 33 + 64) * sizeof(double) + KT_WARPS * 32 * sizeof(int); }
+
+void launch_ktab(bool pr, const Task *tasks, int ntask, int max_warps, const double *edges, int max_panels, const double2 *coefAB,
+                 int nu_stride, const double *lfac_tab, double *partM, int *partE, cudaStream_t st)
+{
+    static bool attr_set = false;
+    const size_t sm = ktab_smem_bytes();
+    if (!attr_set) {
+        CK(cudaFuncSetAttribute(k_ktab<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        CK(cudaFuncSetAttribute(k_ktab<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr_set = true;
+    }
+    dim3 g((max_warps + KT_WARPS - 1) / KT_WARPS, ntask);
+    if (pr) k_ktab<true><<<g, KT_WARPS * 32, sm, st>>>(tasks, edges, max_panels, coefAB, nu_stride, lfac_tab, partM, partE, max_warps);
+    else k_ktab<false><<<g, KT_WARPS * 32, sm, st>>>(tasks, edges, max_panels, coefAB, nu_stride, lfac_tab, partM, partE, max_warps);
+    CK(cudaGetLastError());
+}
+
+void launch_kred(const Task *tasks, int ntask, int max_nnu, const double *partM, const int *partE, int max_warps, int nu_stride,
+                 sd *K, int *status, cudaStream_t st)
+{
+    dim3 g((max_nnu + 127) / 128, ntask);
+    k_kred<<<g, 128, 0, st>>>(tasks, ntask, partM, partE, max_warps, nu_stride, K, status);
+    CK(cudaGetLastError());
+}
+
+void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lfac_tab, sd *I, int *status,
+                 cudaStream_t st)
+{
+    const long long L = ldim + 2, npair = L * (L + 1) / 2;
+    dim3 g((unsigned)((npair + 127) / 128), ntask);
+    k_itab<<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lfac_tab, I, status);
+    CK(cudaGetLastError());
+}
+
+void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv, double *A,
+                 size_t lda, size_t mat_stride, int *status, cudaStream_t st)
+{
+    dim3 g((ldim + 127) / 128, ldim, ntask);
+    k_elem<<<g, 128, 0, st>>>(tasks, ntask, ldim, I, Sa, Sb, uv, A, lda, mat_stride, status);
+    CK(cudaGetLastError());
+}
+
+void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode, double *trace,
+                  double *result, int *status, cudaStream_t st)
+{
+    k_stats<<<ntask, 256, 0, st>>>(tasks, ntask, n, A, lda, mat_stride, mode, trace, result, status);
+    CK(cudaGetLastError());
+}
+
+} // namespace capsgpu

@@ -1,0 +1,33 @@
+// internal.h -- launchers shared between the translation units of the library.
+#pragma once
+#include <cstdio>
+#include <cstdlib>
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace capsgpu {
+
+[[noreturn]] void fatal(const char *file, int line, const char *what);
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) ::capsgpu::fatal(__FILE__, __LINE__, cudaGetErrorString(e_)); } while (0)
+
+void upload_gauss_legendre(const double *x, const double *w);
+void launch_setup(Task *tasks, int ntask, double *edges, int max_panels, double2 *coefAB, int nu_stride, double c_width,
+                  int *status, cudaStream_t st);
+void launch_mie(const double *xi, const double *epsm1, int nxi, double LbyR, int lmax, double *lna, double *lnb, cudaStream_t st);
+void launch_scale(const Task *tasks, int ntask, int ldim, const double *lna, const double *lnb, int lmax, const double *lfac_tab,
+                  sd *Sa, sd *Sb, double2 *uv, cudaStream_t st);
+size_t ktab_smem_bytes();
+void launch_ktab(bool pr, const Task *tasks, int ntask, int max_warps, const double *edges, int max_panels, const double2 *coefAB,
+                 int nu_stride, const double *lfac_tab, double *partM, int *partE, cudaStream_t st);
+void launch_kred(const Task *tasks, int ntask, int max_nnu, const double *partM, const int *partE, int max_warps, int nu_stride,
+                 sd *K, int *status, cudaStream_t st);
+void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lfac_tab, sd *I, int *status,
+                 cudaStream_t st);
+void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv, double *A,
+                 size_t lda, size_t mat_stride, int *status, cudaStream_t st);
+void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode, double *trace,
+                  double *result, int *status, cudaStream_t st);
+void launch_cholesky(int ntask, int n, double *A, size_t lda, size_t mstride, int *status, double *logdiag, cudaStream_t st);
+void launch_final(int ntask, int n, const double *logdiag, const double *trace, int *status, double *result, int mode, cudaStream_t st);
+
+} // namespace capsgpu

@@ -1,0 +1,112 @@
+// kgrid.cuh -- panel grid for the K integrals of one (xi, m) matrix.
+//
+// K_{nu,p}^{(m)}(alpha) = int_1^inf r_p(x) e^{-alpha x} P_nu^mu(x) (x^2-1)^{-s} dx,
+// mu = 2 max(m,1), s = (m>0)  (integration.c:257-286).  With x = cosh t the
+// integrand of degree nu is a single peak in t; its position moves right with nu
+// and its width is ~ kappa(t)^{-1/2}.  All degrees nu = mu..nu_max share ONE
+// panel grid in t whose panel width follows the local peak width:
+//   kappa(t) = alpha cosh t + k_eff cosh t / sinh^2 t,
+// the curvature of -log of the integrand from the e^{-alpha cosh t} factor and
+// from the sinh^k t behaviour near t = 0 (k = mu + 1 - 2s).  Each panel carries
+// GLN Gauss-Legendre nodes.  Because every degree uses the same nodes, the K
+// kernel obtains all P_nu^mu(x_k) from one forward recurrence in nu per node.
+//
+// The grid starts where even the lowest degree is negligible (e^-46 of its
+// peak) -- or at t = 0 when k is small and the sinh^k factor is a low-order
+// polynomial -- and ends once the highest degree has decayed by e^-52 past
+// its peak.  The host/device function below writes the panel edges.
+#pragma once
+#include <math.h>
+
+#ifndef __CUDACC__
+#define KG_HD inline
+#else
+#define KG_HD __host__ __device__ inline
+#endif
+
+namespace capsgpu {
+
+struct KGridParams {
+    double c_width;   // panel width in units of the local peak width
+    double neg_left;  // log-ratio below the lowest peak where the grid starts
+    double neg_right; // log-ratio below the highest peak where the grid ends
+    int kpoly;        // k <= kpoly: start at t=0, no sinh^-2 term in kappa
+};
+
+KG_HD KGridParams kgrid_default() { return KGridParams{1.0, 46.0, 52.0, 12}; }
+
+// log of the lowest-degree integrand up to a constant: k log sinh t - alpha cosh t
+KG_HD double kg_g0(double t, int k, double alpha) { return k * log(sinh(t)) - alpha * cosh(t); }
+
+// d/dt log of the degree-nu integrand, Liouville-Green estimate of P_nu^mu
+KG_HD double kg_dlog(double t, double nu, double mu, int s, double alpha)
+{
+    const double sh = sinh(t), ch = cosh(t), ct = ch / sh;
+    const double y = -0.5 * ct + sqrt(0.25 * ct * ct + nu * (nu + 1) + mu * mu / (sh * sh));
+    return y - alpha * sh + (1 - 2 * s) * ct;
+}
+
+KG_HD double kg_kappa(double t, double alpha, double keff)
+{
+    const double sh = sinh(t), ch = cosh(t);
+    return alpha * ch + keff * ch / (sh * sh);
+}
+
+// Writes panel edges edges[0..np] (np panels) and returns np, or -1 if more
+// than max_panels would be needed.
+KG_HD int kgrid_build(double alpha, int mu, int s, int nu_max, const KGridParams &P, double *edges, int max_panels)
+{
+    const int k = mu + 1 - 2 * s;
+    const double keff = (k <= P.kpoly) ? 0.0 : (double)(mu + 1);
+
+    // peak of the lowest degree: k coth t = alpha sinh t  <=> sinh t tanh t = k/alpha
+    const double r = (double)k / alpha;
+    const double u = 0.5 * (r * r + sqrt(r * r * r * r + 4 * r * r));
+    const double tp0 = asinh(sqrt(u));
+
+    double t0 = 0.0;
+    if (k > P.kpoly) {
+        // left edge: g0(t) = g0(tp0) - neg_left, bisection in log t
+        const double gt = kg_g0(tp0, k, alpha) - P.neg_left;
+        double lo = log(tp0) - 80.0, hi = log(tp0);
+        for (int it = 0; it < 100; it++) {
+            const double mid = 0.5 * (lo + hi);
+            if (kg_g0(exp(mid), k, alpha) < gt) lo = mid; else hi = mid;
+        }
+        t0 = exp(lo);
+    }
+
+    // peak of the highest degree: dlog = 0 (dlog decreases in t)
+    double tlo = 1e-6, thi = 1.0;
+    while (kg_dlog(thi, nu_max, mu, s, alpha) > 0 && thi < 700) thi *= 2;
+    if (kg_dlog(tlo, nu_max, mu, s, alpha) < 0) tlo = 1e-12;
+    for (int it = 0; it < 200; it++) {
+        const double mid = 0.5 * (tlo + thi);
+        if (kg_dlog(mid, nu_max, mu, s, alpha) > 0) tlo = mid; else thi = mid;
+    }
+    const double tpk = 0.5 * (tlo + thi);
+
+    int np = 0;
+    double t = t0;
+    edges[0] = t0;
+    double drop = 0.0;           // integrated dlog of the highest degree past its peak
+    bool past = false;
+    while (np < max_panels) {
+        double h1 = P.c_width / sqrt(kg_kappa(t > 0 ? t : 1e-300, alpha, keff));
+        if (t == 0.0) h1 = P.c_width / sqrt(alpha + (k > 0 ? 0.0 : 0.0));
+        const double h2 = P.c_width / sqrt(kg_kappa(t + h1, alpha, keff));
+        const double h = h1 < h2 ? h1 : h2;
+        const double tn = t + h;
+        if (past || tn > tpk) {
+            const double a = past ? t : tpk;
+            if (tn > a) drop += 0.5 * (tn - a) * (kg_dlog(a, nu_max, mu, s, alpha) + kg_dlog(tn, nu_max, mu, s, alpha));
+            past = true;
+        }
+        t = tn;
+        edges[++np] = t;
+        if (past && drop < -P.neg_right) return np;
+    }
+    return -1;
+}
+
+} // namespace capsgpu

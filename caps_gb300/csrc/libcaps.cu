@@ -1,0 +1,753 @@
+// libcaps.cu -- host side of the GB300 CaPS library: the reference's C API
+// (src/include/libcaps.h) on top of the batched GPU pipeline.
+//
+// A batch is a list of (xi_, m) matrices of one geometry.  The host evaluates
+// the dielectric callbacks once per distinct frequency (the reference calls
+// them per quadrature node with the same argument, integration.c:277), then
+// the device runs: setup -> Mie -> K -> I -> elements -> stats -> Cholesky ->
+// log-det, in chunks sized to the free device memory.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/libcaps.h"
+#include "internal.h"
+
+using namespace capsgpu;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+static void set_error(const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+namespace capsgpu {
+[[noreturn]] void fatal(const char *file, int line, const char *what)
+{
+    fprintf(stderr, "libcaps_gb300: CUDA failure at %s:%d: %s\n", file, line, what);
+    abort();
+}
+} // namespace capsgpu
+
+// contract violation: same behaviour as the reference's TERMINATE (utils.h:31)
+#define TERMINATE(cond, ...)                                                              \
+    do {                                                                                  \
+        if (cond) {                                                                       \
+            fprintf(stderr, "libcaps_gb300: %s:%d: ", __FILE__, __LINE__);               \
+            fprintf(stderr, __VA_ARGS__);                                                 \
+            fprintf(stderr, "\n");                                                        \
+            abort();                                                                      \
+        }                                                                                 \
+    } while (0)
+
+extern "C" const char *caps_gpu_last_error(void) { return g_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------
+// log n! table shared by host and device (logfac.c:66615-66628)
+// ---------------------------------------------------------------------------
+static double h_lfac_tab[1024];
+static std::once_flag g_tab_once;
+static void init_host_tables()
+{
+    for (int n = 0; n < 1024; n++) h_lfac_tab[n] = lgamma(n + 1.0);
+}
+static double host_lfac(unsigned n)
+{
+    std::call_once(g_tab_once, init_host_tables);
+    if (n < 1024) return h_lfac_tab[n];
+    const double dn = n;
+    return (dn + 0.5) * log(dn) - dn + HALF_LOG_2PI + (1.0 / 12) / dn;
+}
+
+// ---------------------------------------------------------------------------
+// device engine: stream, constant tables, grow-only workspace
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    void *get(size_t need)
+    {
+        if (need > bytes) {
+            if (p) CK(cudaFree(p));
+            bytes = std::max(need, bytes + bytes / 4);
+            CK(cudaMalloc(&p, bytes));
+        }
+        return p;
+    }
+};
+
+struct Engine {
+    bool ready = false;
+    int device = 0;
+    cudaStream_t own = nullptr, user = nullptr;
+    double *d_lfac = nullptr;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps;
+    std::vector<double> host_pinned_dummy;
+    double timings[6] = {0, 0, 0, 0, 0, 0};
+    cudaEvent_t ev[7];
+    std::mutex mu;
+    cudaStream_t stream() const { return user ? user : own; }
+};
+static Engine g_eng;
+
+static void engine_init()
+{
+    if (g_eng.ready) return;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        fprintf(stderr, "libcaps_gb300: no CUDA device available (%s); this library has no CPU path\n",
+                e == cudaSuccess ? "0 devices" : cudaGetErrorString(e));
+        abort();
+    }
+    CK(cudaGetDevice(&g_eng.device));
+    CK(cudaStreamCreateWithFlags(&g_eng.own, cudaStreamNonBlocking));
+    std::call_once(g_tab_once, init_host_tables);
+    CK(cudaMalloc(&g_eng.d_lfac, 1024 * sizeof(double)));
+    CK(cudaMemcpy(g_eng.d_lfac, h_lfac_tab, 1024 * sizeof(double), cudaMemcpyHostToDevice));
+    // Gauss-Legendre nodes on [-1,1] by Newton iteration on P_GLN
+    double x[GLN], w[GLN];
+    for (int i = 0; i < GLN; i++) {
+        double z = cos(PI * (i + 0.75) / (GLN + 0.5)), pp = 0;
+        for (int it = 0; it < 100; it++) {
+            double p1 = 1, p2 = 0;
+            for (int j = 1; j <= GLN; j++) { double p3 = p2; p2 = p1; p1 = ((2 * j - 1) * z * p2 - (j - 1) * p3) / j; }
+            pp = GLN * (z * p1 - p2) / (z * z - 1);
+            const double z1 = z;
+            z = z1 - p1 / pp;
+            if (fabs(z - z1) < 1e-16) break;
+        }
+        x[i] = z;
+        w[i] = 2 / ((1 - z * z) * pp * pp);
+    }
+    upload_gauss_legendre(x, w);
+    for (int i = 0; i < 7; i++) CK(cudaEventCreate(&g_eng.ev[i]));
+    g_eng.ready = true;
+}
+
+extern "C" void caps_gpu_set_stream(void *stream)
+{
+    std::lock_guard<std::mutex> lk(g_eng.mu);
+    engine_init();
+    g_eng.user = (cudaStream_t)stream;
+}
+
+extern "C" int caps_gpu_timings(double *ms, int n)
+{
+    int k = std::min(n, 6);
+    for (int i = 0; i < k; i++) ms[i] = g_eng.timings[i];
+    return k;
+}
+
+// ---------------------------------------------------------------------------
+// caps_t API (libcaps.c:45-457)
+// ---------------------------------------------------------------------------
+extern "C" double caps_lnLambda(int l1, int l2, int m)
+{
+    return (log(2. * l1 + 1) + log(2. * l2 + 1) - log((double)l1) - log(l1 + 1.) - log((double)l2) - log(l2 + 1.)
+            + host_lfac(l1 - m) + host_lfac(l2 - m) - host_lfac(l1 + m) - host_lfac(l2 + m)) / 2.0;
+}
+
+extern "C" int caps_estimate_lminmax(caps_t *self, int m, size_t *lmin_p, size_t *lmax_p)
+{
+    const int ldim = self->ldim;
+    if (m == 0) { *lmin_p = 1; *lmax_p = 1 + ldim; return 0; }
+    const int l = (int)round(m / sqrt(2 * self->LbyR));
+    int lmin = l - ldim / 2;
+    if (lmin < m) lmin = m;
+    *lmin_p = lmin;
+    *lmax_p = lmin + ldim;
+    return l;
+}
+
+extern "C" double caps_epsilonm1_perf(double xi_, void *userdata) { (void)xi_; (void)userdata; return INFINITY; }
+
+extern "C" double caps_epsilonm1_drude(double xi, void *userdata)
+{
+    const double *p = (const double *)userdata;
+    return p[0] * p[0] / (xi * (xi + p[1]));
+}
+
+extern "C" caps_t *caps_init(double R, double L)
+{
+    if (L <= 0 || R <= 0) return NULL;
+    caps_t *s = (caps_t *)calloc(1, sizeof(caps_t));
+    if (!s) { fprintf(stderr, "libcaps_gb300: out of memory\n"); abort(); }
+    const double LbyR = L / R;
+    s->LbyR = LbyR; s->L = L; s->R = R; s->calL = L + R;
+    s->y = -LN2 - log1p(LbyR);
+    s->ldim = (int)ceil(std::max((double)CAPS_MINIMUM_LDIM, CAPS_FACTOR_LDIM / LbyR));
+    s->epsilonm1_plate = caps_epsilonm1_perf;
+    s->epsilonm1_sphere = caps_epsilonm1_perf;
+    s->userdata_plate = s->userdata_sphere = NULL;
+    s->epsrel = CAPS_EPSREL;
+    s->detalg = DETALG_HODLR;
+    s->precision = CAPS_PREC_FP64;
+    return s;
+}
+
+extern "C" void caps_free(caps_t *self) { free(self); }
+
+extern "C" void caps_build(FILE *stream, const char *prefix)
+{
+    if (!prefix) prefix = "";
+    fprintf(stream, "%sversion: 0.5 (GB300 port of the logdetD path)\n", prefix);
+    fprintf(stream, "%scompiler: nvcc %d.%d\n", prefix, __CUDACC_VER_MAJOR__, __CUDACC_VER_MINOR__);
+    fprintf(stream, "%scompile time: %s %s\n", prefix, __DATE__, __TIME__);
+}
+
+extern "C" void caps_info(caps_t *self, FILE *stream, const char *prefix)
+{
+    const char *d;
+    if (!prefix) prefix = "";
+    switch (self->detalg) {
+    case DETALG_HODLR: d = "HODLR"; break;
+    case DETALG_LU: d = "LU"; break;
+    case DETALG_QR: d = "QR"; break;
+    case DETALG_CHOLESKY: d = "CHOLESKY"; break;
+    default: d = "unknown";
+    }
+    fprintf(stream, "%sL/R    = %.16g\n", prefix, self->LbyR);
+    fprintf(stream, "%sL      = %.16g\n", prefix, self->L);
+    fprintf(stream, "%sR      = %.16g\n", prefix, self->R);
+    fprintf(stream, "%sldim   = %d\n", prefix, self->ldim);
+    fprintf(stream, "%sepsrel = %.1e\n", prefix, self->epsrel);
+    fprintf(stream, "%sdetalg = %s\n", prefix, d);
+}
+
+extern "C" int caps_set_epsrel(caps_t *self, double epsrel) { if (epsrel <= 0) return 0; self->epsrel = epsrel; return 1; }
+extern "C" double caps_get_epsrel(caps_t *self) { return self->epsrel; }
+extern "C" void caps_set_epsilonm1_plate(caps_t *self, double (*f)(double, void *), void *ud) { self->epsilonm1_plate = f; self->userdata_plate = ud; }
+extern "C" void caps_set_epsilonm1_sphere(caps_t *self, double (*f)(double, void *), void *ud) { self->epsilonm1_sphere = f; self->userdata_sphere = ud; }
+extern "C" void caps_set_epsilonm1(caps_t *self, double (*f)(double, void *), void *ud) { caps_set_epsilonm1_plate(self, f, ud); caps_set_epsilonm1_sphere(self, f, ud); }
+extern "C" int caps_set_detalg(caps_t *self, detalg_t d) { self->detalg = d; return 1; }
+extern "C" detalg_t caps_get_detalg(caps_t *self) { return self->detalg; }
+extern "C" int caps_set_ldim(caps_t *self, int ldim) { if (ldim < 1) return 0; self->ldim = ldim; return 1; }
+extern "C" int caps_get_ldim(caps_t *self) { return self->ldim; }
+extern "C" int caps_gpu_set_precision(caps_t *self, int p)
+{
+    if (p != CAPS_PREC_FP64 && p != CAPS_PREC_MIXED) return 0;
+    self->precision = p;
+    return 1;
+}
+
+extern "C" double caps_epsilonm1_plate(caps_t *self, double xi_) { return self->epsilonm1_plate(xi_ * CAPS_c / self->calL, self->userdata_plate); }
+extern "C" double caps_epsilonm1_sphere(caps_t *self, double xi_) { return self->epsilonm1_sphere(xi_ * CAPS_c / self->calL, self->userdata_sphere); }
+
+// Fresnel coefficients (libcaps.c:616): a scalar helper of the API; the GPU
+// evaluates the same formula per quadrature node inside the K kernel
+extern "C" void caps_fresnel(caps_t *self, double xi_, double k_, double *r_TE, double *r_TM)
+{
+    const double epsm1 = caps_epsilonm1_plate(self, xi_);
+    if (std::isinf(epsm1)) { *r_TM = 1.0; *r_TE = -1.0; return; }
+    const double x = xi_ * xi_ / (xi_ * xi_ + k_ * k_) * epsm1;
+    const double bm1 = x / (sqrt(1 + x) + 1);
+    *r_TE = -bm1 / (2 + bm1);
+    *r_TM = (epsm1 - bm1) / (epsm1 + 2 + bm1);
+}
+
+// ---------------------------------------------------------------------------
+// the batch pipeline
+// ---------------------------------------------------------------------------
+struct BatchOpts {
+    int mode = 1;            // 0 dense semantics (Mercator shortcut), 1 HODLR semantics
+    bool factor = true;      // false: stop after assembly (caps_M_init)
+    double *M_out = nullptr; // host buffer for the dense M of a single task (row-major)
+    double *mie_out_a = nullptr, *mie_out_b = nullptr; // Mie of task 0's window
+};
+
+static const double KGRID_WIDTH = 2.0;
+static const int MAX_PANELS = 2048;
+
+static int lmin_of(const caps_t *c, int m)
+{
+    size_t lo, hi;
+    caps_estimate_lminmax(const_cast<caps_t *>(c), m, &lo, &hi);
+    return (int)lo;
+}
+
+static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, double *out, int *status_out, const BatchOpts &O)
+{
+    std::lock_guard<std::mutex> lk(g_eng.mu);
+    engine_init();
+    g_last_error.clear();
+    const cudaStream_t st = g_eng.stream();
+    const int ldim = caps->ldim, dim = 2 * ldim, L = ldim + 2;
+    for (int i = 0; i < n; i++) TERMINATE(!(xi_[i] > 0), "Matsubara frequency must be positive");
+
+    // material per distinct xi (host callbacks, evaluated once per frequency)
+    const bool is_pr = std::isinf(caps_epsilonm1_plate(caps, INFINITY));
+    std::map<double, int> xi_index;
+    std::vector<double> xis, eps_sphere;
+    std::vector<Task> tasks(n);
+    int lmax_mie = 1;
+    for (int i = 0; i < n; i++) {
+        auto it = xi_index.find(xi_[i]);
+        int ix;
+        if (it == xi_index.end()) {
+            ix = (int)xis.size();
+            xi_index[xi_[i]] = ix;
+            xis.push_back(xi_[i]);
+            eps_sphere.push_back(caps_epsilonm1_sphere(caps, xi_[i]));
+        } else ix = it->second;
+        Task &T = tasks[i];
+        T.xi_ = xi_[i];
+        T.alpha = 2 * xi_[i];
+        T.epsm1_plate = caps_epsilonm1_plate(caps, xi_[i]);
+        T.epsm1_sphere = eps_sphere[ix];
+        T.m = ms[i];
+        TERMINATE(ms[i] < 0, "m must be non-negative");
+        T.lmin = lmin_of(caps, ms[i]);
+        T.mu = 2 * std::max(ms[i], 1);
+        T.s = ms[i] > 0 ? 1 : 0;
+        T.nu_max = 2 * (T.lmin + ldim);
+        T.xi_index = ix;
+        T.is_pr = is_pr ? 1 : 0;
+        T.npanel = 0;
+        lmax_mie = std::max(lmax_mie, T.lmin + ldim);
+    }
+    const int nxi = (int)xis.size();
+    int nnu_max = 0;
+    for (auto &T : tasks) nnu_max = std::max(nnu_max, T.nu_max - T.mu + 1);
+    const int nu_stride = (nnu_max + 31) / 32 * 32;
+
+    // chunk size from free memory
+    size_t freeb = 0, totb = 0;
+    CK(cudaMemGetInfo(&freeb, &totb));
+    const size_t per_task = (size_t)dim * dim * 8 + (size_t)2 * L * L * sizeof(sd) + (size_t)2 * nu_stride * sizeof(sd)
+                          + (size_t)nu_stride * sizeof(double2) + (size_t)3 * L * sizeof(sd) + (size_t)dim * 8
+                          + (size_t)2 * 256 * nu_stride * 12; // partial sums, up to 256 warps
+    size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes));
+    int chunk = (int)std::max<size_t>(1, std::min<size_t>(budget / per_task, 65535));
+    chunk = std::min(chunk, n);
+
+    // Mie table for all distinct xi at once
+    double *d_xi = (double *)g_eng.xi.get(nxi * sizeof(double));
+    double *d_eps = (double *)g_eng.eps.get(nxi * sizeof(double));
+    CK(cudaMemcpyAsync(d_xi, xis.data(), nxi * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_eps, eps_sphere.data(), nxi * sizeof(double), cudaMemcpyHostToDevice, st));
+    double *d_lna = (double *)g_eng.mie_a.get((size_t)nxi * (lmax_mie + 1) * sizeof(double));
+    double *d_lnb = (double *)g_eng.mie_b.get((size_t)nxi * (lmax_mie + 1) * sizeof(double));
+
+    double tsum[6] = {0, 0, 0, 0, 0, 0};
+    int nerr = 0;
+    for (int c0 = 0; c0 < n; c0 += chunk) {
+        const int nt = std::min(chunk, n - c0);
+        CK(cudaEventRecord(g_eng.ev[0], st));
+        if (c0 == 0) launch_mie(d_xi, d_eps, nxi, caps->LbyR, lmax_mie, d_lna, d_lnb, st);
+        Task *d_tasks = (Task *)g_eng.tasks.get(nt * sizeof(Task));
+        CK(cudaMemcpyAsync(d_tasks, tasks.data() + c0, nt * sizeof(Task), cudaMemcpyHostToDevice, st));
+        int *d_status = (int *)g_eng.status.get(nt * sizeof(int));
+        CK(cudaMemsetAsync(d_status, 0, nt * sizeof(int), st));
+        double *d_edges = (double *)g_eng.edges.get((size_t)nt * (MAX_PANELS + 1) * sizeof(double));
+        double2 *d_coef = (double2 *)g_eng.coef.get((size_t)nt * nu_stride * sizeof(double2));
+        launch_setup(d_tasks, nt, d_edges, MAX_PANELS, d_coef, nu_stride, KGRID_WIDTH, d_status, st);
+        // panel counts decide the size of the partial-sum buffers
+        std::vector<Task> tback(nt);
+        CK(cudaMemcpyAsync(tback.data(), d_tasks, nt * sizeof(Task), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        int max_warps = 1;
+        for (auto &T : tback) max_warps = std::max(max_warps, (T.npanel + 1) / 2);
+        sd *d_Sa = (sd *)g_eng.Sa.get((size_t)nt * L * sizeof(sd));
+        sd *d_Sb = (sd *)g_eng.Sb.get((size_t)nt * L * sizeof(sd));
+        double2 *d_uv = (double2 *)g_eng.uv.get((size_t)nt * L * sizeof(double2));
+        launch_scale(d_tasks, nt, ldim, d_lna, d_lnb, lmax_mie, g_eng.d_lfac, d_Sa, d_Sb, d_uv, st);
+        CK(cudaEventRecord(g_eng.ev[1], st));
+
+        double *d_pM = (double *)g_eng.partM.get((size_t)nt * 2 * max_warps * nu_stride * sizeof(double));
+        int *d_pE = (int *)g_eng.partE.get((size_t)nt * 2 * max_warps * nu_stride * sizeof(int));
+        sd *d_K = (sd *)g_eng.K.get((size_t)nt * 2 * nu_stride * sizeof(sd));
+        launch_ktab(is_pr, d_tasks, nt, max_warps, d_edges, MAX_PANELS, d_coef, nu_stride, g_eng.d_lfac, d_pM, d_pE, st);
+        launch_kred(d_tasks, nt, nnu_max, d_pM, d_pE, max_warps, nu_stride, d_K, d_status, st);
+        CK(cudaEventRecord(g_eng.ev[2], st));
+
+        sd *d_I = (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
+        launch_itab(d_tasks, nt, ldim, d_K, nu_stride, g_eng.d_lfac, d_I, d_status, st);
+        CK(cudaEventRecord(g_eng.ev[3], st));
+
+        const size_t lda = dim, mstride = (size_t)dim * dim;
+        double *d_A = (double *)g_eng.A.get((size_t)nt * mstride * sizeof(double));
+        launch_elem(d_tasks, nt, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, lda, mstride, d_status, st);
+        double *d_trace = (double *)g_eng.trace.get(nt * sizeof(double));
+        double *d_res = (double *)g_eng.result.get(nt * sizeof(double));
+        if (O.factor) launch_stats(d_tasks, nt, dim, d_A, lda, mstride, O.mode, d_trace, d_res, d_status, st);
+        CK(cudaEventRecord(g_eng.ev[4], st));
+
+        if (O.factor) {
+            double *d_ld = (double *)g_eng.logdiag.get((size_t)nt * dim * sizeof(double));
+            launch_cholesky(nt, dim, d_A, lda, mstride, d_status, d_ld, st);
+            launch_final(nt, dim, d_ld, d_trace, d_status, d_res, O.mode, st);
+        }
+        CK(cudaEventRecord(g_eng.ev[5], st));
+
+        std::vector<int> hst(nt);
+        CK(cudaMemcpyAsync(hst.data(), d_status, nt * sizeof(int), cudaMemcpyDeviceToHost, st));
+        if (O.factor) CK(cudaMemcpyAsync(out + c0, d_res, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (O.M_out) {
+            // dense row-major M from the lower triangle of 1-M
+            std::vector<double> Ah((size_t)dim * dim);
+            CK(cudaMemcpyAsync(Ah.data(), d_A, (size_t)dim * dim * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            for (int j = 0; j < dim; j++)
+                for (int i = j; i < dim; i++) {
+                    const double v = (i == j ? 1.0 : 0.0) - Ah[(size_t)j * dim + i];
+                    O.M_out[(size_t)i * dim + j] = v;
+                    O.M_out[(size_t)j * dim + i] = v;
+                }
+        }
+        if (O.mie_out_a) {
+            const Task &T = tasks[0];
+            CK(cudaMemcpyAsync(O.mie_out_a, d_lna + (size_t)T.xi_index * (lmax_mie + 1) + T.lmin, ldim * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(O.mie_out_b, d_lnb + (size_t)T.xi_index * (lmax_mie + 1) + T.lmin, ldim * sizeof(double), cudaMemcpyDeviceToHost, st));
+        }
+        CK(cudaStreamSynchronize(st));
+        float f;
+        for (int k = 0; k < 5; k++) { CK(cudaEventElapsedTime(&f, g_eng.ev[k], g_eng.ev[k + 1])); tsum[k] += f; }
+        CK(cudaEventElapsedTime(&f, g_eng.ev[0], g_eng.ev[5])); tsum[5] += f;
+        for (int i = 0; i < nt; i++) {
+            if (status_out) status_out[c0 + i] = hst[i];
+            if (hst[i] & ~0xF) {
+                nerr++;
+                set_error("matrix %d (xi_=%.17g, m=%d): status %d", c0 + i, tasks[c0 + i].xi_, tasks[c0 + i].m, hst[i]);
+            }
+        }
+    }
+    for (int k = 0; k < 6; k++) g_eng.timings[k] = tsum[k];
+    return nerr;
+}
+
+static int detalg_mode(const caps_t *c) { return c->detalg == DETALG_HODLR ? 1 : 0; }
+
+extern "C" int caps_logdetD_batch(caps_t *self, const double *xi_, const int *m, int n, double *out, int *status)
+{
+    if (n <= 0) return 0;
+    BatchOpts O;
+    O.mode = detalg_mode(self);
+    return run_batch(self, xi_, m, n, out, status, O);
+}
+
+extern "C" double caps_logdetD(caps_t *self, double xi_, int m)
+{
+    TERMINATE(xi_ <= 0, "Matsubara frequency must be positive");
+    double r = NAN;
+    BatchOpts O;
+    O.mode = detalg_mode(self);
+    run_batch(self, &xi_, &m, 1, &r, NULL, O);
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Mie coefficients through the device kernel (single evaluation)
+// ---------------------------------------------------------------------------
+static void mie_device(caps_t *self, double xi_, int l, double epsm1, double *lna, double *lnb)
+{
+    std::lock_guard<std::mutex> lk(g_eng.mu);
+    engine_init();
+    const cudaStream_t st = g_eng.stream();
+    double *d_xi = (double *)g_eng.xi.get(sizeof(double));
+    double *d_eps = (double *)g_eng.eps.get(sizeof(double));
+    CK(cudaMemcpyAsync(d_xi, &xi_, sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_eps, &epsm1, sizeof(double), cudaMemcpyHostToDevice, st));
+    double *d_a = (double *)g_eng.mie_a.get((size_t)(l + 1) * sizeof(double));
+    double *d_b = (double *)g_eng.mie_b.get((size_t)(l + 1) * sizeof(double));
+    launch_mie(d_xi, d_eps, 1, self->LbyR, l, d_a, d_b, st);
+    CK(cudaMemcpyAsync(lna, d_a + l, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(lnb, d_b + l, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+}
+
+extern "C" void caps_mie(caps_t *self, double xi_, int l, double *lna, double *lnb)
+{
+    mie_device(self, xi_, l, caps_epsilonm1_sphere(self, xi_), lna, lnb);
+}
+
+extern "C" void caps_mie_perf(caps_t *self, double xi_, int l, double *lna, double *lnb)
+{
+    mie_device(self, xi_, l, INFINITY, lna, lnb);
+}
+
+// ---------------------------------------------------------------------------
+// element API (libcaps.c:673-846): the GPU materialises the whole matrix
+// ---------------------------------------------------------------------------
+extern "C" caps_M_t *caps_M_init(caps_t *self, int m, double xi_)
+{
+    TERMINATE(xi_ <= 0, "Matsubara frequency must be positive");
+    caps_M_t *M = (caps_M_t *)calloc(1, sizeof(caps_M_t));
+    const int ldim = self->ldim, dim = 2 * ldim;
+    M->caps = self; M->m = m; M->ldim = ldim; M->xi_ = xi_;
+    M->lmin = lmin_of(self, m);
+    M->al = (double *)malloc(ldim * sizeof(double));
+    M->bl = (double *)malloc(ldim * sizeof(double));
+    M->M = (double *)malloc((size_t)dim * dim * sizeof(double));
+    BatchOpts O;
+    O.factor = false;
+    O.M_out = M->M;
+    O.mie_out_a = M->al;
+    O.mie_out_b = M->bl;
+    run_batch(self, &xi_, &m, 1, NULL, NULL, O);
+    return M;
+}
+
+extern "C" double caps_M_elem(caps_M_t *self, int l1, int l2, char p1, char p2)
+{
+    const int dim = 2 * self->ldim;
+    const int i = 2 * (l1 - self->lmin) + (p1 == 'M'), j = 2 * (l2 - self->lmin) + (p2 == 'M');
+    return self->M[(size_t)i * dim + j];
+}
+
+extern "C" double caps_kernel_M(int i, int j, void *args_)
+{
+    caps_M_t *a = (caps_M_t *)args_;
+    return a->M[(size_t)i * 2 * a->ldim + j];
+}
+
+extern "C" void caps_M_free(caps_M_t *self)
+{
+    if (!self) return;
+    free(self->al); free(self->bl); free(self->M); free(self);
+}
+
+// ---------------------------------------------------------------------------
+// xi = 0 (libcaps.c:860-1145): closed-form EE/MM kernels; element callbacks
+// ---------------------------------------------------------------------------
+extern "C" double caps_kernel_M0_EE(int i, int j, void *args_)
+{
+    caps_M_t *a = (caps_M_t *)args_;
+    const double y = a->caps->y;
+    const int l1 = i + a->lmin, l2 = j + a->lmin, m = a->m;
+    return exp((l1 + l2 + 1) * y + host_lfac(l1 + l2) - 0.5 * (host_lfac(l1 + m) + host_lfac(l1 - m) + host_lfac(l2 + m) + host_lfac(l2 - m)));
+}
+
+extern "C" double caps_kernel_M0_MM(int i, int j, void *args_)
+{
+    caps_M_t *a = (caps_M_t *)args_;
+    const int l1 = i + a->lmin, l2 = j + a->lmin;
+    return caps_kernel_M0_EE(i, j, args_) * sqrt(((double)l1 * l2) / ((l1 + 1.) * (l2 + 1.)));
+}
+
+extern "C" double caps_kernel_M0_MM_plasma(int i, int j, void *args_)
+{
+    (void)i; (void)j; (void)args_;
+    set_error("caps_kernel_M0_MM_plasma: the plasma xi=0 kernel is not implemented on the GPU");
+    return NAN;
+}
+
+extern "C" double caps_ht_drude(caps_t *caps)
+{
+    const double x = caps->LbyR, x2 = x * x;
+    const double Z = (1 + x) * (1 - sqrt((x2 + 2 * x) / (x2 + 2 * x + 1)));
+    double s1 = 0, s2 = 0;
+    for (int l = 1;; l++) {
+        const double a = pow(Z, 2 * l), b = a * Z;
+        const double v1 = (2 * l + 1) * log1p(-b), v2 = b * (1 - a) / (1 - b);
+        s1 += v1; s2 += v2;
+        if (fabs(v1 / s1) < 1e-15 && fabs(v2 / s2) < 1e-15) break;
+    }
+    return 0.5 * (s1 + log1p(-(1 - Z * Z) * s2));
+}
+
+// xi=0 EE/MM determinants are assembled and factored on the GPU
+int logdetD0_batch(caps_t *self, const int *ms, int n, int which, double *out);
+
+extern "C" void caps_logdetD0(caps_t *self, int m, double omegap, double *EE, double *MM, double *MM_plasma)
+{
+    (void)omegap;
+    if (EE) logdetD0_batch(self, &m, 1, 0, EE);
+    if (MM) logdetD0_batch(self, &m, 1, 1, MM);
+    if (MM_plasma) { *MM_plasma = NAN; set_error("caps_logdetD0: MM_plasma (plasma xi=0 block) is not implemented on the GPU"); }
+}
+
+extern "C" double caps_ht_perf(caps_t *caps, double eps)
+{
+    const double LbyR = caps->LbyR;
+    const double drude = caps_ht_drude(caps);
+    double MM = 0;
+    const double Z = 1. / (1 + LbyR + sqrt(LbyR * (2 + LbyR)));
+    for (int l = 0;; l++) {
+        const double v = 0.5 * log1p(-pow(Z, 2 * l + 3));
+        MM += v;
+        if (fabs(v / MM) < eps) break;
+    }
+    // m = 1, 2, ... in batches of 16 on the GPU; summed up to the first m that meets the cutoff
+    for (int m0 = 1;; m0 += 16) {
+        int ms[16];
+        double v[16];
+        for (int k = 0; k < 16; k++) ms[k] = m0 + k;
+        logdetD0_batch(caps, ms, 16, 1, v);
+        for (int k = 0; k < 16; k++) {
+            MM += v[k];
+            if (fabs(v[k] / MM) < eps) return drude + MM;
+        }
+    }
+}
+
+extern "C" double caps_ht_plasma(caps_t *caps, double omegap_, double eps)
+{
+    (void)caps; (void)omegap_; (void)eps;
+    set_error("caps_ht_plasma: the plasma xi=0 block is not implemented on the GPU");
+    return NAN;
+}
+
+// ---------------------------------------------------------------------------
+// free energy: Matsubara sum with the reference's truncation rules
+// (src/caps.c:307-396 F_xi, :749-852 master), batched on the GPU
+// ---------------------------------------------------------------------------
+static double kahan_sum(const double *v, size_t n)
+{
+    double s = 0, c = 0;
+    for (size_t i = 0; i < n; i++) { const double y = v[i] - c, t = s + y; c = (t - s) - y; s = t; }
+    return s;
+}
+
+// which xi = 0 rule applies: 0 perfect reflectors, 1 Drude (analytic), 2 plasma
+static int xi0_model(const caps_t *c)
+{
+    if (c->epsilonm1_plate == caps_epsilonm1_perf) return 0;
+    if (c->epsilonm1_plate == caps_epsilonm1_drude && c->userdata_plate) {
+        const double *p = (const double *)c->userdata_plate;
+        return p[1] > 0 ? 1 : 2;
+    }
+    return 1;
+}
+
+struct MState {
+    std::vector<double> v;  // logdetD per m (NAN = not yet computed)
+    int mstop = -1;         // first m meeting the cutoff
+    int next = 0;           // next m to schedule
+    bool done() const { return mstop >= 0; }
+};
+
+// number of m to schedule next for one frequency, from the decay of the
+// values so far (log-linear extrapolation to the cutoff), clamped
+static int m_chunk(const MState &s, double cutoff)
+{
+    const int k = s.next;
+    if (k < 8) return 32;
+    const double v0 = s.v[0], a = fabs(s.v[k - 1]), b = fabs(s.v[k - 8]);
+    if (!(a > 0) || !(b > a)) return 32;
+    const double rate = log(b / a) / 7.0;          // e-folds per m
+    const double need = log(a / (cutoff * fabs(v0))) / rate;
+    int w = (int)ceil(need) + 4;
+    return std::max(8, std::min(w, 256));
+}
+
+extern "C" double caps_free_energy(caps_t *self, double T, double cutoff, double epsrel, caps_energy_info_t *info)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    TERMINATE(!(T > 0), "temperature must be positive");
+    const double Ts = 2 * PI * CAPS_kB * (self->R + self->L) * T / (CAPS_hbar * CAPS_c);
+    int ndet = 0, nwasted = 0;
+
+    // xi = 0
+    double v0;
+    const int model = xi0_model(self);
+    if (model == 1) v0 = caps_ht_drude(self);
+    else if (model == 0) {
+        // drude_HT + sum'_m logdetD0 MM with the m cutoff (caps.c:329-395, worker :925)
+        const double drude = caps_ht_drude(self);
+        std::vector<double> terms;
+        int mstop = -1;
+        for (int m0 = 0; mstop < 0 && m0 < 4096; m0 += 32) {
+            int ms[32]; double v[32];
+            for (int k = 0; k < 32; k++) ms[k] = m0 + k;
+            logdetD0_batch(self, ms, 32, 1, v);
+            ndet += 32;
+            for (int k = 0; k < 32; k++) {
+                terms.push_back(v[k]);
+                if (mstop < 0 && (v[k] == 0 || v[k] / terms[0] < cutoff)) mstop = m0 + k;
+            }
+        }
+        nwasted += (int)terms.size() - (mstop + 1);
+        terms[0] /= 2;
+        v0 = drude + kahan_sum(terms.data(), mstop + 1);
+    } else {
+        set_error("caps_free_energy: plasma model xi=0 term is not implemented");
+        return NAN;
+    }
+
+    std::vector<double> vn(1, v0);      // per-frequency sums, index n
+    std::vector<MState> st;             // st[n-1] for xi_n
+    int nmax_known = -1;                // n where |v_n/v_0| < epsrel
+    int nactive = 4;
+    st.resize(nactive);
+    for (;;) {
+        // schedule
+        std::vector<double> bx; std::vector<int> bm; std::vector<std::pair<int, int>> who;
+        const int nlim = nmax_known > 0 ? nmax_known : nactive;
+        for (int i = 0; i < nlim; i++) {
+            MState &s = st[i];
+            if (s.done()) continue;
+            const int w = m_chunk(s, cutoff);
+            for (int k = 0; k < w; k++) { bx.push_back((i + 1) * Ts); bm.push_back(s.next + k); who.push_back({i, s.next + k}); }
+            s.next += w;
+            s.v.resize(s.next, NAN);
+        }
+        if (bx.empty()) break;
+        std::vector<double> out(bx.size());
+        caps_logdetD_batch(self, bx.data(), bm.data(), (int)bx.size(), out.data(), NULL);
+        ndet += (int)bx.size();
+        for (size_t k = 0; k < bx.size(); k++) st[who[k].first].v[who[k].second] = out[k];
+        for (int i = 0; i < nlim; i++) {
+            MState &s = st[i];
+            if (s.done()) continue;
+            for (int m = 0; m < s.next; m++)
+                if (s.v[m] == 0 || s.v[m] / s.v[0] < cutoff) { s.mstop = m; break; }
+        }
+        // Matsubara truncation in order of n
+        if (nmax_known < 0) {
+            bool grow = true;
+            for (int i = 0; i < (int)st.size(); i++) {
+                if (!st[i].done()) { grow = false; break; }
+                std::vector<double> t(st[i].v.begin(), st[i].v.begin() + st[i].mstop + 1);
+                t[0] /= 2;
+                const double v = kahan_sum(t.data(), t.size());
+                if (fabs(v / v0) < epsrel) { nmax_known = i + 1; grow = false; break; }
+            }
+            if (grow && nmax_known < 0) { nactive *= 2; st.resize(nactive); }
+        }
+        if (nmax_known > 0) {
+            bool all = true;
+            for (int i = 0; i < nmax_known; i++) all = all && st[i].done();
+            if (all) break;
+        }
+        TERMINATE(nactive > 4096, "Matsubara sum did not converge");
+    }
+    for (int i = 0; i < (int)st.size(); i++) {
+        if (i < nmax_known) nwasted += st[i].next - (st[i].mstop + 1);
+        else nwasted += st[i].next;
+    }
+    for (int i = 0; i < nmax_known; i++) {
+        std::vector<double> t(st[i].v.begin(), st[i].v.begin() + st[i].mstop + 1);
+        t[0] /= 2;
+        vn.push_back(kahan_sum(t.data(), t.size()));
+    }
+    if (info) {
+        info->nxi = (int)vn.size();
+        info->ndet = ndet;
+        info->nwasted = nwasted;
+        for (size_t i = 0; i < vn.size() && i < 4096; i++) {
+            if (info->xi) info->xi[i] = i * Ts;
+            if (info->logdetD) info->logdetD[i] = vn[i];
+        }
+    }
+    std::vector<double> w(vn);
+    w[0] /= 2;
+    const double E = Ts / PI * kahan_sum(w.data(), w.size());
+    if (info) info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return E;
+}

@@ -1,0 +1,182 @@
+/*
+ * libcaps.h -- GB300 implementation of the CaPS v0.5 public C API for the
+ * round-trip-matrix log-det path (plane-sphere Casimir geometry).
+ *
+ * Every reference prototype below keeps the reference's name, argument meaning
+ * and error behaviour; the comment beside each names the reference
+ * declaration (src/include/libcaps.h) and definition it replaces.  All
+ * matrix assembly and factorisation runs on the GPU; the host evaluates the
+ * dielectric callbacks once per frequency and ships the scalars.
+ *
+ * Error behaviour: contract violations (xi <= 0, as in the reference) print a
+ * message and abort(); a missing or failing CUDA device prints and aborts (no
+ * CPU fallback); numerical trouble inside a kernel yields NaN for that matrix
+ * and a status code, readable through caps_gpu_last_error().
+ */
+#ifndef LIBCAPS_H
+#define LIBCAPS_H
+
+#include <stdarg.h>
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdio.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* src/include/libcaps.h:17 */
+typedef enum { TE, TM } polarization_t;
+/* src/include/matrix.h:14 */
+typedef enum { DETALG_HODLR, DETALG_LU, DETALG_QR, DETALG_CHOLESKY } detalg_t;
+/* src/include/constants.h:15 */
+typedef signed char sign_t;
+
+/* src/include/constants.h:45-48 */
+#define CAPS_hbar    1.0545718e-34
+#define CAPS_hbar_eV 6.582119514e-16
+#define CAPS_kB      1.38064852e-23
+#define CAPS_c       299792458.
+
+/* src/include/libcaps.h:29-33 */
+#define CAPS_MINIMUM_LDIM 20
+#define CAPS_FACTOR_LDIM 5
+#define CAPS_EPSREL 1e-8
+
+/* The CaPS object.  The public fields keep the layout of the reference
+ * (src/include/libcaps.h:41-78); private GPU settings follow them. */
+typedef struct caps
+{
+    double L;    /* separation of plane and sphere */
+    double R;    /* radius of sphere */
+    double calL; /* L+R */
+    double LbyR; /* L/R */
+    double y;    /* log(R/(R+L)/2) */
+    double (*epsilonm1_plate)(double xi_, void *userdata);
+    void *userdata_plate;
+    double (*epsilonm1_sphere)(double xi_, void *userdata);
+    void *userdata_sphere;
+    int ldim;
+    double epsrel;
+    detalg_t detalg;
+    /* private: arithmetic of the factorisation, see caps_gpu_set_precision */
+    int precision;
+} caps_t;
+
+/* Matrix object of one (xi, m) (src/include/libcaps.h:101-109).  The GPU
+ * builds the whole matrix at caps_M_init; caps_M_elem serves it. */
+typedef struct
+{
+    caps_t *caps;
+    int m, lmin, ldim;
+    void *integration;        /* unused; kept for layout */
+    void *integration_plasma; /* unused; kept for layout */
+    double xi_;
+    double *al, *bl;          /* log|a_l|, log|b_l| for l = lmin .. lmin+ldim-1 */
+    double *M;                /* private: dense M, row-major 2ldim x 2ldim */
+} caps_M_t;
+
+/* ---- reference API (src/include/libcaps.h:113-163) ---- */
+void caps_build(FILE *stream, const char *prefix);                 /* libcaps.h:113, libcaps.c:239 */
+void caps_info(caps_t *self, FILE *stream, const char *prefix);    /* libcaps.h:114, libcaps.c:273 */
+
+double caps_lnLambda(int l1, int l2, int m);                        /* libcaps.h:116, libcaps.c:45 */
+
+caps_t *caps_init(double R, double L);                              /* libcaps.h:118, libcaps.c:183 */
+void caps_free(caps_t *self);                                       /* libcaps.h:119, libcaps.c:224 */
+
+double caps_epsilonm1_plate(caps_t *self, double xi_);              /* libcaps.h:121, libcaps.c:104 */
+double caps_epsilonm1_sphere(caps_t *self, double xi_);             /* libcaps.h:122, libcaps.c:116 */
+
+void caps_set_epsilonm1(caps_t *self, double (*epsilonm1)(double xi_, void *userdata), void *userdata);        /* libcaps.h:124, libcaps.c:337 */
+void caps_set_epsilonm1_plate(caps_t *self, double (*epsilonm1)(double xi_, void *userdata), void *userdata);  /* libcaps.h:125, libcaps.c:358 */
+void caps_set_epsilonm1_sphere(caps_t *self, double (*epsilonm1)(double xi_, void *userdata), void *userdata); /* libcaps.h:126, libcaps.c:379 */
+
+int caps_get_ldim(caps_t *self);                                    /* libcaps.h:128, libcaps.c:454 */
+int caps_set_ldim(caps_t *self, int ldim);                          /* libcaps.h:129, libcaps.c:436 */
+
+detalg_t caps_get_detalg(caps_t *self);                             /* libcaps.h:131, libcaps.c:418 */
+int caps_set_detalg(caps_t *self, detalg_t detalg);                 /* libcaps.h:132, libcaps.c:400 */
+
+double caps_get_epsrel(caps_t *self);                               /* libcaps.h:134, libcaps.c:322 */
+int    caps_set_epsrel(caps_t *self, double epsrel);                /* libcaps.h:135, libcaps.c:306 */
+
+void caps_mie(caps_t *self, double xi_, int l, double *lna, double *lnb);       /* libcaps.h:137, libcaps.c:557 */
+void caps_mie_perf(caps_t *self, double xi_, int l, double *lna, double *lnb);  /* libcaps.h:138, libcaps.c:485 */
+
+double caps_kernel_M(int i, int j, void *args_);                    /* libcaps.h:140, libcaps.c:717 */
+
+caps_M_t *caps_M_init(caps_t *self, int m, double xi_);             /* libcaps.h:142, libcaps.c:673 */
+double caps_M_elem(caps_M_t *self, int l1, int l2, char p1, char p2); /* libcaps.h:143, libcaps.c:761 */
+void caps_M_free(caps_M_t *self);                                   /* libcaps.h:144, libcaps.c:840 */
+
+double caps_logdetD(caps_t *self, double xi_, int m);               /* libcaps.h:146, libcaps.c:950 */
+
+void caps_fresnel(caps_t *self, double xi_, double k, double *r_TE, double *r_TM); /* libcaps.h:148, libcaps.c:616 */
+
+int caps_estimate_lminmax(caps_t *self, int m, size_t *lmin_p, size_t *lmax_p);   /* libcaps.h:150, libcaps.c:63 */
+
+double caps_epsilonm1_perf(double xi_, void *userdata);             /* libcaps.h:152, libcaps.c:129 */
+double caps_epsilonm1_drude(double xi_, void *userdata);            /* libcaps.h:153, libcaps.c:150 */
+
+double caps_ht_drude(caps_t *caps);                                 /* libcaps.h:155, libcaps.c:1043 */
+double caps_ht_perf(caps_t *caps, double eps);                      /* libcaps.h:156, libcaps.c:1089 */
+double caps_ht_plasma(caps_t *caps, double omegap_, double eps);    /* libcaps.h:157, libcaps.c:1127 */
+
+double caps_kernel_M0_EE(int i, int j, void *args);                 /* libcaps.h:159, libcaps.c:860 */
+double caps_kernel_M0_MM(int i, int j, void *args);                 /* libcaps.h:160, libcaps.c:920 */
+double caps_kernel_M0_MM_plasma(int i, int j, void *args_);         /* libcaps.h:161, libcaps.c:882 */
+
+void caps_logdetD0(caps_t *self, int m, double omegap, double *EE, double *MM, double *MM_plasma); /* libcaps.h:163, libcaps.c:985 */
+
+/* ---- batch extensions (no reference counterpart; additive) ---- */
+
+/* status codes of a batch entry */
+#define CAPS_ST_TRACE     1   /* trace shortcut |tr M| < 1e-8 (matrix.c:78) */
+#define CAPS_ST_MERCATOR  2   /* Mercator shortcut (matrix.c:494-505) */
+#define CAPS_ST_FACTOR    3   /* full factorisation */
+#define CAPS_ST_ERR_PIVOT 16  /* non-positive pivot: result NaN */
+#define CAPS_ST_ERR_NONFINITE 32 /* non-finite integral or element: result NaN */
+#define CAPS_ST_ERR_GRID  64  /* quadrature grid exceeded its node budget: result NaN */
+
+/* log det(1-M) for n (xi_[i], m[i]) pairs of one geometry, all matrices
+ * assembled and factored as one GPU batch (replaces n calls of caps_logdetD,
+ * the per-task worker at src/caps.c:946).  status may be NULL.
+ * Returns the number of entries with an error status (0 on full success). */
+int caps_logdetD_batch(caps_t *self, const double *xi_, const int *m, int n, double *out, int *status);
+
+/* precision of the factorisation */
+#define CAPS_PREC_FP64  0  /* plain FP64 Cholesky */
+#define CAPS_PREC_MIXED 1  /* tensor-core factorisation + FP64 log-det correction */
+int caps_gpu_set_precision(caps_t *self, int precision);
+
+/* Free energy E (L+R)/(hbar c) at temperature T via the Matsubara sum with the
+ * reference's m cutoff and xi truncation (src/caps.c:307-396, 749-852).
+ * The xi = 0 term follows the reference's material rules.  info arrays may be
+ * NULL.  Returns E; nxi/ndet report the frequencies and determinants used. */
+typedef struct {
+    int nxi;          /* number of frequencies including xi = 0 */
+    int ndet;         /* number of (xi,m) determinants evaluated on the GPU */
+    int nwasted;      /* determinants computed beyond the cutoff (speculation) */
+    double seconds;   /* wall time */
+    double *xi;       /* optional [4096]: xi (L+R)/c per frequency */
+    double *logdetD;  /* optional [4096]: m-summed term per frequency */
+} caps_energy_info_t;
+double caps_free_energy(caps_t *self, double T, double cutoff, double epsrel, caps_energy_info_t *info);
+
+/* last error text of this thread's most recent GPU call ("" if none) */
+const char *caps_gpu_last_error(void);
+
+/* run subsequent GPU work on this CUDA stream (a cudaStream_t; NULL = library stream) */
+void caps_gpu_set_stream(void *stream);
+
+/* device time of the phases of the most recent batch, milliseconds:
+ * [0] setup+Mie, [1] K integrals, [2] I integrals, [3] elements+stats,
+ * [4] factorisation, [5] total; returns the number written */
+int caps_gpu_timings(double *ms, int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,41 @@
+"""The C-ABI library loads without a GPU and exports every symbol declared in
+include/libcaps.h.  No compute call is made here."""
+import ctypes as C
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "libcaps.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^[A-Za-z_][\w \*]*?\b(caps_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_parsed():
+    names = declared_functions()
+    assert "caps_logdetD" in names and "caps_logdetD_batch" in names and len(names) >= 38
+
+
+def test_library_exports_all():
+    import caps_gb300
+    lib = C.CDLL(caps_gb300.LIB_PATH)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_host_helpers_match_oracle():
+    import caps_gb300 as cg
+    from oracle import binding as ob
+    for l1, l2, m in [(1, 1, 0), (5, 9, 3), (300, 1200, 200), (2000, 2100, 1000)]:
+        assert abs(cg.lib.caps_lnLambda(l1, l2, m) - ob.lib.oracle_lnLambda(l1, l2, m)) < 1e-12
+    c = cg.Caps(150e-6, 1e-6, ldim=1050)
+    for m in (0, 1, 10, 68, 69, 200, 400):
+        assert c.lminmax(m)[0] == ob.lib.oracle_lmin(1e-6 / 150e-6, 1050, m)
+    assert c.ldim == 1050
+    d = cg.Caps(20e-6, 1e-6)
+    assert d.ldim == 101  # ceil(max(20, 5/(L/R))) in floating point, as the reference computes it
+    assert cg.lib.caps_init(-1.0, 1.0) is None
+    assert cg.lib.caps_set_ldim(d._h, 0) == 0
