@@ -52,6 +52,10 @@ def _load():
         "caps_gpu_last_error": (C.c_char_p, []),
         "caps_gpu_set_stream": (None, [vp]),
         "caps_gpu_timings": (i, [dp, i]),
+        "caps_gpu_reset_timings": (None, []),
+        "caps_gpu_counters": (None, [C.POINTER(C.c_longlong)] * 3 + [i]),
+        "caps_gpu_fp64_peak": (d, []),
+        "caps_gpu_work": (None, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -72,10 +76,31 @@ def set_stream(handle):
     lib.caps_gpu_set_stream(C.c_void_p(handle) if handle else None)
 
 
-def timings():
-    buf = (C.c_double * 6)()
-    lib.caps_gpu_timings(buf, 6)
-    return list(buf)
+def timings(cumulative=False):
+    """device milliseconds per phase: setup+Mie, K, I, elements+stats, factorisation, total"""
+    buf = (C.c_double * 12)()
+    lib.caps_gpu_timings(buf, 12)
+    return list(buf[6:12]) if cumulative else list(buf[:6])
+
+
+def reset_timings():
+    lib.caps_gpu_reset_timings()
+
+
+def counters(reset=False):
+    a, b, c = C.c_longlong(), C.c_longlong(), C.c_longlong()
+    lib.caps_gpu_counters(C.byref(a), C.byref(b), C.byref(c), int(reset))
+    return dict(launches=a.value, h2d=b.value, d2h=c.value)
+
+
+def work():
+    a, b, c = C.c_longlong(), C.c_longlong(), C.c_double()
+    lib.caps_gpu_work(C.byref(a), C.byref(b), C.byref(c))
+    return dict(nmat=a.value, nfactor=b.value, factor_flops=c.value)
+
+
+def fp64_peak():
+    return lib.caps_gpu_fp64_peak()
 
 
 class Caps:

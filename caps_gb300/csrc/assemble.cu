@@ -224,12 +224,12 @@ __global__ void k_kred(const Task *tasks, int ntask, const double *partM, const 
 // ---------------------------------------------------------------------------
 // I integrals: q-sum of K with the three-term a_q recurrence (integration.c:497)
 // ---------------------------------------------------------------------------
-CAPS_DEV double falpha(double p, double n, double nu)
-{
-    const double p2 = p * p;
-    return ((p2 - (n + nu + 1) * (n + nu + 1)) * (p2 - (n - nu) * (n - nu))) / (4 * p2 - 1);
-}
-
+// The recurrence coefficients of eqs. (26)-(28) are rewritten so that every
+// factor that depends on p alone comes from tables (per task: the integer
+// products K0..K3 of p, p1=p-2m, p2=p+2m; per batch: x^2 and 1/(4x^2-1)),
+// the common factor Ap cancels, and alpha(p+3), alpha(p+4) are carried over
+// from the previous step.  One division per step remains.  log n! comes from
+// a table covering every argument of the batch.
 struct QAcc {
     double s; int e; bool on; int count; double v0;
 };
@@ -254,8 +254,23 @@ CAPS_DEV void qacc_check(QAcc &A, double aq, int lscale2, sd Kv)
     else A.count = 0;
 }
 
-__global__ void k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lfac_tab,
-                       sd *I, int *status)
+// per task: K0..K3 of p for p in [0, pmax)
+__global__ void k_ptab(const Task *tasks, int ntask, double4 *ptab, int pstride)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int task = blockIdx.y;
+    if (p >= pstride || task >= ntask) return;
+    const double m = tasks[task].m > 0 ? tasks[task].m : 1;
+    const double pp = p, p1 = pp - 2 * m, p2 = pp + 2 * m;
+    ptab[(size_t)task * pstride + p] = make_double4((pp + 2) * (pp + 3) * ((p1 + 1) * (p1 + 2)),
+                                                    (pp + 1) * (pp + 3) * ((p1 + 2) * (p2 + 2)),
+                                                    (pp + 2) * (pp + 4) * ((p1 + 3) * (p2 + 3)),
+                                                    (pp + 2) * (pp + 3) * ((p2 + 3) * (p2 + 4)));
+}
+
+__global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride,
+                                              const double *__restrict__ lft, const double2 *__restrict__ xtab,
+                                              const double4 *__restrict__ ptab, int pstride, sd *I, int *status)
 {
     const int L = ldim + 2;
     const long long npair = (long long)L * (L + 1) / 2;
@@ -284,8 +299,8 @@ __global__ void k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int 
     const int l12 = l1 + l2;
     const int qmax = min(min(l1, l2), (l12 - 2 * mm) / 2);
     const double Ap = -2 * m * (n - nu) * (n + nu + 1);
-    const double log_a0 = lfac(lfac_tab, 2 * l1) - lfac(lfac_tab, l1) + lfac(lfac_tab, 2 * l2) - lfac(lfac_tab, l2) + lfac(lfac_tab, l12)
-                        - lfac(lfac_tab, 2 * l12) + lfac(lfac_tab, l12 - 2 * mm) - lfac(lfac_tab, l1 - mm) - lfac(lfac_tab, l2 - mm);
+    const double log_a0 = __ldg(lft + 2 * l1) - __ldg(lft + l1) + __ldg(lft + 2 * l2) - __ldg(lft + l2) + __ldg(lft + l12)
+                        - __ldg(lft + 2 * l12) + __ldg(lft + l12 - 2 * mm) - __ldg(lft + l1 - mm) - __ldg(lft + l2 - mm);
 
     const sd *KTM = K + (size_t)(task * 2 + 1) * nu_stride - T.mu; // indexed by nu
     const sd *KTE = K + (size_t)(task * 2 + 0) * nu_stride - T.mu;
@@ -318,26 +333,34 @@ __global__ void k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int 
         if (both) { const sd ke = KTE[l12 - 4]; qacc_add(aE, a2q * ke.m, ke.e); }
         aqm2 = aqm1; aqm1 = a2q;
     }
-    for (int q = 3; q <= qmax && (aT.on || aE.on); q++) {
-        const double p = n + nu - 2 * q, p1 = p - 2 * m, p2 = p + 2 * m;
-        double aq;
-        if (Ap != 0) {
-            const double c0 = (p + 2) * (p + 3) * (p1 + 1) * (p1 + 2) * Ap * falpha(p + 1, n, nu);
-            const double c1 = Ap * (Ap * Ap + (p + 1) * (p + 3) * (p1 + 2) * (p2 + 2) * falpha(p + 2, n, nu)
-                                         + (p + 2) * (p + 4) * (p1 + 3) * (p2 + 3) * falpha(p + 3, n, nu));
-            const double c2 = -(p + 2) * (p + 3) * (p2 + 3) * (p2 + 4) * Ap * falpha(p + 4, n, nu);
-            aq = (c1 * aqm1 + c2 * aqm2) / c0;
-        } else
-            aq = (p + 1) * (p2 + 2) * falpha(p + 2, n, nu) * aqm1 / ((p + 2) * (p1 + 1) * falpha(p + 1, n, nu));
-        // exact power-of-two rescaling of the recurrence (the reference rescales by |a_q| at 1e+-100)
-        if (aq != 0.0) {
-            const int k = expo(aq);
-            if (k > 300 || k < -300) { aq = shift2(aq, -k); aqm1 = shift2(aqm1, -k); lscale2 += k; }
+    if (qmax >= 3) {
+        // alpha(x) = ((x^2 - (n+nu+1)^2)(x^2 - (n-nu)^2)) / (4x^2 - 1)   (integration.c:492)
+        const double S2 = (n + nu + 1) * (n + nu + 1), D2 = (n - nu) * (n - nu), Ap2 = Ap * Ap;
+        auto alpha = [&](int x) { const double2 t = __ldg(xtab + x); return (t.x - S2) * (t.x - D2) * t.y; };
+        const double4 *pt = ptab + (size_t)task * pstride;
+        int ip = l12 - 6;                 // p of q = 3
+        double al3 = alpha(ip + 3), al4 = alpha(ip + 4);
+        for (int q = 3; q <= qmax && (aT.on || aE.on); q++, ip -= 2) {
+            const double al1 = alpha(ip + 1), al2 = alpha(ip + 2);
+            double aq;
+            if (Ap != 0) {
+                const double4 k = pt[ip];
+                // a_q = (c1 a_{q-1} + c2 a_{q-2}) / c0 with the common factor Ap divided out
+                aq = (fma(k.z, al3, fma(k.y, al2, Ap2)) * aqm1 - k.w * al4 * aqm2) / (k.x * al1);
+            } else {
+                const double p = ip, p1 = p - 2 * m, p2 = p + 2 * m;
+                aq = (p + 1) * (p2 + 2) * al2 * aqm1 / ((p + 2) * (p1 + 1) * al1); // eq. (30)
+            }
+            al3 = al1; al4 = al2;
+            // exact power-of-two rescaling of the recurrence (the reference rescales by |a_q| at 1e+-100)
+            if (aq != 0.0) {
+                const int kx = expo(aq);
+                if (kx > 300 || kx < -300) { aq = shift2(aq, -kx); aqm1 = shift2(aqm1, -kx); lscale2 += kx; }
+            }
+            if (aT.on) { const sd kt = KTM[ip]; qacc_add(aT, aq * kt.m, kt.e + lscale2); if (aq != 0.0) qacc_check(aT, aq, lscale2, kt); }
+            if (aE.on) { const sd ke = KTE[ip]; qacc_add(aE, aq * ke.m, ke.e + lscale2); if (aq != 0.0) qacc_check(aE, aq, lscale2, ke); }
+            aqm2 = aqm1; aqm1 = aq;
         }
-        const int nuq = l12 - 2 * q;
-        if (aT.on) { const sd kt = KTM[nuq]; qacc_add(aT, aq * kt.m, kt.e + lscale2); if (aq != 0.0) qacc_check(aT, aq, lscale2, kt); }
-        if (aE.on) { const sd ke = KTE[nuq]; qacc_add(aE, aq * ke.m, ke.e + lscale2); if (aq != 0.0) qacc_check(aE, aq, lscale2, ke); }
-        aqm2 = aqm1; aqm1 = aq;
     }
     const sd a0 = sd_from_log(log_a0, 1);
     const sd rT = sd_mul(a0, sd_norm(aT.s, aT.e));
@@ -347,6 +370,15 @@ __global__ void k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int 
     if (both) rE = sd_mul(a0, sd_norm(aE.s, aE.e));
     else rE = sd{-rT.m, rT.e};
     I_TE[o12] = rE; I_TE[o21] = rE;
+}
+
+// per batch: log n! for n < nlf (table below 1024, Stirling above) and
+// x^2, 1/(4x^2-1) for x < nx
+__global__ void k_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, int nx)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nlf) lft[i] = lfac(lfac_tab, i);
+    if (i < nx) { const double x = i; xtab[i] = make_double2(x * x, 1.0 / (4 * x * x - 1)); }
 }
 
 // ---------------------------------------------------------------------------
@@ -459,6 +491,7 @@ void launch_setup(Task *tasks, int ntask, double *edges, int max_panels, double2
                   int *status, cudaStream_t st)
 {
     k_setup<<<ntask, 256, 0, st>>>(tasks, ntask, edges, max_panels, coefAB, nu_stride, c_width, status);
+    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
@@ -466,6 +499,7 @@ void launch_mie(const double *xi, const double *epsm1, int nxi, double LbyR, int
 {
     dim3 g((lmax + 127) / 128, nxi);
     k_mie<<<g, 128, 0, st>>>(xi, epsm1, nxi, LbyR, lmax, lna, lnb);
+    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
@@ -474,6 +508,7 @@ void launch_scale(const Task *tasks, int ntask, int ldim, const double *lna, con
 {
     dim3 g((ldim + 2 + 127) / 128, ntask);
     k_scale<<<g, 128, 0, st>>>(tasks, ntask, ldim, lna, lnb, lmax, lfac_tab, Sa, Sb, uv);
+    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
@@ -492,6 +527,7 @@ void launch_ktab(bool pr, const Task *tasks, int ntask, int max_warps, const dou
     dim3 g((max_warps + KT_WARPS - 1) / KT_WARPS, ntask);
     if (pr) k_ktab<true><<<g, KT_WARPS * 32, sm, st>>>(tasks, edges, max_panels, coefAB, nu_stride, lfac_tab, partM, partE, max_warps);
     else k_ktab<false><<<g, KT_WARPS * 32, sm, st>>>(tasks, edges, max_panels, coefAB, nu_stride, lfac_tab, partM, partE, max_warps);
+    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
@@ -500,15 +536,28 @@ void launch_kred(const Task *tasks, int ntask, int max_nnu, const double *partM,
 {
     dim3 g((max_nnu + 127) / 128, ntask);
     k_kred<<<g, 128, 0, st>>>(tasks, ntask, partM, partE, max_warps, nu_stride, K, status);
+    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
-void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lfac_tab, sd *I, int *status,
-                 cudaStream_t st)
+void launch_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, int nx, cudaStream_t st)
 {
+    const int n = nlf > nx ? nlf : nx;
+    k_tables<<<(n + 255) / 256, 256, 0, st>>>(lfac_tab, lft, nlf, xtab, nx);
+    COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
+}
+
+void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
+                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st)
+{
+    dim3 gp((pstride + 127) / 128, ntask);
+    k_ptab<<<gp, 128, 0, st>>>(tasks, ntask, ptab, pstride);
+    COUNT_LAUNCH(1);
     const long long L = ldim + 2, npair = L * (L + 1) / 2;
     dim3 g((unsigned)((npair + 127) / 128), ntask);
-    k_itab<<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lfac_tab, I, status);
+    k_itab<<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status);
+    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
@@ -517,6 +566,7 @@ void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *
 {
     dim3 g((ldim + 127) / 128, ldim, ntask);
     k_elem<<<g, 128, 0, st>>>(tasks, ntask, ldim, I, Sa, Sb, uv, A, lda, mat_stride, status);
+    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
@@ -524,6 +574,7 @@ void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t l
                   double *result, int *status, cudaStream_t st)
 {
     k_stats<<<ntask, 256, 0, st>>>(tasks, ntask, n, A, lda, mat_stride, mode, trace, result, status);
+    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 

@@ -178,13 +178,16 @@ void launch_cholesky(int ntask, int n, double *A, size_t lda, size_t mstride, in
     }
     for (int k0 = 0; k0 < n; k0 += NB) {
         k_potf2<<<ntask, 256, 0, st>>>(ntask, n, k0, A, lda, mstride, status, logdiag);
+        COUNT_LAUNCH(1);
         const int rest = n - k0 - NB;
         if (rest <= 0) break;
         dim3 gt((rest + TRSM_T - 1) / TRSM_T, ntask);
         k_trsm<<<gt, TRSM_T, trsm_sm, st>>>(ntask, n, k0, A, lda, mstride, status);
+        COUNT_LAUNCH(1);
         const int nt = (rest + 63) / 64;
         dim3 gs(nt * (nt + 1) / 2, ntask);
         k_syrk<<<gs, 256, syrk_sm, st>>>(ntask, n, k0, A, lda, mstride, status);
+        COUNT_LAUNCH(1);
     }
     CK(cudaGetLastError());
 }
@@ -192,6 +195,7 @@ void launch_cholesky(int ntask, int n, double *A, size_t lda, size_t mstride, in
 void launch_final(int ntask, int n, const double *logdiag, const double *trace, int *status, double *result, int mode, cudaStream_t st)
 {
     k_final<<<(ntask + 127) / 128, 128, 0, st>>>(ntask, n, logdiag, trace, status, result, mode);
+    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 

@@ -10,6 +10,11 @@ namespace capsgpu {
 [[noreturn]] void fatal(const char *file, int line, const char *what);
 #define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) ::capsgpu::fatal(__FILE__, __LINE__, cudaGetErrorString(e_)); } while (0)
 
+// counters of kernel launches and host<->device bytes since the last reset
+struct Counters { long long launches = 0, h2d = 0, d2h = 0, nfactor = 0, nmat = 0; double factor_flops = 0; };
+extern Counters g_counters;
+#define COUNT_LAUNCH(n) (::capsgpu::g_counters.launches += (n))
+
 void upload_gauss_legendre(const double *x, const double *w);
 void launch_setup(Task *tasks, int ntask, double *edges, int max_panels, double2 *coefAB, int nu_stride, double c_width,
                   int *status, cudaStream_t st);
@@ -21,8 +26,9 @@ void launch_ktab(bool pr, const Task *tasks, int ntask, int max_warps, const dou
                  int nu_stride, const double *lfac_tab, double *partM, int *partE, cudaStream_t st);
 void launch_kred(const Task *tasks, int ntask, int max_nnu, const double *partM, const int *partE, int max_warps, int nu_stride,
                  sd *K, int *status, cudaStream_t st);
-void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lfac_tab, sd *I, int *status,
-                 cudaStream_t st);
+void launch_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, int nx, cudaStream_t st);
+void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
+                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st);
 void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv, double *A,
                  size_t lda, size_t mat_stride, int *status, cudaStream_t st);
 void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode, double *trace,

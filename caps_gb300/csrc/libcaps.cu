@@ -37,6 +37,7 @@ static void set_error(const char *fmt, ...)
 }
 
 namespace capsgpu {
+Counters g_counters;
 [[noreturn]] void fatal(const char *file, int line, const char *what)
 {
     fprintf(stderr, "libcaps_gb300: CUDA failure at %s:%d: %s\n", file, line, what);
@@ -96,9 +97,10 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
+    double timings_cum[6] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t ev[7];
     std::mutex mu;
     cudaStream_t stream() const { return user ? user : own; }
@@ -147,11 +149,70 @@ extern "C" void caps_gpu_set_stream(void *stream)
     g_eng.user = (cudaStream_t)stream;
 }
 
+extern "C" void caps_gpu_counters(long long *launches, long long *h2d_bytes, long long *d2h_bytes, int reset)
+{
+    if (launches) *launches = g_counters.launches;
+    if (h2d_bytes) *h2d_bytes = g_counters.h2d;
+    if (d2h_bytes) *d2h_bytes = g_counters.d2h;
+    if (reset) g_counters = Counters();
+}
+
+extern "C" void caps_gpu_work(long long *nmat, long long *nfactor, double *factor_flops)
+{
+    if (nmat) *nmat = g_counters.nmat;
+    if (nfactor) *nfactor = g_counters.nfactor;
+    if (factor_flops) *factor_flops = g_counters.factor_flops;
+}
+
+// sustained FP64 FMA throughput of this device (independent FMA chains on every SM)
+__global__ void k_fp64_probe(double *out, int iters, double a)
+{
+    double x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = threadIdx.x + k;
+    for (int i = 0; i < iters; i++)
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = fma(x[k], a, 1.0);
+    double s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += x[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+extern "C" double caps_gpu_fp64_peak(void)
+{
+    std::lock_guard<std::mutex> lk(g_eng.mu);
+    engine_init();
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_eng.device));
+    const int blocks = sms * 8, threads = 256, iters = 20000;
+    double *d;
+    CK(cudaMalloc(&d, (size_t)blocks * threads * sizeof(double)));
+    cudaStream_t st = g_eng.stream();
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+        CK(cudaEventRecord(g_eng.ev[0], st));
+        k_fp64_probe<<<blocks, threads, 0, st>>>(d, iters, 0.999);
+        CK(cudaEventRecord(g_eng.ev[1], st));
+        CK(cudaEventSynchronize(g_eng.ev[1]));
+        float ms;
+        CK(cudaEventElapsedTime(&ms, g_eng.ev[0], g_eng.ev[1]));
+        best = std::min(best, ms);
+    }
+    CK(cudaFree(d));
+    return 2.0 * 8 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+}
+
 extern "C" int caps_gpu_timings(double *ms, int n)
 {
-    int k = std::min(n, 6);
-    for (int i = 0; i < k; i++) ms[i] = g_eng.timings[i];
+    int k = std::min(n, 12);
+    for (int i = 0; i < k; i++) ms[i] = i < 6 ? g_eng.timings[i] : g_eng.timings_cum[i - 6];
     return k;
+}
+
+extern "C" void caps_gpu_reset_timings(void)
+{
+    for (int i = 0; i < 6; i++) g_eng.timings_cum[i] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -271,6 +332,17 @@ struct BatchOpts {
     double *mie_out_a = nullptr, *mie_out_b = nullptr; // Mie of task 0's window
 };
 
+static void h2d(void *dst, const void *src, size_t bytes, cudaStream_t st)
+{
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    g_counters.h2d += (long long)bytes;
+}
+static void d2h(void *dst, const void *src, size_t bytes, cudaStream_t st)
+{
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+    g_counters.d2h += (long long)bytes;
+}
+
 static const double KGRID_WIDTH = 2.0;
 static const int MAX_PANELS = 2048;
 
@@ -331,7 +403,8 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     CK(cudaMemGetInfo(&freeb, &totb));
     const size_t per_task = (size_t)dim * dim * 8 + (size_t)2 * L * L * sizeof(sd) + (size_t)2 * nu_stride * sizeof(sd)
                           + (size_t)nu_stride * sizeof(double2) + (size_t)3 * L * sizeof(sd) + (size_t)dim * 8
-                          + (size_t)2 * 256 * nu_stride * 12; // partial sums, up to 256 warps
+                          + (size_t)2 * 256 * nu_stride * 12  // partial sums, up to 256 warps
+                          + (size_t)(2 * (caps->ldim + 4096)) * sizeof(double4); // p table
     size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes));
     int chunk = (int)std::max<size_t>(1, std::min<size_t>(budget / per_task, 65535));
     chunk = std::min(chunk, n);
@@ -339,10 +412,18 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     // Mie table for all distinct xi at once
     double *d_xi = (double *)g_eng.xi.get(nxi * sizeof(double));
     double *d_eps = (double *)g_eng.eps.get(nxi * sizeof(double));
-    CK(cudaMemcpyAsync(d_xi, xis.data(), nxi * sizeof(double), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(d_eps, eps_sphere.data(), nxi * sizeof(double), cudaMemcpyHostToDevice, st));
+    h2d(d_xi, xis.data(), nxi * sizeof(double), st);
+    h2d(d_eps, eps_sphere.data(), nxi * sizeof(double), st);
     double *d_lna = (double *)g_eng.mie_a.get((size_t)nxi * (lmax_mie + 1) * sizeof(double));
     double *d_lnb = (double *)g_eng.mie_b.get((size_t)nxi * (lmax_mie + 1) * sizeof(double));
+
+    // batch tables: log n! over every argument of the I q-sums, x^2 and 1/(4x^2-1)
+    int lmax_all = 0;
+    for (auto &T : tasks) lmax_all = std::max(lmax_all, T.lmin + ldim + 2);
+    const int nlf = 4 * lmax_all + 8, nx = 2 * lmax_all + 8, pstride = 2 * lmax_all + 8;
+    double *d_lft = (double *)g_eng.lft.get((size_t)nlf * sizeof(double));
+    double2 *d_xtab = (double2 *)g_eng.xtab.get((size_t)nx * sizeof(double2));
+    launch_tables(g_eng.d_lfac, d_lft, nlf, d_xtab, nx, st);
 
     double tsum[6] = {0, 0, 0, 0, 0, 0};
     int nerr = 0;
@@ -351,7 +432,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         CK(cudaEventRecord(g_eng.ev[0], st));
         if (c0 == 0) launch_mie(d_xi, d_eps, nxi, caps->LbyR, lmax_mie, d_lna, d_lnb, st);
         Task *d_tasks = (Task *)g_eng.tasks.get(nt * sizeof(Task));
-        CK(cudaMemcpyAsync(d_tasks, tasks.data() + c0, nt * sizeof(Task), cudaMemcpyHostToDevice, st));
+        h2d(d_tasks, tasks.data() + c0, nt * sizeof(Task), st);
         int *d_status = (int *)g_eng.status.get(nt * sizeof(int));
         CK(cudaMemsetAsync(d_status, 0, nt * sizeof(int), st));
         double *d_edges = (double *)g_eng.edges.get((size_t)nt * (MAX_PANELS + 1) * sizeof(double));
@@ -359,7 +440,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         launch_setup(d_tasks, nt, d_edges, MAX_PANELS, d_coef, nu_stride, KGRID_WIDTH, d_status, st);
         // panel counts decide the size of the partial-sum buffers
         std::vector<Task> tback(nt);
-        CK(cudaMemcpyAsync(tback.data(), d_tasks, nt * sizeof(Task), cudaMemcpyDeviceToHost, st));
+        d2h(tback.data(), d_tasks, nt * sizeof(Task), st);
         CK(cudaStreamSynchronize(st));
         int max_warps = 1;
         for (auto &T : tback) max_warps = std::max(max_warps, (T.npanel + 1) / 2);
@@ -377,7 +458,8 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         CK(cudaEventRecord(g_eng.ev[2], st));
 
         sd *d_I = (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
-        launch_itab(d_tasks, nt, ldim, d_K, nu_stride, g_eng.d_lfac, d_I, d_status, st);
+        double4 *d_ptab = (double4 *)g_eng.ptab.get((size_t)nt * pstride * sizeof(double4));
+        launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st);
         CK(cudaEventRecord(g_eng.ev[3], st));
 
         const size_t lda = dim, mstride = (size_t)dim * dim;
@@ -396,12 +478,12 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         CK(cudaEventRecord(g_eng.ev[5], st));
 
         std::vector<int> hst(nt);
-        CK(cudaMemcpyAsync(hst.data(), d_status, nt * sizeof(int), cudaMemcpyDeviceToHost, st));
-        if (O.factor) CK(cudaMemcpyAsync(out + c0, d_res, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
+        d2h(hst.data(), d_status, nt * sizeof(int), st);
+        if (O.factor) d2h(out + c0, d_res, nt * sizeof(double), st);
         if (O.M_out) {
             // dense row-major M from the lower triangle of 1-M
             std::vector<double> Ah((size_t)dim * dim);
-            CK(cudaMemcpyAsync(Ah.data(), d_A, (size_t)dim * dim * sizeof(double), cudaMemcpyDeviceToHost, st));
+            d2h(Ah.data(), d_A, (size_t)dim * dim * sizeof(double), st);
             CK(cudaStreamSynchronize(st));
             for (int j = 0; j < dim; j++)
                 for (int i = j; i < dim; i++) {
@@ -412,14 +494,16 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         }
         if (O.mie_out_a) {
             const Task &T = tasks[0];
-            CK(cudaMemcpyAsync(O.mie_out_a, d_lna + (size_t)T.xi_index * (lmax_mie + 1) + T.lmin, ldim * sizeof(double), cudaMemcpyDeviceToHost, st));
-            CK(cudaMemcpyAsync(O.mie_out_b, d_lnb + (size_t)T.xi_index * (lmax_mie + 1) + T.lmin, ldim * sizeof(double), cudaMemcpyDeviceToHost, st));
+            d2h(O.mie_out_a, d_lna + (size_t)T.xi_index * (lmax_mie + 1) + T.lmin, ldim * sizeof(double), st);
+            d2h(O.mie_out_b, d_lnb + (size_t)T.xi_index * (lmax_mie + 1) + T.lmin, ldim * sizeof(double), st);
         }
         CK(cudaStreamSynchronize(st));
         float f;
         for (int k = 0; k < 5; k++) { CK(cudaEventElapsedTime(&f, g_eng.ev[k], g_eng.ev[k + 1])); tsum[k] += f; }
         CK(cudaEventElapsedTime(&f, g_eng.ev[0], g_eng.ev[5])); tsum[5] += f;
+        g_counters.nmat += nt;
         for (int i = 0; i < nt; i++) {
+            if (hst[i] == ST_FACTOR) { g_counters.nfactor++; g_counters.factor_flops += (double)dim * dim * dim / 3.0; }
             if (status_out) status_out[c0 + i] = hst[i];
             if (hst[i] & ~0xF) {
                 nerr++;
@@ -427,7 +511,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             }
         }
     }
-    for (int k = 0; k < 6; k++) g_eng.timings[k] = tsum[k];
+    for (int k = 0; k < 6; k++) { g_eng.timings[k] = tsum[k]; g_eng.timings_cum[k] += tsum[k]; }
     return nerr;
 }
 
@@ -461,13 +545,13 @@ static void mie_device(caps_t *self, double xi_, int l, double epsm1, double *ln
     const cudaStream_t st = g_eng.stream();
     double *d_xi = (double *)g_eng.xi.get(sizeof(double));
     double *d_eps = (double *)g_eng.eps.get(sizeof(double));
-    CK(cudaMemcpyAsync(d_xi, &xi_, sizeof(double), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(d_eps, &epsm1, sizeof(double), cudaMemcpyHostToDevice, st));
+    h2d(d_xi, &xi_, sizeof(double), st);
+    h2d(d_eps, &epsm1, sizeof(double), st);
     double *d_a = (double *)g_eng.mie_a.get((size_t)(l + 1) * sizeof(double));
     double *d_b = (double *)g_eng.mie_b.get((size_t)(l + 1) * sizeof(double));
     launch_mie(d_xi, d_eps, 1, self->LbyR, l, d_a, d_b, st);
-    CK(cudaMemcpyAsync(lna, d_a + l, sizeof(double), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(lnb, d_b + l, sizeof(double), cudaMemcpyDeviceToHost, st));
+    d2h(lna, d_a + l, sizeof(double), st);
+    d2h(lnb, d_b + l, sizeof(double), st);
     CK(cudaStreamSynchronize(st));
 }
 

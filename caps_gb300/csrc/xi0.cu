@@ -69,6 +69,7 @@ int logdetD0_batch(caps_t *self, const int *ms, int n, int which, double *out)
     CK(cudaMemset(d_status, 0, n * sizeof(int)));
     dim3 g((ldim + 127) / 128, ldim, n);
     k_elem0<<<g, 128, 0, st>>>(d_m, d_lmin, n, ldim, self->y, which, d_lfac, d_A, mstride, d_status);
+    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
     const int mode = self->detalg == DETALG_HODLR ? 1 : 0;
     launch_stats(nullptr, n, ldim, d_A, ldim, mstride, mode, d_tr, d_res, d_status, st);

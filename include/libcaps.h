@@ -170,10 +170,23 @@ const char *caps_gpu_last_error(void);
 /* run subsequent GPU work on this CUDA stream (a cudaStream_t; NULL = library stream) */
 void caps_gpu_set_stream(void *stream);
 
-/* device time of the phases of the most recent batch, milliseconds:
- * [0] setup+Mie, [1] K integrals, [2] I integrals, [3] elements+stats,
- * [4] factorisation, [5] total; returns the number written */
+/* device time of the phases, milliseconds, measured with CUDA events on the
+ * library's stream: [0] setup+Mie, [1] K integrals, [2] I integrals,
+ * [3] elements+stats, [4] factorisation, [5] total of the most recent batch;
+ * [6..11] the same phases summed since caps_gpu_reset_timings(); returns the
+ * number written (at most 12) */
 int caps_gpu_timings(double *ms, int n);
+void caps_gpu_reset_timings(void);
+
+/* kernel launches and host<->device bytes since the last reset */
+void caps_gpu_counters(long long *launches, long long *h2d_bytes, long long *d2h_bytes, int reset);
+
+/* matrices assembled, matrices factored and the algorithmic flops of those
+ * factorisations (n^3/3 each) since the last counter reset */
+void caps_gpu_work(long long *nmat, long long *nfactor, double *factor_flops);
+
+/* measured FP64 FMA throughput of the current device, TFLOP/s (a short probe kernel) */
+double caps_gpu_fp64_peak(void);
 
 #ifdef __cplusplus
 }

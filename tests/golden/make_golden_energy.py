@@ -1,0 +1,127 @@
+"""Golden free energies from the unmodified reference library (oracle/_ref).
+
+Restates the serial master loop of the caps driver (src/caps.c:307-396 F_xi,
+:749-852 Matsubara sum) in Python around caps_logdetD of libcaps_ref.so, with
+the m loop farmed out to a process pool (results are summed in m order, so the
+value does not depend on the pool size).  Writes tests/golden/energy_<name>.json.
+
+    python tests/golden/make_golden_energy.py c3      # Drude, R/L=150 (~30 CPU-min)
+    python tests/golden/make_golden_energy.py small   # PR and Drude, R/L=10
+"""
+import ctypes as C
+import json
+import math
+import multiprocessing as mp
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = os.path.join(ROOT, "oracle", "_ref", "libcaps_ref.so")
+HBAR, HBAR_EV, KB, CL = 1.0545718e-34, 6.582119514e-16, 1.38064852e-23, 299792458.0
+_lib = None
+
+
+def _init():
+    global _lib
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    _lib = C.CDLL(REF)
+    _lib.caps_init.restype = C.c_void_p
+    _lib.caps_init.argtypes = [C.c_double, C.c_double]
+    _lib.caps_logdetD.restype = C.c_double
+    _lib.caps_logdetD.argtypes = [C.c_void_p, C.c_double, C.c_int]
+    _lib.caps_set_ldim.argtypes = [C.c_void_p, C.c_int]
+    _lib.caps_set_detalg.argtypes = [C.c_void_p, C.c_int]
+    _lib.caps_set_epsilonm1.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    _lib.caps_free.argtypes = [C.c_void_p]
+    _lib.caps_ht_drude.restype = C.c_double
+    _lib.caps_ht_drude.argtypes = [C.c_void_p]
+    _lib.caps_logdetD0.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+
+
+def _task(args):
+    R, L, ldim, drude, xi, m, detalg = args
+    c = _lib.caps_init(R, L)
+    _lib.caps_set_ldim(c, ldim)
+    _lib.caps_set_detalg(c, detalg)
+    ud = None
+    if drude:
+        ud = (C.c_double * 2)(drude[0] / HBAR_EV, drude[1] / HBAR_EV)
+        _lib.caps_set_epsilonm1(c, C.cast(_lib.caps_epsilonm1_drude, C.c_void_p), C.cast(ud, C.c_void_p))
+    if xi == 0:
+        v = C.c_double()
+        _lib.caps_logdetD0(c, m, 0.0, None, C.byref(v), None)
+        r = v.value
+    else:
+        r = _lib.caps_logdetD(c, xi, m)
+    _lib.caps_free(c)
+    return r
+
+
+def kahan(v):
+    s = c = 0.0
+    for x in v:
+        y = x - c
+        t = s + y
+        c = (t - s) - y
+        s = t
+    return s
+
+
+def F_xi(pool, R, L, ldim, drude, xi, cutoff, detalg, chunk):
+    terms, m0 = [], 0
+    while True:
+        vals = pool.map(_task, [(R, L, ldim, drude, xi, m, detalg) for m in range(m0, m0 + chunk)])
+        for v in vals:
+            terms.append(v)
+            if v == 0 or v / terms[0] < cutoff:
+                t = terms[:]
+                t[0] /= 2
+                return kahan(t), len(terms), len(terms) + (len(vals) - 1 - vals.index(v)) * 0
+        m0 += chunk
+
+
+def energy(R, L, ldim, T, drude, cutoff=1e-9, epsrel=1e-6, detalg=1, procs=8):
+    Ts = 2 * math.pi * KB * (R + L) * T / (HBAR * CL)
+    _init()
+    with mp.Pool(procs, initializer=_init) as pool:
+        c = _lib.caps_init(R, L)
+        _lib.caps_set_ldim(c, ldim)
+        if drude:
+            v0 = _lib.caps_ht_drude(c)
+        else:
+            drude_ht = _lib.caps_ht_drude(c)
+            s, _, _ = F_xi(pool, R, L, ldim, None, 0.0, cutoff, detalg, procs)
+            v0 = drude_ht + s
+        v, xis, ndet = [v0], [0.0], 0
+        n = 1
+        while True:
+            s, nm, _ = F_xi(pool, R, L, ldim, drude, n * Ts, cutoff, detalg, procs)
+            ndet += nm
+            v.append(s)
+            xis.append(n * Ts)
+            print("n=%d xi=%.16g v=%.16g m=%d" % (n, n * Ts, s, nm), file=sys.stderr, flush=True)
+            if abs(s / v[0]) < epsrel:
+                break
+            n += 1
+    w = v[:]
+    w[0] /= 2
+    return Ts / math.pi * kahan(w), dict(xi=xis, logdetD=v, ndet=ndet)
+
+
+if __name__ == "__main__":
+    which = sys.argv[1] if len(sys.argv) > 1 else "small"
+    procs = int(os.environ.get("PROCS", "8"))
+    cases = {
+        "small": [("pr_RbyL10_ldim70_T300", 10e-6, 1e-6, 70, 300.0, None), ("drude_RbyL10_ldim70_T300", 10e-6, 1e-6, 70, 300.0, (9.0, 0.035))],
+        "c2": [("pr_RbyL50_ldim350_T300", 50e-6, 1e-6, 350, 300.0, None)],
+        "c3": [("drude_RbyL150_ldim1050_T300", 150e-6, 1e-6, 1050, 300.0, (9.0, 0.035))],
+    }[which]
+    for name, R, L, ldim, T, drude in cases:
+        t = time.time()
+        E, info = energy(R, L, ldim, T, drude, procs=procs)
+        info.update(R=R, L=L, ldim=ldim, T=T, drude=drude, E=E, cutoff=1e-9, epsrel=1e-6, detalg="LU",
+                    seconds=time.time() - t, procs=procs, source="oracle/_ref/libcaps_ref.so via tests/golden/make_golden_energy.py")
+        json.dump(info, open(os.path.join(HERE, "energy_%s.json" % name), "w"), indent=1)
+        print(name, E, info["ndet"], time.time() - t, file=sys.stderr)
