@@ -334,32 +334,83 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
         aqm2 = aqm1; aqm1 = a2q;
     }
     if (qmax >= 3) {
-        // alpha(x) = ((x^2 - (n+nu+1)^2)(x^2 - (n-nu)^2)) / (4x^2 - 1)   (integration.c:492)
+        // Division-free form of the recurrence: a_q = b_q / D_q with
+        //   b_q = X_q b_{q-1} - Y_q Z_{q-1} b_{q-2},  D_q = D_{q-1} Z_q,
+        //   X_q = Ap^2 + K1 alpha(p+2) + K2 alpha(p+3), Y_q = K3 alpha(p+4), Z_q = K0 alpha(p+1)
+        // (eqs. (26)-(28) with the common factor Ap divided out), and the partial
+        // sums carried as S_q = D_q sum_{j<=q} a_j K_j = Z_q S_{q-1} + b_q K_q.
+        // b, D and each S keep their own power-of-two exponent; the reference's
+        // early stop (term 60 e-folds below the q=0 term, three times in a row)
+        // is decided on those exponents, with logarithms only inside the +-2
+        // binade band around the threshold.  One division per pair remains.
         const double S2 = (n + nu + 1) * (n + nu + 1), D2 = (n - nu) * (n - nu), Ap2 = Ap * Ap;
         auto alpha = [&](int x) { const double2 t = __ldg(xtab + x); return (t.x - S2) * (t.x - D2) * t.y; };
         const double4 *pt = ptab + (size_t)task * pstride;
-        int ip = l12 - 6;                 // p of q = 3
+        struct PS { double S; int eS; bool on; int count; double D; int eD; int e0; double v0; };
+        PS P[2] = {{aT.s, aT.e, true, 0, 1.0, 0, 0, aT.v0}, {aE.s, aE.e, both, 0, 1.0, 0, 0, aE.v0}};
+        P[0].e0 = KTM[l12].e;
+        if (both) P[1].e0 = KTE[l12].e;
+        const sd *Kp[2] = {KTM, KTE};
+        double bm2 = aqm2, bm1 = aqm1, Dq = 1.0, Zprev = 1.0;
+        int eb = 0, eD = 0;
+        int ip = l12 - 6; // p of q = 3
         double al3 = alpha(ip + 3), al4 = alpha(ip + 4);
-        for (int q = 3; q <= qmax && (aT.on || aE.on); q++, ip -= 2) {
+        for (int q = 3; q <= qmax && (P[0].on || P[1].on); q++, ip -= 2) {
             const double al1 = alpha(ip + 1), al2 = alpha(ip + 2);
-            double aq;
+            double X, Y, Z;
             if (Ap != 0) {
                 const double4 k = pt[ip];
-                // a_q = (c1 a_{q-1} + c2 a_{q-2}) / c0 with the common factor Ap divided out
-                aq = (fma(k.z, al3, fma(k.y, al2, Ap2)) * aqm1 - k.w * al4 * aqm2) / (k.x * al1);
-            } else {
+                X = fma(k.z, al3, fma(k.y, al2, Ap2));
+                Y = k.w * al4;
+                Z = k.x * al1;
+            } else { // eq. (30): two-term recurrence for l1 = l2
                 const double p = ip, p1 = p - 2 * m, p2 = p + 2 * m;
-                aq = (p + 1) * (p2 + 2) * al2 * aqm1 / ((p + 2) * (p1 + 1) * al1); // eq. (30)
+                X = (p + 1) * (p2 + 2) * al2;
+                Y = 0.0;
+                Z = (p + 2) * (p1 + 1) * al1;
             }
-            al3 = al1; al4 = al2;
-            // exact power-of-two rescaling of the recurrence (the reference rescales by |a_q| at 1e+-100)
-            if (aq != 0.0) {
-                const int kx = expo(aq);
-                if (kx > 300 || kx < -300) { aq = shift2(aq, -kx); aqm1 = shift2(aqm1, -kx); lscale2 += kx; }
+            const double b = fma(X, bm1, -(Y * Zprev) * bm2);
+            Dq *= Z;
+            al3 = al1; al4 = al2; Zprev = Z;
+            bm2 = bm1; bm1 = b;
+            {   // exact rescaling of b (with b_{q-1}) and D
+                const int kb = expo(b);
+                if (b != 0.0 && (kb > 300 || kb < -300)) { bm1 = shift2(bm1, -kb); bm2 = shift2(bm2, -kb); eb += kb; }
+                const int kd = expo(Dq);
+                if (kd > 300 || kd < -300) { Dq = shift2(Dq, -kd); eD += kd; }
             }
-            if (aT.on) { const sd kt = KTM[ip]; qacc_add(aT, aq * kt.m, kt.e + lscale2); if (aq != 0.0) qacc_check(aT, aq, lscale2, kt); }
-            if (aE.on) { const sd ke = KTE[ip]; qacc_add(aE, aq * ke.m, ke.e + lscale2); if (aq != 0.0) qacc_check(aE, aq, lscale2, ke); }
-            aqm2 = aqm1; aqm1 = aq;
+            const int eDq = expo(Dq) + eD;
+#pragma unroll
+            for (int pi = 0; pi < 2; pi++) {
+                PS &A = P[pi];
+                if (!A.on) continue;
+                const sd Kv = Kp[pi][ip];
+                const double t = bm1 * Kv.m;          // term * D_q / 2^(eb+Ke)
+                const int et = eb + Kv.e;
+                // S_q = Z S_{q-1} + t 2^(et - eS)
+                int d = et - A.eS;
+                if (A.S == 0.0) { A.eS = et; d = 0; }
+                if (d > 64) { A.S = shift2(A.S, -d); A.eS = et; d = 0; }
+                A.S = fma(Z, A.S, d > -1000 ? shift2(t, d) : 0.0);
+                const int ks = expo(A.S);
+                if (A.S != 0.0 && (ks > 300 || ks < -300)) { A.S = shift2(A.S, -ks); A.eS += ks; }
+                // early stop on |a_q K_q| / |K_0| < e^-60, i.e. log2 ratio < -86.5617
+                if (bm1 != 0.0) {
+                    const int approx = expo(bm1) + eb + Kv.e - eDq - A.e0; // true log2 ratio in (approx-2, approx+2)
+                    bool below;
+                    if (approx <= -89) below = true;
+                    else if (approx >= -84) below = false;
+                    else below = log(fabs(bm1)) + eb * LN2 + log(fabs(Kv.m)) + Kv.e * LN2 - log(fabs(Dq)) - eD * LN2 - A.v0 < -60.0;
+                    if (below) { if (++A.count >= 3) { A.on = false; A.D = Dq; A.eD = eD; } }
+                    else A.count = 0;
+                }
+            }
+        }
+        for (int pi = 0; pi < 2; pi++) {
+            PS &A = P[pi];
+            if (A.on) { A.D = Dq; A.eD = eD; }
+            const sd r = sd_norm(A.S / A.D, A.eS - A.eD);
+            if (pi == 0) { aT.s = r.m; aT.e = r.e; } else { aE.s = r.m; aE.e = r.e; }
         }
     }
     const sd a0 = sd_from_log(log_a0, 1);

@@ -776,7 +776,11 @@ extern "C" double caps_free_energy(caps_t *self, double T, double cutoff, double
         for (int i = 0; i < nlim; i++) {
             MState &s = st[i];
             if (s.done()) continue;
-            const int w = m_chunk(s, cutoff);
+            int w = m_chunk(s, cutoff);
+            // the m cutoff falls with the frequency: a known cutoff of a lower frequency bounds the first chunk
+            if (s.next == 0)
+                for (int j = i - 1; j >= 0; j--)
+                    if (st[j].done()) { w = std::min(w, st[j].mstop + 4); break; }
             for (int k = 0; k < w; k++) { bx.push_back((i + 1) * Ts); bm.push_back(s.next + k); who.push_back({i, s.next + k}); }
             s.next += w;
             s.v.resize(s.next, NAN);
@@ -802,7 +806,26 @@ extern "C" double caps_free_energy(caps_t *self, double T, double cutoff, double
                 const double v = kahan_sum(t.data(), t.size());
                 if (fabs(v / v0) < epsrel) { nmax_known = i + 1; grow = false; break; }
             }
-            if (grow && nmax_known < 0) { nactive *= 2; st.resize(nactive); }
+            if (grow && nmax_known < 0) {
+                // extrapolate |v_n/v_0| log-linearly from the last two complete frequencies
+                int grow_to = nactive + 4;
+                const int k = (int)st.size();
+                if (k >= 2 && st[k - 1].done() && st[k - 2].done()) {
+                    auto vsum = [&](const MState &s) {
+                        std::vector<double> t(s.v.begin(), s.v.begin() + s.mstop + 1);
+                        t[0] /= 2;
+                        return fabs(kahan_sum(t.data(), t.size()));
+                    };
+                    const double a = vsum(st[k - 2]), b = vsum(st[k - 1]);
+                    if (a > 0 && b > 0 && b < a) {
+                        const double rate = log(a / b);
+                        const double need = log(b / (epsrel * fabs(v0))) / rate;
+                        grow_to = k + std::max(1, (int)ceil(need));
+                    }
+                }
+                nactive = std::min(std::max(grow_to, nactive + 1), 2 * nactive);
+                st.resize(nactive);
+            }
         }
         if (nmax_known > 0) {
             bool all = true;
