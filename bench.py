@@ -177,7 +177,20 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--cpu-sample", type=int, default=0, help="matrices in the CPU-baseline sample (0: 2 per host thread)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="profiling case: one batch of 8 matrices of the workload (n in {1,5}, m in {0,20,40,60})")
     args = ap.parse_args()
+    if args.ncu_case:
+        import caps_gb300 as cg
+        Ts = 2 * math.pi * 1.38064852e-23 * (R + L) * T / (1.0545718e-34 * 299792458.0)
+        caps = cg.Caps(R, L, ldim=LDIM)
+        caps.set_drude(OMEGAP_EV, GAMMA_EV)
+        caps.set_precision(cg.PREC_MIXED if args.precision == "mixed" else cg.PREC_FP64)
+        xi = [n * Ts for n in (1, 5) for m in (0, 20, 40, 60)]
+        ms = [m for n in (1, 5) for m in (0, 20, 40, 60)]
+        out, st = caps.logdetD_batch(xi, ms)
+        print(json.dumps({"logdetD": list(out), "status": [int(s) for s in st], "phases_ms": cg.timings()}))
+        return
 
     rank, local_rank, world = rank_env()
     dist = None

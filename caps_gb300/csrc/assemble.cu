@@ -231,7 +231,7 @@ __global__ void k_kred(const Task *tasks, int ntask, const double *partM, const 
 // from the previous step.  One division per step remains.  log n! comes from
 // a table covering every argument of the batch.
 struct QAcc {
-    double s; int e; bool on; int count; double v0;
+    double s; int e; bool on; int count;
 };
 
 CAPS_DEV void qacc_add(QAcc &A, double mant, int ex)
@@ -243,18 +243,12 @@ CAPS_DEV void qacc_add(QAcc &A, double mant, int ex)
     if (d > -1000) A.s += shift2(mant, d);
 }
 
-// the early stop of the reference: three consecutive terms 60 e-folds below the q=0 term
-CAPS_DEV void qacc_check(QAcc &A, double aq, int lscale2, sd Kv)
-{
-    const double approx = (double)(expo(aq) + lscale2 + Kv.e) * LN2; // within 2 ln2 of the log
-    double v = approx;
-    if (fabs(approx - A.v0 + 60.0) < 3.0)
-        v = log(fabs(aq)) + lscale2 * LN2 + log(fabs(Kv.m)) + Kv.e * LN2;
-    if (v - A.v0 < -60.0) { if (++A.count >= 3) A.on = false; }
-    else A.count = 0;
-}
-
-// per task: K0..K3 of p for p in [0, pmax)
+// per task, for p in [0, pstride): the p-dependent factors of the recurrence with the
+// alpha denominators 1/(4x^2-1) folded in.  Table 0 (l1 != l2, eqs. (26)-(27)):
+//   {K0/(4(p+1)^2-1), K1/(4(p+2)^2-1), K2/(4(p+3)^2-1), K3/(4(p+4)^2-1)},
+//   K0=(p+2)(p+3)(p1+1)(p1+2), K1=(p+1)(p+3)(p1+2)(p2+2), K2=(p+2)(p+4)(p1+3)(p2+3), K3=(p+2)(p+3)(p2+3)(p2+4);
+// table 1 (l1 == l2, eq. (30)): {(p+2)(p1+1)/(4(p+1)^2-1), (p+1)(p2+2)/(4(p+2)^2-1), 0, 0};
+// p1 = p-2m, p2 = p+2m.
 __global__ void k_ptab(const Task *tasks, int ntask, double4 *ptab, int pstride)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -262,10 +256,14 @@ __global__ void k_ptab(const Task *tasks, int ntask, double4 *ptab, int pstride)
     if (p >= pstride || task >= ntask) return;
     const double m = tasks[task].m > 0 ? tasks[task].m : 1;
     const double pp = p, p1 = pp - 2 * m, p2 = pp + 2 * m;
-    ptab[(size_t)task * pstride + p] = make_double4((pp + 2) * (pp + 3) * ((p1 + 1) * (p1 + 2)),
-                                                    (pp + 1) * (pp + 3) * ((p1 + 2) * (p2 + 2)),
-                                                    (pp + 2) * (pp + 4) * ((p1 + 3) * (p2 + 3)),
-                                                    (pp + 2) * (pp + 3) * ((p2 + 3) * (p2 + 4)));
+    auto invD = [](double x) { return 1.0 / (4 * x * x - 1); };
+    ptab[((size_t)task * 2 + 0) * pstride + p] =
+        make_double4((pp + 2) * (pp + 3) * ((p1 + 1) * (p1 + 2)) * invD(pp + 1),
+                     (pp + 1) * (pp + 3) * ((p1 + 2) * (p2 + 2)) * invD(pp + 2),
+                     (pp + 2) * (pp + 4) * ((p1 + 3) * (p2 + 3)) * invD(pp + 3),
+                     (pp + 2) * (pp + 3) * ((p2 + 3) * (p2 + 4)) * invD(pp + 4));
+    ptab[((size_t)task * 2 + 1) * pstride + p] =
+        make_double4((pp + 2) * (p1 + 1) * invD(pp + 1), (pp + 1) * (p2 + 2) * invD(pp + 2), 0.0, 0.0);
 }
 
 __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride,
@@ -309,9 +307,9 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
     QAcc aT, aE;
     {
         const sd k0 = KTM[l12];
-        aT = QAcc{k0.m, k0.e, true, 0, log(fabs(k0.m)) + k0.e * LN2};
-        if (both) { const sd e0 = KTE[l12]; aE = QAcc{e0.m, e0.e, true, 0, log(fabs(e0.m)) + e0.e * LN2}; }
-        else aE = QAcc{0, 0, false, 0, 0};
+        aT = QAcc{k0.m, k0.e, true, 0};
+        if (both) { const sd e0 = KTE[l12]; aE = QAcc{e0.m, e0.e, true, 0}; }
+        else aE = QAcc{0, 0, false, 0};
     }
     double aqm2 = 0, aqm1 = 1; // a_{q-2}, a_{q-1}
     int lscale2 = 0;
@@ -343,42 +341,43 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
         // early stop (term 60 e-folds below the q=0 term, three times in a row)
         // is decided on those exponents, with logarithms only inside the +-2
         // binade band around the threshold.  One division per pair remains.
-        const double S2 = (n + nu + 1) * (n + nu + 1), D2 = (n - nu) * (n - nu), Ap2 = Ap * Ap;
-        auto alpha = [&](int x) { const double2 t = __ldg(xtab + x); return (t.x - S2) * (t.x - D2) * t.y; };
-        const double4 *pt = ptab + (size_t)task * pstride;
-        struct PS { double S; int eS; bool on; int count; double D; int eD; int e0; double v0; };
-        PS P[2] = {{aT.s, aT.e, true, 0, 1.0, 0, 0, aT.v0}, {aE.s, aE.e, both, 0, 1.0, 0, 0, aE.v0}};
+        // alpha(x) = N(x)/(4x^2-1) with the integer numerator
+        // N(x) = (x-S)(x+S)(x-Dd)(x+Dd), S = l1+l2+1, Dd = l1-l2, formed exactly in int64
+        // (|N| < 2^62 for every degree this library accepts) and converted once.
+        const long long Si = l1 + l2 + 1, Di = l1 - l2;
+        auto Nf = [&](int x) -> double {
+            const long long a = (long long)(x - Si) * (x + Si), c = (long long)(x - Di) * (x + Di);
+            return (double)(a * c);
+        };
+        const bool diag = (l1 == l2); // Ap == 0: eq. (30)
+        const double Ap2 = diag ? 0.0 : Ap * Ap;
+        const double4 *pt = ptab + ((size_t)task * 2 + (diag ? 1 : 0)) * pstride;
+        struct PS { double S; int eS; bool on; int count; double D; int eD; int e0; const sd *K0; };
+        PS P[2] = {{aT.s, aT.e, true, 0, 1.0, 0, 0, KTM + l12}, {aE.s, aE.e, both, 0, 1.0, 0, 0, KTE + l12}};
         P[0].e0 = KTM[l12].e;
         if (both) P[1].e0 = KTE[l12].e;
         const sd *Kp[2] = {KTM, KTE};
         double bm2 = aqm2, bm1 = aqm1, Dq = 1.0, Zprev = 1.0;
         int eb = 0, eD = 0;
         int ip = l12 - 6; // p of q = 3
-        double al3 = alpha(ip + 3), al4 = alpha(ip + 4);
+        double N3 = Nf(ip + 3), N4 = Nf(ip + 4);
         for (int q = 3; q <= qmax && (P[0].on || P[1].on); q++, ip -= 2) {
-            const double al1 = alpha(ip + 1), al2 = alpha(ip + 2);
-            double X, Y, Z;
-            if (Ap != 0) {
-                const double4 k = pt[ip];
-                X = fma(k.z, al3, fma(k.y, al2, Ap2));
-                Y = k.w * al4;
-                Z = k.x * al1;
-            } else { // eq. (30): two-term recurrence for l1 = l2
-                const double p = ip, p1 = p - 2 * m, p2 = p + 2 * m;
-                X = (p + 1) * (p2 + 2) * al2;
-                Y = 0.0;
-                Z = (p + 2) * (p1 + 1) * al1;
-            }
+            const double N1 = Nf(ip + 1), N2 = Nf(ip + 2);
+            const double4 k = pt[ip];
+            const double X = fma(k.z, N3, fma(k.y, N2, Ap2));
+            const double Y = k.w * N4;
+            const double Z = k.x * N1;
             const double b = fma(X, bm1, -(Y * Zprev) * bm2);
             Dq *= Z;
-            al3 = al1; al4 = al2; Zprev = Z;
+            N3 = N1; N4 = N2; Zprev = Z;
             bm2 = bm1; bm1 = b;
             {   // exact rescaling of b (with b_{q-1}) and D
                 const int kb = expo(b);
-                if (b != 0.0 && (kb > 300 || kb < -300)) { bm1 = shift2(bm1, -kb); bm2 = shift2(bm2, -kb); eb += kb; }
+                if (kb > 300 || (kb < -300 && kb > -1023)) { bm1 = shift2(bm1, -kb); bm2 = shift2(bm2, -kb); eb += kb; }
                 const int kd = expo(Dq);
                 if (kd > 300 || kd < -300) { Dq = shift2(Dq, -kd); eD += kd; }
             }
+            const int eb1 = expo(bm1);
             const int eDq = expo(Dq) + eD;
 #pragma unroll
             for (int pi = 0; pi < 2; pi++) {
@@ -389,18 +388,20 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
                 const int et = eb + Kv.e;
                 // S_q = Z S_{q-1} + t 2^(et - eS)
                 int d = et - A.eS;
-                if (A.S == 0.0) { A.eS = et; d = 0; }
-                if (d > 64) { A.S = shift2(A.S, -d); A.eS = et; d = 0; }
-                A.S = fma(Z, A.S, d > -1000 ? shift2(t, d) : 0.0);
+                const int es = expo(A.S);
+                if (es == -1023) { A.eS = et; d = 0; }
+                else if (d > 64) { A.S = shift2(A.S, -d); A.eS = et; d = 0; }
+                A.S = fma(Z, A.S, shift2(t, d));
                 const int ks = expo(A.S);
-                if (A.S != 0.0 && (ks > 300 || ks < -300)) { A.S = shift2(A.S, -ks); A.eS += ks; }
+                if (ks > 300 || (ks < -300 && ks > -1023)) { A.S = shift2(A.S, -ks); A.eS += ks; }
                 // early stop on |a_q K_q| / |K_0| < e^-60, i.e. log2 ratio < -86.5617
-                if (bm1 != 0.0) {
-                    const int approx = expo(bm1) + eb + Kv.e - eDq - A.e0; // true log2 ratio in (approx-2, approx+2)
+                if (eb1 != -1023) {
+                    const int approx = eb1 + eb + Kv.e - eDq - A.e0; // true log2 ratio in (approx-2, approx+2)
                     bool below;
                     if (approx <= -89) below = true;
                     else if (approx >= -84) below = false;
-                    else below = log(fabs(bm1)) + eb * LN2 + log(fabs(Kv.m)) + Kv.e * LN2 - log(fabs(Dq)) - eD * LN2 - A.v0 < -60.0;
+                    else below = log(fabs(bm1)) + eb * LN2 + log(fabs(Kv.m)) + Kv.e * LN2 - log(fabs(Dq)) - eD * LN2
+                                 - (log(fabs(A.K0->m)) + A.K0->e * LN2) < -60.0;
                     if (below) { if (++A.count >= 3) { A.on = false; A.D = Dq; A.eD = eD; } }
                     else A.count = 0;
                 }

@@ -31,16 +31,18 @@ CAPS_DEV double pow2i(int k) { return __longlong_as_double((long long)(k + 1023)
 // exponent of a normal nonzero double (value in [2^k, 2^(k+1)))
 CAPS_DEV int expo(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1023; }
 
-// x * 2^k for |x| normal and the result normal; flushes to 0 below 2^-1020
+// x * 2^k for |x| normal and the result normal; flushes to 0 below 2^-1020.
+// Integer work only (no FP64 instruction): zero and subnormal inputs give 0.
 CAPS_DEV double shift2(double x, int k)
 {
-    if (x == 0.0) return 0.0;
-    long long b = __double_as_longlong(x);
-    int ex = (int)((b >> 52) & 0x7ff);
-    int ne = ex + k;
-    if (ne <= 2) return 0.0;
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7ff);
+    if (ex == 0 || ex + k <= 2) return 0.0;
     return __longlong_as_double(b + ((long long)k << 52));
 }
+
+// x == 0 (either sign) tested on the bit pattern
+CAPS_DEV bool dzero(double x) { return (__double_as_longlong(x) << 1) == 0; }
 
 // normalise so that |m| is in [1,2)
 CAPS_DEV sd sd_norm(double m, int e)

@@ -385,6 +385,8 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         T.m = ms[i];
         TERMINATE(ms[i] < 0, "m must be non-negative");
         T.lmin = lmin_of(caps, ms[i]);
+        // the I recurrence forms (x^2-(l1+l2+1)^2)(x^2-(l1-l2)^2) exactly in 64-bit integers
+        TERMINATE(T.lmin + ldim > 27000, "l window beyond 27000 (lmin+ldim=%d) is not supported", T.lmin + ldim);
         T.mu = 2 * std::max(ms[i], 1);
         T.s = ms[i] > 0 ? 1 : 0;
         T.nu_max = 2 * (T.lmin + ldim);
@@ -404,7 +406,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     const size_t per_task = (size_t)dim * dim * 8 + (size_t)2 * L * L * sizeof(sd) + (size_t)2 * nu_stride * sizeof(sd)
                           + (size_t)nu_stride * sizeof(double2) + (size_t)3 * L * sizeof(sd) + (size_t)dim * 8
                           + (size_t)2 * 256 * nu_stride * 12  // partial sums, up to 256 warps
-                          + (size_t)(2 * (caps->ldim + 4096)) * sizeof(double4); // p table
+                          + (size_t)(4 * (caps->ldim + 4096)) * sizeof(double4); // p tables
     size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes));
     int chunk = (int)std::max<size_t>(1, std::min<size_t>(budget / per_task, 65535));
     chunk = std::min(chunk, n);
@@ -458,7 +460,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         CK(cudaEventRecord(g_eng.ev[2], st));
 
         sd *d_I = (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
-        double4 *d_ptab = (double4 *)g_eng.ptab.get((size_t)nt * pstride * sizeof(double4));
+        double4 *d_ptab = (double4 *)g_eng.ptab.get((size_t)nt * 2 * pstride * sizeof(double4));
         launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st);
         CK(cudaEventRecord(g_eng.ev[3], st));
 
