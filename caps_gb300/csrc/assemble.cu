@@ -400,8 +400,14 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
                     bool below;
                     if (approx <= -89) below = true;
                     else if (approx >= -84) below = false;
-                    else below = log(fabs(bm1)) + eb * LN2 + log(fabs(Kv.m)) + Kv.e * LN2 - log(fabs(Dq)) - eD * LN2
-                                 - (log(fabs(A.K0->m)) + A.K0->e * LN2) < -60.0;
+                    else {
+                        // exact test without logarithms: with mantissas in [1,2),
+                        // ratio = 2^approx * (mb mK)/(mD m0) < e^-60  <=>  mb mK < 2^(-60/ln2 - approx) mD m0
+                        const double c = approx == -88 ? 2.710008819393852 : approx == -87 ? 1.355004409696926
+                                       : approx == -86 ? 0.677502204848463 : 0.3387511024242315;
+                        const double mb = shift2(bm1, -eb1), mD = shift2(Dq, -expo(Dq));
+                        below = fabs(mb * Kv.m) < c * fabs(mD * A.K0->m);
+                    }
                     if (below) { if (++A.count >= 3) { A.on = false; A.D = Dq; A.eD = eD; } }
                     else A.count = 0;
                 }
