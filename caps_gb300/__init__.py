@@ -56,6 +56,8 @@ def _load():
         "caps_gpu_counters": (None, [C.POINTER(C.c_longlong)] * 3 + [i]),
         "caps_gpu_fp64_peak": (d, []),
         "caps_gpu_work": (None, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
+        "caps_logdetD_noalloc": (i, [vp, d, i, dp]),
+        "caps_noalloc_last_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -188,6 +188,22 @@ void caps_gpu_work(long long *nmat, long long *nfactor, double *factor_flops);
 /* measured FP64 FMA throughput of the current device, TFLOP/s (a short probe kernel) */
 double caps_gpu_fp64_peak(void);
 
+/* log det(1-M) of one (xi_, m), like caps_logdetD, for callers that cannot
+ * allocate device memory at call time (a framework that owns the whole device
+ * through its own pool, or code running while a stream is being captured).
+ * No counterpart in the reference.  All scratch lives in one fixed 32 MiB
+ * file-scope device array (held on every GPU that loads the library until
+ * exit); no cudaMalloc/cudaFree or allocating library call is made.
+ * Limits: ldim <= 512, lmin+ldim <= 2048, <= 256 K-quadrature panels; larger
+ * cases return a negative code with a message (caps_noalloc_last_error()).
+ * The first call on a device resolves the array's address (cudaGetSymbolAddress)
+ * and uploads constant tables: make it before any stream capture.  Calls share
+ * the array: calls that overlap on the GPU race.  Runs on the legacy default
+ * stream.  Returns 0, a negative code for rejected input, or the status bits
+ * of a numerical failure (CAPS_ST_ERR_*); *logdet receives the result. */
+int caps_logdetD_noalloc(caps_t *self, double xi_, int m, double *logdet);
+const char *caps_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
