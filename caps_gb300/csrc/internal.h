@@ -34,6 +34,8 @@ void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *
 void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode, double *trace,
                   double *result, int *status, cudaStream_t st);
 void launch_cholesky(int ntask, int n, double *A, size_t lda, size_t mstride, int *status, double *logdiag, cudaStream_t st);
+void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
+                           const double *trace, double *result, int mode, cudaStream_t st);
 void launch_final(int ntask, int n, const double *logdiag, const double *trace, int *status, double *result, int mode, cudaStream_t st);
 
 } // namespace capsgpu

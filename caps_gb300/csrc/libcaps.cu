@@ -97,7 +97,7 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -403,11 +403,11 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     // chunk size from free memory
     size_t freeb = 0, totb = 0;
     CK(cudaMemGetInfo(&freeb, &totb));
-    const size_t per_task = (size_t)dim * dim * 8 + (size_t)2 * L * L * sizeof(sd) + (size_t)2 * nu_stride * sizeof(sd)
+    const size_t per_task = (size_t)dim * dim * (caps->precision == CAPS_PREC_MIXED ? 12 : 8) + (size_t)2 * L * L * sizeof(sd) + (size_t)2 * nu_stride * sizeof(sd)
                           + (size_t)nu_stride * sizeof(double2) + (size_t)3 * L * sizeof(sd) + (size_t)dim * 8
                           + (size_t)2 * 256 * nu_stride * 12  // partial sums, up to 256 warps
                           + (size_t)(4 * (caps->ldim + 4096)) * sizeof(double4); // p tables
-    size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes));
+    size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes + g_eng.S32.bytes));
     int chunk = (int)std::max<size_t>(1, std::min<size_t>(budget / per_task, 65535));
     chunk = std::min(chunk, n);
 
@@ -472,7 +472,10 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         if (O.factor) launch_stats(d_tasks, nt, dim, d_A, lda, mstride, O.mode, d_trace, d_res, d_status, st);
         CK(cudaEventRecord(g_eng.ev[4], st));
 
-        if (O.factor) {
+        if (O.factor && caps->precision == CAPS_PREC_MIXED) {
+            float *d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
+            launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_trace, d_res, O.mode, st);
+        } else if (O.factor) {
             double *d_ld = (double *)g_eng.logdiag.get((size_t)nt * dim * sizeof(double));
             launch_cholesky(nt, dim, d_A, lda, mstride, d_status, d_ld, st);
             launch_final(nt, dim, d_ld, d_trace, d_status, d_res, O.mode, st);

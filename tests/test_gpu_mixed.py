@@ -1,0 +1,55 @@
+"""Mixed-precision factorisation (CAPS_PREC_MIXED): delta-form FP32 Cholesky with
+FP64 pivot logarithms and an FP64 trace correction.  Bars: per matrix
+|dlogdetD| <= 5e-8 max(1,|logdetD|) against the reference's values, and the
+free energy within |dE/E| <= 1e-6 of the FP64 oracle."""
+import pytest
+
+from conftest import rel, relx
+
+pytestmark = pytest.mark.gpu
+TOL_MIXED = 5e-8
+
+
+@pytest.fixture(scope="module")
+def cg():
+    import caps_gb300
+    return caps_gb300
+
+
+def test_mixed_unit_vectors_RbyL100(cg, unit_vectors):
+    cases = [v for v in unit_vectors["test_logdetD"]["cases"] if v["ldim"] == 500]
+    c = cg.Caps(1.0, 0.01, ldim=500)
+    c.set_precision(cg.PREC_MIXED)
+    out, st = c.logdetD_batch([v["xi"] for v in cases], [v["m"] for v in cases])
+    for v, got, s in zip(cases, out, st):
+        assert s < 16, (v, s)
+        assert abs(got - v["logdetD"]) <= TOL_MIXED * max(1.0, abs(v["logdetD"])), (v, got)
+
+
+@pytest.mark.parametrize("name", ["drude_RbyL150_ldim1050", "pr_RbyL50_ldim350", "drude_RbyL20_ldim140"])
+def test_mixed_vs_reference_fixtures(cg, ref_values, name):
+    if name not in ref_values:
+        pytest.skip("fixture set not generated")
+    cases = ref_values[name]
+    c0 = cases[0]
+    c = cg.Caps(c0["R"], c0["L"], ldim=c0["ldim"], detalg=cg.DETALG_LU)
+    if c0["drude"]:
+        c.set_drude(*c0["drude"])
+    c.set_precision(cg.PREC_MIXED)
+    out, st = c.logdetD_batch([v["xi"] for v in cases], [v["m"] for v in cases])
+    for v, got, s in zip(cases, out, st):
+        assert s < 16
+        assert abs(got - v["LU"]) <= TOL_MIXED * max(1.0, abs(v["LU"])), (v, got)
+
+
+def test_mixed_free_energy(cg):
+    from oracle import binding as ob
+    R, L, T, ldim = 10e-6, 1e-6, 300.0, 70
+    for drude in (None, (9.0, 0.035)):
+        c = cg.Caps(R, L, ldim=ldim, detalg=cg.DETALG_LU)
+        if drude:
+            c.set_drude(*drude)
+        c.set_precision(cg.PREC_MIXED)
+        E, info = c.free_energy(T)
+        Eo, _ = ob.free_energy(R, L, ldim, T, drude, threads=8)
+        assert abs(E - Eo) <= 1e-6 * abs(Eo), (E, Eo)
