@@ -243,13 +243,70 @@ CAPS_DEV void qacc_add(QAcc &A, double mant, int ex)
     if (d > -1000) A.s += shift2(mant, d);
 }
 
+
+// ---- float-float arithmetic on the FP32 pipe (about 48 significant bits) ----
+// value = h + l with |l| <= ulp(h)/2; error-free transformations of Dekker/Knuth.
+struct ff { float h, l; };
+struct ffe { float h, l; int e, pad; }; // (h + l) * 2^e
+CAPS_DEV ff ff_fast2(float a, float b) { const float s = a + b; return ff{s, b - (s - a)}; }
+CAPS_DEV ff ff_mul(ff x, ff y)
+{
+    const float p = x.h * y.h;
+    float e = fmaf(x.h, y.h, -p);
+    e = fmaf(x.h, y.l, e);
+    e = fmaf(x.l, y.h, e);
+    return ff_fast2(p, e);
+}
+CAPS_DEV ff ff_add(ff x, ff y)
+{
+    const float s = x.h + y.h, bb = s - x.h;
+    float e = (x.h - (s - bb)) + (y.h - bb);
+    e += x.l + y.l;
+    return ff_fast2(s, e);
+}
+CAPS_DEV ff ff_neg(ff x) { return ff{-x.h, -x.l}; }
+CAPS_DEV int fexpo(float x) { return (int)((__float_as_uint(x) >> 23) & 0xff) - 127; }
+// x * 2^k on the bit patterns; flushes to zero below 2^-120
+CAPS_DEV float fshift(float x, int k)
+{
+    const unsigned b = __float_as_uint(x);
+    const int ex = (int)((b >> 23) & 0xff);
+    if (ex == 0 || ex + k <= 6) return 0.0f;
+    return __uint_as_float(b + ((unsigned)k << 23));
+}
+CAPS_DEV ff ff_shift(ff x, int k) { return ff{fshift(x.h, k), fshift(x.l, k)}; }
+CAPS_DEV ff ff_from_d(double x) { const float h = (float)x; return ff{h, (float)(x - (double)h)}; }
+CAPS_DEV double ff_to_d(ff x) { return (double)x.h + (double)x.l; }
+// exact int64 -> float-float (48 of the 63 bits kept) times 2^k
+CAPS_DEV ff ff_from_ll(long long v, int k)
+{
+    const float h = (float)v;
+    const long long r = v - (long long)h;
+    return ff{fshift(h, k), fshift((float)r, k)};
+}
+
+// float-float copy of the K table (mantissa split into two floats, same exponent)
+__global__ void k_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, ffe *KF)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int task = blockIdx.y;
+    if (task >= ntask) return;
+    const Task &T = tasks[task];
+    if (i >= T.nu_max - T.mu + 1) return;
+    for (int p = 0; p < 2; p++) {
+        const sd k = K[(size_t)(task * 2 + p) * nu_stride + i];
+        const ff f = ff_from_d(k.m);
+        KF[(size_t)(task * 2 + p) * nu_stride + i] = ffe{f.h, f.l, k.e, 0};
+    }
+}
+
 // per task, for p in [0, pstride): the p-dependent factors of the recurrence with the
 // alpha denominators 1/(4x^2-1) folded in.  Table 0 (l1 != l2, eqs. (26)-(27)):
 //   {K0/(4(p+1)^2-1), K1/(4(p+2)^2-1), K2/(4(p+3)^2-1), K3/(4(p+4)^2-1)},
 //   K0=(p+2)(p+3)(p1+1)(p1+2), K1=(p+1)(p+3)(p1+2)(p2+2), K2=(p+2)(p+4)(p1+3)(p2+3), K3=(p+2)(p+3)(p2+3)(p2+4);
 // table 1 (l1 == l2, eq. (30)): {(p+2)(p1+1)/(4(p+1)^2-1), (p+1)(p2+2)/(4(p+2)^2-1), 0, 0};
 // p1 = p-2m, p2 = p+2m.
-__global__ void k_ptab(const Task *tasks, int ntask, double4 *ptab, int pstride)
+__global__ void k_ptab(const Task *tasks, int ntask, double4 *ptab, float4 *ptabf, int pstride)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int task = blockIdx.y;
@@ -264,11 +321,22 @@ __global__ void k_ptab(const Task *tasks, int ntask, double4 *ptab, int pstride)
                      (pp + 2) * (pp + 3) * ((p2 + 3) * (p2 + 4)) * invD(pp + 4));
     ptab[((size_t)task * 2 + 1) * pstride + p] =
         make_double4((pp + 2) * (p1 + 1) * invD(pp + 1), (pp + 1) * (p2 + 2) * invD(pp + 2), 0.0, 0.0);
+    if (ptabf) {
+        for (int t = 0; t < 2; t++) {
+            const double4 v = ptab[((size_t)task * 2 + t) * pstride + p];
+            const double s = 0x1p-30;
+            const ff x = ff_from_d(v.x * s), y = ff_from_d(v.y * s), z = ff_from_d(v.z * s), w = ff_from_d(v.w * s);
+            ptabf[(((size_t)task * 2 + t) * pstride + p) * 2 + 0] = make_float4(x.h, y.h, z.h, w.h);
+            ptabf[(((size_t)task * 2 + t) * pstride + p) * 2 + 1] = make_float4(x.l, y.l, z.l, w.l);
+        }
+    }
 }
 
+template <bool FF>
 __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride,
                                               const double *__restrict__ lft, const double2 *__restrict__ xtab,
-                                              const double4 *__restrict__ ptab, int pstride, sd *I, int *status)
+                                              const double4 *__restrict__ ptab, int pstride, sd *I, int *status,
+                                              const ffe *__restrict__ KF, const float4 *__restrict__ ptabf)
 {
     const int L = ldim + 2;
     const long long npair = (long long)L * (L + 1) / 2;
@@ -331,7 +399,95 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
         if (both) { const sd ke = KTE[l12 - 4]; qacc_add(aE, a2q * ke.m, ke.e); }
         aqm2 = aqm1; aqm1 = a2q;
     }
-    if (qmax >= 3) {
+    if (FF && qmax >= 3) {
+        // The same recurrence in float-float on the FP32 pipe.  The coefficient
+        // table carries 2^-30 and N(x) a per-pair 2^-sig, so X, Y, Z are scaled by
+        // lam = 2^-(30+sig); the recurrence is homogeneous, so b_q and D_q both pick
+        // up lam^(q-2) and a_q = b_q/D_q, S_q/D_q are unchanged.  b, D, S keep
+        // their own power-of-two exponents and are renormalised every step.
+        const long long Si = l1 + l2 + 1, Di = l1 - l2;
+        auto Nll = [&](int x) -> long long { return ((long long)(x - Si) * (x + Si)) * ((long long)(x - Di) * (x + Di)); };
+        int ip = l12 - 6; // p of q = 3
+        const long long n1st = Nll(ip + 1);
+        const int sig = (n1st == 0 ? 0 : (63 - __clzll(n1st < 0 ? -n1st : n1st))) - 20;
+        // N(x) = a c with a = x^2-(l1+l2+1)^2, c = x^2-(l1-l2)^2 (each |.| < 2^31): each
+        // factor splits exactly into two floats, the product is a float-float product
+        const int sa = sig / 2, sc = sig - sa;
+        auto split = [](int v, int k) { const float h = (float)v; return ff{fshift(h, k), fshift((float)(v - (int)h), k)}; };
+        auto Nf = [&](int x) {
+            const int av = (int)((long long)(x - Si) * (x + Si)), cv = (int)((long long)(x - Di) * (x + Di));
+            return ff_mul(split(av, -sa), split(cv, -sc));
+        };
+        const bool diag = (l1 == l2);
+        const ff Ap2 = diag ? ff{0.0f, 0.0f} : ff_from_d(Ap * Ap * ldexp(1.0, -30 - sig));
+        const float4 *pt = ptabf + ((size_t)task * 2 + (diag ? 1 : 0)) * pstride * 2;
+        const ffe *KFp[2] = {KF + (size_t)(task * 2 + 1) * nu_stride - T.mu, KF + (size_t)(task * 2 + 0) * nu_stride - T.mu};
+        struct PF { ff S; int eS; bool on; int count; ff D; int eD; int e0; float m0; };
+        PF P[2];
+        for (int pi = 0; pi < 2; pi++) {
+            const QAcc &Q = pi == 0 ? aT : aE;
+            const ffe k0 = KFp[pi][l12];
+            P[pi] = PF{ff_from_d(Q.s), Q.e, pi == 0 ? true : both, 0, ff{1.0f, 0.0f}, 0, k0.e, k0.h};
+        }
+        const int e_b = expo(aqm1);
+        ff bm2 = ff_from_d(shift2(aqm2, -e_b)), bm1 = ff_from_d(shift2(aqm1, -e_b));
+        int eb = e_b;
+        ff Dq{1.0f, 0.0f}, Zprev{1.0f, 0.0f};
+        int eD = 0;
+        ff N3 = Nf(ip + 3), N4 = Nf(ip + 4);
+        for (int q = 3; q <= qmax && (P[0].on || P[1].on); q++, ip -= 2) {
+            const ff N1 = Nf(ip + 1), N2 = Nf(ip + 2);
+            const float4 kh = pt[2 * ip], kl = pt[2 * ip + 1];
+            const ff X = ff_add(Ap2, ff_add(ff_mul(ff{kh.y, kl.y}, N2), ff_mul(ff{kh.z, kl.z}, N3)));
+            const ff Y = ff_mul(ff{kh.w, kl.w}, N4);
+            const ff Z = ff_mul(ff{kh.x, kl.x}, N1);
+            const ff b = ff_add(ff_mul(X, bm1), ff_neg(ff_mul(ff_mul(Y, Zprev), bm2)));
+            Dq = ff_mul(Dq, Z);
+            N3 = N1; N4 = N2; Zprev = Z;
+            bm2 = bm1; bm1 = b;
+            {
+                const int kb = fexpo(bm1.h);
+                if (kb > 40 || (kb < -40 && kb > -127)) { bm1 = ff_shift(bm1, -kb); bm2 = ff_shift(bm2, -kb); eb += kb; }
+                const int kd = fexpo(Dq.h);
+                if (kd > 40 || kd < -40) { Dq = ff_shift(Dq, -kd); eD += kd; }
+            }
+            const int eb1 = fexpo(bm1.h);
+            const int eDq = fexpo(Dq.h) + eD;
+#pragma unroll
+            for (int pi = 0; pi < 2; pi++) {
+                PF &A = P[pi];
+                if (!A.on) continue;
+                const ffe Kv = KFp[pi][ip];
+                const ff t = ff_mul(bm1, ff{Kv.h, Kv.l});
+                const int et = eb + Kv.e;
+                int d = et - A.eS;
+                if (fexpo(A.S.h) == -127) { A.eS = et; d = 0; }
+                else if (d > 30) { A.S = ff_shift(A.S, -d); A.eS = et; d = 0; }
+                A.S = ff_add(ff_mul(Z, A.S), d < -100 ? ff{0.0f, 0.0f} : ff_shift(t, d));
+                const int ks = fexpo(A.S.h);
+                if (ks > 40 || (ks < -40 && ks > -127)) { A.S = ff_shift(A.S, -ks); A.eS += ks; }
+                if (eb1 != -127) {
+                    const int approx = eb1 + eb + Kv.e - eDq - A.e0;
+                    bool below;
+                    if (approx <= -89) below = true;
+                    else if (approx >= -84) below = false;
+                    else {
+                        const float c = approx == -88 ? 2.710008819393852f : approx == -87 ? 1.355004409696926f
+                                      : approx == -86 ? 0.677502204848463f : 0.3387511024242315f;
+                        below = fabsf(fshift(bm1.h, -eb1) * Kv.h) < c * fabsf(fshift(Dq.h, -fexpo(Dq.h)) * A.m0);
+                    }
+                    if (below) { if (++A.count >= 3) { A.on = false; A.D = Dq; A.eD = eD; } }
+                    else A.count = 0;
+                }
+            }
+        }
+        for (int pi = 0; pi < 2; pi++) {
+            PF &A = P[pi];
+            if (A.on) { A.D = Dq; A.eD = eD; }
+            const sd r = sd_norm(ff_to_d(A.S) / ff_to_d(A.D), A.eS - A.eD);
+            if (pi == 0) { aT.s = r.m; aT.e = r.e; } else { aE.s = r.m; aE.e = r.e; }
+        }
+    } else if (qmax >= 3) {
         // Division-free form of the recurrence: a_q = b_q / D_q with
         //   b_q = X_q b_{q-1} - Y_q Z_{q-1} b_{q-2},  D_q = D_{q-1} Z_q,
         //   X_q = Ap^2 + K1 alpha(p+2) + K2 alpha(p+3), Y_q = K3 alpha(p+4), Z_q = K0 alpha(p+1)
@@ -607,14 +763,20 @@ void launch_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, 
 }
 
 void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
-                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st)
+                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF, float4 *ptabf)
 {
     dim3 gp((pstride + 127) / 128, ntask);
-    k_ptab<<<gp, 128, 0, st>>>(tasks, ntask, ptab, pstride);
+    k_ptab<<<gp, 128, 0, st>>>(tasks, ntask, ptab, ptabf, pstride);
     COUNT_LAUNCH(1);
     const long long L = ldim + 2, npair = L * (L + 1) / 2;
     dim3 g((unsigned)((npair + 127) / 128), ntask);
-    k_itab<<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status);
+    if (KF) {
+        dim3 gk((nu_stride + 127) / 128, ntask);
+        k_kff<<<gk, 128, 0, st>>>(tasks, ntask, K, nu_stride, KF);
+        COUNT_LAUNCH(1);
+        k_itab<true><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, KF, ptabf);
+    } else
+        k_itab<false><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, nullptr, nullptr);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

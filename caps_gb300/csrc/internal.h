@@ -27,8 +27,9 @@ void launch_ktab(bool pr, const Task *tasks, int ntask, int max_warps, const dou
 void launch_kred(const Task *tasks, int ntask, int max_nnu, const double *partM, const int *partE, int max_warps, int nu_stride,
                  sd *K, int *status, cudaStream_t st);
 void launch_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, int nx, cudaStream_t st);
+struct ffe;
 void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
-                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st);
+                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF = nullptr, float4 *ptabf = nullptr);
 void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv, double *A,
                  size_t lda, size_t mat_stride, int *status, cudaStream_t st);
 void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode, double *trace,

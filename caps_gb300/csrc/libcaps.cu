@@ -97,7 +97,7 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -461,7 +461,13 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
 
         sd *d_I = (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
         double4 *d_ptab = (double4 *)g_eng.ptab.get((size_t)nt * 2 * pstride * sizeof(double4));
-        launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st);
+        if (caps->precision == CAPS_PREC_MIXED) {
+            // mixed form: the q-sums in float-float on the FP32 pipe
+            ffe *d_KF = (ffe *)g_eng.KF.get((size_t)nt * 2 * nu_stride * 16);
+            float4 *d_ptabf = (float4 *)g_eng.ptabf.get((size_t)nt * 2 * pstride * 2 * sizeof(float4));
+            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_KF, d_ptabf);
+        } else
+            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st);
         CK(cudaEventRecord(g_eng.ev[3], st));
 
         const size_t lda = dim, mstride = (size_t)dim * dim;

@@ -53,3 +53,16 @@ def test_mixed_free_energy(cg):
         E, info = c.free_energy(T)
         Eo, _ = ob.free_energy(R, L, ldim, T, drude, threads=8)
         assert abs(E - Eo) <= 1e-6 * abs(Eo), (E, Eo)
+
+
+def test_mixed_dense_M_reference(cg, ref_values):
+    """the float-float q-sums of the mixed form keep element-level parity"""
+    import numpy as np
+    for v in ref_values["dense_M"]:
+        c = cg.Caps(v["R"], v["L"], ldim=v["ldim"])
+        if v["drude"]:
+            c.set_drude(*v["drude"])
+        c.set_precision(cg.PREC_MIXED)
+        M = c.M(v["xi"], v["m"])
+        Mr = np.array(v["M"])
+        assert np.abs(M - Mr).max() < 1e-10 * np.abs(Mr).max(), v["m"]
