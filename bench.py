@@ -177,6 +177,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--cpu-sample", type=int, default=0, help="matrices in the CPU-baseline sample (0: 2 per host thread)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--learned", action="store_true",
+                    help="learned truncation: train the network (untimed) and let it size the batch")
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: one batch of 8 matrices of the workload (n in {1,5}, m in {0,20,40,60})")
     args = ap.parse_args()
@@ -213,9 +215,16 @@ def main():
     caps.set_drude(OMEGAP_EV, GAMMA_EV)
     caps.set_precision(cg.PREC_MIXED if args.precision == "mixed" else cg.PREC_FP64)
 
+    net, train_info = None, None
+    if args.learned:
+        from caps_gb300 import learned
+        t_tr = time.time()
+        net, train_info = learned.train(seed=0)
+        train_info["seconds"] = time.time() - t_tr
+
     E = None
     for _ in range(args.warmup):
-        E, info = caps.free_energy(T, CUTOFF, EPSREL)
+        E, info = caps.free_energy(T, CUTOFF, EPSREL, mlp=net)
 
     clocks = ClockSampler(local_rank if "CUDA_VISIBLE_DEVICES" not in os.environ else os.environ["CUDA_VISIBLE_DEVICES"].split(",")[0])
     barrier(dist)
@@ -225,7 +234,7 @@ def main():
     t0 = time.time()
     infos = []
     for _ in range(args.steps):
-        E, info = caps.free_energy(T, CUTOFF, EPSREL)
+        E, info = caps.free_energy(T, CUTOFF, EPSREL, mlp=net)
         infos.append(info)
     wall = time.time() - t0
     clk = clocks.stop()
@@ -263,6 +272,8 @@ def main():
         "dtype": "f64" if args.precision == "fp64" else "f64 assembly + bf16x3 tensor factor + f64 correction",
         "data": "synthetic (inputs fully set by the geometry/material scalars)",
         "config": {"workload": WORKLOAD, "matrices_per_step": ndet / args.steps, "precision": args.precision,
+                   "truncation": "learned (MLP proposal, reference rules verify)" if args.learned else "plain (extrapolating schedule)",
+                   "wasted_matrices_per_step": sum(i["nwasted"] for i in infos) / args.steps,
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "no flush needed: every matrix (35 MB) and the per-chunk working set (>10 GB) exceed L2"},
         "time_to_E_s": wall_max / args.steps,
@@ -274,6 +285,7 @@ def main():
                      "peak_source": "measured live: DFMA-chain probe kernel (caps_gpu_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
                      "traffic": None},
         "cpu_baseline": cpu,
+        "learned_training": train_info,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": ctr["h2d"] / args.steps, "d2h_bytes_per_step": ctr["d2h"] / args.steps},
         "gpu_launches": ctr["launches"],
         "clocks": clk,

@@ -57,6 +57,14 @@ def _load():
         "caps_gpu_fp64_peak": (d, []),
         "caps_gpu_work": (None, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
         "caps_logdetD_noalloc": (i, [vp, d, i, dp]),
+        "caps_mlp_create": (vp, [C.c_uint]), "caps_mlp_free": (None, [vp]), "caps_mlp_nparams": (i, []),
+        "caps_mlp_get_params": (None, [vp, C.POINTER(C.c_float)]), "caps_mlp_set_params": (None, [vp, C.POINTER(C.c_float)]),
+        "caps_mlp_features": (None, [d, d, i, d, d, C.POINTER(C.c_float)]),
+        "caps_mlp_loss_grad": (d, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), i, C.POINTER(C.c_float)]),
+        "caps_mlp_train": (d, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), i, i, C.c_float]),
+        "caps_mlp_predict": (None, [vp, C.POINTER(C.c_float), i, C.POINTER(C.c_float)]),
+        "caps_mlp_proposal": (i, [vp, d, d, d, vp, i, ip]),
+        "caps_free_energy_learned": (d, [vp, d, d, d, vp, C.POINTER(_EnergyInfo)]),
         "caps_noalloc_last_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
@@ -199,11 +207,73 @@ class Caps:
     def ht_perf(self, eps):
         return lib.caps_ht_perf(self._h, eps)
 
-    def free_energy(self, T, cutoff=1e-9, epsrel=1e-6):
+    def free_energy(self, T, cutoff=1e-9, epsrel=1e-6, mlp=None):
+        """free energy E (L+R)/(hbar c); with mlp (an MLP) the learned proposal sizes the batch"""
         xi = (C.c_double * 4096)()
         v = (C.c_double * 4096)()
         info = _EnergyInfo(0, 0, 0, 0.0, C.cast(xi, C.POINTER(C.c_double)), C.cast(v, C.POINTER(C.c_double)))
-        E = lib.caps_free_energy(self._h, float(T), float(cutoff), float(epsrel), C.byref(info))
+        if mlp is not None:
+            E = lib.caps_free_energy_learned(self._h, float(T), float(cutoff), float(epsrel), mlp._h, C.byref(info))
+        else:
+            E = lib.caps_free_energy(self._h, float(T), float(cutoff), float(epsrel), C.byref(info))
         n = info.nxi
         return E, dict(nxi=n, ndet=info.ndet, nwasted=info.nwasted, seconds=info.seconds,
                        xi=list(xi[:n]), logdetD=list(v[:n]))
+
+
+class MLP:
+    """the learned-truncation network (caps_mlp_t): 5-64-64-64-1 SiLU, trained on the GPU"""
+
+    def __init__(self, seed=0):
+        self._h = lib.caps_mlp_create(seed)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib.caps_mlp_free(h)
+            self._h = None
+
+    @staticmethod
+    def nparams():
+        return lib.caps_mlp_nparams()
+
+    def params(self):
+        out = np.empty(self.nparams(), dtype=np.float32)
+        lib.caps_mlp_get_params(self._h, out.ctypes.data_as(C.POINTER(C.c_float)))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        lib.caps_mlp_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float)))
+
+    @staticmethod
+    def features(RbyL, xi_, m, omegap_eV, gamma_eV):
+        x = (C.c_float * 5)()
+        lib.caps_mlp_features(RbyL, xi_, m, omegap_eV, gamma_eV, x)
+        return np.array(x[:], dtype=np.float32)
+
+    def loss_grad(self, X, y):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.empty(self.nparams(), dtype=np.float32)
+        loss = lib.caps_mlp_loss_grad(self._h, X.ctypes.data_as(C.POINTER(C.c_float)), y.ctypes.data_as(C.POINTER(C.c_float)),
+                                      len(y), g.ctypes.data_as(C.POINTER(C.c_float)))
+        return loss, g
+
+    def train(self, X, y, epochs=2000, lr=3e-3):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        return lib.caps_mlp_train(self._h, X.ctypes.data_as(C.POINTER(C.c_float)), y.ctypes.data_as(C.POINTER(C.c_float)),
+                                  len(y), epochs, lr)
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.empty(len(X), dtype=np.float32)
+        lib.caps_mlp_predict(self._h, X.ctypes.data_as(C.POINTER(C.c_float)), len(X), y.ctypes.data_as(C.POINTER(C.c_float)))
+        return y
+
+    def proposal(self, caps, T, cutoff=1e-9, epsrel=1e-6, nmax=256):
+        ch = np.zeros(nmax, dtype=np.int32)
+        N = lib.caps_mlp_proposal(caps._h, float(T), float(cutoff), float(epsrel), self._h, nmax,
+                                  ch.ctypes.data_as(C.POINTER(C.c_int)))
+        return N, ch[:max(N, 0)]

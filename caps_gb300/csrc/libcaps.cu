@@ -741,7 +741,10 @@ static int m_chunk(const MState &s, double cutoff)
     return std::max(8, std::min(w, 256));
 }
 
-extern "C" double caps_free_energy(caps_t *self, double T, double cutoff, double epsrel, caps_energy_info_t *info)
+// first_chunk[i] (i < n_first): number of m to compute in the first batch for xi_{i+1}
+// (from a proposal); nullptr: the extrapolating schedule of the plain method.
+static double energy_impl(caps_t *self, double T, double cutoff, double epsrel, const int *first_chunk, int n_first,
+                          caps_energy_info_t *info)
 {
     const auto t0 = std::chrono::steady_clock::now();
     TERMINATE(!(T > 0), "temperature must be positive");
@@ -778,7 +781,7 @@ extern "C" double caps_free_energy(caps_t *self, double T, double cutoff, double
     std::vector<double> vn(1, v0);      // per-frequency sums, index n
     std::vector<MState> st;             // st[n-1] for xi_n
     int nmax_known = -1;                // n where |v_n/v_0| < epsrel
-    int nactive = 4;
+    int nactive = first_chunk ? std::max(1, n_first) : 4;
     st.resize(nactive);
     for (;;) {
         // schedule
@@ -788,10 +791,11 @@ extern "C" double caps_free_energy(caps_t *self, double T, double cutoff, double
             MState &s = st[i];
             if (s.done()) continue;
             int w = m_chunk(s, cutoff);
-            // the m cutoff falls with the frequency: a known cutoff of a lower frequency bounds the first chunk
-            if (s.next == 0)
+            if (s.next == 0 && first_chunk && i < n_first) w = std::max(1, first_chunk[i]);
+            else if (s.next == 0 && !first_chunk)
+                // a known cutoff of a neighbouring frequency sizes the first chunk
                 for (int j = i - 1; j >= 0; j--)
-                    if (st[j].done()) { w = std::min(w, st[j].mstop + 4); break; }
+                    if (st[j].done()) { w = std::min(w, st[j].mstop + 8); break; }
             for (int k = 0; k < w; k++) { bx.push_back((i + 1) * Ts); bm.push_back(s.next + k); who.push_back({i, s.next + k}); }
             s.next += w;
             s.v.resize(s.next, NAN);
@@ -868,4 +872,63 @@ extern "C" double caps_free_energy(caps_t *self, double T, double cutoff, double
     const double E = Ts / PI * kahan_sum(w.data(), w.size());
     if (info) info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return E;
+}
+
+extern "C" double caps_free_energy(caps_t *self, double T, double cutoff, double epsrel, caps_energy_info_t *info)
+{
+    return energy_impl(self, T, cutoff, epsrel, nullptr, 0, info);
+}
+
+// material features of the learned proposal: perfect reflectors are encoded as
+// omega_p = 50 eV, gamma = 0; Drude callbacks carry (omega_p, gamma) in rad/s
+static bool material_features(const caps_t *c, double *wp_eV, double *g_eV)
+{
+    if (c->epsilonm1_plate == caps_epsilonm1_perf) { *wp_eV = 50.0; *g_eV = 0.0; return true; }
+    if (c->epsilonm1_plate == caps_epsilonm1_drude && c->userdata_plate) {
+        const double *p = (const double *)c->userdata_plate;
+        *wp_eV = p[0] * CAPS_hbar_eV;
+        *g_eV = p[1] * CAPS_hbar_eV;
+        return true;
+    }
+    return false;
+}
+
+extern "C" void caps_mlp_features(double RbyL, double xi_, int m, double omegap_eV, double gamma_eV, float *x);
+extern "C" void caps_mlp_predict(caps_mlp_t *m, const float *X, int n, float *y);
+
+extern "C" int caps_mlp_proposal(caps_t *self, double T, double cutoff, double epsrel, caps_mlp_t *mlp, int nmax, int *mchunk)
+{
+    double wp, ga;
+    if (!material_features(self, &wp, &ga)) return -1;
+    const double Ts = 2 * PI * CAPS_kB * (self->R + self->L) * T / (CAPS_hbar * CAPS_c);
+    const int MCAP = 1024, NPROBE = std::min(nmax, 256);
+    std::vector<float> X((size_t)NPROBE * MCAP * 5), Y((size_t)NPROBE * MCAP);
+    for (int n = 1; n <= NPROBE; n++)
+        for (int m = 0; m < MCAP; m++)
+            caps_mlp_features(1.0 / self->LbyR, n * Ts, m, wp, ga, &X[(((size_t)(n - 1) * MCAP) + m) * 5]);
+    caps_mlp_predict(mlp, X.data(), NPROBE * MCAP, Y.data());
+    // the xi = 0 term (analytic for Drude; drude term as the scale for other materials)
+    const double v0 = fabs(caps_ht_drude(self));
+    const double lc = log(cutoff);
+    int N = NPROBE;
+    for (int n = 1; n <= NPROBE; n++) {
+        const float *y = &Y[(size_t)(n - 1) * MCAP];
+        int mstop = MCAP - 1;
+        for (int m = 1; m < MCAP; m++)
+            if (y[m] - y[0] < lc) { mstop = m; break; }
+        mchunk[n - 1] = mstop + 1 + 2; // two extra m beyond the predicted cutoff
+        double v = 0.5 * exp((double)y[0]);
+        for (int m = 1; m <= mstop; m++) v += exp((double)y[m]);
+        if (v / v0 < epsrel) { N = n; break; }
+    }
+    return N;
+}
+
+extern "C" double caps_free_energy_learned(caps_t *self, double T, double cutoff, double epsrel, caps_mlp_t *mlp,
+                                           caps_energy_info_t *info)
+{
+    std::vector<int> chunk(256, 32);
+    const int N = mlp ? caps_mlp_proposal(self, T, cutoff, epsrel, mlp, 256, chunk.data()) : -1;
+    if (N <= 0) return energy_impl(self, T, cutoff, epsrel, nullptr, 0, info);
+    return energy_impl(self, T, cutoff, epsrel, chunk.data(), N, info);
 }

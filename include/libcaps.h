@@ -164,6 +164,32 @@ typedef struct {
 } caps_energy_info_t;
 double caps_free_energy(caps_t *self, double T, double cutoff, double epsrel, caps_energy_info_t *info);
 
+/* ---- learned truncation (no reference counterpart) ----
+ * A 5-64-64-64-1 SiLU network (FP32), trained on the GPU by the library's own
+ * forward/backward/Adam kernels on log|logdetD| values computed by the plain
+ * method, predicts log|logdetD(xi, m)| from (log R/L, log xi_, m, omega_p,
+ * gamma).  caps_free_energy_learned() uses it to propose the m cutoff of every
+ * Matsubara frequency and the number of frequencies, computes the proposed
+ * matrices as one GPU batch, then applies the reference's cutoff rules to the
+ * computed values and extends the batch where the proposal fell short -- so
+ * its result is the plain method's result. */
+typedef struct caps_mlp caps_mlp_t;
+caps_mlp_t *caps_mlp_create(unsigned seed);
+void caps_mlp_free(caps_mlp_t *mlp);
+int caps_mlp_nparams(void);
+void caps_mlp_get_params(caps_mlp_t *mlp, float *out);
+void caps_mlp_set_params(caps_mlp_t *mlp, const float *in);
+/* features of one sample (5 floats) in the normalisation the network uses */
+void caps_mlp_features(double RbyL, double xi_, int m, double omegap_eV, double gamma_eV, float *x);
+/* mean squared error of a batch and (if grad != NULL) its gradient w.r.t. all parameters */
+double caps_mlp_loss_grad(caps_mlp_t *mlp, const float *X, const float *y, int n, float *grad);
+/* full-batch Adam for the given epochs; returns the final loss */
+double caps_mlp_train(caps_mlp_t *mlp, const float *X, const float *y, int n, int epochs, float lr);
+void caps_mlp_predict(caps_mlp_t *mlp, const float *X, int n, float *y);
+/* proposal: mchunk[n-1] = number of m to compute for xi_n; returns the number of frequencies (<= nmax) */
+int caps_mlp_proposal(caps_t *self, double T, double cutoff, double epsrel, caps_mlp_t *mlp, int nmax, int *mchunk);
+double caps_free_energy_learned(caps_t *self, double T, double cutoff, double epsrel, caps_mlp_t *mlp, caps_energy_info_t *info);
+
 /* last error text of this thread's most recent GPU call ("" if none) */
 const char *caps_gpu_last_error(void);
 
