@@ -174,11 +174,13 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--cpu-sample", type=int, default=0, help="matrices in the CPU-baseline sample (0: 2 per host thread)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--learned", action="store_true",
-                    help="learned truncation: train the network (untimed) and let it size the batch")
+    ap.add_argument("--plain", action="store_true",
+                    help="plain truncation schedule instead of the learned proposal")
+    ap.add_argument("--no-fp64-reference", action="store_true",
+                    help="skip the side measurement of the plain FP64 form")
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: one batch of 8 matrices of the workload (n in {1,5}, m in {0,20,40,60})")
     args = ap.parse_args()
@@ -211,11 +213,13 @@ def main():
     import caps_gb300 as cg
 
     fp64_peak = cg.fp64_peak()
+    fp32_peak = cg.fp32_peak()
     caps = cg.Caps(R, L, ldim=LDIM)
     caps.set_drude(OMEGAP_EV, GAMMA_EV)
     caps.set_precision(cg.PREC_MIXED if args.precision == "mixed" else cg.PREC_FP64)
 
     net, train_info = None, None
+    args.learned = not args.plain
     if args.learned:
         from caps_gb300 import learned
         t_tr = time.time()
@@ -245,6 +249,23 @@ def main():
 
     ndet = sum(i["ndet"] for i in infos)
     dev_s = ph[5] * 1e-3
+
+    # the plain FP64 GPU form on the same workload (1 warm-up + 2 timed calls), for the
+    # mixed+learned vs FP64 ratio of the metric
+    fp64 = None
+    if not args.no_fp64_reference and (args.learned or args.precision != "fp64"):
+        c64 = cg.Caps(R, L, ldim=LDIM)
+        c64.set_drude(OMEGAP_EV, GAMMA_EV)
+        c64.free_energy(T, CUTOFF, EPSREL)
+        cg.reset_timings()
+        t64 = time.time()
+        E64 = None
+        for _ in range(2):
+            E64, i64 = c64.free_energy(T, CUTOFF, EPSREL)
+        t64 = (time.time() - t64) / 2
+        d64 = cg.timings(cumulative=True)[5] * 1e-3 / 2
+        fp64 = {"time_to_E_s": t64, "value": i64["ndet"] / d64, "matrices": i64["ndet"], "E": E64,
+                "phases_ms": dict(zip(["setup_mie", "K", "I", "elements", "factor", "total"], [x / 2 for x in cg.timings(cumulative=True)]))}
     wall_max = allmax(dist, wall)
     dev_max = allmax(dist, dev_s)
     ndet_all = allsum(dist, ndet)
@@ -269,7 +290,8 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": wall_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f64 assembly + bf16x3 tensor factor + f64 correction",
+        "dtype": "f64" if args.precision == "fp64" else
+                 "f64 (Mie, K, log-factorials, exponents, pivot logs, correction) + float-float q-sums + f32 delta-Cholesky",
         "data": "synthetic (inputs fully set by the geometry/material scalars)",
         "config": {"workload": WORKLOAD, "matrices_per_step": ndet / args.steps, "precision": args.precision,
                    "truncation": "learned (MLP proposal, reference rules verify)" if args.learned else "plain (extrapolating schedule)",
@@ -279,13 +301,20 @@ def main():
         "time_to_E_s": wall_max / args.steps,
         "E": E, "E_reference": ref["E"] if ref else None, "E_rel_err": err,
         "phases_ms_per_step": {k: v / args.steps for k, v in zip(["setup_mie", "K", "I", "elements", "factor", "total"], ph)},
-        "roofline": {"bound": "fp64", "kernel": "FP64 Cholesky (potf2+trsm+syrk), n^3/3 flops per factored matrix",
-                     "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp64_peak if achieved else None,
-                     "peak_source": "measured live: DFMA-chain probe kernel (caps_gpu_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
-                     "traffic": None},
+        "roofline": ({"bound": "fp64", "kernel": "FP64 Cholesky (potf2+trsm+syrk), n^3/3 flops per factored matrix",
+                      "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                      "frac": achieved / fp64_peak if achieved else None,
+                      "peak_source": "measured live: DFMA-chain probe kernel (caps_gpu_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
+                      "traffic": None} if args.precision == "fp64" else
+                     {"bound": "fp32", "kernel": "FP32 delta-form Cholesky (potf2_d+trsm_d+syrk_f), n^3/3 flops per factored matrix",
+                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                      "frac": achieved / fp32_peak if achieved else None,
+                      "peak_source": "measured live: FFMA-chain probe kernel (caps_gpu_fp32_peak); MEASURED_PEAKS.json has no FP32 SIMT figure",
+                      "traffic": None}),
         "cpu_baseline": cpu,
         "learned_training": train_info,
+        "fp64_plain_form": fp64,
+        "time_to_E_speedup_vs_fp64_plain": (fp64["time_to_E_s"] / (wall_max / args.steps)) if fp64 else None,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": ctr["h2d"] / args.steps, "d2h_bytes_per_step": ctr["d2h"] / args.steps},
         "gpu_launches": ctr["launches"],
         "clocks": clk,

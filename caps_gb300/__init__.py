@@ -55,6 +55,7 @@ def _load():
         "caps_gpu_reset_timings": (None, []),
         "caps_gpu_counters": (None, [C.POINTER(C.c_longlong)] * 3 + [i]),
         "caps_gpu_fp64_peak": (d, []),
+        "caps_gpu_fp32_peak": (d, []),
         "caps_gpu_work": (None, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
         "caps_logdetD_noalloc": (i, [vp, d, i, dp]),
         "caps_mlp_create": (vp, [C.c_uint]), "caps_mlp_free": (None, [vp]), "caps_mlp_nparams": (i, []),
@@ -107,6 +108,10 @@ def work():
     a, b, c = C.c_longlong(), C.c_longlong(), C.c_double()
     lib.caps_gpu_work(C.byref(a), C.byref(b), C.byref(c))
     return dict(nmat=a.value, nfactor=b.value, factor_flops=c.value)
+
+
+def fp32_peak():
+    return lib.caps_gpu_fp32_peak()
 
 
 def fp64_peak():

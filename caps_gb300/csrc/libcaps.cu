@@ -179,6 +179,45 @@ __global__ void k_fp64_probe(double *out, int iters, double a)
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+__global__ void k_fp32_probe(float *out, int iters, float a)
+{
+    float x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = threadIdx.x + k;
+    for (int i = 0; i < iters; i++)
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = fmaf(x[k], a, 1.0f);
+    float s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += x[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// sustained FP32 FMA throughput (independent FMA chains on every SM), TFLOP/s
+extern "C" double caps_gpu_fp32_peak(void)
+{
+    std::lock_guard<std::mutex> lk(g_eng.mu);
+    engine_init();
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g_eng.device));
+    const int blocks = sms * 8, threads = 256, iters = 100000;
+    float *d;
+    CK(cudaMalloc(&d, (size_t)blocks * threads * sizeof(float)));
+    cudaStream_t st = g_eng.stream();
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+        CK(cudaEventRecord(g_eng.ev[0], st));
+        k_fp32_probe<<<blocks, threads, 0, st>>>(d, iters, 0.999f);
+        CK(cudaEventRecord(g_eng.ev[1], st));
+        CK(cudaEventSynchronize(g_eng.ev[1]));
+        float ms;
+        CK(cudaEventElapsedTime(&ms, g_eng.ev[0], g_eng.ev[1]));
+        best = std::min(best, ms);
+    }
+    CK(cudaFree(d));
+    return 2.0 * 8 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+}
+
 extern "C" double caps_gpu_fp64_peak(void)
 {
     std::lock_guard<std::mutex> lk(g_eng.mu);

@@ -213,6 +213,8 @@ void caps_gpu_work(long long *nmat, long long *nfactor, double *factor_flops);
 
 /* measured FP64 FMA throughput of the current device, TFLOP/s (a short probe kernel) */
 double caps_gpu_fp64_peak(void);
+/* measured FP32 FMA throughput of the current device, TFLOP/s (a short probe kernel) */
+double caps_gpu_fp32_peak(void);
 
 /* log det(1-M) of one (xi_, m), like caps_logdetD, for callers that cannot
  * allocate device memory at call time (a framework that owns the whole device
