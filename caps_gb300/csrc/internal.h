@@ -36,7 +36,7 @@ void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t l
                   double *result, int *status, cudaStream_t st);
 void launch_cholesky(int ntask, int n, double *A, size_t lda, size_t mstride, int *status, double *logdiag, cudaStream_t st);
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
-                           const double *trace, double *result, int mode, cudaStream_t st);
+                           const double *trace, double *result, int mode, cudaStream_t st, bool tc = true);
 void launch_final(int ntask, int n, const double *logdiag, const double *trace, int *status, double *result, int mode, cudaStream_t st);
 
 } // namespace capsgpu

@@ -519,7 +519,9 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
 
         if (O.factor && caps->precision == CAPS_PREC_MIXED) {
             float *d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
-            launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_trace, d_res, O.mode, st);
+            // CAPS_MIXED_SIMT=1 selects the FP32 FFMA trailing update instead of split-TF32 tensor cores
+            static const bool tc = getenv("CAPS_MIXED_SIMT") == nullptr;
+            launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_trace, d_res, O.mode, st, tc);
         } else if (O.factor) {
             double *d_ld = (double *)g_eng.logdiag.get((size_t)nt * dim * sizeof(double));
             launch_cholesky(nt, dim, d_A, lda, mstride, d_status, d_ld, st);

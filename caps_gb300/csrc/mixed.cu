@@ -160,6 +160,95 @@ __global__ void __launch_bounds__(64) k_syrk_f(int ntask, int n, int k0, float *
     }
 }
 
+
+// Tensor-core trailing update: S_tile -= A B^T over the 64 panel columns with
+// split TF32 (x = hi + lo, both TF32; A B^T ~ hi hi + hi lo + lo hi, FP32
+// accumulation) on mma.sync.m16n8k8.  64x64 output tile per CTA of 4 warps,
+// each warp a 32x32 quadrant of 2x4 m16n8 fragments.
+__device__ __forceinline__ unsigned tf32_of(float x)
+{
+    unsigned r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const unsigned (&a)[4], const unsigned (&b)[2])
+{
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__global__ void __launch_bounds__(128) k_syrk_tc(int ntask, int n, int k0, float *S, size_t sstride, const int *status)
+{
+    const int task = blockIdx.y;
+    if (task >= ntask || status[task] != ST_FACTOR) return;
+    const int nb = min(MB, n - k0);
+    const int t0 = k0 + nb;
+    const int p = blockIdx.x;
+    int ti = (int)((sqrt(8.0 * p + 1.0) - 1.0) * 0.5);
+    while ((ti + 1) * (ti + 2) / 2 <= p) ti++;
+    while (ti * (ti + 1) / 2 > p) ti--;
+    const int tj = p - ti * (ti + 1) / 2;
+    const int row0 = t0 + ti * 64, col0 = t0 + tj * 64;
+    if (row0 >= n) return;
+    __shared__ float As[64][MB + 4]; // [row][k]
+    __shared__ float Bs[64][MB + 4]; // [col][k]
+    float *Sm = S + (size_t)task * sstride;
+    for (int e = threadIdx.x; e < 64 * MB; e += 128) {
+        const int k = e / 64, r = e % 64;
+        As[r][k] = (row0 + r < n && k < nb) ? Sm[(size_t)(k0 + k) * n + row0 + r] : 0.0f;
+        Bs[r][k] = (col0 + r < n && k < nb) ? Sm[(size_t)(k0 + k) * n + col0 + r] : 0.0f;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) acc[i][j][q] = 0.0f;
+#pragma unroll 2
+    for (int ks = 0; ks < MB; ks += 8) {
+        unsigned ah[2][4], al[2][4], bh[4][2], bl[4][2];
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int r = wm + i * 16 + g;
+            const float x[4] = {As[r][ks + t], As[r + 8][ks + t], As[r][ks + t + 4], As[r + 8][ks + t + 4]};
+#pragma unroll
+            for (int q = 0; q < 4; q++) { ah[i][q] = tf32_of(x[q]); al[i][q] = tf32_of(x[q] - __uint_as_float(ah[i][q])); }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int c = wn + j * 8 + g;
+            const float y[2] = {Bs[c][ks + t], Bs[c][ks + t + 4]};
+#pragma unroll
+            for (int q = 0; q < 2; q++) { bh[j][q] = tf32_of(y[q]); bl[j][q] = tf32_of(y[q] - __uint_as_float(bh[j][q])); }
+        }
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                mma_tf32(acc[i][j], al[i], bh[j]);
+                mma_tf32(acc[i][j], ah[i], bl[j]);
+                mma_tf32(acc[i][j], ah[i], bh[j]);
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int r = row0 + wm + i * 16 + g + (q >= 2 ? 8 : 0);
+                const int c = col0 + wn + j * 8 + 2 * t + (q & 1);
+                if (r < n && c < n && r >= c) Sm[(size_t)c * n + r] -= acc[i][j][q];
+            }
+}
+
 // log det = 2 sum log1p(Lam_jj) + tr(A-I) - 2 tr Lam - ||Lam||_F^2, all sums FP64;
 // one CTA per task, fixed reduction order
 __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const float *S, size_t sstride, const double *A, size_t lda,
@@ -200,7 +289,7 @@ __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const flo
 }
 
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
-                           const double *trace, double *result, int mode, cudaStream_t st)
+                           const double *trace, double *result, int mode, cudaStream_t st, bool tc)
 {
     {
         dim3 g(256, ntask);
@@ -217,7 +306,8 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         COUNT_LAUNCH(1);
         const int nt = (rest + 63) / 64;
         dim3 gs(nt * (nt + 1) / 2, ntask);
-        k_syrk_f<<<gs, 64, 0, st>>>(ntask, n, k0, S, sstride, status);
+        if (tc) k_syrk_tc<<<gs, 128, 0, st>>>(ntask, n, k0, S, sstride, status);
+        else k_syrk_f<<<gs, 64, 0, st>>>(ntask, n, k0, S, sstride, status);
         COUNT_LAUNCH(1);
     }
     k_final_mixed<<<ntask, 256, 0, st>>>(ntask, n, S, sstride, A, lda, mstride, trace, status, result, mode);
