@@ -332,11 +332,56 @@ __global__ void k_ptab(const Task *tasks, int ntask, double4 *ptab, float4 *ptab
     }
 }
 
+// per distinct m of a chunk and per (l1>=l2) pair: a_0 (as a scaled double), a_1,
+// a_2 of the q-sum (eqs. (20), (29), (35)) -- they depend on (l1, l2, m) but not on
+// xi, so every frequency with the same m shares them.  Evaluated with the
+// reference's formulas and order of operations: the m=0 q-sums cancel strongly
+// and the reference's results carry exactly this rounding of a_2.
+struct A012 { double a1, a2, a0m; int a0e, pad; };
+
+__global__ void k_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *__restrict__ lft, A012 *tab)
+{
+    const int L = ldim + 2;
+    const long long npair = (long long)L * (L + 1) / 2;
+    const long long pid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = blockIdx.y;
+    if (pid >= npair || g >= ngroup) return;
+    int a1 = (int)((sqrt(8.0 * (double)pid + 1.0) - 1.0) * 0.5);
+    while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
+    while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
+    const int a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
+    const int mt = group_m[g];
+    const int l1 = group_lmin[g] - 1 + a1, l2 = group_lmin[g] - 1 + a2;
+    const int mm = mt > 0 ? mt : 1;
+    A012 r{0.0, 0.0, 0.0, 0, 0};
+    if (!(l2 < mm || l2 < mt || l1 < 1)) {
+        const double n = l1, nu = l2, m = mm;
+        const double n4 = l1 + l2 - 2 * mm;
+        const int l12 = l1 + l2;
+        const int qmax = min(min(l1, l2), (l12 - 2 * mm) / 2);
+        const double log_a0 = __ldg(lft + 2 * l1) - __ldg(lft + l1) + __ldg(lft + 2 * l2) - __ldg(lft + l2) + __ldg(lft + l12)
+                            - __ldg(lft + 2 * l12) + __ldg(lft + l12 - 2 * mm) - __ldg(lft + l1 - mm) - __ldg(lft + l2 - mm);
+        const sd a0 = sd_from_log(log_a0, 1);
+        r.a0m = a0.m;
+        r.a0e = a0.e;
+        if (qmax >= 1)
+            r.a1 = (n + nu - 1.5) * (1 - (2 * n + 2 * nu - 1) / (n4 * (n4 - 1)) * ((m - n) * (m - n + 1) / (2 * n - 1) + (m - nu) * (m - nu + 1) / (2 * nu - 1)));
+        if (qmax >= 2)
+            r.a2 = (2 * n + 2 * nu - 1) * (2 * n + 2 * nu - 7) / 4 * ((2 * n + 2 * nu - 3) / (n4 * (n4 - 1)) * ((2 * n + 2 * nu - 5) / (2 * (n4 - 2) * (n4 - 3))
+                  * ((m - n) * (m - n + 1) * (m - n + 2) * (m - n + 3) / (2 * n - 1) / (2 * n - 3)
+                  + 2 * (m - n) * (m - n + 1) * (m - nu) * (m - nu + 1) / ((2 * n - 1) * (2 * nu - 1))
+                  + (m - nu) * (m - nu + 1) * (m - nu + 2) * (m - nu + 3) / (2 * nu - 1) / (2 * nu - 3)) - (m - n) * (m - n + 1) / (2 * n - 1)
+                  - (m - nu) * (m - nu + 1) / (2 * nu - 1)) + 0.5);
+    }
+    tab[(size_t)g * npair + pid] = r;
+}
+
 template <bool FF>
 __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride,
                                               const double *__restrict__ lft, const double2 *__restrict__ xtab,
                                               const double4 *__restrict__ ptab, int pstride, sd *I, int *status,
-                                              const ffe *__restrict__ KF, const float4 *__restrict__ ptabf)
+                                              const ffe *__restrict__ KF, const float4 *__restrict__ ptabf,
+                                              const A012 *__restrict__ a12)
 {
     const int L = ldim + 2;
     const long long npair = (long long)L * (L + 1) / 2;
@@ -365,8 +410,7 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
     const int l12 = l1 + l2;
     const int qmax = min(min(l1, l2), (l12 - 2 * mm) / 2);
     const double Ap = -2 * m * (n - nu) * (n + nu + 1);
-    const double log_a0 = __ldg(lft + 2 * l1) - __ldg(lft + l1) + __ldg(lft + 2 * l2) - __ldg(lft + l2) + __ldg(lft + l12)
-                        - __ldg(lft + 2 * l12) + __ldg(lft + l12 - 2 * mm) - __ldg(lft + l1 - mm) - __ldg(lft + l2 - mm);
+    const A012 A12 = a12[(size_t)T.mgroup * npair + pid];
 
     const sd *KTM = K + (size_t)(task * 2 + 1) * nu_stride - T.mu; // indexed by nu
     const sd *KTE = K + (size_t)(task * 2 + 0) * nu_stride - T.mu;
@@ -382,18 +426,14 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
     double aqm2 = 0, aqm1 = 1; // a_{q-2}, a_{q-1}
     int lscale2 = 0;
     if (qmax >= 1) {
-        const double a1q = (n + nu - 1.5) * (1 - (2 * n + 2 * nu - 1) / (n4 * (n4 - 1)) * ((m - n) * (m - n + 1) / (2 * n - 1) + (m - nu) * (m - nu + 1) / (2 * nu - 1)));
+        const double a1q = A12.a1;
         const sd kt = KTM[l12 - 2];
         qacc_add(aT, a1q * kt.m, kt.e);
         if (both) { const sd ke = KTE[l12 - 2]; qacc_add(aE, a1q * ke.m, ke.e); }
         aqm2 = 1; aqm1 = a1q;
     }
     if (qmax >= 2) {
-        const double a2q = (2 * n + 2 * nu - 1) * (2 * n + 2 * nu - 7) / 4 * ((2 * n + 2 * nu - 3) / (n4 * (n4 - 1)) * ((2 * n + 2 * nu - 5) / (2 * (n4 - 2) * (n4 - 3))
-                  * ((m - n) * (m - n + 1) * (m - n + 2) * (m - n + 3) / (2 * n - 1) / (2 * n - 3)
-                  + 2 * (m - n) * (m - n + 1) * (m - nu) * (m - nu + 1) / ((2 * n - 1) * (2 * nu - 1))
-                  + (m - nu) * (m - nu + 1) * (m - nu + 2) * (m - nu + 3) / (2 * nu - 1) / (2 * nu - 3)) - (m - n) * (m - n + 1) / (2 * n - 1)
-                  - (m - nu) * (m - nu + 1) / (2 * nu - 1)) + 0.5);
+        const double a2q = A12.a2;
         const sd kt = KTM[l12 - 4];
         qacc_add(aT, a2q * kt.m, kt.e);
         if (both) { const sd ke = KTE[l12 - 4]; qacc_add(aE, a2q * ke.m, ke.e); }
@@ -576,7 +616,7 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
             if (pi == 0) { aT.s = r.m; aT.e = r.e; } else { aE.s = r.m; aE.e = r.e; }
         }
     }
-    const sd a0 = sd_from_log(log_a0, 1);
+    const sd a0 = sd{A12.a0m, A12.a0e};
     const sd rT = sd_mul(a0, sd_norm(aT.s, aT.e));
     if (!isfinite(rT.m) || rT.m == 0.0) atomicOr(status + task, ST_ERR_NONFINITE);
     I_TM[o12] = rT; I_TM[o21] = rT;
@@ -762,8 +802,23 @@ void launch_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, 
     CK(cudaGetLastError());
 }
 
+void launch_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, cudaStream_t st)
+{
+    const long long L = ldim + 2, npair = L * (L + 1) / 2;
+    dim3 g((unsigned)((npair + 127) / 128), ngroup);
+    k_a12<<<g, 128, 0, st>>>(group_m, group_lmin, ngroup, ldim, lft, (A012 *)tab);
+    COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
+}
+
+size_t a12_bytes(int ldim, int ngroup)
+{
+    const size_t L = ldim + 2;
+    return L * (L + 1) / 2 * ngroup * sizeof(A012);
+}
+
 void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
-                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF, float4 *ptabf)
+                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF, float4 *ptabf, const void *a12)
 {
     dim3 gp((pstride + 127) / 128, ntask);
     k_ptab<<<gp, 128, 0, st>>>(tasks, ntask, ptab, ptabf, pstride);
@@ -774,9 +829,9 @@ void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_str
         dim3 gk((nu_stride + 127) / 128, ntask);
         k_kff<<<gk, 128, 0, st>>>(tasks, ntask, K, nu_stride, KF);
         COUNT_LAUNCH(1);
-        k_itab<true><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, KF, ptabf);
+        k_itab<true><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, KF, ptabf, (const A012 *)a12);
     } else
-        k_itab<false><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, nullptr, nullptr);
+        k_itab<false><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, nullptr, nullptr, (const A012 *)a12);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

@@ -112,6 +112,7 @@ struct Task {
     int xi_index;        // row of the Mie table
     int is_pr;           // plate is a perfect reflector: K_TE = -K_TM
     int npanel;          // number of quadrature panels of K
+    int mgroup;          // row of the per-m table of a_0, a_1, a_2 in the current chunk
 };
 
 // per-task result/status slots

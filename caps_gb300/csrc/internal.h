@@ -29,7 +29,10 @@ void launch_kred(const Task *tasks, int ntask, int max_nnu, const double *partM,
 void launch_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, int nx, cudaStream_t st);
 struct ffe;
 void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
-                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF = nullptr, float4 *ptabf = nullptr);
+                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF, float4 *ptabf, const void *a12);
+// a_0, a_1, a_2 per distinct m of a chunk (groups), shared by all frequencies
+void launch_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, cudaStream_t st);
+size_t a12_bytes(int ldim, int ngroup);
 void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv, double *A,
                  size_t lda, size_t mat_stride, int *status, cudaStream_t st);
 void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode, double *trace,

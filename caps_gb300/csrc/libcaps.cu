@@ -97,7 +97,7 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -445,8 +445,9 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     const size_t per_task = (size_t)dim * dim * (caps->precision == CAPS_PREC_MIXED ? 12 : 8) + (size_t)2 * L * L * sizeof(sd) + (size_t)2 * nu_stride * sizeof(sd)
                           + (size_t)nu_stride * sizeof(double2) + (size_t)3 * L * sizeof(sd) + (size_t)dim * 8
                           + (size_t)2 * 256 * nu_stride * 12  // partial sums, up to 256 warps
-                          + (size_t)(4 * (caps->ldim + 4096)) * sizeof(double4); // p tables
-    size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes + g_eng.S32.bytes));
+                          + (size_t)(4 * (caps->ldim + 4096)) * sizeof(double4)  // p tables
+                          + (size_t)L * (L + 1) / 2 * 32;                         // a_0..a_2 table (at most one row per task)
+    size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes + g_eng.S32.bytes + g_eng.a12.bytes));
     int chunk = (int)std::max<size_t>(1, std::min<size_t>(budget / per_task, 65535));
     chunk = std::min(chunk, n);
 
@@ -472,6 +473,23 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         const int nt = std::min(chunk, n - c0);
         CK(cudaEventRecord(g_eng.ev[0], st));
         if (c0 == 0) launch_mie(d_xi, d_eps, nxi, caps->LbyR, lmax_mie, d_lna, d_lnb, st);
+        // group the chunk's tasks by m: a_0, a_1, a_2 of the q-sums depend on (l1, l2, m) only
+        std::map<int, int> gidx;
+        std::vector<int> gm, glm;
+        for (int i = c0; i < c0 + nt; i++) {
+            auto it = gidx.find(tasks[i].m);
+            if (it == gidx.end()) {
+                it = gidx.emplace(tasks[i].m, (int)gm.size()).first;
+                gm.push_back(tasks[i].m);
+                glm.push_back(tasks[i].lmin);
+            }
+            tasks[i].mgroup = it->second;
+        }
+        const int ngroup = (int)gm.size();
+        int *d_gm = (int *)g_eng.gm.get(ngroup * sizeof(int));
+        int *d_glm = (int *)g_eng.glmin.get(ngroup * sizeof(int));
+        h2d(d_gm, gm.data(), ngroup * sizeof(int), st);
+        h2d(d_glm, glm.data(), ngroup * sizeof(int), st);
         Task *d_tasks = (Task *)g_eng.tasks.get(nt * sizeof(Task));
         h2d(d_tasks, tasks.data() + c0, nt * sizeof(Task), st);
         int *d_status = (int *)g_eng.status.get(nt * sizeof(int));
@@ -500,13 +518,15 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
 
         sd *d_I = (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
         double4 *d_ptab = (double4 *)g_eng.ptab.get((size_t)nt * 2 * pstride * sizeof(double4));
+        void *d_a12 = g_eng.a12.get(a12_bytes(ldim, ngroup));
+        launch_a12(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, st);
         if (caps->precision == CAPS_PREC_MIXED) {
             // mixed form: the q-sums in float-float on the FP32 pipe
             ffe *d_KF = (ffe *)g_eng.KF.get((size_t)nt * 2 * nu_stride * 16);
             float4 *d_ptabf = (float4 *)g_eng.ptabf.get((size_t)nt * 2 * pstride * 2 * sizeof(float4));
-            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_KF, d_ptabf);
+            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_KF, d_ptabf, d_a12);
         } else
-            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st);
+            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, nullptr, nullptr, d_a12);
         CK(cudaEventRecord(g_eng.ev[3], st));
 
         const size_t lda = dim, mstride = (size_t)dim * dim;

@@ -143,6 +143,7 @@ extern "C" int caps_logdetD_noalloc(caps_t *self, double xi_, int m, double *log
     T.s = m > 0 ? 1 : 0;
     T.nu_max = 2 * (lmin + ldim);
     T.xi_index = 0;
+    T.mgroup = 0;
     T.is_pr = std::isinf(caps_epsilonm1_plate(self, INFINITY)) ? 1 : 0;
     const int nnu = T.nu_max - T.mu + 1;
     const int nu_stride = (nnu + 31) / 32 * 32;
@@ -170,6 +171,12 @@ extern "C" int caps_logdetD_noalloc(caps_t *self, double xi_, int m, double *log
     double *d_A = C.take<double>((size_t)dim * dim);
     double *d_ld = C.take<double>(dim);
     double *d_trace = C.take<double>(1), *d_res = C.take<double>(1);
+    int *d_gm = C.take<int>(1), *d_glm = C.take<int>(1);
+    // the a_0..a_2 table of this m reuses the K partial-sum region when it fits there
+    // (k_kred has read the partials before k_a12 writes the table, both on one stream);
+    // otherwise nu_stride is small and the table gets a region of its own
+    void *d_a12 = d_pM;
+    if (a12_bytes(ldim, 1) > (size_t)2 * max_warps * nu_stride * sizeof(double)) d_a12 = C.take<unsigned char>(a12_bytes(ldim, 1));
     if (!C.ok) return noalloc_fail(-2, "workspace of this geometry exceeds the 32 MiB scratch array");
 
     // only the status word must start at zero; every other piece is written before it is read
@@ -187,7 +194,11 @@ extern "C" int caps_logdetD_noalloc(caps_t *self, double xi_, int m, double *log
     launch_tables(g_lfac_ptr[dev], d_lft, nlf, d_xtab, nx, st);
     launch_ktab(T.is_pr != 0, d_task, 1, max_warps, d_edges, NOALLOC_MAX_PANELS, d_coef, nu_stride, g_lfac_ptr[dev], d_pM, d_pE, st);
     launch_kred(d_task, 1, nnu, d_pM, d_pE, max_warps, nu_stride, d_K, d_status, st);
-    launch_itab(d_task, 1, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st);
+    const int gm_h[2] = {m, lmin};
+    NA_CK(cudaMemcpyAsync(d_gm, &gm_h[0], sizeof(int), cudaMemcpyHostToDevice, st));
+    NA_CK(cudaMemcpyAsync(d_glm, &gm_h[1], sizeof(int), cudaMemcpyHostToDevice, st));
+    launch_a12(d_gm, d_glm, 1, ldim, d_lft, d_a12, st);
+    launch_itab(d_task, 1, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, nullptr, nullptr, d_a12);
     launch_elem(d_task, 1, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, dim, (size_t)dim * dim, d_status, st);
     const int mode = self->detalg == DETALG_HODLR ? 1 : 0;
     launch_stats(d_task, 1, dim, d_A, dim, (size_t)dim * dim, mode, d_trace, d_res, d_status, st);
