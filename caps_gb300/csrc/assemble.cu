@@ -11,6 +11,7 @@
 //                                                                   integration.c:762-888)
 //   k_stats   per task: Kahan trace, Frobenius norm, shortcut decision (matrix.c:57-119,489-505)
 #include "common.cuh"
+#include "ff.cuh"
 #include "special.cuh"
 #include "kgrid.cuh"
 #include "internal.h"
@@ -246,45 +247,6 @@ CAPS_DEV void qacc_add(QAcc &A, double mant, int ex)
 
 // ---- float-float arithmetic on the FP32 pipe (about 48 significant bits) ----
 // value = h + l with |l| <= ulp(h)/2; error-free transformations of Dekker/Knuth.
-struct ff { float h, l; };
-struct ffe { float h, l; int e, pad; }; // (h + l) * 2^e
-CAPS_DEV ff ff_fast2(float a, float b) { const float s = a + b; return ff{s, b - (s - a)}; }
-CAPS_DEV ff ff_mul(ff x, ff y)
-{
-    const float p = x.h * y.h;
-    float e = fmaf(x.h, y.h, -p);
-    e = fmaf(x.h, y.l, e);
-    e = fmaf(x.l, y.h, e);
-    return ff_fast2(p, e);
-}
-CAPS_DEV ff ff_add(ff x, ff y)
-{
-    const float s = x.h + y.h, bb = s - x.h;
-    float e = (x.h - (s - bb)) + (y.h - bb);
-    e += x.l + y.l;
-    return ff_fast2(s, e);
-}
-CAPS_DEV ff ff_neg(ff x) { return ff{-x.h, -x.l}; }
-CAPS_DEV int fexpo(float x) { return (int)((__float_as_uint(x) >> 23) & 0xff) - 127; }
-// x * 2^k on the bit patterns; flushes to zero below 2^-120
-CAPS_DEV float fshift(float x, int k)
-{
-    const unsigned b = __float_as_uint(x);
-    const int ex = (int)((b >> 23) & 0xff);
-    if (ex == 0 || ex + k <= 6) return 0.0f;
-    return __uint_as_float(b + ((unsigned)k << 23));
-}
-CAPS_DEV ff ff_shift(ff x, int k) { return ff{fshift(x.h, k), fshift(x.l, k)}; }
-CAPS_DEV ff ff_from_d(double x) { const float h = (float)x; return ff{h, (float)(x - (double)h)}; }
-CAPS_DEV double ff_to_d(ff x) { return (double)x.h + (double)x.l; }
-// exact int64 -> float-float (48 of the 63 bits kept) times 2^k
-CAPS_DEV ff ff_from_ll(long long v, int k)
-{
-    const float h = (float)v;
-    const long long r = v - (long long)h;
-    return ff{fshift(h, k), fshift((float)r, k)};
-}
-
 // float-float copy of the K table (mantissa split into two floats, same exponent)
 __global__ void k_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, ffe *KF)
 {
@@ -381,7 +343,7 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
                                               const double *__restrict__ lft, const double2 *__restrict__ xtab,
                                               const double4 *__restrict__ ptab, int pstride, sd *I, int *status,
                                               const ffe *__restrict__ KF, const float4 *__restrict__ ptabf,
-                                              const A012 *__restrict__ a12)
+                                              const A012 *__restrict__ a12, bool ffe_out)
 {
     const int L = ldim + 2;
     const long long npair = (long long)L * (L + 1) / 2;
@@ -506,14 +468,17 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
                 A.S = ff_add(ff_mul(Z, A.S), d < -100 ? ff{0.0f, 0.0f} : ff_shift(t, d));
                 const int ks = fexpo(A.S.h);
                 if (ks > 40 || (ks < -40 && ks > -127)) { A.S = ff_shift(A.S, -ks); A.eS += ks; }
+                // float-float carries ~2^-48 of the q=0 term, so the stop threshold is
+                // e^-40 (2^-57.71) instead of the FP64 form's e^-60: smaller terms, and
+                // the geometric tail after three of them, cannot change the sum
                 if (eb1 != -127) {
                     const int approx = eb1 + eb + Kv.e - eDq - A.e0;
                     bool below;
-                    if (approx <= -89) below = true;
-                    else if (approx >= -84) below = false;
+                    if (approx <= -60) below = true;
+                    else if (approx >= -55) below = false;
                     else {
-                        const float c = approx == -88 ? 2.710008819393852f : approx == -87 ? 1.355004409696926f
-                                      : approx == -86 ? 0.677502204848463f : 0.3387511024242315f;
+                        const float c = approx == -59 ? 2.4490094900568353f : approx == -58 ? 1.2245047450284177f
+                                      : approx == -57 ? 0.6122523725142088f : 0.3061261862571044f;
                         below = fabsf(fshift(bm1.h, -eb1) * Kv.h) < c * fabsf(fshift(Dq.h, -fexpo(Dq.h)) * A.m0);
                     }
                     if (below) { if (++A.count >= 3) { A.on = false; A.D = Dq; A.eD = eD; } }
@@ -619,10 +584,18 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
     const sd a0 = sd{A12.a0m, A12.a0e};
     const sd rT = sd_mul(a0, sd_norm(aT.s, aT.e));
     if (!isfinite(rT.m) || rT.m == 0.0) atomicOr(status + task, ST_ERR_NONFINITE);
-    I_TM[o12] = rT; I_TM[o21] = rT;
     sd rE;
     if (both) rE = sd_mul(a0, sd_norm(aE.s, aE.e));
     else rE = sd{-rT.m, rT.e};
+    if (FF && ffe_out) {
+        // the float-float element kernel reads the table as (h + l) 2^e
+        const ff fT = ff_from_d(rT.m), fE = ff_from_d(rE.m);
+        ffe *FT = reinterpret_cast<ffe *>(I_TM), *FE = reinterpret_cast<ffe *>(I_TE);
+        FT[o12] = FT[o21] = ffe{fT.h, fT.l, rT.e, 0};
+        FE[o12] = FE[o21] = ffe{fE.h, fE.l, rE.e, 0};
+        return;
+    }
+    I_TM[o12] = rT; I_TM[o21] = rT;
     I_TE[o12] = rE; I_TE[o21] = rE;
 }
 
@@ -657,7 +630,9 @@ __global__ void k_elem(const Task *tasks, int ntask, int ldim, const sd *I, cons
     const sd sa1 = Sa[so + i1], sa2 = Sa[so + i2], sb1 = Sb[so + i1], sb2 = Sb[so + i2];
     const double2 uv1 = uv[so + i1], uv2 = uv[so + i2];
     const double m = T.m;
-    auto Iv = [&](const sd *t, int x, int y) { return t[(size_t)x * L + y]; };
+    // the table is symmetric; I(x, y) is read at t[y L + x] so that consecutive threads
+    // (consecutive x) read consecutive entries
+    auto Iv = [&](const sd *t, int x, int y) { return t[(size_t)y * L + x]; };
 
     sd EE, MM, EM = sd{0, 0}, ME = sd{0, 0};
     if (T.m == 0) {
@@ -674,7 +649,7 @@ __global__ void k_elem(const Task *tasks, int ntask, int ldim, const sd *I, cons
         };
         // C_p(l1,l2) = m (v(l2) I(l1,l2+1) - u(l2) I(l1,l2-1)); D_p(l1,l2) = C_p(l2,l1)
         auto Cv = [&](const sd *t) { return sdx(m, sd_add(sdx(uv2.y, Iv(t, i1, i2 + 1)), sdx(-uv2.x, Iv(t, i1, i2 - 1)))); };
-        auto Dv = [&](const sd *t) { return sdx(m, sd_add(sdx(uv1.y, Iv(t, i2, i1 + 1)), sdx(-uv1.x, Iv(t, i2, i1 - 1)))); };
+        auto Dv = [&](const sd *t) { return sdx(m, sd_add(sdx(uv1.y, Iv(t, i1 + 1, i2)), sdx(-uv1.x, Iv(t, i1 - 1, i2)))); };
         EE = sd_mul(sd_mul(sa1, sa2), sd_add(Bv(ITM), sdx(-m2, Iv(ITE, i1, i2))));
         MM = sd_mul(sd_mul(sb1, sb2), sd_add(sdx(m2, Iv(ITM, i1, i2)), sd_neg(Bv(ITE))));
         EM = sd_mul(sd_mul(sa1, sb2), sd_add(Dv(ITM), sd_neg(Cv(ITE))));
@@ -818,7 +793,8 @@ size_t a12_bytes(int ldim, int ngroup)
 }
 
 void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
-                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF, float4 *ptabf, const void *a12)
+                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF, float4 *ptabf, const void *a12,
+                 bool ffe_out)
 {
     dim3 gp((pstride + 127) / 128, ntask);
     k_ptab<<<gp, 128, 0, st>>>(tasks, ntask, ptab, ptabf, pstride);
@@ -829,9 +805,9 @@ void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_str
         dim3 gk((nu_stride + 127) / 128, ntask);
         k_kff<<<gk, 128, 0, st>>>(tasks, ntask, K, nu_stride, KF);
         COUNT_LAUNCH(1);
-        k_itab<true><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, KF, ptabf, (const A012 *)a12);
+        k_itab<true><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, KF, ptabf, (const A012 *)a12, ffe_out);
     } else
-        k_itab<false><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, nullptr, nullptr, (const A012 *)a12);
+        k_itab<false><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, nullptr, nullptr, (const A012 *)a12, false);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

@@ -1,0 +1,229 @@
+// elem_ff.cu -- mixed-precision assembly of 1 - M(xi, m).
+//
+// The mixed form factorises A = 1 - M in FP32 delta form (A - I = -M, see mixed.cu),
+// so an element only has to reach FP32 accuracy once it is assembled; what it must
+// survive on the way is the cancellation inside the B, C, D combinations (up to ~1e5
+// for m = 0).  The combinations are therefore formed in float-float with a separate
+// power-of-two exponent ("fe" below, ~48-bit mantissa) from the float-float I table
+// that k_itab<true> writes, and the result goes straight into the FP32 delta matrix:
+// no FP64 matrix is formed, and the FP64 pipe is used only for the diagonal, which
+// the logdet correction needs in FP64.  Per element block the kernel also leaves a
+// per-warp sum of squares, from which k_stats_ff takes the Frobenius norm for the
+// reference's trace / Mercator shortcuts.
+//
+// Formulas: elements as in libcaps.c:717-831 (caps_M_elem / caps_kernel_M) with A, B,
+// C, D from integration.c:762-888; shortcut decision as in matrix.c:57-119
+// (kernel_logdet) and matrix.c:489-505 (Mercator bound).
+#include "common.cuh"
+#include "ff.cuh"
+#include "internal.h"
+
+namespace capsgpu {
+
+constexpr int EB = 128; // threads per element block (one 2x2 block of M each)
+
+struct fe { float h, l; int e; }; // (h + l) 2^e with |h| in [1,2], or h == 0
+
+// normalise |h| into [1,2); zero (or a result below 2^-126 after cancellation) is 0,
+// inf / NaN are kept so that the element check sees them
+CAPS_DEV fe fe_norm(ff x, int e)
+{
+    const int k = fexpo(x.h);
+    if (k == -127) return fe{0.0f, 0.0f, 0};
+    if (k == 128) return fe{x.h, 0.0f, 0};
+    return fe{fshift(x.h, -k), fshift(x.l, -k), e + k};
+}
+CAPS_DEV fe fe_ld(const ffe &v) { return fe{v.h, v.l, v.e}; }
+CAPS_DEV fe fe_neg(fe a) { return fe{-a.h, -a.l, a.e}; }
+CAPS_DEV fe fe_mul(fe a, fe b) { return fe_norm(ff_mul(ff{a.h, a.l}, ff{b.h, b.l}), a.e + b.e); }
+// c a for a float-float constant c of moderate size
+CAPS_DEV fe fe_scale(ff c, fe a) { return fe_norm(ff_mul(c, ff{a.h, a.l}), a.e); }
+CAPS_DEV fe fe_add(fe a, fe b)
+{
+    if (a.h == 0.0f) return b;
+    if (b.h == 0.0f) return a;
+    if (a.e < b.e) { const fe t = a; a = b; b = t; }
+    const int d = b.e - a.e;
+    const ff bs = d < -60 ? ff{0.0f, 0.0f} : ff_shift(ff{b.h, b.l}, d);
+    return fe_norm(ff_add(ff{a.h, a.l}, bs), a.e);
+}
+// to FP32: values below 2^-120 flush to 0; non-finite or >= 2^126 set *bad
+CAPS_DEV float fe_to_float(fe a, bool &bad)
+{
+    if (a.h == 0.0f) return 0.0f;
+    if (fexpo(a.h) == 128 || a.e > 125) { bad = true; return a.h; }
+    if (a.e < -120) return 0.0f;
+    return fshift(a.h + a.l, a.e);
+}
+CAPS_DEV double fe_to_double(fe a)
+{
+    if (a.h == 0.0f) return 0.0;
+    return shift2((double)a.h + (double)a.l, a.e);
+}
+
+// float-float copies of the per-l scale factors and u, v coefficients (k_scale)
+__global__ void k_scale_ff(int ntask, int L, const sd *Sa, const sd *Sb, const double2 *uv, ffe *Saf, ffe *Sbf, float4 *uvf)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int task = blockIdx.y;
+    if (a >= L || task >= ntask) return;
+    const size_t o = (size_t)task * L + a;
+    const sd sa = Sa[o], sb = Sb[o];
+    const ff fa = ff_from_d(sa.m), fb = ff_from_d(sb.m);
+    Saf[o] = ffe{fa.h, fa.l, sa.e, 0};
+    Sbf[o] = ffe{fb.h, fb.l, sb.e, 0};
+    const double2 w = uv[o];
+    const ff u = ff_from_d(w.x), v = ff_from_d(w.y);
+    uvf[o] = make_float4(u.h, u.l, v.h, v.l);
+}
+
+// grid (ceil(ldim/EB), ldim, ntask); thread (a, b) with a >= b owns rows 2a, 2a+1 and
+// columns 2b, 2b+1 of M.  S receives -M (the delta form of A = 1 - M), lower triangle,
+// column-major with leading dimension n; diag receives the FP64 diagonal of A; part
+// receives, per warp, the sum of squares of M over the warp's blocks (strict lower
+// entries twice).  Blocks entirely above the diagonal exit before doing anything.
+__global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, int ntask, int ldim, const ffe *__restrict__ I,
+                                                const ffe *__restrict__ Saf, const ffe *__restrict__ Sbf,
+                                                const float4 *__restrict__ uvf, float *S, size_t sstride, double *diag,
+                                                float *part, int *status)
+{
+    const int L = ldim + 2, n = 2 * ldim;
+    const int b = blockIdx.y;
+    const int task = blockIdx.z;
+    if (task >= ntask || (int)blockIdx.x < b / EB) return; // uniform per block
+    const int a = blockIdx.x * EB + threadIdx.x;
+    const bool valid = a < ldim && b <= a;
+    float wsum = 0.0f;
+    if (valid) {
+        const Task &T = tasks[task];
+        const ffe *ITM = I + (size_t)(task * 2 + 1) * L * L;
+        const ffe *ITE = I + (size_t)(task * 2 + 0) * L * L;
+        const int i1 = a + 1, i2 = b + 1; // index into [lmin-1, lmin+ldim]
+        const size_t so = (size_t)task * L;
+        const fe sa1 = fe_ld(Saf[so + i1]), sa2 = fe_ld(Saf[so + i2]);
+        const fe sb1 = fe_ld(Sbf[so + i1]), sb2 = fe_ld(Sbf[so + i2]);
+        // the table is symmetric; I(x, y) is read at t[y L + x] so that consecutive
+        // threads (consecutive x) read consecutive entries
+        auto Iv = [&](const ffe *t, int x, int y) { return fe_ld(t[(size_t)y * L + x]); };
+        fe EE, MM, EM{0.0f, 0.0f, 0}, ME{0.0f, 0.0f, 0};
+        if (T.m == 0) {
+            EE = fe_mul(fe_mul(sa1, sa2), Iv(ITM, i1, i2));          // B_TM, A = 0
+            MM = fe_neg(fe_mul(fe_mul(sb1, sb2), Iv(ITE, i1, i2)));  // -B_TE
+        } else {
+            const float mf = (float)T.m, m2h = mf * mf;
+            const ff m1{mf, 0.0f}, m2{m2h, fmaf(mf, mf, -m2h)};
+            const float4 w1 = uvf[so + i1], w2 = uvf[so + i2];
+            const ff U1{w1.x, w1.y}, V1{w1.z, w1.w}, U2{w2.x, w2.y}, V2{w2.z, w2.w};
+            const ff cUU = ff_mul(U1, U2), cVU = ff_mul(V1, U2), cUV = ff_mul(U1, V2), cVV = ff_mul(V1, V2);
+            // B_p = u1 u2 I(l1-1,l2-1) - v1 u2 I(l1+1,l2-1) - u1 v2 I(l1-1,l2+1) + v1 v2 I(l1+1,l2+1)
+            auto Bv = [&](const ffe *t) {
+                fe r = fe_scale(cUU, Iv(t, i1 - 1, i2 - 1));
+                r = fe_add(r, fe_neg(fe_scale(cVU, Iv(t, i1 + 1, i2 - 1))));
+                r = fe_add(r, fe_neg(fe_scale(cUV, Iv(t, i1 - 1, i2 + 1))));
+                return fe_add(r, fe_scale(cVV, Iv(t, i1 + 1, i2 + 1)));
+            };
+            // C_p(l1,l2) = m (v2 I(l1,l2+1) - u2 I(l1,l2-1)); D_p(l1,l2) = C_p(l2,l1)
+            auto Cv = [&](const ffe *t) {
+                return fe_scale(m1, fe_add(fe_scale(V2, Iv(t, i1, i2 + 1)), fe_neg(fe_scale(U2, Iv(t, i1, i2 - 1)))));
+            };
+            auto Dv = [&](const ffe *t) {
+                return fe_scale(m1, fe_add(fe_scale(V1, Iv(t, i1 + 1, i2)), fe_neg(fe_scale(U1, Iv(t, i1 - 1, i2)))));
+            };
+            EE = fe_mul(fe_mul(sa1, sa2), fe_add(Bv(ITM), fe_neg(fe_scale(m2, Iv(ITE, i1, i2)))));
+            MM = fe_mul(fe_mul(sb1, sb2), fe_add(fe_scale(m2, Iv(ITM, i1, i2)), fe_neg(Bv(ITE))));
+            EM = fe_mul(fe_mul(sa1, sb2), fe_add(Dv(ITM), fe_neg(Cv(ITE))));
+            ME = fe_mul(fe_mul(sb1, sa2), fe_add(Cv(ITM), fe_neg(Dv(ITE))));
+        }
+        bool bad = false;
+        const float ee = fe_to_float(EE, bad), mm = fe_to_float(MM, bad);
+        const float em = fe_to_float(EM, bad), me = fe_to_float(ME, bad);
+        if (bad) atomicOr(status + task, ST_ERR_NONFINITE);
+        float *Sm = S + (size_t)task * sstride;
+        const int r0 = 2 * a, c0 = 2 * b;
+        Sm[(size_t)c0 * n + r0] = -ee;
+        Sm[(size_t)c0 * n + r0 + 1] = -me;
+        Sm[(size_t)(c0 + 1) * n + r0 + 1] = -mm;
+        if (a != b) {
+            Sm[(size_t)(c0 + 1) * n + r0] = -em;
+            wsum = 2.0f * (ee * ee + me * me + mm * mm + em * em);
+        } else {
+            diag[(size_t)task * n + r0] = 1.0 - fe_to_double(EE);
+            diag[(size_t)task * n + r0 + 1] = 1.0 - fe_to_double(MM);
+            wsum = ee * ee + mm * mm + 2.0f * me * me;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
+    if ((threadIdx.x & 31) == 0)
+        part[(((size_t)task * ldim + b) * gridDim.x + blockIdx.x) * (EB / 32) + threadIdx.x / 32] = wsum;
+}
+
+// per task: Kahan trace of M over the FP64 diagonal (index order, misc.c:26), the
+// Frobenius norm from the element partials (fixed order), and the reference's
+// shortcut decision: |tr| < 1e-8 -> -tr; dense modes: Mercator when its error bound is
+// below 1e-8 relative; otherwise factorise.
+__global__ void k_stats_ff(int ntask, int ldim, const double *diag, const float *part, int nbx, int mode, double *trace_out,
+                           double *result, int *status)
+{
+    const int task = blockIdx.x;
+    if (task >= ntask) return;
+    const int n = 2 * ldim, per_b = nbx * (EB / 32);
+    const float *p = part + (size_t)task * ldim * per_b;
+    __shared__ double red[256];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < ldim * per_b; i += blockDim.x) {
+        const int b = i / per_b, x = (i % per_b) / (EB / 32);
+        if (x >= b / EB) s += p[i];
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const double *dg = diag + (size_t)task * n;
+    double tr = 0.0, c = 0.0;
+    for (int i = 0; i < n; i++) {
+        const double y = (1.0 - dg[i]) - c;
+        const double t = tr + y;
+        c = (t - tr) - y;
+        tr = t;
+    }
+    trace_out[task] = tr;
+    if (status[task] & ~0xF) { result[task] = NAN; return; }
+    if (fabs(tr) < 1e-8) { result[task] = -tr; status[task] = ST_TRACE; return; }
+    const double fro2 = red[0], fro = sqrt(fro2);
+    if (mode == 0 && fro < 1) {
+        const double merc = -tr - fro2 / 2;
+        const double err = fabs(fro2 / 2 + fro + log1p(-fro));
+        if (fabs(err / merc) < 1e-8) { result[task] = merc; status[task] = ST_MERCATOR; return; }
+    }
+    status[task] = ST_FACTOR;
+}
+
+size_t elem_ff_part_floats(int ldim) { return (size_t)ldim * ((ldim + EB - 1) / EB) * (EB / 32); }
+
+void launch_elem_ff(const Task *tasks, int ntask, int ldim, const sd *Sa, const sd *Sb, const double2 *uv, void *Saf, void *Sbf,
+                    float4 *uvf, const void *I, float *S, size_t sstride, double *diag, float *part, int *status,
+                    cudaStream_t st)
+{
+    const int L = ldim + 2;
+    dim3 gs((L + 127) / 128, ntask);
+    k_scale_ff<<<gs, 128, 0, st>>>(ntask, L, Sa, Sb, uv, (ffe *)Saf, (ffe *)Sbf, uvf);
+    COUNT_LAUNCH(1);
+    dim3 g((ldim + EB - 1) / EB, ldim, ntask);
+    k_elem_ff<<<g, EB, 0, st>>>(tasks, ntask, ldim, (const ffe *)I, (const ffe *)Saf, (const ffe *)Sbf, uvf, S, sstride, diag,
+                                part, status);
+    COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
+}
+
+void launch_stats_ff(int ntask, int ldim, const double *diag, const float *part, int mode, double *trace, double *result,
+                     int *status, cudaStream_t st)
+{
+    k_stats_ff<<<ntask, 256, 0, st>>>(ntask, ldim, diag, part, (ldim + EB - 1) / EB, mode, trace, result, status);
+    COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
+}
+
+} // namespace capsgpu

@@ -29,7 +29,8 @@ void launch_kred(const Task *tasks, int ntask, int max_nnu, const double *partM,
 void launch_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, int nx, cudaStream_t st);
 struct ffe;
 void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
-                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF, float4 *ptabf, const void *a12);
+                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF, float4 *ptabf, const void *a12,
+                 bool ffe_out = false);
 // a_0, a_1, a_2 per distinct m of a chunk (groups), shared by all frequencies
 void launch_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, cudaStream_t st);
 size_t a12_bytes(int ldim, int ngroup);
@@ -37,9 +38,16 @@ void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *
                  size_t lda, size_t mat_stride, int *status, cudaStream_t st);
 void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode, double *trace,
                   double *result, int *status, cudaStream_t st);
+// mixed form: elements in float-float straight into the FP32 delta matrix (elem_ff.cu)
+size_t elem_ff_part_floats(int ldim);
+void launch_elem_ff(const Task *tasks, int ntask, int ldim, const sd *Sa, const sd *Sb, const double2 *uv, void *Saf, void *Sbf,
+                    float4 *uvf, const void *I, float *S, size_t sstride, double *diag, float *part, int *status,
+                    cudaStream_t st);
+void launch_stats_ff(int ntask, int ldim, const double *diag, const float *part, int mode, double *trace, double *result,
+                     int *status, cudaStream_t st);
 void launch_cholesky(int ntask, int n, double *A, size_t lda, size_t mstride, int *status, double *logdiag, cudaStream_t st);
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
-                           const double *trace, double *result, int mode, cudaStream_t st, bool tc = true);
+                           const double *trace, double *result, int mode, cudaStream_t st, bool tc = true, bool convert = true);
 void launch_final(int ntask, int n, const double *logdiag, const double *trace, int *status, double *result, int mode, cudaStream_t st);
 
 } // namespace capsgpu

@@ -97,7 +97,7 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -442,12 +442,17 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     // chunk size from free memory
     size_t freeb = 0, totb = 0;
     CK(cudaMemGetInfo(&freeb, &totb));
-    const size_t per_task = (size_t)dim * dim * (caps->precision == CAPS_PREC_MIXED ? 12 : 8) + (size_t)2 * L * L * sizeof(sd) + (size_t)2 * nu_stride * sizeof(sd)
+    // mixed precision without a dense-M request: elements go straight into the FP32 delta
+    // matrix (no FP64 matrix)
+    const bool ff_elem = caps->precision == CAPS_PREC_MIXED && O.factor && !O.M_out;
+    const size_t mat_bytes = ff_elem ? 4 + 1 : (caps->precision == CAPS_PREC_MIXED ? 12 : 8);
+    const size_t per_task = (size_t)dim * dim * mat_bytes + (size_t)2 * L * L * sizeof(sd) + (size_t)2 * nu_stride * sizeof(sd)
                           + (size_t)nu_stride * sizeof(double2) + (size_t)3 * L * sizeof(sd) + (size_t)dim * 8
                           + (size_t)2 * 256 * nu_stride * 12  // partial sums, up to 256 warps
                           + (size_t)(4 * (caps->ldim + 4096)) * sizeof(double4)  // p tables
                           + (size_t)L * (L + 1) / 2 * 32;                         // a_0..a_2 table (at most one row per task)
-    size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes + g_eng.S32.bytes + g_eng.a12.bytes));
+    size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes + g_eng.S32.bytes
+                                             + g_eng.a12.bytes + g_eng.part.bytes));
     int chunk = (int)std::max<size_t>(1, std::min<size_t>(budget / per_task, 65535));
     chunk = std::min(chunk, n);
 
@@ -524,23 +529,38 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             // mixed form: the q-sums in float-float on the FP32 pipe
             ffe *d_KF = (ffe *)g_eng.KF.get((size_t)nt * 2 * nu_stride * 16);
             float4 *d_ptabf = (float4 *)g_eng.ptabf.get((size_t)nt * 2 * pstride * 2 * sizeof(float4));
-            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_KF, d_ptabf, d_a12);
+            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_KF, d_ptabf, d_a12,
+                        ff_elem);
         } else
             launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, nullptr, nullptr, d_a12);
         CK(cudaEventRecord(g_eng.ev[3], st));
 
         const size_t lda = dim, mstride = (size_t)dim * dim;
-        double *d_A = (double *)g_eng.A.get((size_t)nt * mstride * sizeof(double));
-        launch_elem(d_tasks, nt, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, lda, mstride, d_status, st);
         double *d_trace = (double *)g_eng.trace.get(nt * sizeof(double));
         double *d_res = (double *)g_eng.result.get(nt * sizeof(double));
-        if (O.factor) launch_stats(d_tasks, nt, dim, d_A, lda, mstride, O.mode, d_trace, d_res, d_status, st);
+        double *d_A = nullptr, *d_dg = nullptr;
+        float *d_S = nullptr;
+        if (ff_elem) {
+            d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
+            d_dg = (double *)g_eng.diag.get((size_t)nt * dim * sizeof(double));
+            float *d_part = (float *)g_eng.part.get((size_t)nt * elem_ff_part_floats(ldim) * sizeof(float));
+            void *d_Saf = g_eng.Saf.get((size_t)nt * L * 16), *d_Sbf = g_eng.Sbf.get((size_t)nt * L * 16);
+            float4 *d_uvf = (float4 *)g_eng.uvf.get((size_t)nt * L * sizeof(float4));
+            launch_elem_ff(d_tasks, nt, ldim, d_Sa, d_Sb, d_uv, d_Saf, d_Sbf, d_uvf, d_I, d_S, mstride, d_dg, d_part, d_status, st);
+            launch_stats_ff(nt, ldim, d_dg, d_part, O.mode, d_trace, d_res, d_status, st);
+        } else {
+            d_A = (double *)g_eng.A.get((size_t)nt * mstride * sizeof(double));
+            launch_elem(d_tasks, nt, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, lda, mstride, d_status, st);
+            if (O.factor) launch_stats(d_tasks, nt, dim, d_A, lda, mstride, O.mode, d_trace, d_res, d_status, st);
+        }
         CK(cudaEventRecord(g_eng.ev[4], st));
 
-        if (O.factor && caps->precision == CAPS_PREC_MIXED) {
-            float *d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
-            // CAPS_MIXED_SIMT=1 selects the FP32 FFMA trailing update instead of split-TF32 tensor cores
-            static const bool tc = getenv("CAPS_MIXED_SIMT") == nullptr;
+        // CAPS_MIXED_SIMT=1 selects the FP32 FFMA trailing update instead of split-TF32 tensor cores
+        static const bool tc = getenv("CAPS_MIXED_SIMT") == nullptr;
+        if (ff_elem) {
+            launch_cholesky_mixed(nt, dim, d_dg, 0, dim, d_status, d_S, mstride, d_trace, d_res, O.mode, st, tc, false);
+        } else if (O.factor && caps->precision == CAPS_PREC_MIXED) {
+            d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
             launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_trace, d_res, O.mode, st, tc);
         } else if (O.factor) {
             double *d_ld = (double *)g_eng.logdiag.get((size_t)nt * dim * sizeof(double));

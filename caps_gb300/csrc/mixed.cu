@@ -289,9 +289,11 @@ __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const flo
 }
 
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
-                           const double *trace, double *result, int mode, cudaStream_t st, bool tc)
+                           const double *trace, double *result, int mode, cudaStream_t st, bool tc, bool convert)
 {
-    {
+    // convert: A is the FP64 matrix 1 - M and S receives its delta form here; otherwise S
+    // already holds the delta form and A addresses only the FP64 diagonal (lda 0, mstride n)
+    if (convert) {
         dim3 g(256, ntask);
         k_to_delta32<<<g, 256, 0, st>>>(ntask, n, A, lda, mstride, status, S, sstride);
         COUNT_LAUNCH(1);
