@@ -299,7 +299,6 @@ __global__ void k_ptab(const Task *tasks, int ntask, double4 *ptab, float4 *ptab
 // xi, so every frequency with the same m shares them.  Evaluated with the
 // reference's formulas and order of operations: the m=0 q-sums cancel strongly
 // and the reference's results carry exactly this rounding of a_2.
-struct A012 { double a1, a2, a0m; int a0e, pad; };
 
 __global__ void k_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *__restrict__ lft, A012 *tab)
 {
@@ -338,12 +337,10 @@ __global__ void k_a12(const int *group_m, const int *group_lmin, int ngroup, int
     tab[(size_t)g * npair + pid] = r;
 }
 
-template <bool FF>
 __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride,
                                               const double *__restrict__ lft, const double2 *__restrict__ xtab,
                                               const double4 *__restrict__ ptab, int pstride, sd *I, int *status,
-                                              const ffe *__restrict__ KF, const float4 *__restrict__ ptabf,
-                                              const A012 *__restrict__ a12, bool ffe_out)
+                                              const A012 *__restrict__ a12)
 {
     const int L = ldim + 2;
     const long long npair = (long long)L * (L + 1) / 2;
@@ -401,98 +398,7 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
         if (both) { const sd ke = KTE[l12 - 4]; qacc_add(aE, a2q * ke.m, ke.e); }
         aqm2 = aqm1; aqm1 = a2q;
     }
-    if (FF && qmax >= 3) {
-        // The same recurrence in float-float on the FP32 pipe.  The coefficient
-        // table carries 2^-30 and N(x) a per-pair 2^-sig, so X, Y, Z are scaled by
-        // lam = 2^-(30+sig); the recurrence is homogeneous, so b_q and D_q both pick
-        // up lam^(q-2) and a_q = b_q/D_q, S_q/D_q are unchanged.  b, D, S keep
-        // their own power-of-two exponents and are renormalised every step.
-        const long long Si = l1 + l2 + 1, Di = l1 - l2;
-        auto Nll = [&](int x) -> long long { return ((long long)(x - Si) * (x + Si)) * ((long long)(x - Di) * (x + Di)); };
-        int ip = l12 - 6; // p of q = 3
-        const long long n1st = Nll(ip + 1);
-        const int sig = (n1st == 0 ? 0 : (63 - __clzll(n1st < 0 ? -n1st : n1st))) - 20;
-        // N(x) = a c with a = x^2-(l1+l2+1)^2, c = x^2-(l1-l2)^2 (each |.| < 2^31): each
-        // factor splits exactly into two floats, the product is a float-float product
-        const int sa = sig / 2, sc = sig - sa;
-        auto split = [](int v, int k) { const float h = (float)v; return ff{fshift(h, k), fshift((float)(v - (int)h), k)}; };
-        auto Nf = [&](int x) {
-            const int av = (int)((long long)(x - Si) * (x + Si)), cv = (int)((long long)(x - Di) * (x + Di));
-            return ff_mul(split(av, -sa), split(cv, -sc));
-        };
-        const bool diag = (l1 == l2);
-        const ff Ap2 = diag ? ff{0.0f, 0.0f} : ff_from_d(Ap * Ap * ldexp(1.0, -30 - sig));
-        const float4 *pt = ptabf + ((size_t)task * 2 + (diag ? 1 : 0)) * pstride * 2;
-        const ffe *KFp[2] = {KF + (size_t)(task * 2 + 1) * nu_stride - T.mu, KF + (size_t)(task * 2 + 0) * nu_stride - T.mu};
-        struct PF { ff S; int eS; bool on; int count; ff D; int eD; int e0; float m0; };
-        PF P[2];
-        for (int pi = 0; pi < 2; pi++) {
-            const QAcc &Q = pi == 0 ? aT : aE;
-            const ffe k0 = KFp[pi][l12];
-            P[pi] = PF{ff_from_d(Q.s), Q.e, pi == 0 ? true : both, 0, ff{1.0f, 0.0f}, 0, k0.e, k0.h};
-        }
-        const int e_b = expo(aqm1);
-        ff bm2 = ff_from_d(shift2(aqm2, -e_b)), bm1 = ff_from_d(shift2(aqm1, -e_b));
-        int eb = e_b;
-        ff Dq{1.0f, 0.0f}, Zprev{1.0f, 0.0f};
-        int eD = 0;
-        ff N3 = Nf(ip + 3), N4 = Nf(ip + 4);
-        for (int q = 3; q <= qmax && (P[0].on || P[1].on); q++, ip -= 2) {
-            const ff N1 = Nf(ip + 1), N2 = Nf(ip + 2);
-            const float4 kh = pt[2 * ip], kl = pt[2 * ip + 1];
-            const ff X = ff_add(Ap2, ff_add(ff_mul(ff{kh.y, kl.y}, N2), ff_mul(ff{kh.z, kl.z}, N3)));
-            const ff Y = ff_mul(ff{kh.w, kl.w}, N4);
-            const ff Z = ff_mul(ff{kh.x, kl.x}, N1);
-            const ff b = ff_add(ff_mul(X, bm1), ff_neg(ff_mul(ff_mul(Y, Zprev), bm2)));
-            Dq = ff_mul(Dq, Z);
-            N3 = N1; N4 = N2; Zprev = Z;
-            bm2 = bm1; bm1 = b;
-            {
-                const int kb = fexpo(bm1.h);
-                if (kb > 40 || (kb < -40 && kb > -127)) { bm1 = ff_shift(bm1, -kb); bm2 = ff_shift(bm2, -kb); eb += kb; }
-                const int kd = fexpo(Dq.h);
-                if (kd > 40 || kd < -40) { Dq = ff_shift(Dq, -kd); eD += kd; }
-            }
-            const int eb1 = fexpo(bm1.h);
-            const int eDq = fexpo(Dq.h) + eD;
-#pragma unroll
-            for (int pi = 0; pi < 2; pi++) {
-                PF &A = P[pi];
-                if (!A.on) continue;
-                const ffe Kv = KFp[pi][ip];
-                const ff t = ff_mul(bm1, ff{Kv.h, Kv.l});
-                const int et = eb + Kv.e;
-                int d = et - A.eS;
-                if (fexpo(A.S.h) == -127) { A.eS = et; d = 0; }
-                else if (d > 30) { A.S = ff_shift(A.S, -d); A.eS = et; d = 0; }
-                A.S = ff_add(ff_mul(Z, A.S), d < -100 ? ff{0.0f, 0.0f} : ff_shift(t, d));
-                const int ks = fexpo(A.S.h);
-                if (ks > 40 || (ks < -40 && ks > -127)) { A.S = ff_shift(A.S, -ks); A.eS += ks; }
-                // float-float carries ~2^-48 of the q=0 term, so the stop threshold is
-                // e^-40 (2^-57.71) instead of the FP64 form's e^-60: smaller terms, and
-                // the geometric tail after three of them, cannot change the sum
-                if (eb1 != -127) {
-                    const int approx = eb1 + eb + Kv.e - eDq - A.e0;
-                    bool below;
-                    if (approx <= -60) below = true;
-                    else if (approx >= -55) below = false;
-                    else {
-                        const float c = approx == -59 ? 2.4490094900568353f : approx == -58 ? 1.2245047450284177f
-                                      : approx == -57 ? 0.6122523725142088f : 0.3061261862571044f;
-                        below = fabsf(fshift(bm1.h, -eb1) * Kv.h) < c * fabsf(fshift(Dq.h, -fexpo(Dq.h)) * A.m0);
-                    }
-                    if (below) { if (++A.count >= 3) { A.on = false; A.D = Dq; A.eD = eD; } }
-                    else A.count = 0;
-                }
-            }
-        }
-        for (int pi = 0; pi < 2; pi++) {
-            PF &A = P[pi];
-            if (A.on) { A.D = Dq; A.eD = eD; }
-            const sd r = sd_norm(ff_to_d(A.S) / ff_to_d(A.D), A.eS - A.eD);
-            if (pi == 0) { aT.s = r.m; aT.e = r.e; } else { aE.s = r.m; aE.e = r.e; }
-        }
-    } else if (qmax >= 3) {
+    if (qmax >= 3) {
         // Division-free form of the recurrence: a_q = b_q / D_q with
         //   b_q = X_q b_{q-1} - Y_q Z_{q-1} b_{q-2},  D_q = D_{q-1} Z_q,
         //   X_q = Ap^2 + K1 alpha(p+2) + K2 alpha(p+3), Y_q = K3 alpha(p+4), Z_q = K0 alpha(p+1)
@@ -587,14 +493,6 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
     sd rE;
     if (both) rE = sd_mul(a0, sd_norm(aE.s, aE.e));
     else rE = sd{-rT.m, rT.e};
-    if (FF && ffe_out) {
-        // the float-float element kernel reads the table as (h + l) 2^e
-        const ff fT = ff_from_d(rT.m), fE = ff_from_d(rE.m);
-        ffe *FT = reinterpret_cast<ffe *>(I_TM), *FE = reinterpret_cast<ffe *>(I_TE);
-        FT[o12] = FT[o21] = ffe{fT.h, fT.l, rT.e, 0};
-        FE[o12] = FE[o21] = ffe{fE.h, fE.l, rE.e, 0};
-        return;
-    }
     I_TM[o12] = rT; I_TM[o21] = rT;
     I_TE[o12] = rE; I_TE[o21] = rE;
 }
@@ -792,22 +690,27 @@ size_t a12_bytes(int ldim, int ngroup)
     return L * (L + 1) / 2 * ngroup * sizeof(A012);
 }
 
-void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
-                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF, float4 *ptabf, const void *a12,
-                 bool ffe_out)
+void launch_ptab_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, double4 *ptab, float4 *ptabf, int pstride, ffe *KF,
+                     cudaStream_t st)
 {
     dim3 gp((pstride + 127) / 128, ntask);
     k_ptab<<<gp, 128, 0, st>>>(tasks, ntask, ptab, ptabf, pstride);
     COUNT_LAUNCH(1);
+    dim3 gk((nu_stride + 127) / 128, ntask);
+    k_kff<<<gk, 128, 0, st>>>(tasks, ntask, K, nu_stride, KF);
+    COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
+}
+
+void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
+                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, const void *a12)
+{
+    dim3 gp((pstride + 127) / 128, ntask);
+    k_ptab<<<gp, 128, 0, st>>>(tasks, ntask, ptab, nullptr, pstride);
+    COUNT_LAUNCH(1);
     const long long L = ldim + 2, npair = L * (L + 1) / 2;
     dim3 g((unsigned)((npair + 127) / 128), ntask);
-    if (KF) {
-        dim3 gk((nu_stride + 127) / 128, ntask);
-        k_kff<<<gk, 128, 0, st>>>(tasks, ntask, K, nu_stride, KF);
-        COUNT_LAUNCH(1);
-        k_itab<true><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, KF, ptabf, (const A012 *)a12, ffe_out);
-    } else
-        k_itab<false><<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, nullptr, nullptr, (const A012 *)a12, false);
+    k_itab<<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, (const A012 *)a12);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

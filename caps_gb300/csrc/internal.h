@@ -29,8 +29,14 @@ void launch_kred(const Task *tasks, int ntask, int max_nnu, const double *partM,
 void launch_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, int nx, cudaStream_t st);
 struct ffe;
 void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
-                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, ffe *KF, float4 *ptabf, const void *a12,
-                 bool ffe_out = false);
+                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, const void *a12);
+void launch_ptab_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, double4 *ptab, float4 *ptabf, int pstride, ffe *KF,
+                     cudaStream_t st);
+// mixed form: q-sums with one a_q recurrence per (pair, subgroup of same-m tasks) (itab_ff.cu)
+int itab_group_size();
+void launch_itab_grp(const Task *tasks, int ntask, const int4 *groups, int ngroups, int ldim, const sd *K, int nu_stride,
+                     double4 *ptab, int pstride, ffe *KF, float4 *ptabf, const void *a12, void *Iout, bool ffe_out, int *status,
+                     cudaStream_t st);
 // a_0, a_1, a_2 per distinct m of a chunk (groups), shared by all frequencies
 void launch_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, cudaStream_t st);
 size_t a12_bytes(int ldim, int ngroup);

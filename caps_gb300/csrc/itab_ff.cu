@@ -1,0 +1,248 @@
+// itab_ff.cu -- mixed-precision I q-sums, one a_q recurrence shared by every
+// frequency of the same m.
+//
+// I_{l1 l2,p}^{(m)}(xi) = a_0 sum_q a_q K_{l1+l2-2q,p}(xi)        (integration.c:491-609)
+//
+// The coefficients a_q (eqs. (26)-(30) of the reference's integration.c) depend on
+// (l1, l2, m) only; the frequency enters through K alone.  A thread therefore owns one
+// (l1 >= l2) pair and a subgroup of up to G tasks that share m: it runs the projective
+// recurrence b_q = X b_{q-1} - Y Z_{q-1} b_{q-2}, D_q = Z D_{q-1} once, forms
+// a_q = b_q / D_q with one float-float division per q, and each task and polarisation
+// only accumulates a_q K_q and applies the reference's early stop to its own terms.
+// Everything is float-float (two FP32 words) with separate power-of-two exponents;
+// the FP64 pipe is touched only by per-pair set-up.
+//
+// The early stop is the reference's rule (three consecutive terms below a threshold
+// relative to the q = 0 term, integration.c:563-575) with the threshold e^-40 instead
+// of e^-60: float-float carries ~2^-48 of the q = 0 term, so smaller terms, and the
+// geometric tail after three of them, cannot change the sum.
+#include "common.cuh"
+#include "ff.cuh"
+#include "internal.h"
+
+namespace capsgpu {
+
+// float-float quotient x / y (Dekker 1971: one correction of the leading quotient)
+CAPS_DEV ff ff_div(ff x, ff y)
+{
+    const float r = __frcp_rn(y.h);
+    const float q1 = x.h * r;
+    const ff p = ff_mul(ff{q1, 0.0f}, y);
+    const ff rem = ff_add(x, ff_neg(p));
+    return ff_fast2(q1, rem.h * r);
+}
+
+struct IAcc {
+    float h, l; // running sum (h + l) 2^e
+    int e;
+    int e0;     // exponent and mantissa of the q = 0 term
+    float m0;
+    int count;
+    bool on;
+};
+
+// sum += t 2^et, keeping |h| within 2^+-40 by exact power-of-two shifts
+CAPS_DEV void iacc_add(IAcc &A, ff t, int et)
+{
+    if (t.h == 0.0f) return;
+    if (A.h == 0.0f) { A.h = t.h; A.l = t.l; A.e = et; return; }
+    int d = et - A.e;
+    if (d > 30) {
+        const ff s = ff_shift(ff{A.h, A.l}, -d);
+        A.h = s.h; A.l = s.l; A.e = et; d = 0;
+    }
+    // 2^d for -100 <= d <= 30 is a normal float: the alignment is one exact multiply
+    const float p2 = __uint_as_float((unsigned)(127 + d) << 23);
+    const ff s = ff_add(ff{A.h, A.l}, d < -100 ? ff{0.0f, 0.0f} : ff{t.h * p2, t.l * p2});
+    A.h = s.h; A.l = s.l;
+    const int ks = fexpo(A.h);
+    if (ks > 40 || (ks < -40 && ks > -127)) {
+        const ff r = ff_shift(ff{A.h, A.l}, -ks);
+        A.h = r.h; A.l = r.l; A.e += ks;
+    }
+}
+
+// grid (ceil(npair/128), ngroups); groups[g] = {first task, count <= G, a_0..a_2 row}.
+// The tasks of a group are consecutive, share m (hence lmin, mu, the p table and the
+// a_0..a_2 row) and the material.  Output: I tables as float-float (ffe) or, with
+// ffe_out false, as scaled doubles.
+template <int G>
+__global__ void __launch_bounds__(128, 3) k_itab_grp(const Task *tasks, const int4 *groups, int ngroups, int ldim,
+                                                  const ffe *__restrict__ KF, int nu_stride, const float4 *__restrict__ ptabf,
+                                                  int pstride, const A012 *__restrict__ a12, void *Iout, bool ffe_out,
+                                                  int *status)
+{
+    const int L = ldim + 2;
+    const long long npair = (long long)L * (L + 1) / 2;
+    const long long pid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int gi = blockIdx.y;
+    if (pid >= npair || gi >= ngroups) return;
+    const int4 grp = groups[gi];
+    const int t0 = grp.x, ng = grp.y;
+    // pair index -> (a1 >= a2); the float root is exact to +-1 and corrected in integers
+    int a1 = (int)((sqrtf(8.0f * (float)pid + 1.0f) - 1.0f) * 0.5f);
+    while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
+    while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
+    const int a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
+
+    const Task &T = tasks[t0];
+    const int l1 = T.lmin - 1 + a1, l2 = T.lmin - 1 + a2;
+    const int mm = T.m > 0 ? T.m : 1;
+    const size_t o12 = (size_t)a1 * L + a2, o21 = (size_t)a2 * L + a1;
+    const size_t LL = (size_t)L * L;
+    auto store = [&](int g, int pol, float h, float l, int e) { // pol 1 = TM, 0 = TE (table order of K and I)
+        const size_t base = (size_t)((t0 + g) * 2 + pol) * LL;
+        if (ffe_out) {
+            ffe *F = reinterpret_cast<ffe *>(Iout) + base;
+            F[o12] = F[o21] = ffe{h, l, e, 0};
+        } else {
+            sd *D = reinterpret_cast<sd *>(Iout) + base;
+            const sd v = sd_norm((double)h + (double)l, e);
+            D[o12] = D[o21] = v;
+        }
+    };
+    if (l2 < mm || l2 < T.m || l1 < 1) { // I = 0 for l < m (integration.c:631)
+        for (int g = 0; g < ng; g++) { store(g, 1, 0.0f, 0.0f, 0); store(g, 0, 0.0f, 0.0f, 0); }
+        return;
+    }
+    const bool both = !T.is_pr;
+    const int l12 = l1 + l2;
+    const int qmax = min(min(l1, l2), (l12 - 2 * mm) / 2);
+    const A012 A12 = a12[(size_t)grp.z * npair + pid];
+
+    // accumulators: j = 2 g + (0: TM, 1: TE); K table of task t, polarisation p at
+    // KF[(t*2 + p) nu_stride - mu + nu] with p = 1 for TM
+    IAcc acc[2 * G];
+    auto Kat = [&](int j, int nu) { return KF[(size_t)((t0 + (j >> 1)) * 2 + ((j & 1) ? 0 : 1)) * nu_stride + (nu - T.mu)]; };
+#pragma unroll
+    for (int j = 0; j < 2 * G; j++) {
+        const bool live = (j >> 1) < ng && ((j & 1) == 0 || both);
+        IAcc &A = acc[j];
+        A = IAcc{0.0f, 0.0f, 0, 0, 1.0f, 0, live};
+        if (!live) continue;
+        const ffe k0 = Kat(j, l12);
+        A.h = k0.h; A.l = k0.l; A.e = k0.e; A.e0 = k0.e; A.m0 = fabsf(k0.h);
+        if (qmax >= 1) { const ffe k = Kat(j, l12 - 2); iacc_add(A, ff_mul(ff_from_d(A12.a1), ff{k.h, k.l}), k.e); }
+        if (qmax >= 2) { const ffe k = Kat(j, l12 - 4); iacc_add(A, ff_mul(ff_from_d(A12.a2), ff{k.h, k.l}), k.e); }
+    }
+
+    if (qmax >= 3) {
+        // X, Y, Z carry lam = 2^-(30+sig) (p table 2^-30, N(x) 2^-sig); b_q and D_q both
+        // pick up lam^(q-2), so a_q = b_q / D_q is unchanged
+        const long long Si = l1 + l2 + 1, Di = l1 - l2;
+        int ip = l12 - 6; // p of q = 3
+        const long long n1st = ((long long)(ip + 1 - Si) * (ip + 1 + Si)) * ((long long)(ip + 1 - Di) * (ip + 1 + Di));
+        const int sig = (n1st == 0 ? 0 : (63 - __clzll(n1st < 0 ? -n1st : n1st))) - 20;
+        const int sa = sig / 2, sc = sig - sa;
+        const float fS = (float)Si, fD = (float)Di;
+        const float sA = __uint_as_float((unsigned)(127 - sa) << 23), sC = __uint_as_float((unsigned)(127 - sc) << 23);
+        // N(x) = (x^2 - S^2)(x^2 - D^2): each factor is an exact float-float product of
+        // two integers below 2^24 (fmaf gives the rounding error exactly), scaled by a
+        // power of two (-20 <= sig <= 41, so 2^-sa and 2^-sc are normal and the scaling exact)
+        auto Nf = [&](float x) {
+            const float p1 = x - fS, p2 = x + fS, q1 = x - fD, q2 = x + fD;
+            const float ah = p1 * p2, ch = q1 * q2;
+            const ff av{ah * sA, fmaf(p1, p2, -ah) * sA}, cv{ch * sC, fmaf(q1, q2, -ch) * sC};
+            return ff_mul(av, cv);
+        };
+        const bool diag = (l1 == l2);
+        const double Ap = -2.0 * mm * (double)(l1 - l2) * (double)(l1 + l2 + 1);
+        const ff Ap2 = diag ? ff{0.0f, 0.0f} : ff_from_d(Ap * Ap * ldexp(1.0, -30 - sig));
+        const float4 *pt = ptabf + ((size_t)t0 * 2 + (diag ? 1 : 0)) * pstride * 2;
+        // b_{q-2} = a_1, b_{q-1} = a_2, D_2 = 1, normalised by the exponent of a_2
+        const int e_b = expo(A12.a2);
+        ff bm2 = ff_from_d(shift2(A12.a1, -e_b)), bm1 = ff_from_d(shift2(A12.a2, -e_b));
+        int eb = e_b, eD = 0;
+        ff Dq{1.0f, 0.0f}, Zprev{1.0f, 0.0f};
+        float fx = (float)(ip + 1);
+        ff N3 = Nf(fx + 2.0f), N4 = Nf(fx + 3.0f);
+        bool any = true;
+        for (int q = 3; q <= qmax && any; q++, ip -= 2, fx -= 2.0f) {
+            const ff N1 = Nf(fx), N2 = Nf(fx + 1.0f);
+            const float4 kh = pt[2 * ip], kl = pt[2 * ip + 1];
+            const ff X = ff_add(Ap2, ff_add(ff_mul(ff{kh.y, kl.y}, N2), ff_mul(ff{kh.z, kl.z}, N3)));
+            const ff Y = ff_mul(ff{kh.w, kl.w}, N4);
+            const ff Z = ff_mul(ff{kh.x, kl.x}, N1);
+            const ff b = ff_add(ff_mul(X, bm1), ff_neg(ff_mul(ff_mul(Y, Zprev), bm2)));
+            Dq = ff_mul(Dq, Z);
+            N3 = N1; N4 = N2; Zprev = Z;
+            bm2 = bm1; bm1 = b;
+            {
+                const int kb = fexpo(bm1.h);
+                if (kb > 40 || (kb < -40 && kb > -127)) { bm1 = ff_shift(bm1, -kb); bm2 = ff_shift(bm2, -kb); eb += kb; }
+                const int kd = fexpo(Dq.h);
+                if (kd > 40 || kd < -40) { Dq = ff_shift(Dq, -kd); eD += kd; }
+            }
+            const ff aq = ff_div(bm1, Dq);
+            const int ea = eb - eD;
+            any = false;
+#pragma unroll
+            for (int j = 0; j < 2 * G; j++) {
+                IAcc &A = acc[j];
+                if (!A.on) continue;
+                const ffe Kv = Kat(j, ip);
+                const ff t = ff_mul(aq, ff{Kv.h, Kv.l});
+                const int et = ea + Kv.e;
+                iacc_add(A, t, et);
+                if (t.h != 0.0f) {
+                    // |term| / |q=0 term| = (mt / m0) 2^approx with mt, m0 in [1,2):
+                    // below e^-40 = 2^-57.708 for approx <= -59, above for approx >= -56
+                    const int kt = fexpo(t.h);
+                    const int approx = kt + et - A.e0;
+                    bool below;
+                    if (approx <= -59) below = true;
+                    else if (approx >= -56) below = false;
+                    else below = fabsf(fshift(t.h, -kt)) < (approx == -58 ? 1.2245047450284177f : 0.6122523725142088f) * A.m0;
+                    if (below) { if (++A.count >= 3) A.on = false; }
+                    else A.count = 0;
+                }
+                any |= A.on;
+            }
+        }
+    }
+
+    // I = a_0 sum; TE of a perfect reflector is -TM
+    const ff a0f = ff_from_d(A12.a0m);
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+        if (g >= ng) break;
+        const IAcc &AT = acc[2 * g];
+        ff r = ff_mul(a0f, ff{AT.h, AT.l});
+        int k = fexpo(r.h);
+        if (k == -127 || k == 128) atomicOr(status + t0 + g, ST_ERR_NONFINITE);
+        if (k == 128 || k == -127) k = 0;
+        r = ff_shift(r, -k);
+        const int eT = AT.e + A12.a0e + k;
+        store(g, 1, r.h, r.l, eT);
+        if (both) {
+            const IAcc &AE = acc[2 * g + 1];
+            ff s = ff_mul(a0f, ff{AE.h, AE.l});
+            int ke = fexpo(s.h);
+            if (ke == 128 || ke == -127) ke = 0;
+            s = ff_shift(s, -ke);
+            store(g, 0, s.h, s.l, AE.e + A12.a0e + ke);
+        } else
+            store(g, 0, -r.h, -r.l, eT);
+    }
+}
+
+// tasks per subgroup.  Measured on the R/L=150 free energy: 2 beats 1 (the recurrence is
+// shared) and 4 (145 registers cost occupancy, and a subgroup runs to the term count of
+// its slowest frequency, which grows linearly with the Matsubara index)
+constexpr int IGRP = 2;
+int itab_group_size() { return IGRP; }
+
+void launch_itab_grp(const Task *tasks, int ntask, const int4 *groups, int ngroups, int ldim, const sd *K, int nu_stride,
+                     double4 *ptab, int pstride, ffe *KF, float4 *ptabf, const void *a12, void *Iout, bool ffe_out, int *status,
+                     cudaStream_t st)
+{
+    launch_ptab_kff(tasks, ntask, K, nu_stride, ptab, ptabf, pstride, KF, st);
+    const long long L = ldim + 2, npair = L * (L + 1) / 2;
+    dim3 g((unsigned)((npair + 127) / 128), ngroups);
+    k_itab_grp<IGRP><<<g, 128, 0, st>>>(tasks, groups, ngroups, (int)ldim, KF, nu_stride, ptabf, pstride, (const A012 *)a12, Iout,
+                                        ffe_out, status);
+    COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
+}
+
+} // namespace capsgpu

@@ -97,7 +97,7 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -405,29 +405,35 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     const bool is_pr = std::isinf(caps_epsilonm1_plate(caps, INFINITY));
     std::map<double, int> xi_index;
     std::vector<double> xis, eps_sphere;
+    // tasks run in (m, xi) order: consecutive frequencies of one m share the I recurrence;
+    // results go back to the caller's order through `order`
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ms[a] != ms[b] ? ms[a] < ms[b] : xi_[a] < xi_[b]; });
     std::vector<Task> tasks(n);
     int lmax_mie = 1;
     for (int i = 0; i < n; i++) {
-        auto it = xi_index.find(xi_[i]);
+        const int src = order[i];
+        auto it = xi_index.find(xi_[src]);
         int ix;
         if (it == xi_index.end()) {
             ix = (int)xis.size();
-            xi_index[xi_[i]] = ix;
-            xis.push_back(xi_[i]);
-            eps_sphere.push_back(caps_epsilonm1_sphere(caps, xi_[i]));
+            xi_index[xi_[src]] = ix;
+            xis.push_back(xi_[src]);
+            eps_sphere.push_back(caps_epsilonm1_sphere(caps, xi_[src]));
         } else ix = it->second;
         Task &T = tasks[i];
-        T.xi_ = xi_[i];
-        T.alpha = 2 * xi_[i];
-        T.epsm1_plate = caps_epsilonm1_plate(caps, xi_[i]);
+        T.xi_ = xi_[src];
+        T.alpha = 2 * xi_[src];
+        T.epsm1_plate = caps_epsilonm1_plate(caps, xi_[src]);
         T.epsm1_sphere = eps_sphere[ix];
-        T.m = ms[i];
-        TERMINATE(ms[i] < 0, "m must be non-negative");
-        T.lmin = lmin_of(caps, ms[i]);
+        T.m = ms[src];
+        TERMINATE(ms[src] < 0, "m must be non-negative");
+        T.lmin = lmin_of(caps, ms[src]);
         // the I recurrence forms (x^2-(l1+l2+1)^2)(x^2-(l1-l2)^2) exactly in 64-bit integers
         TERMINATE(T.lmin + ldim > 27000, "l window beyond 27000 (lmin+ldim=%d) is not supported", T.lmin + ldim);
-        T.mu = 2 * std::max(ms[i], 1);
-        T.s = ms[i] > 0 ? 1 : 0;
+        T.mu = 2 * std::max(ms[src], 1);
+        T.s = ms[src] > 0 ? 1 : 0;
         T.nu_max = 2 * (T.lmin + ldim);
         T.xi_index = ix;
         T.is_pr = is_pr ? 1 : 0;
@@ -491,12 +497,22 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             tasks[i].mgroup = it->second;
         }
         const int ngroup = (int)gm.size();
+        // subgroups of at most itab_group_size() consecutive tasks of one m for the mixed q-sums
+        std::vector<int4> sub;
+        for (int i = c0; i < c0 + nt; i++) {
+            if (sub.empty() || tasks[i].m != tasks[c0 + sub.back().x].m || sub.back().y == itab_group_size())
+                sub.push_back(make_int4(i - c0, 0, tasks[i].mgroup, 0));
+            sub.back().y++;
+        }
+        const int nsub = (int)sub.size();
         int *d_gm = (int *)g_eng.gm.get(ngroup * sizeof(int));
         int *d_glm = (int *)g_eng.glmin.get(ngroup * sizeof(int));
         h2d(d_gm, gm.data(), ngroup * sizeof(int), st);
         h2d(d_glm, glm.data(), ngroup * sizeof(int), st);
         Task *d_tasks = (Task *)g_eng.tasks.get(nt * sizeof(Task));
         h2d(d_tasks, tasks.data() + c0, nt * sizeof(Task), st);
+        int4 *d_sub = (int4 *)g_eng.groups.get(nsub * sizeof(int4));
+        h2d(d_sub, sub.data(), nsub * sizeof(int4), st);
         int *d_status = (int *)g_eng.status.get(nt * sizeof(int));
         CK(cudaMemsetAsync(d_status, 0, nt * sizeof(int), st));
         double *d_edges = (double *)g_eng.edges.get((size_t)nt * (MAX_PANELS + 1) * sizeof(double));
@@ -529,10 +545,10 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             // mixed form: the q-sums in float-float on the FP32 pipe
             ffe *d_KF = (ffe *)g_eng.KF.get((size_t)nt * 2 * nu_stride * 16);
             float4 *d_ptabf = (float4 *)g_eng.ptabf.get((size_t)nt * 2 * pstride * 2 * sizeof(float4));
-            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_KF, d_ptabf, d_a12,
-                        ff_elem);
+            launch_itab_grp(d_tasks, nt, d_sub, nsub, ldim, d_K, nu_stride, d_ptab, pstride, d_KF, d_ptabf, d_a12, d_I, ff_elem,
+                            d_status, st);
         } else
-            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, nullptr, nullptr, d_a12);
+            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_a12);
         CK(cudaEventRecord(g_eng.ev[3], st));
 
         const size_t lda = dim, mstride = (size_t)dim * dim;
@@ -570,8 +586,9 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         CK(cudaEventRecord(g_eng.ev[5], st));
 
         std::vector<int> hst(nt);
+        std::vector<double> hres(nt);
         d2h(hst.data(), d_status, nt * sizeof(int), st);
-        if (O.factor) d2h(out + c0, d_res, nt * sizeof(double), st);
+        if (O.factor) d2h(hres.data(), d_res, nt * sizeof(double), st);
         if (O.M_out) {
             // dense row-major M from the lower triangle of 1-M
             std::vector<double> Ah((size_t)dim * dim);
@@ -595,11 +612,13 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         CK(cudaEventElapsedTime(&f, g_eng.ev[0], g_eng.ev[5])); tsum[5] += f;
         g_counters.nmat += nt;
         for (int i = 0; i < nt; i++) {
+            const int dst = order[c0 + i];
+            if (O.factor) out[dst] = hres[i];
             if (hst[i] == ST_FACTOR) { g_counters.nfactor++; g_counters.factor_flops += (double)dim * dim * dim / 3.0; }
-            if (status_out) status_out[c0 + i] = hst[i];
+            if (status_out) status_out[dst] = hst[i];
             if (hst[i] & ~0xF) {
                 nerr++;
-                set_error("matrix %d (xi_=%.17g, m=%d): status %d", c0 + i, tasks[c0 + i].xi_, tasks[c0 + i].m, hst[i]);
+                set_error("matrix %d (xi_=%.17g, m=%d): status %d", dst, tasks[c0 + i].xi_, tasks[c0 + i].m, hst[i]);
             }
         }
     }

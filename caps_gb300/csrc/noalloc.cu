@@ -198,7 +198,7 @@ extern "C" int caps_logdetD_noalloc(caps_t *self, double xi_, int m, double *log
     NA_CK(cudaMemcpyAsync(d_gm, &gm_h[0], sizeof(int), cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(d_glm, &gm_h[1], sizeof(int), cudaMemcpyHostToDevice, st));
     launch_a12(d_gm, d_glm, 1, ldim, d_lft, d_a12, st);
-    launch_itab(d_task, 1, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, nullptr, nullptr, d_a12);
+    launch_itab(d_task, 1, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_a12);
     launch_elem(d_task, 1, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, dim, (size_t)dim * dim, d_status, st);
     const int mode = self->detalg == DETALG_HODLR ? 1 : 0;
     launch_stats(d_task, 1, dim, d_A, dim, (size_t)dim * dim, mode, d_trace, d_res, d_status, st);
