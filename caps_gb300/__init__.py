@@ -46,7 +46,9 @@ def _load():
         "caps_M_init": (vp, [vp, i, d]), "caps_M_elem": (d, [vp, i, i, C.c_char, C.c_char]),
         "caps_M_free": (None, [vp]), "caps_kernel_M": (d, [i, i, vp]),
         "caps_logdetD0": (None, [vp, i, d, dp, dp, dp]),
-        "caps_ht_drude": (d, [vp]), "caps_ht_perf": (d, [vp, d]),
+        "caps_ht_drude": (d, [vp]), "caps_ht_perf": (d, [vp, d]), "caps_ht_plasma": (d, [vp, d, d]),
+        "caps_integrate_plasma_init": (vp, [vp, d, d]), "caps_integrate_plasma_free": (None, [vp]),
+        "caps_integrate_plasma": (d, [vp, i, i, i, dp, dp]),
         "caps_free_energy": (d, [vp, d, d, d, C.POINTER(_EnergyInfo)]),
         "caps_gpu_set_precision": (i, [vp, i]),
         "caps_gpu_last_error": (C.c_char_p, []),
@@ -205,6 +207,29 @@ class Caps:
         ee, mm = C.c_double(np.nan), C.c_double(np.nan)
         lib.caps_logdetD0(self._h, int(m), 0.0, C.byref(ee) if EE else None, C.byref(mm) if MM else None, None)
         return ee.value, mm.value
+
+    def logdetD0_plasma(self, m, omegap):
+        """xi=0 MM block of the plasma model; omegap in rad/s"""
+        v = C.c_double(np.nan)
+        lib.caps_logdetD0(self._h, int(m), float(omegap), None, None, C.byref(v))
+        return v.value
+
+    def ht_plasma(self, omegap, eps):
+        """high-temperature free energy of the plasma model (units of kB T); omegap in rad/s"""
+        return lib.caps_ht_plasma(self._h, float(omegap), float(eps))
+
+    def integrate_plasma(self, omegap, pairs):
+        """[(I, ratio1, ratio2)] of caps_integrate_plasma for (l1, l2, m) triples"""
+        h = lib.caps_integrate_plasma_init(self._h, float(omegap), 1e-8)
+        try:
+            out = []
+            for l1, l2, m in pairs:
+                r1, r2 = C.c_double(), C.c_double()
+                v = lib.caps_integrate_plasma(h, int(l1), int(l2), int(m), C.byref(r1), C.byref(r2))
+                out.append((v, r1.value, r2.value))
+            return out
+        finally:
+            lib.caps_integrate_plasma_free(h)
 
     def ht_drude(self):
         return lib.caps_ht_drude(self._h)

@@ -735,11 +735,59 @@ extern "C" double caps_kernel_M0_MM(int i, int j, void *args_)
     return caps_kernel_M0_EE(i, j, args_) * sqrt(((double)l1 * l2) / ((l1 + 1.) * (l2 + 1.)));
 }
 
+// plasma xi=0 integrals for the element-wise interface: the tables I_nu and
+// I_{l-1/2}/I_{l+1/2} are computed on the GPU (xi0.cu) and served from host copies,
+// grown on demand (integration.c:897-1031)
+void plasma_tables_host(double omegap_, double alpha, int numax, int lmax, std::vector<double> &I, std::vector<double> &ratio);
+struct PlasmaTables { std::vector<double> I, ratio; };
+
+extern "C" integration_plasma_t *caps_integrate_plasma_init(caps_t *caps, double omegap, double epsrel)
+{
+    integration_plasma_t *self = (integration_plasma_t *)calloc(1, sizeof(integration_plasma_t));
+    self->LbyR = caps->LbyR;
+    self->omegap_ = omegap * caps->calL / CAPS_c;
+    self->alpha = self->omegap_ / (1 + caps->LbyR);
+    self->epsrel = epsrel;
+    self->cache = new PlasmaTables;
+    self->cache_ratio = nullptr;
+    return self;
+}
+
+extern "C" double caps_integrate_plasma(integration_plasma_t *self, int l1, int l2, int m, double *ratio1, double *ratio2)
+{
+    (void)m;
+    PlasmaTables *t = (PlasmaTables *)self->cache;
+    const int lmax = std::max(l1, l2), numax = l1 + l2;
+    if ((int)t->I.size() <= numax || (int)t->ratio.size() <= lmax) {
+        const int l = std::max(2 * lmax, 64);
+        plasma_tables_host(self->omegap_, self->alpha, 2 * l, l, t->I, t->ratio);
+    }
+    if (ratio1) *ratio1 = t->ratio[l1];
+    if (ratio2) *ratio2 = t->ratio[l2];
+    return t->I[numax];
+}
+
+extern "C" void caps_integrate_plasma_free(integration_plasma_t *self)
+{
+    if (!self) return;
+    delete (PlasmaTables *)self->cache;
+    free(self);
+}
+
 extern "C" double caps_kernel_M0_MM_plasma(int i, int j, void *args_)
 {
-    (void)i; (void)j; (void)args_;
-    set_error("caps_kernel_M0_MM_plasma: the plasma xi=0 kernel is not implemented on the GPU");
-    return NAN;
+    caps_M_t *a = (caps_M_t *)args_;
+    integration_plasma_t *ip = (integration_plasma_t *)a->integration_plasma;
+    TERMINATE(!ip, "caps_kernel_M0_MM_plasma: integration_plasma not set (caps_integrate_plasma_init)");
+    const double y = a->caps->y;
+    const int l1 = i + a->lmin, l2 = j + a->lmin, m = a->m;
+    double ratio1, ratio2;
+    const double I = caps_integrate_plasma(ip, l1, l2, m, &ratio1, &ratio2);
+    const double alpha = ip->alpha;
+    const double factor1 = 1 - (2 * l1 + 1.) / (alpha * ratio1);
+    const double factor2 = 1 - (2 * l2 + 1.) / (alpha * ratio2);
+    const double factor = sqrt(l1 * factor1 / (l1 + 1.) * l2 * factor2 / (l2 + 1.));
+    return factor * exp(host_lfac(l1 + l2) - 0.5 * (host_lfac(l1 + m) + host_lfac(l1 - m) + host_lfac(l2 + m) + host_lfac(l2 - m)) + (l1 + l2 + 1) * y) * I;
 }
 
 extern "C" double caps_ht_drude(caps_t *caps)
@@ -757,14 +805,13 @@ extern "C" double caps_ht_drude(caps_t *caps)
 }
 
 // xi=0 EE/MM determinants are assembled and factored on the GPU
-int logdetD0_batch(caps_t *self, const int *ms, int n, int which, double *out);
+int logdetD0_batch(caps_t *self, const int *ms, int n, int which, double *out, double omegap);
 
 extern "C" void caps_logdetD0(caps_t *self, int m, double omegap, double *EE, double *MM, double *MM_plasma)
 {
-    (void)omegap;
-    if (EE) logdetD0_batch(self, &m, 1, 0, EE);
-    if (MM) logdetD0_batch(self, &m, 1, 1, MM);
-    if (MM_plasma) { *MM_plasma = NAN; set_error("caps_logdetD0: MM_plasma (plasma xi=0 block) is not implemented on the GPU"); }
+    if (EE) logdetD0_batch(self, &m, 1, 0, EE, 0.0);
+    if (MM) logdetD0_batch(self, &m, 1, 1, MM, 0.0);
+    if (MM_plasma) logdetD0_batch(self, &m, 1, 2, MM_plasma, omegap);
 }
 
 extern "C" double caps_ht_perf(caps_t *caps, double eps)
@@ -783,7 +830,7 @@ extern "C" double caps_ht_perf(caps_t *caps, double eps)
         int ms[16];
         double v[16];
         for (int k = 0; k < 16; k++) ms[k] = m0 + k;
-        logdetD0_batch(caps, ms, 16, 1, v);
+        logdetD0_batch(caps, ms, 16, 1, v, 0.0);
         for (int k = 0; k < 16; k++) {
             MM += v[k];
             if (fabs(v[k] / MM) < eps) return drude + MM;
@@ -791,11 +838,22 @@ extern "C" double caps_ht_perf(caps_t *caps, double eps)
     }
 }
 
-extern "C" double caps_ht_plasma(caps_t *caps, double omegap_, double eps)
+// libcaps.c:1127-1145: drude + sum'_m MM_plasma (m = 0 with weight 1/2) until the first m
+// with |v / sum| < eps; m in batches of 16 on the GPU, summed in order up to that m
+extern "C" double caps_ht_plasma(caps_t *caps, double omegap, double eps)
 {
-    (void)caps; (void)omegap_; (void)eps;
-    set_error("caps_ht_plasma: the plasma xi=0 block is not implemented on the GPU");
-    return NAN;
+    const double drude = caps_ht_drude(caps);
+    double sum = 0;
+    for (int m0 = 0;; m0 += 16) {
+        int ms[16];
+        double v[16];
+        for (int k = 0; k < 16; k++) ms[k] = m0 + k;
+        logdetD0_batch(caps, ms, 16, 2, v, omegap);
+        for (int k = 0; k < 16; k++) {
+            sum += ms[k] == 0 ? v[k] / 2 : v[k];
+            if (fabs(v[k] / sum) < eps) return drude + sum;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -855,15 +913,18 @@ static double energy_impl(caps_t *self, double T, double cutoff, double epsrel, 
     double v0;
     const int model = xi0_model(self);
     if (model == 1) v0 = caps_ht_drude(self);
-    else if (model == 0) {
-        // drude_HT + sum'_m logdetD0 MM with the m cutoff (caps.c:329-395, worker :925)
+    else {
+        // drude_HT + sum'_m logdetD0 MM (perfect reflectors) or MM_plasma (plasma model)
+        // with the m cutoff (caps.c:329-395, worker :921-929)
+        const int which = model == 0 ? 1 : 2;
+        const double omegap = model == 2 ? ((const double *)self->userdata_plate)[0] : 0.0;
         const double drude = caps_ht_drude(self);
         std::vector<double> terms;
         int mstop = -1;
         for (int m0 = 0; mstop < 0 && m0 < 4096; m0 += 32) {
             int ms[32]; double v[32];
             for (int k = 0; k < 32; k++) ms[k] = m0 + k;
-            logdetD0_batch(self, ms, 32, 1, v);
+            logdetD0_batch(self, ms, 32, which, v, omegap);
             ndet += 32;
             for (int k = 0; k < 32; k++) {
                 terms.push_back(v[k]);
@@ -873,9 +934,6 @@ static double energy_impl(caps_t *self, double T, double cutoff, double epsrel, 
         nwasted += (int)terms.size() - (mstop + 1);
         terms[0] /= 2;
         v0 = drude + kahan_sum(terms.data(), mstop + 1);
-    } else {
-        set_error("caps_free_energy: plasma model xi=0 term is not implemented");
-        return NAN;
     }
 
     std::vector<double> vn(1, v0);      // per-frequency sums, index n

@@ -76,6 +76,16 @@ typedef struct
     double *M;                /* private: dense M, row-major 2ldim x 2ldim */
 } caps_M_t;
 
+/* Plasma-model xi=0 integration object (src/include/libcaps.h:93-98).  The public
+ * fields keep the reference's meaning; the two pointers are private (GPU-computed
+ * tables served to the element-wise interface). */
+typedef struct
+{
+    double LbyR, alpha, omegap_, epsrel;
+    void *cache;
+    void *cache_ratio;
+} integration_plasma_t;
+
 /* ---- reference API (src/include/libcaps.h:113-163) ---- */
 void caps_build(FILE *stream, const char *prefix);                 /* libcaps.h:113, libcaps.c:239 */
 void caps_info(caps_t *self, FILE *stream, const char *prefix);    /* libcaps.h:114, libcaps.c:273 */
@@ -128,6 +138,11 @@ double caps_kernel_M0_MM(int i, int j, void *args);                 /* libcaps.h
 double caps_kernel_M0_MM_plasma(int i, int j, void *args_);         /* libcaps.h:161, libcaps.c:882 */
 
 void caps_logdetD0(caps_t *self, int m, double omegap, double *EE, double *MM, double *MM_plasma); /* libcaps.h:163, libcaps.c:985 */
+
+/* ---- plasma xi=0 integrals (src/include/integration.h:24-26) ---- */
+integration_plasma_t *caps_integrate_plasma_init(caps_t *caps, double omegap, double epsrel); /* integration.h:24, integration.c:897 */
+double caps_integrate_plasma(integration_plasma_t *self, int l1, int l2, int m, double *ratio1, double *ratio2); /* integration.h:25, integration.c:954 */
+void caps_integrate_plasma_free(integration_plasma_t *self);                                   /* integration.h:26, integration.c:1026 */
 
 /* ---- batch extensions (no reference counterpart; additive) ---- */
 

@@ -45,6 +45,9 @@ def _load():
         "oracle_ht_drude": (d, [d]),
         "oracle_logdetD0_MM": (d, [gp, i]),
         "oracle_ht_perf": (d, [gp, d]),
+        "oracle_plasma_I": (d, [i, d]),
+        "oracle_logdetD0_MM_plasma": (d, [gp, i, d]),
+        "oracle_ht_plasma": (d, [gp, d, d]),
         "oracle_logdetD_batch": (None, [gp, i, dp, C.POINTER(C.c_int), dp, i]),
         "oracle_free_energy": (d, [gp, d, d, d, i, dp, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "oracle_logdet_1mM": (d, [dp, i, C.POINTER(C.c_int)]),
@@ -102,3 +105,22 @@ def free_energy(R, L, ldim, T, drude=None, cutoff=1e-9, epsrel=1e-6, threads=1):
     nxi, ndet = C.c_int(), C.c_int()
     E = lib.oracle_free_energy(C.byref(g), T, cutoff, epsrel, threads, xi, v, C.byref(nxi), C.byref(ndet))
     return E, dict(nxi=nxi.value, ndet=ndet.value, xi=list(xi[:nxi.value]), logdetD=list(v[:nxi.value]))
+
+
+C_LIGHT = 299792458.0
+
+
+def plasma_I(nu, omegap_):
+    """I_nu of the plasma xi=0 block; omegap_ = omegap (L+R)/c"""
+    return lib.oracle_plasma_I(int(nu), float(omegap_))
+
+
+def logdetD0_MM_plasma(R, L, ldim, m, omegap_scaled):
+    """omegap_scaled: plasma frequency in units of c/(L+R)"""
+    g = geom(R, L, ldim)
+    return lib.oracle_logdetD0_MM_plasma(C.byref(g), int(m), omegap_scaled * C_LIGHT / (L + R))
+
+
+def ht_plasma(R, L, ldim, omegap_scaled, eps):
+    g = geom(R, L, ldim)
+    return lib.oracle_ht_plasma(C.byref(g), omegap_scaled * C_LIGHT / (L + R), float(eps))

@@ -27,6 +27,7 @@
 #include "caps_oracle.h"
 
 #define O_LOG2   0.69314718055994530942
+#define O_C      299792458.0 /* speed of light, constants.h */
 #define O_LOGPI  1.14472988584940017414
 #define O_HALF_LOG_2PI 0.91893853320467274178
 #ifndef M_PI
@@ -969,6 +970,120 @@ double oracle_ht_perf(const oracle_geom_t *g, double eps) /* libcaps.c:1089 */
 }
 
 /* ------------------------------------------------------------------------- */
+/* plasma model, xi = 0 (integration.c:897-1031, libcaps.c:882-909, 1127-1145)  */
+/* ------------------------------------------------------------------------- */
+typedef struct { int nu; double omegap_, log_prefactor; } pargs_t;
+
+/* -r_TE e^{-t} t^nu / nu!, r_TE = -b/(2+b), b = sqrtpm1((2 omegap_/t)^2) (integration.c:921) */
+static double plasma_integrand(double t, const pargs_t *a)
+{
+    const double x = 2 * a->omegap_ / t;
+    const double betam1 = sqrtpm1(x * x);
+    return betam1 / (2 + betam1) * exp(a->log_prefactor - t + a->nu * log(t));
+}
+
+static double pl_panel(const pargs_t *a, double lo, double hi)
+{
+    const double h = (hi - lo) / 2, c = (lo + hi) / 2;
+    double s = 0;
+    for (int i = 0; i < GLN; i++) s += gl_w[i] * plasma_integrand(c + h * gl_x[i], a);
+    return s * h;
+}
+
+static double pl_adapt(const pargs_t *a, double lo, double hi, double whole, double tol, int depth)
+{
+    const double mid = (lo + hi) / 2;
+    const double l = pl_panel(a, lo, mid), r = pl_panel(a, mid, hi);
+    if (fabs(l + r - whole) <= tol || depth >= 50) return l + r;
+    return pl_adapt(a, lo, mid, l, tol / 1.4142135623730951, depth + 1) + pl_adapt(a, mid, hi, r, tol / 1.4142135623730951, depth + 1);
+}
+
+static double pl_integrate(const pargs_t *a, double lo, double hi, double tol_abs)
+{
+    const double w = pl_panel(a, lo, hi);
+    return pl_adapt(a, lo, hi, w, fmax(tol_abs, 1e-14 * fabs(w)), 0);
+}
+
+/* I_nu = int_0^inf dt (-r_TE) e^{-t} t^nu / nu! on the reference's intervals [0,a],
+ * [a,b], [b,inf) with a = max(0, nu - 5/sqrt(nu)), b = nu + 5/sqrt(nu)
+ * (integration.c:979-1013); [b,inf) is cut where e^{-t} t^nu / nu! < 1e-40 */
+double oracle_plasma_I(int nu, double omegap_)
+{
+    pthread_once(&tables_once, tables_init);
+    pthread_once(&gl_once, gl_init);
+    pargs_t args = { nu, omegap_, -oracle_lfac(nu) };
+    const double width = 1 / sqrt((double)nu), a = fmax(0, nu - 5 * width), b = nu + 5 * width;
+    const double I2 = pl_integrate(&args, a, b, 0);
+    const double I1 = a > 0 ? pl_integrate(&args, 0, a, 1e-16 * I2) : 0;
+    double c = b + 10;
+    while (args.log_prefactor - c + nu * log(c) > -92) c += 10 + sqrt((double)nu);
+    const double I3 = pl_integrate(&args, b, c, 1e-16 * I2);
+    return I1 + I2 + I3;
+}
+
+/* log det(1-M0) of the plasma xi=0 MM block (libcaps.c:882-909, 985-1016);
+ * Itab[nu] = oracle_plasma_I(nu, omegap_) for nu up to 2(lmin+ldim-1) */
+static double logdetD0_MM_plasma_tab(const oracle_geom_t *g, int m, double omegap, const double *Itab)
+{
+    const double LbyR = g->L / g->R, y = -O_LOG2 - log1p(LbyR);
+    const double omegap_ = omegap * (g->L + g->R) / O_C, alpha = omegap_ / (1 + LbyR);
+    const int n = g->ldim, lmin = oracle_lmin(LbyR, g->ldim, m);
+    double *f = malloc((size_t)n * sizeof(double));
+    for (int i = 0; i < n; i++) {
+        const int l = i + lmin;
+        f[i] = 1 - (2 * l + 1.) / (alpha * oracle_ratioI(l - 0.5, alpha));
+    }
+    double *M = malloc((size_t)n * n * sizeof(double));
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) {
+            const int l1 = i + lmin, l2 = j + lmin;
+            const double factor = sqrt(l1 * f[i] / (l1 + 1.) * l2 * f[j] / (l2 + 1.));
+            M[(size_t)i * n + j] = factor * exp(oracle_lfac(l1 + l2) - 0.5 * (oracle_lfac(l1 + m) + oracle_lfac(l1 - m) + oracle_lfac(l2 + m)
+                                                                            + oracle_lfac(l2 - m)) + (l1 + l2 + 1) * y) * Itab[l1 + l2];
+        }
+    const double r = oracle_logdet_1mM(M, n, NULL);
+    free(M); free(f);
+    return r;
+}
+
+static double *plasma_table(const oracle_geom_t *g, int numax, double omegap)
+{
+    const double omegap_ = omegap * (g->L + g->R) / O_C;
+    double *Itab = malloc((size_t)(numax + 1) * sizeof(double));
+    Itab[0] = NAN;
+    for (int nu = 1; nu <= numax; nu++) Itab[nu] = oracle_plasma_I(nu, omegap_);
+    return Itab;
+}
+
+double oracle_logdetD0_MM_plasma(const oracle_geom_t *g, int m, double omegap)
+{
+    const int lmin = oracle_lmin(g->L / g->R, g->ldim, m);
+    double *Itab = plasma_table(g, 2 * (lmin + g->ldim - 1), omegap);
+    const double r = logdetD0_MM_plasma_tab(g, m, omegap, Itab);
+    free(Itab);
+    return r;
+}
+
+/* caps_ht_plasma (libcaps.c:1127): drude + sum'_m MM_plasma until |v/sum| < eps */
+double oracle_ht_plasma(const oracle_geom_t *g, double omegap, double eps)
+{
+    const double drude = oracle_ht_drude(g->L / g->R);
+    int numax = 0;
+    double *Itab = NULL, sum = 0;
+    for (int m = 0;; m++) {
+        const int need = 2 * (oracle_lmin(g->L / g->R, g->ldim, m) + g->ldim - 1);
+        if (need > numax) {
+            free(Itab);
+            numax = need + 256;
+            Itab = plasma_table(g, numax, omegap);
+        }
+        const double v = logdetD0_MM_plasma_tab(g, m, omegap, Itab);
+        sum += m == 0 ? v / 2 : v;
+        if (fabs(v / sum) < eps) { free(Itab); return drude + sum; }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
 /* batch evaluation on host threads (CPU baseline)                            */
 /* ------------------------------------------------------------------------- */
 typedef struct {
@@ -1013,14 +1128,23 @@ double oracle_free_energy(const oracle_geom_t *g, double T, double cutoff, doubl
     const double Ts = 2 * M_PI * kB * (g->R + g->L) * T / (hbar * c);
     const double LbyR = g->L / g->R;
     double v[4096]; int nv = 0, dets = 0;
-    /* xi = 0: Drude analytic; perfect reflectors: drude_HT + sum'_m logdetD0 MM with
-     * the m cutoff and half weight for m=0, as F_xi(0) does (caps.c:329-395) */
-    if (g->plate.kind == ORACLE_PERFECT) {
-        double t0[4096]; int ms = -1;
+    /* xi = 0 (caps.c:329-395): Drude (gamma > 0) analytic; perfect reflectors and the
+     * plasma model (gamma = 0): drude_HT + sum'_m of the logdetD0 MM (resp. MM_plasma)
+     * blocks with the m cutoff and half weight for m=0 */
+    const int plasma = g->plate.kind == ORACLE_DRUDE && g->plate.gamma == 0;
+    if (g->plate.kind == ORACLE_PERFECT || plasma) {
+        double t0[4096]; int ms = -1, numax = 0;
+        double *Itab = NULL;
         for (int m = 0; m < 4096; m++) {
-            t0[m] = oracle_logdetD0_MM(g, m);
+            if (plasma) {
+                const int need = 2 * (oracle_lmin(LbyR, g->ldim, m) + g->ldim - 1);
+                if (need > numax) { free(Itab); numax = need + 256; Itab = plasma_table(g, numax, g->plate.omegap); }
+                t0[m] = logdetD0_MM_plasma_tab(g, m, g->plate.omegap, Itab);
+            } else
+                t0[m] = oracle_logdetD0_MM(g, m);
             if (t0[m] == 0 || t0[m] / t0[0] < cutoff) { ms = m; break; }
         }
+        free(Itab);
         t0[0] /= 2;
         v[nv++] = oracle_ht_drude(LbyR) + kahan(t0, ms + 1);
     } else

@@ -45,6 +45,9 @@ double oracle_I(const oracle_geom_t *g, double xi_, int m, int l1, int l2, int p
 double oracle_ht_drude(double LbyR);
 double oracle_logdetD0_MM(const oracle_geom_t *g, int m);
 double oracle_ht_perf(const oracle_geom_t *g, double eps);
+double oracle_plasma_I(int nu, double omegap_);
+double oracle_logdetD0_MM_plasma(const oracle_geom_t *g, int m, double omegap);
+double oracle_ht_plasma(const oracle_geom_t *g, double omegap, double eps);
 
 void   oracle_logdetD_batch(const oracle_geom_t *g, int n, const double *xi, const int *m, double *out, int nthreads);
 double oracle_free_energy(const oracle_geom_t *g, double T, double cutoff, double epsrel, int nthreads,

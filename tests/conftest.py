@@ -24,6 +24,15 @@ def ref_values():
     return json.load(open(os.path.join(GOLDEN, "reference_values.json")))
 
 
+SMALL_ENERGIES = ["pr_RbyL10_ldim70_T300", "drude_RbyL10_ldim70_T300", "plasma_RbyL10_ldim70_T300"]
+
+
+@pytest.fixture(scope="session")
+def energy_golden():
+    """free energies from the unmodified reference library (tests/golden/make_golden_energy.py)"""
+    return {n: json.load(open(os.path.join(GOLDEN, "energy_%s.json" % n))) for n in SMALL_ENERGIES}
+
+
 def rel(a, b):
     return abs(a - b) / max(1.0, abs(b))
 

@@ -53,6 +53,17 @@ def parse_tests(ref):
         cases.append(dict(R=1.0, L=0.001, ldim=10000, xi=float(xi), m=int(m), logdetD=float(v)))
     out["test_logdetD"] = dict(source="src/tests/test_logdetD.c:13-102", tolerance=1e-10, detalg="HODLR", cases=cases)
 
+    body0 = t[t.index("int test_logdetD0()"):]
+    eps = float(re.search(r"const double eps = ([\d.e-]+);", body0).group(1))
+    cases = []
+    for wp, v in re.findall(r"caps_ht_plasma\(caps,\s*([\d.]+)\*CAPS_c/\(L\+R\), eps\), (-?[\d.]+)\)", body0):
+        cases.append(dict(R=100e-6, L=1e-6, ldim=500, omegap_scaled=float(wp), eps=eps, ht_plasma=float(v)))
+    an = re.search(r"caps_logdetD0\(caps, 0, INFINITY, &EE, &MM, NULL\);\s*AssertAlmostEqual\(&test, EE, (-?[\d.]+)\);"
+                   r"\s*AssertAlmostEqual\(&test, MM, (-?[\d.]+)\);", body0)
+    out["test_logdetD0"] = dict(source="src/tests/test_logdetD.c:108-142", tolerance=1e-10, detalg="HODLR",
+                                note="omegap in units of c/(L+R)", ht_plasma=cases,
+                                m0_RbyL1000=dict(R=1.0, L=0.001, ldim=12000, m=0, EE=float(an.group(1)), MM=float(an.group(2))))
+
     t = _read_c(os.path.join(ref, "src/tests/test_mie.c"))
     cases = []
     for xi, l, blk in re.findall(r"caps_mie_perf\(self, ([\d.]+), (\d+), &lna, &lnb\);(.*?)(?=caps_mie_perf|caps_free)", t, re.S):

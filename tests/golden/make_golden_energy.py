@@ -7,6 +7,7 @@ value does not depend on the pool size).  Writes tests/golden/energy_<name>.json
 
     python tests/golden/make_golden_energy.py c3      # Drude, R/L=150 (~30 CPU-min)
     python tests/golden/make_golden_energy.py small   # PR and Drude, R/L=10
+    python tests/golden/make_golden_energy.py plasma  # plasma model (gamma = 0), R/L=10
 """
 import ctypes as C
 import json
@@ -49,7 +50,12 @@ def _task(args):
     if drude:
         ud = (C.c_double * 2)(drude[0] / HBAR_EV, drude[1] / HBAR_EV)
         _lib.caps_set_epsilonm1(c, C.cast(_lib.caps_epsilonm1_drude, C.c_void_p), C.cast(ud, C.c_void_p))
-    if xi == 0:
+    if xi == 0 and drude:
+        # plasma model (gamma = 0): the MM_plasma block (caps.c:927-929)
+        v = C.c_double()
+        _lib.caps_logdetD0(c, m, drude[0] / HBAR_EV, None, None, C.byref(v))
+        r = v.value
+    elif xi == 0:
         v = C.c_double()
         _lib.caps_logdetD0(c, m, 0.0, None, C.byref(v), None)
         r = v.value
@@ -88,11 +94,12 @@ def energy(R, L, ldim, T, drude, cutoff=1e-9, epsrel=1e-6, detalg=1, procs=8):
     with mp.Pool(procs, initializer=_init) as pool:
         c = _lib.caps_init(R, L)
         _lib.caps_set_ldim(c, ldim)
-        if drude:
+        if drude and drude[1] > 0:
             v0 = _lib.caps_ht_drude(c)
         else:
+            # perfect reflectors and the plasma model (caps.c:329-395)
             drude_ht = _lib.caps_ht_drude(c)
-            s, _, _ = F_xi(pool, R, L, ldim, None, 0.0, cutoff, detalg, procs)
+            s, _, _ = F_xi(pool, R, L, ldim, drude, 0.0, cutoff, detalg, procs)
             v0 = drude_ht + s
         v, xis, ndet = [v0], [0.0], 0
         n = 1
@@ -115,6 +122,7 @@ if __name__ == "__main__":
     procs = int(os.environ.get("PROCS", "8"))
     cases = {
         "small": [("pr_RbyL10_ldim70_T300", 10e-6, 1e-6, 70, 300.0, None), ("drude_RbyL10_ldim70_T300", 10e-6, 1e-6, 70, 300.0, (9.0, 0.035))],
+        "plasma": [("plasma_RbyL10_ldim70_T300", 10e-6, 1e-6, 70, 300.0, (9.0, 0.0))],
         "c2": [("pr_RbyL50_ldim350_T300", 50e-6, 1e-6, 350, 300.0, None)],
         "c3": [("drude_RbyL150_ldim1050_T300", 150e-6, 1e-6, 1050, 300.0, (9.0, 0.035))],
     }[which]

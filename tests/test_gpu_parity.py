@@ -148,3 +148,62 @@ def test_free_energy_vs_oracle(cg, ob):
         Eo, io = ob.free_energy(R, L, ldim, T, drude, threads=8)
         assert info["nxi"] == io["nxi"]
         assert abs(E - Eo) <= 1e-10 * abs(Eo), (E, Eo, info, io)
+
+
+@pytest.mark.parametrize("name", ["pr_RbyL10_ldim70_T300", "drude_RbyL10_ldim70_T300", "plasma_RbyL10_ldim70_T300"])
+def test_free_energy_golden(cg, energy_golden, name):
+    """caps_free_energy against the reference library's free energy (PR, Drude, plasma)"""
+    d = energy_golden[name]
+    c = cg.Caps(d["R"], d["L"], ldim=d["ldim"], detalg=cg.DETALG_LU)
+    if d["drude"]:
+        c.set_drude(*d["drude"])
+    E, info = c.free_energy(d["T"])
+    assert info["nxi"] == len(d["xi"])
+    assert abs(E - d["E"]) <= TOL * abs(d["E"]), (E, d["E"])
+
+
+def test_ht_plasma_golden(cg, unit_vectors):
+    """caps_ht_plasma against the reference's own vectors (src/tests/test_logdetD.c:121-126)"""
+    t = unit_vectors["test_logdetD0"]
+    CL = 299792458.0
+    for v in t["ht_plasma"]:
+        c = cg.Caps(v["R"], v["L"], ldim=v["ldim"])
+        got = c.ht_plasma(v["omegap_scaled"] * CL / (v["L"] + v["R"]), v["eps"])
+        assert abs(got - v["ht_plasma"]) <= t["tolerance"] * abs(v["ht_plasma"]), (v, got)
+
+
+def test_xi0_MM_plasma_vs_oracle(cg, ob):
+    R, L, ldim = 20e-6, 1e-6, 60
+    c = cg.Caps(R, L, ldim=ldim, detalg=cg.DETALG_LU)
+    for wps in (0.01, 9.0 / 6.582119514e-16 * (L + R) / 299792458.0, 500.0):
+        for m in (0, 1, 5, 11):
+            got = c.logdetD0_plasma(m, wps * 299792458.0 / (L + R))
+            want = ob.logdetD0_MM_plasma(R, L, ldim, m, wps)
+            assert rel(got, want) < TOL, (wps, m, got, want)
+
+
+def test_integrate_plasma_vs_oracle(cg, ob):
+    """caps_integrate_plasma: I_nu and the Bessel ratios, GPU tables against the oracle's
+    adaptive quadrature on the reference's intervals"""
+    R, L = 20e-6, 1e-6
+    c = cg.Caps(R, L, ldim=40)
+    CL = 299792458.0
+    for wps in (0.01, 3.0, 700.0):
+        omegap = wps * CL / (L + R)
+        alpha = wps / (1 + L / R)
+        trip = [(1, 1, 0), (2, 1, 1), (7, 3, 2), (40, 40, 5), (333, 120, 9), (1500, 1400, 30)]
+        for (l1, l2, m), (I, r1, r2) in zip(trip, c.integrate_plasma(omegap, trip)):
+            want = ob.plasma_I(l1 + l2, wps)
+            assert abs(I - want) <= 1e-12 * abs(want), (wps, l1, l2, I, want)
+            assert relx(r1, ob.lib.oracle_ratioI(l1 - 0.5, alpha)) < 1e-14
+            assert relx(r2, ob.lib.oracle_ratioI(l2 - 0.5, alpha)) < 1e-14
+
+
+@pytest.mark.skipif(os.environ.get("CAPS_SKIP_HEAVY") == "1", reason="heavy case disabled")
+def test_logdetD0_m0_RbyL1000_analytic(cg, unit_vectors):
+    """the reference's analytic m=0 xi=0 vectors at R/L=1000, ldim 12000 (test_logdetD.c:131-139)"""
+    t = unit_vectors["test_logdetD0"]["m0_RbyL1000"]
+    c = cg.Caps(t["R"], t["L"], ldim=t["ldim"])
+    ee, mm = c.logdetD0(t["m"])
+    assert relx(ee, t["EE"]) < 1e-10, (ee, t["EE"])
+    assert relx(mm, t["MM"]) < 1e-10, (mm, t["MM"])

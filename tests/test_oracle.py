@@ -83,3 +83,34 @@ def test_ht_drude_limit():
     # Drude high-temperature term is negative and grows with R/L
     a, b = ob.lib.oracle_ht_drude(1 / 20), ob.lib.oracle_ht_drude(1 / 150)
     assert b < a < 0
+
+
+def test_ht_plasma_golden(unit_vectors):
+    """the plasma-model xi=0 free energy against the reference's own vectors
+    (src/tests/test_logdetD.c:121-126, 1e-10)"""
+    t = unit_vectors["test_logdetD0"]
+    for c in t["ht_plasma"]:
+        got = ob.ht_plasma(c["R"], c["L"], c["ldim"], c["omegap_scaled"], c["eps"])
+        assert abs(got - c["ht_plasma"]) <= t["tolerance"] * abs(c["ht_plasma"]), (c, got)
+
+
+def test_plasma_I_limits():
+    """I_nu is an average of -r_TE over a Gamma(nu+1) density: in (0,1), increasing
+    with omegap, and 1 - I_nu ~ nu/omegap for omegap >> nu (-r_TE ~ 1 - t/omegap)"""
+    for nu in (2, 17, 300):
+        vals = [ob.plasma_I(nu, w) for w in (0.01, 1.0, 100.0, 1e5)]
+        assert all(0 < v < 1 for v in vals)
+        assert vals == sorted(vals)
+        assert 1 - vals[-1] < 4 * (nu + 1) / 1e5
+
+
+@pytest.mark.parametrize("name", ["pr_RbyL10_ldim70_T300", "drude_RbyL10_ldim70_T300", "plasma_RbyL10_ldim70_T300"])
+def test_free_energy_golden(energy_golden, name):
+    """the oracle's Matsubara sum (incl. the xi=0 rule of each material model) against the
+    reference library run through the serial restatement of its driver"""
+    d = energy_golden[name]
+    drude = tuple(d["drude"]) if d["drude"] else None
+    E, info = ob.free_energy(d["R"], d["L"], d["ldim"], d["T"], drude, threads=8)
+    assert info["nxi"] == len(d["xi"])
+    assert abs(E - d["E"]) <= 1e-10 * abs(d["E"]), (E, d["E"])
+    assert abs(info["logdetD"][0] - d["logdetD"][0]) <= 1e-10 * abs(d["logdetD"][0])
