@@ -5,6 +5,17 @@
 #include <cuda_runtime.h>
 #include "common.cuh"
 
+// contract violation: same behaviour as the reference's TERMINATE (utils.h:31)
+#define TERMINATE(cond, ...)                                                              \
+    do {                                                                                  \
+        if (cond) {                                                                       \
+            fprintf(stderr, "libcaps_gb300: %s:%d: ", __FILE__, __LINE__);               \
+            fprintf(stderr, __VA_ARGS__);                                                 \
+            fprintf(stderr, "\n");                                                        \
+            abort();                                                                      \
+        }                                                                                 \
+    } while (0)
+
 namespace capsgpu {
 
 [[noreturn]] void fatal(const char *file, int line, const char *what);

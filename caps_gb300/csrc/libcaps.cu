@@ -45,17 +45,6 @@ Counters g_counters;
 }
 } // namespace capsgpu
 
-// contract violation: same behaviour as the reference's TERMINATE (utils.h:31)
-#define TERMINATE(cond, ...)                                                              \
-    do {                                                                                  \
-        if (cond) {                                                                       \
-            fprintf(stderr, "libcaps_gb300: %s:%d: ", __FILE__, __LINE__);               \
-            fprintf(stderr, __VA_ARGS__);                                                 \
-            fprintf(stderr, "\n");                                                        \
-            abort();                                                                      \
-        }                                                                                 \
-    } while (0)
-
 extern "C" const char *caps_gpu_last_error(void) { return g_last_error.c_str(); }
 
 // ---------------------------------------------------------------------------
@@ -901,15 +890,53 @@ static int m_chunk(const MState &s, double cutoff)
 
 // first_chunk[i] (i < n_first): number of m to compute in the first batch for xi_{i+1}
 // (from a proposal); nullptr: the extrapolating schedule of the plain method.
-static double energy_impl(caps_t *self, double T, double cutoff, double epsrel, const int *first_chunk, int n_first,
-                          caps_energy_info_t *info)
+// F(xi_k) = sum'_m logdetD(xi_k, m) (m = 0 with weight 1/2) up to the first m with
+// v_m == 0 or v_m / v_0 < cutoff, Kahan-summed in m order (caps.c:307-396), for n
+// frequencies at once: the m chunks of every unfinished frequency share one GPU batch
+// per round.  A non-finite term ends that frequency with F = NaN.
+void fxi_batch(caps_t *self, const double *xi, int n, double cutoff, double *out, int *ndet, int *nwasted)
 {
-    const auto t0 = std::chrono::steady_clock::now();
-    TERMINATE(!(T > 0), "temperature must be positive");
-    const double Ts = 2 * PI * CAPS_kB * (self->R + self->L) * T / (CAPS_hbar * CAPS_c);
-    int ndet = 0, nwasted = 0;
+    std::vector<MState> st(n);
+    std::vector<char> bad(n, 0);
+    for (;;) {
+        std::vector<double> bx; std::vector<int> bm; std::vector<std::pair<int, int>> who;
+        for (int i = 0; i < n; i++) {
+            MState &s = st[i];
+            if (s.done()) continue;
+            TERMINATE(s.next >= 4096, "sum over m did not converge (xi_=%g)", xi[i]);
+            const int w = std::min(m_chunk(s, cutoff), 4096 - s.next);
+            for (int k = 0; k < w; k++) { bx.push_back(xi[i]); bm.push_back(s.next + k); who.push_back({i, s.next + k}); }
+            s.next += w;
+            s.v.resize(s.next, NAN);
+        }
+        if (bx.empty()) break;
+        std::vector<double> r(bx.size());
+        caps_logdetD_batch(self, bx.data(), bm.data(), (int)bx.size(), r.data(), NULL);
+        if (ndet) *ndet += (int)bx.size();
+        for (size_t k = 0; k < bx.size(); k++) st[who[k].first].v[who[k].second] = r[k];
+        for (int i = 0; i < n; i++) {
+            MState &s = st[i];
+            if (s.done()) continue;
+            for (int m = 0; m < s.next; m++) {
+                if (!std::isfinite(s.v[m])) { s.mstop = m; bad[i] = 1; break; }
+                if (s.v[m] == 0 || s.v[m] / s.v[0] < cutoff) { s.mstop = m; break; }
+            }
+        }
+    }
+    for (int i = 0; i < n; i++) {
+        MState &s = st[i];
+        if (nwasted) *nwasted += s.next - (s.mstop + 1);
+        if (bad[i]) { out[i] = NAN; continue; }
+        std::vector<double> t(s.v.begin(), s.v.begin() + s.mstop + 1);
+        t[0] /= 2;
+        out[i] = kahan_sum(t.data(), t.size());
+    }
+}
 
-    // xi = 0
+// xi = 0 term of the free energy by the reference's material rules (caps.c:329-395, 760-808)
+double xi0_term(caps_t *self, double cutoff, int *ndet_, int *nwasted_)
+{
+    int ndet = 0, nwasted = 0;
     double v0;
     const int model = xi0_model(self);
     if (model == 1) v0 = caps_ht_drude(self);
@@ -935,6 +962,23 @@ static double energy_impl(caps_t *self, double T, double cutoff, double epsrel, 
         terms[0] /= 2;
         v0 = drude + kahan_sum(terms.data(), mstop + 1);
     }
+
+    *ndet_ += ndet;
+    *nwasted_ += nwasted;
+    return v0;
+}
+
+static double energy_impl(caps_t *self, double T, double cutoff, double epsrel, const int *first_chunk, int n_first,
+                          caps_energy_info_t *info)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    TERMINATE(!(T > 0), "temperature must be positive");
+    const double Ts = 2 * PI * CAPS_kB * (self->R + self->L) * T / (CAPS_hbar * CAPS_c);
+    int ndet = 0, nwasted = 0;
+
+    // xi = 0
+    const double v0 = xi0_term(self, cutoff, &ndet, &nwasted);
+    if (std::isnan(v0)) return NAN;
 
     std::vector<double> vn(1, v0);      // per-frequency sums, index n
     std::vector<MState> st;             // st[n-1] for xi_n

@@ -179,6 +179,25 @@ typedef struct {
 } caps_energy_info_t;
 double caps_free_energy(caps_t *self, double T, double cutoff, double epsrel, caps_energy_info_t *info);
 
+/* Free energy at T = 0 (src/caps.c:722-748): E = 1/(alpha pi) int_0^inf dx F(x/alpha),
+ * x = 2 xi L/c, alpha = 2L/(L+R), with the reference's PFA cut of the integrand
+ * (caps.c:235-267).  method 0: QUADPACK qagi with relative tolerance epsrel (the
+ * reference's default); 1: Fourier-Chebyshev quadrature (fcqs.c:107).  Every step's
+ * function values are evaluated as one GPU batch.  info (optional): nxi = integrand
+ * evaluations; xi/logdetD record the first 4096 of them. */
+double caps_free_energy_T0(caps_t *self, double cutoff, double epsrel, int method, caps_energy_info_t *info);
+/* Free energy at T > 0 by Pade spectrum decomposition (src/caps.c:811-831) of the given
+ * order (<= 0: the reference's automatic order, caps.c:635-639); all poles in one batch. */
+double caps_free_energy_psd(caps_t *self, double T, double cutoff, double epsrel, int order, caps_energy_info_t *info);
+
+/* The quadratures and PSD poles behind these drivers, on a host callback: the same
+ * algorithms as the reference's dqagi (cquadpack/src/dqagi.c:40), fcqs_semiinf
+ * (src/fcqs.c:107) and psd (src/psd.c:80), with the same arguments and results. */
+double caps_dqagi(double (*f)(double, void *), void *userdata, double bound, int inf, double epsabs, double epsrel,
+                  double *abserr, int *neval, int *ier);
+double caps_fcqs_semiinf(double (*f)(double, void *), void *userdata, double *epsrel, int *neval, double L, int *ier);
+int caps_psd(int N, double *xi, double *eta);
+
 /* ---- learned truncation (no reference counterpart) ----
  * A 5-64-64-64-1 SiLU network (FP32), trained on the GPU by the library's own
  * forward/backward/Adam kernels on log|logdetD| values computed by the plain
