@@ -512,8 +512,10 @@ __global__ void k_tables(const double *lfac_tab, double *lft, int nlf, double2 *
 CAPS_DEV sd sdx(double c, sd a) { return sd_norm(c * a.m, a.e); }
 CAPS_DEV sd sd_neg(sd a) { return sd{-a.m, a.e}; }
 
+// A = 1 - M (lower triangle); mdiag receives M_ii itself, so that the trace keeps its
+// relative precision when M_ii is far below the unit diagonal of A
 __global__ void k_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv,
-                       double *A, size_t lda, size_t mat_stride, int *status)
+                       double *A, size_t lda, size_t mat_stride, double *mdiag, int *status)
 {
     const int L = ldim + 2;
     const int a = blockIdx.x * blockDim.x + threadIdx.x; // row block
@@ -561,6 +563,10 @@ __global__ void k_elem(const Task *tasks, int ntask, int ldim, const sd *I, cons
     Am[(size_t)c0 * lda + r0 + 1] = -me;
     Am[(size_t)(c0 + 1) * lda + r0 + 1] = (a == b ? 1.0 : 0.0) - mm;
     if (a != b) Am[(size_t)(c0 + 1) * lda + r0] = -em;
+    else {
+        mdiag[(size_t)task * 2 * ldim + r0] = ee;
+        mdiag[(size_t)task * 2 * ldim + r0 + 1] = mm;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -568,8 +574,11 @@ __global__ void k_elem(const Task *tasks, int ntask, int ldim, const sd *I, cons
 // ---------------------------------------------------------------------------
 // mode: 0 = dense semantics (trace + Mercator shortcut), 1 = HODLR semantics
 // (trace shortcut only; |tr| > |logdet| checked after the factorisation).
+// trace and Frobenius norm of M from its strict lower triangle (-A) and its diagonal
+// M_ii (mdiag, n per task), as the reference takes them from the elements of M
+// (matrix.c:57-119): 1 - A_ii would lose every M_ii below the rounding of 1
 __global__ void k_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode,
-                        double *trace_out, double *result, int *status)
+                        const double *mdiag, double *trace_out, double *result, int *status)
 {
     const int task = blockIdx.x;
     if (task >= ntask) return;
@@ -580,7 +589,7 @@ __global__ void k_stats(const Task *tasks, int ntask, int n, const double *A, si
     for (int j = 0; j < n; j++) {
         const double *col = Am + (size_t)j * lda;
         for (int i = j + threadIdx.x; i < n; i += blockDim.x) {
-            const double v = (i == j) ? 1.0 - col[i] : -col[i];
+            const double v = (i == j) ? mdiag[(size_t)task * n + i] : -col[i];
             s += (i == j ? 1.0 : 2.0) * v * v;
         }
     }
@@ -594,7 +603,7 @@ __global__ void k_stats(const Task *tasks, int ntask, int n, const double *A, si
     // Kahan trace in index order (misc.c:26)
     double tr = 0.0, c = 0.0;
     for (int i = 0; i < n; i++) {
-        const double y = (1.0 - Am[(size_t)i * lda + i]) - c;
+        const double y = mdiag[(size_t)task * n + i] - c;
         const double t = tr + y;
         c = (t - tr) - y;
         tr = t;
@@ -716,18 +725,18 @@ void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_str
 }
 
 void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv, double *A,
-                 size_t lda, size_t mat_stride, int *status, cudaStream_t st)
+                 size_t lda, size_t mat_stride, double *mdiag, int *status, cudaStream_t st)
 {
     dim3 g((ldim + 127) / 128, ldim, ntask);
-    k_elem<<<g, 128, 0, st>>>(tasks, ntask, ldim, I, Sa, Sb, uv, A, lda, mat_stride, status);
+    k_elem<<<g, 128, 0, st>>>(tasks, ntask, ldim, I, Sa, Sb, uv, A, lda, mat_stride, mdiag, status);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
-void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode, double *trace,
-                  double *result, int *status, cudaStream_t st)
+void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, const double *mdiag, int mode,
+                  double *trace, double *result, int *status, cudaStream_t st)
 {
-    k_stats<<<ntask, 256, 0, st>>>(tasks, ntask, n, A, lda, mat_stride, mode, trace, result, status);
+    k_stats<<<ntask, 256, 0, st>>>(tasks, ntask, n, A, lda, mat_stride, mode, mdiag, trace, result, status);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

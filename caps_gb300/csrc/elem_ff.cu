@@ -79,7 +79,7 @@ __global__ void k_scale_ff(int ntask, int L, const sd *Sa, const sd *Sb, const d
 
 // grid (ceil(ldim/EB), ldim, ntask); thread (a, b) with a >= b owns rows 2a, 2a+1 and
 // columns 2b, 2b+1 of M.  S receives -M (the delta form of A = 1 - M), lower triangle,
-// column-major with leading dimension n; diag receives the FP64 diagonal of A; part
+// column-major with leading dimension n; diag receives M_ii in FP64; part
 // receives, per warp, the sum of squares of M over the warp's blocks (strict lower
 // entries twice).  Blocks entirely above the diagonal exit before doing anything.
 __global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, int ntask, int ldim, const ffe *__restrict__ I,
@@ -147,8 +147,8 @@ __global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, int ntask, in
             Sm[(size_t)(c0 + 1) * n + r0] = -em;
             wsum = 2.0f * (ee * ee + me * me + mm * mm + em * em);
         } else {
-            diag[(size_t)task * n + r0] = 1.0 - fe_to_double(EE);
-            diag[(size_t)task * n + r0 + 1] = 1.0 - fe_to_double(MM);
+            diag[(size_t)task * n + r0] = fe_to_double(EE);
+            diag[(size_t)task * n + r0 + 1] = fe_to_double(MM);
             wsum = ee * ee + mm * mm + 2.0f * me * me;
         }
     }
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, int ntask, in
         part[(((size_t)task * ldim + b) * gridDim.x + blockIdx.x) * (EB / 32) + threadIdx.x / 32] = wsum;
 }
 
-// per task: Kahan trace of M over the FP64 diagonal (index order, misc.c:26), the
+// per task: Kahan trace of M over its FP64 diagonal (index order, misc.c:26), the
 // Frobenius norm from the element partials (fixed order), and the reference's
 // shortcut decision: |tr| < 1e-8 -> -tr; dense modes: Mercator when its error bound is
 // below 1e-8 relative; otherwise factorise.
@@ -184,7 +184,7 @@ __global__ void k_stats_ff(int ntask, int ldim, const double *diag, const float 
     const double *dg = diag + (size_t)task * n;
     double tr = 0.0, c = 0.0;
     for (int i = 0; i < n; i++) {
-        const double y = (1.0 - dg[i]) - c;
+        const double y = dg[i] - c;
         const double t = tr + y;
         c = (t - tr) - y;
         tr = t;

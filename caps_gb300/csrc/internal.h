@@ -52,9 +52,9 @@ void launch_itab_grp(const Task *tasks, int ntask, const int4 *groups, int ngrou
 void launch_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, cudaStream_t st);
 size_t a12_bytes(int ldim, int ngroup);
 void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv, double *A,
-                 size_t lda, size_t mat_stride, int *status, cudaStream_t st);
-void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode, double *trace,
-                  double *result, int *status, cudaStream_t st);
+                 size_t lda, size_t mat_stride, double *mdiag, int *status, cudaStream_t st);
+void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, const double *mdiag, int mode,
+                  double *trace, double *result, int *status, cudaStream_t st);
 // mixed form: elements in float-float straight into the FP32 delta matrix (elem_ff.cu)
 size_t elem_ff_part_floats(int ldim);
 void launch_elem_ff(const Task *tasks, int ntask, int ldim, const sd *Sa, const sd *Sb, const double2 *uv, void *Saf, void *Sbf,
@@ -64,7 +64,8 @@ void launch_stats_ff(int ntask, int ldim, const double *diag, const float *part,
                      int *status, cudaStream_t st);
 void launch_cholesky(int ntask, int n, double *A, size_t lda, size_t mstride, int *status, double *logdiag, cudaStream_t st);
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
-                           const double *trace, double *result, int mode, cudaStream_t st, bool tc = true, bool convert = true);
+                           const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc = true,
+                           bool convert = true);
 void launch_final(int ntask, int n, const double *logdiag, const double *trace, int *status, double *result, int mode, cudaStream_t st);
 
 } // namespace capsgpu

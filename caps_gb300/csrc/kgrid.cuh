@@ -95,7 +95,18 @@ KG_HD int kgrid_build(double alpha, int mu, int s, int nu_max, const KGridParams
         double h1 = P.c_width / sqrt(kg_kappa(t > 0 ? t : 1e-300, alpha, keff));
         if (t == 0.0) h1 = P.c_width / sqrt(alpha + (k > 0 ? 0.0 : 0.0));
         const double h2 = P.c_width / sqrt(kg_kappa(t + h1, alpha, keff));
-        const double h = h1 < h2 ? h1 : h2;
+        double h = h1 < h2 ? h1 : h2;
+        if (h2 < 0.25 * h1) {
+            // the local width overshoots into a far narrower region (small alpha, where
+            // kappa grows like e^t over one step): take the self-consistent width
+            // h = c / sqrt(kappa(t + h)) instead of the look-ahead's, which would crawl
+            double lo = 0.0, hi = h1;
+            for (int it = 0; it < 60; it++) {
+                const double mid = 0.5 * (lo + hi);
+                if (mid < P.c_width / sqrt(kg_kappa(t + mid, alpha, keff))) lo = mid; else hi = mid;
+            }
+            if (lo > h) h = lo;
+        }
         const double tn = t + h;
         if (past || tn > tpk) {
             const double a = past ? t : tpk;

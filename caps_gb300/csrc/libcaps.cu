@@ -555,18 +555,19 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             launch_stats_ff(nt, ldim, d_dg, d_part, O.mode, d_trace, d_res, d_status, st);
         } else {
             d_A = (double *)g_eng.A.get((size_t)nt * mstride * sizeof(double));
-            launch_elem(d_tasks, nt, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, lda, mstride, d_status, st);
-            if (O.factor) launch_stats(d_tasks, nt, dim, d_A, lda, mstride, O.mode, d_trace, d_res, d_status, st);
+            d_dg = (double *)g_eng.diag.get((size_t)nt * dim * sizeof(double));
+            launch_elem(d_tasks, nt, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, lda, mstride, d_dg, d_status, st);
+            if (O.factor) launch_stats(d_tasks, nt, dim, d_A, lda, mstride, d_dg, O.mode, d_trace, d_res, d_status, st);
         }
         CK(cudaEventRecord(g_eng.ev[4], st));
 
         // CAPS_MIXED_SIMT=1 selects the FP32 FFMA trailing update instead of split-TF32 tensor cores
         static const bool tc = getenv("CAPS_MIXED_SIMT") == nullptr;
         if (ff_elem) {
-            launch_cholesky_mixed(nt, dim, d_dg, 0, dim, d_status, d_S, mstride, d_trace, d_res, O.mode, st, tc, false);
+            launch_cholesky_mixed(nt, dim, nullptr, 0, 0, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, false);
         } else if (O.factor && caps->precision == CAPS_PREC_MIXED) {
             d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
-            launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_trace, d_res, O.mode, st, tc);
+            launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc);
         } else if (O.factor) {
             double *d_ld = (double *)g_eng.logdiag.get((size_t)nt * dim * sizeof(double));
             launch_cholesky(nt, dim, d_A, lda, mstride, d_status, d_ld, st);

@@ -251,8 +251,8 @@ __global__ void __launch_bounds__(128) k_syrk_tc(int ntask, int n, int k0, float
 
 // log det = 2 sum log1p(Lam_jj) + tr(A-I) - 2 tr Lam - ||Lam||_F^2, all sums FP64;
 // one CTA per task, fixed reduction order
-__global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const float *S, size_t sstride, const double *A, size_t lda,
-                                                     size_t mstride, const double *trace, int *status, double *result, int mode)
+__global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const float *S, size_t sstride, const double *mdiag,
+                                                     const double *trace, int *status, double *result, int mode)
 {
     const int task = blockIdx.x;
     if (task >= ntask) return;
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const flo
     for (int j = 0; j < n; j++) {
         const double lam = Sm[(size_t)j * n + j];
         const double y1 = log1p(lam) - cl; const double t1 = sl + y1; cl = (t1 - sl) - y1; sl = t1;
-        const double y2 = (A[(size_t)task * mstride + (size_t)j * lda + j] - 1.0) - ca; const double t2 = sa + y2; ca = (t2 - sa) - y2; sa = t2;
+        const double y2 = -mdiag[(size_t)task * n + j] - ca; const double t2 = sa + y2; ca = (t2 - sa) - y2; sa = t2;
         const double y3 = lam - ct; const double t3 = st_ + y3; ct = (t3 - st_) - y3; st_ = t3;
     }
     const double trDelta = sa - 2.0 * st_ - red[0];
@@ -289,10 +289,10 @@ __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const flo
 }
 
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
-                           const double *trace, double *result, int mode, cudaStream_t st, bool tc, bool convert)
+                           const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc, bool convert)
 {
     // convert: A is the FP64 matrix 1 - M and S receives its delta form here; otherwise S
-    // already holds the delta form and A addresses only the FP64 diagonal (lda 0, mstride n)
+    // already holds it.  mdiag: M_ii in FP64, n per task (tr(A - I) = -tr M)
     if (convert) {
         dim3 g(256, ntask);
         k_to_delta32<<<g, 256, 0, st>>>(ntask, n, A, lda, mstride, status, S, sstride);
@@ -312,7 +312,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         else k_syrk_f<<<gs, 64, 0, st>>>(ntask, n, k0, S, sstride, status);
         COUNT_LAUNCH(1);
     }
-    k_final_mixed<<<ntask, 256, 0, st>>>(ntask, n, S, sstride, A, lda, mstride, trace, status, result, mode);
+    k_final_mixed<<<ntask, 256, 0, st>>>(ntask, n, S, sstride, mdiag, trace, status, result, mode);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

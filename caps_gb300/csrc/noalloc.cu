@@ -170,6 +170,7 @@ extern "C" int caps_logdetD_noalloc(caps_t *self, double xi_, int m, double *log
     sd *d_I = C.take<sd>((size_t)2 * L * L);
     double *d_A = C.take<double>((size_t)dim * dim);
     double *d_ld = C.take<double>(dim);
+    double *d_md = C.take<double>(dim);
     double *d_trace = C.take<double>(1), *d_res = C.take<double>(1);
     int *d_gm = C.take<int>(1), *d_glm = C.take<int>(1);
     // the a_0..a_2 table of this m reuses the K partial-sum region when it fits there
@@ -199,9 +200,9 @@ extern "C" int caps_logdetD_noalloc(caps_t *self, double xi_, int m, double *log
     NA_CK(cudaMemcpyAsync(d_glm, &gm_h[1], sizeof(int), cudaMemcpyHostToDevice, st));
     launch_a12(d_gm, d_glm, 1, ldim, d_lft, d_a12, st);
     launch_itab(d_task, 1, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_a12);
-    launch_elem(d_task, 1, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, dim, (size_t)dim * dim, d_status, st);
+    launch_elem(d_task, 1, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, dim, (size_t)dim * dim, d_md, d_status, st);
     const int mode = self->detalg == DETALG_HODLR ? 1 : 0;
-    launch_stats(d_task, 1, dim, d_A, dim, (size_t)dim * dim, mode, d_trace, d_res, d_status, st);
+    launch_stats(d_task, 1, dim, d_A, dim, (size_t)dim * dim, d_md, mode, d_trace, d_res, d_status, st);
     launch_cholesky(1, dim, d_A, dim, (size_t)dim * dim, d_status, d_ld, st);
     launch_final(1, dim, d_ld, d_trace, d_status, d_res, mode, st);
     int status = 0;

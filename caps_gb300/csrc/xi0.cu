@@ -90,7 +90,7 @@ __global__ void k_plasma_ratio(int lmax, double alpha, double *ratio, double *f)
 // M0_MM = M0_EE sqrt(l1 l2 / ((l1+1)(l2+1)))
 // M0_MM_plasma = sqrt(l1 f1/(l1+1) l2 f2/(l2+1)) exp(lfac(l1+l2) - (...)/2 + (l1+l2+1) y) I_{l1+l2}
 __global__ void k_elem0(const int *ms, const int *lmins, int ntask, int ldim, double y, int which, const double *lfac_tab,
-                        const double *Itab, const double *ftab, double *A, size_t mstride, int *status)
+                        const double *Itab, const double *ftab, double *A, size_t mstride, double *mdiag, int *status)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y;
@@ -109,6 +109,7 @@ __global__ void k_elem0(const int *ms, const int *lmins, int ntask, int ldim, do
     }
     if (!isfinite(v)) atomicOr(status + task, ST_ERR_NONFINITE);
     A[(size_t)task * mstride + (size_t)j * ldim + i] = (i == j ? 1.0 : 0.0) - v;
+    if (i == j) mdiag[(size_t)task * ldim + i] = v;
 }
 
 static double *lfac_table_device()
@@ -167,13 +168,14 @@ int logdetD0_batch(caps_t *self, const int *ms, int n, int which, double *out, d
         plasma_tables_device(omegap_, omegap_ / (1 + self->LbyR), 2 * lmax, lmax, &d_I, &d_ratio, &d_f);
     }
     int *d_m, *d_lmin, *d_status;
-    double *d_A, *d_ld, *d_tr, *d_res;
+    double *d_A, *d_ld, *d_md, *d_tr, *d_res;
     const size_t mstride = (size_t)ldim * ldim;
     CK(cudaMalloc(&d_m, n * sizeof(int)));
     CK(cudaMalloc(&d_lmin, n * sizeof(int)));
     CK(cudaMalloc(&d_status, n * sizeof(int)));
     CK(cudaMalloc(&d_A, n * mstride * sizeof(double)));
     CK(cudaMalloc(&d_ld, (size_t)n * ldim * sizeof(double)));
+    CK(cudaMalloc(&d_md, (size_t)n * ldim * sizeof(double)));
     CK(cudaMalloc(&d_tr, n * sizeof(double)));
     CK(cudaMalloc(&d_res, n * sizeof(double)));
     cudaStream_t st = 0;
@@ -181,18 +183,18 @@ int logdetD0_batch(caps_t *self, const int *ms, int n, int which, double *out, d
     CK(cudaMemcpy(d_lmin, lmins.data(), n * sizeof(int), cudaMemcpyHostToDevice));
     CK(cudaMemset(d_status, 0, n * sizeof(int)));
     dim3 g((ldim + 127) / 128, ldim, n);
-    k_elem0<<<g, 128, 0, st>>>(d_m, d_lmin, n, ldim, self->y, which, d_lfac, d_I, d_f, d_A, mstride, d_status);
+    k_elem0<<<g, 128, 0, st>>>(d_m, d_lmin, n, ldim, self->y, which, d_lfac, d_I, d_f, d_A, mstride, d_md, d_status);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
     const int mode = self->detalg == DETALG_HODLR ? 1 : 0;
-    launch_stats(nullptr, n, ldim, d_A, ldim, mstride, mode, d_tr, d_res, d_status, st);
+    launch_stats(nullptr, n, ldim, d_A, ldim, mstride, d_md, mode, d_tr, d_res, d_status, st);
     launch_cholesky(n, ldim, d_A, ldim, mstride, d_status, d_ld, st);
     launch_final(n, ldim, d_ld, d_tr, d_status, d_res, mode, st);
     std::vector<int> hs(n);
     CK(cudaMemcpy(out, d_res, n * sizeof(double), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(hs.data(), d_status, n * sizeof(int), cudaMemcpyDeviceToHost));
     CK(cudaFree(d_m)); CK(cudaFree(d_lmin)); CK(cudaFree(d_status)); CK(cudaFree(d_A));
-    CK(cudaFree(d_ld)); CK(cudaFree(d_tr)); CK(cudaFree(d_res));
+    CK(cudaFree(d_ld)); CK(cudaFree(d_md)); CK(cudaFree(d_tr)); CK(cudaFree(d_res));
     if (d_I) { CK(cudaFree(d_I)); CK(cudaFree(d_ratio)); CK(cudaFree(d_f)); }
     int nerr = 0;
     for (int k = 0; k < n; k++) nerr += (hs[k] & ~0xF) != 0;
