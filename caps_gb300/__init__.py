@@ -50,6 +50,8 @@ def _load():
         "caps_integrate_plasma_init": (vp, [vp, d, d]), "caps_integrate_plasma_free": (None, [vp]),
         "caps_integrate_plasma": (d, [vp, i, i, i, dp, dp]),
         "caps_free_energy": (d, [vp, d, d, d, C.POINTER(_EnergyInfo)]),
+        "caps_free_energy_T0": (d, [vp, d, d, i, C.POINTER(_EnergyInfo)]),
+        "caps_free_energy_psd": (d, [vp, d, d, d, i, C.POINTER(_EnergyInfo)]),
         "caps_gpu_set_precision": (i, [vp, i]),
         "caps_gpu_last_error": (C.c_char_p, []),
         "caps_gpu_set_stream": (None, [vp]),
@@ -249,6 +251,24 @@ class Caps:
         n = info.nxi
         return E, dict(nxi=n, ndet=info.ndet, nwasted=info.nwasted, seconds=info.seconds,
                        xi=list(xi[:n]), logdetD=list(v[:n]))
+
+    def _energy(self, call):
+        xi = (C.c_double * 4096)()
+        v = (C.c_double * 4096)()
+        info = _EnergyInfo(0, 0, 0, 0.0, C.cast(xi, C.POINTER(C.c_double)), C.cast(v, C.POINTER(C.c_double)))
+        E = call(C.byref(info))
+        n = min(info.nxi, 4096)
+        return E, dict(nxi=info.nxi, ndet=info.ndet, nwasted=info.nwasted, seconds=info.seconds,
+                       xi=list(xi[:n]), logdetD=list(v[:n]))
+
+    def free_energy_T0(self, cutoff=1e-9, epsrel=1e-6, method="qagi"):
+        """free energy at T = 0, E (L+R)/(hbar c); method "qagi" (the reference's default) or "fcqs"."""
+        m = {"qagi": 0, "fcqs": 1}[method]
+        return self._energy(lambda info: lib.caps_free_energy_T0(self._h, float(cutoff), float(epsrel), m, info))
+
+    def free_energy_psd(self, T, cutoff=1e-9, epsrel=1e-6, order=0):
+        """free energy at T > 0 by Pade spectrum decomposition (order <= 0: automatic)"""
+        return self._energy(lambda info: lib.caps_free_energy_psd(self._h, float(T), float(cutoff), float(epsrel), int(order), info))
 
 
 class MLP:

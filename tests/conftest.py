@@ -24,7 +24,8 @@ def ref_values():
     return json.load(open(os.path.join(GOLDEN, "reference_values.json")))
 
 
-SMALL_ENERGIES = ["pr_RbyL10_ldim70_T300", "drude_RbyL10_ldim70_T300", "plasma_RbyL10_ldim70_T300"]
+SMALL_ENERGIES = ["pr_RbyL10_ldim70_T300", "drude_RbyL10_ldim70_T300", "plasma_RbyL10_ldim70_T300",
+                  "t0_drude_RbyL20_ldim100", "psd_drude_RbyL10_ldim70_T300"]
 
 
 @pytest.fixture(scope="session")

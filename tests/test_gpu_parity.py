@@ -207,3 +207,56 @@ def test_logdetD0_m0_RbyL1000_analytic(cg, unit_vectors):
     ee, mm = c.logdetD0(t["m"])
     assert relx(ee, t["EE"]) < 1e-10, (ee, t["EE"])
     assert relx(mm, t["MM"]) < 1e-10, (mm, t["MM"])
+
+
+def test_free_energy_T0_golden(cg, energy_golden):
+    """T = 0 through caps_free_energy_T0 (qagi, the reference's default) against the
+    reference's dqagi over its own logdetD (tests/golden/make_golden_energy.py t0): the
+    same abscissae (neval), the same PFA cuts, E to 1e-10"""
+    d = energy_golden["t0_drude_RbyL20_ldim100"]
+    c = cg.Caps(d["R"], d["L"], ldim=d["ldim"], detalg=cg.DETALG_LU)
+    c.set_drude(*d["drude"])
+    E, info = c.free_energy_T0()
+    assert info["nxi"] == d["neval"]
+    assert sum(1 for v in info["logdetD"] if v == 0) == sum(1 for v in d["logdetD"] if v == 0)
+    assert abs(E - d["E"]) <= TOL * abs(d["E"]), (E, d["E"])
+    # the Fourier-Chebyshev scheme is a different rule: it agrees within the quadrature tolerance
+    E2, _ = c.free_energy_T0(epsrel=1e-7, method="fcqs")
+    assert abs(E2 - d["E"]) <= 1e-6 * abs(d["E"]), (E2, d["E"])
+
+
+def test_free_energy_psd_golden(cg, energy_golden):
+    """Pade spectrum decomposition through caps_free_energy_psd against the reference's psd
+    poles over its own logdetD, and the Matsubara sum of the same geometry within epsrel"""
+    d = energy_golden["psd_drude_RbyL10_ldim70_T300"]
+    c = cg.Caps(d["R"], d["L"], ldim=d["ldim"], detalg=cg.DETALG_LU)
+    c.set_drude(*d["drude"])
+    E, info = c.free_energy_psd(d["T"])
+    assert info["nxi"] == d["order"] + 1
+    assert abs(E - d["E"]) <= TOL * abs(d["E"]), (E, d["E"])
+    Em = energy_golden["drude_RbyL10_ldim70_T300"]["E"]
+    assert abs(E - Em) <= 1e-6 * abs(Em), (E, Em)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_logdetD_extreme_xi_vs_oracle(cg, ob, prec):
+    """the frequencies a T=0 quadrature visits: xi_ down to 3e-4 (the K grid must stay in
+    budget when e^{-alpha cosh t} barely decays) and up to 400 (logdetD ~ 1e-17: the trace
+    must come from M itself, not from 1 - A_ii)"""
+    R, L, ldim = 20e-6, 1e-6, 60
+    drude = (9.0, 0.035)
+    c = cg.Caps(R, L, ldim=ldim, detalg=cg.DETALG_LU)
+    c.set_drude(*drude)
+    c.set_precision(cg.PREC_MIXED if prec == "mixed" else cg.PREC_FP64)
+    tol = TOL if prec == "fp64" else 5e-8
+    xs = [3.5e-4, 1.4e-3, 0.05, 150.0, 300.0, 402.0]
+    ms = [0, 1, 7]
+    bx = [x for x in xs for _ in ms]
+    bm = [m for _ in xs for m in ms]
+    got, st = c.logdetD_batch(bx, bm)
+    want = ob.logdetD_batch(R, L, ldim, bx, bm, drude, threads=8)
+    for x, m, g, s, w in zip(bx, bm, got, st, want):
+        assert s < 16, (x, m, s)
+        # relative to the value itself: tiny logdetD must keep their own digits
+        bar = tol * abs(w) if (prec == "fp64" or abs(w) < 1e-8) else tol * max(1.0, abs(w))
+        assert abs(g - w) <= bar, (x, m, g, w)
