@@ -15,6 +15,7 @@ HBAR, KB, CL = 1.0545718e-34, 1.38064852e-23, 299792458.0
 GEOMETRIES = [(20e-6, 1e-6, 140), (50e-6, 1e-6, 350), (100e-6, 1e-6, 700), (150e-6, 1e-6, 1050)]
 MATERIALS = [None, (9.0, 0.035), (7.0, 0.02), (10.0, 0.05)]
 PERFECT_OMEGAP_EV = 50.0   # feature value that encodes a perfect reflector
+TAIL_FLOOR = 1e-16         # smallest |logdetD| kept as a training target
 
 
 def training_set(geometries=GEOMETRIES, materials=MATERIALS, nxi=9, ms=None, precision=PREC_FP64):
@@ -36,7 +37,9 @@ def training_set(geometries=GEOMETRIES, materials=MATERIALS, nxi=9, ms=None, pre
             out, st = c.logdetD_batch(bx, bm)
             count += len(bx)
             for xi_, m, v, s in zip(bx, bm, out, st):
-                if s >= 16 or not (v < 0):
+                # the truncation rules only look at values within ~1e-15 of the leading
+                # term (m cutoff 1e-9 of v_0, v_0 >= 1e-6): a deeper tail is left out
+                if s >= 16 or not (v < -TAIL_FLOOR):
                     continue
                 X.append(MLP.features(RbyL, xi_, m, wp, ga))
                 y.append(math.log(-v))
