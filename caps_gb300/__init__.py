@@ -35,6 +35,8 @@ def _load():
         "caps_set_detalg": (i, [vp, i]), "caps_get_detalg": (i, [vp]),
         "caps_set_epsrel": (i, [vp, d]), "caps_get_epsrel": (d, [vp]),
         "caps_set_epsilonm1": (None, [vp, vp, vp]),
+        "material_init": (vp, [C.c_char_p, d]), "material_free": (None, [vp]),
+        "material_epsilonm1": (d, [d, vp]), "material_get_extrapolation": (None, [vp, dp, dp, dp, dp]),
         "caps_set_epsilonm1_plate": (None, [vp, vp, vp]),
         "caps_set_epsilonm1_sphere": (None, [vp, vp, vp]),
         "caps_logdetD": (d, [vp, d, i]),
@@ -130,6 +132,7 @@ class Caps:
         if not self._h:
             raise ValueError("caps_init failed (R and L must be positive)")
         self._ud = None
+        self._mat = None
         self.R, self.L = R, L
         if ldim is not None:
             lib.caps_set_ldim(self._h, ldim)
@@ -141,6 +144,22 @@ class Caps:
         if h:
             lib.caps_free(h)
             self._h = None
+        m = getattr(self, "_mat", None)
+        if m:
+            lib.material_free(m)
+            self._mat = None
+
+    def set_material(self, path):
+        """plate and sphere from a tabulated optical-data file (material_init +
+        material_epsilonm1, as the reference driver's --material)"""
+        m = lib.material_init(os.fsencode(path), self.L + self.R)
+        if not m:
+            raise ValueError("material_init failed: %s (missing file or wrong format)" % path)
+        fn = C.cast(lib.material_epsilonm1, C.c_void_p)
+        lib.caps_set_epsilonm1(self._h, fn, m)
+        if self._mat:
+            lib.material_free(self._mat)
+        self._mat = m
 
     @property
     def ldim(self):

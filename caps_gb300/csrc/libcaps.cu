@@ -857,7 +857,8 @@ static double kahan_sum(const double *v, size_t n)
     return s;
 }
 
-// which xi = 0 rule applies: 0 perfect reflectors, 1 Drude (analytic), 2 plasma
+// which xi = 0 rule applies: 0 perfect reflectors, 1 Drude (analytic), 2 plasma; a
+// tabulated material follows its low-frequency extrapolation (caps.c:782-803)
 static int xi0_model(const caps_t *c)
 {
     if (c->epsilonm1_plate == caps_epsilonm1_perf) return 0;
@@ -865,7 +866,16 @@ static int xi0_model(const caps_t *c)
         const double *p = (const double *)c->userdata_plate;
         return p[1] > 0 ? 1 : 2;
     }
+    if (c->epsilonm1_plate == material_epsilonm1 && c->userdata_plate)
+        return ((const material_t *)c->userdata_plate)->gamma_low > 0 ? 1 : 2;
     return 1;
+}
+
+// plasma frequency (rad/s) of the plasma model's xi = 0 term
+static double xi0_omegap(const caps_t *c)
+{
+    if (c->epsilonm1_plate == material_epsilonm1) return ((const material_t *)c->userdata_plate)->omegap_low;
+    return ((const double *)c->userdata_plate)[0];
 }
 
 struct MState {
@@ -945,7 +955,7 @@ double xi0_term(caps_t *self, double cutoff, int *ndet_, int *nwasted_)
         // drude_HT + sum'_m logdetD0 MM (perfect reflectors) or MM_plasma (plasma model)
         // with the m cutoff (caps.c:329-395, worker :921-929)
         const int which = model == 0 ? 1 : 2;
-        const double omegap = model == 2 ? ((const double *)self->userdata_plate)[0] : 0.0;
+        const double omegap = model == 2 ? xi0_omegap(self) : 0.0;
         const double drude = caps_ht_drude(self);
         std::vector<double> terms;
         int mstop = -1;

@@ -139,6 +139,27 @@ double caps_kernel_M0_MM_plasma(int i, int j, void *args_);         /* libcaps.h
 
 void caps_logdetD0(caps_t *self, int m, double omegap, double *EE, double *MM, double *MM_plasma); /* libcaps.h:163, libcaps.c:985 */
 
+/* ---- tabulated materials (src/include/material.h:11-30) ---- */
+typedef struct {
+    char filename[512]; /* material file */
+    double calL;        /* L+R */
+    double xi_min;      /* lowest tabulated frequency (rad/s) */
+    double xi_max;      /* highest tabulated frequency (rad/s) */
+    size_t points;      /* number of tabulated points */
+    double *xi;         /* tabulated frequencies (rad/s) */
+    double *epsm1;      /* tabulated eps(i xi) - 1 */
+    double omegap_low;  /* Drude extrapolation below the table (rad/s) */
+    double gamma_low;
+    double omegap_high; /* Drude extrapolation above the table (rad/s) */
+    double gamma_high;
+} material_t;
+material_t *material_init(const char *filename, double calL);            /* material.h:24, material.c:63 */
+void material_info(material_t *material, FILE *stream, const char *prefix); /* material.h:25, material.c:225 */
+void material_free(material_t *material);                                 /* material.h:26, material.c:205 */
+void material_get_extrapolation(material_t *material, double *omegap_low, double *gamma_low, double *omegap_high,
+                                double *gamma_high);                      /* material.h:28, material.c:189 */
+double material_epsilonm1(double xi, void *args);                         /* material.h:30, material.c:251 */
+
 /* ---- plasma xi=0 integrals (src/include/integration.h:24-26) ---- */
 integration_plasma_t *caps_integrate_plasma_init(caps_t *caps, double omegap, double epsrel); /* integration.h:24, integration.c:897 */
 double caps_integrate_plasma(integration_plasma_t *self, int l1, int l2, int m, double *ratio1, double *ratio2); /* integration.h:25, integration.c:954 */

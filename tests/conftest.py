@@ -25,7 +25,7 @@ def ref_values():
 
 
 SMALL_ENERGIES = ["pr_RbyL10_ldim70_T300", "drude_RbyL10_ldim70_T300", "plasma_RbyL10_ldim70_T300",
-                  "t0_drude_RbyL20_ldim100", "psd_drude_RbyL10_ldim70_T300"]
+                  "t0_drude_RbyL20_ldim100", "psd_drude_RbyL10_ldim70_T300", "material_RbyL10_ldim70_T300"]
 
 
 @pytest.fixture(scope="session")

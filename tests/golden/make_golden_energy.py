@@ -10,6 +10,7 @@ value does not depend on the pool size).  Writes tests/golden/energy_<name>.json
     python tests/golden/make_golden_energy.py plasma  # plasma model (gamma = 0), R/L=10
     python tests/golden/make_golden_energy.py t0      # T = 0 (reference dqagi), Drude, R/L=20
     python tests/golden/make_golden_energy.py psd     # Pade spectrum decomposition, Drude, R/L=10
+    python tests/golden/make_golden_energy.py material  # tabulated material (tests/golden/material_synthetic.txt)
 """
 import ctypes as C
 import json
@@ -41,6 +42,9 @@ def _init():
     _lib.caps_ht_drude.restype = C.c_double
     _lib.caps_ht_drude.argtypes = [C.c_void_p]
     _lib.caps_logdetD0.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    _lib.material_init.restype = C.c_void_p
+    _lib.material_init.argtypes = [C.c_char_p, C.c_double]
+    _lib.material_free.argtypes = [C.c_void_p]
 
 
 def _task(args):
@@ -49,7 +53,12 @@ def _task(args):
     _lib.caps_set_ldim(c, ldim)
     _lib.caps_set_detalg(c, detalg)
     ud = None
-    if drude:
+    mat = None
+    if isinstance(drude, str):
+        # tabulated material (the caps driver's --material, caps.c:573-586)
+        mat = _lib.material_init(os.path.join(ROOT, drude).encode(), R + L)
+        _lib.caps_set_epsilonm1(c, C.cast(_lib.material_epsilonm1, C.c_void_p), C.c_void_p(mat))
+    elif drude:
         ud = (C.c_double * 2)(drude[0] / HBAR_EV, drude[1] / HBAR_EV)
         _lib.caps_set_epsilonm1(c, C.cast(_lib.caps_epsilonm1_drude, C.c_void_p), C.cast(ud, C.c_void_p))
     if xi == 0 and drude:
@@ -64,6 +73,8 @@ def _task(args):
     else:
         r = _lib.caps_logdetD(c, xi, m)
     _lib.caps_free(c)
+    if mat:
+        _lib.material_free(mat)
     return r
 
 
@@ -96,7 +107,8 @@ def energy(R, L, ldim, T, drude, cutoff=1e-9, epsrel=1e-6, detalg=1, procs=8):
     with mp.Pool(procs, initializer=_init) as pool:
         c = _lib.caps_init(R, L)
         _lib.caps_set_ldim(c, ldim)
-        if drude and drude[1] > 0:
+        if isinstance(drude, str) or (drude and drude[1] > 0):
+            # Drude, or a material whose low-frequency extrapolation is Drude (gamma_low > 0)
             v0 = _lib.caps_ht_drude(c)
         else:
             # perfect reflectors and the plasma model (caps.c:329-395)
@@ -185,6 +197,7 @@ if __name__ == "__main__":
     cases = {
         "small": [("pr_RbyL10_ldim70_T300", 10e-6, 1e-6, 70, 300.0, None), ("drude_RbyL10_ldim70_T300", 10e-6, 1e-6, 70, 300.0, (9.0, 0.035))],
         "plasma": [("plasma_RbyL10_ldim70_T300", 10e-6, 1e-6, 70, 300.0, (9.0, 0.0))],
+        "material": [("material_RbyL10_ldim70_T300", 10e-6, 1e-6, 70, 300.0, "tests/golden/material_synthetic.txt")],
         "t0": [("t0_drude_RbyL20_ldim100", 20e-6, 1e-6, 100, 0.0, (9.0, 0.035))],
         "psd": [("psd_drude_RbyL10_ldim70_T300", 10e-6, 1e-6, 70, 300.0, (9.0, 0.035))],
         "c2": [("pr_RbyL50_ldim350_T300", 50e-6, 1e-6, 350, 300.0, None)],

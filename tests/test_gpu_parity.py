@@ -260,3 +260,14 @@ def test_logdetD_extreme_xi_vs_oracle(cg, ob, prec):
         # relative to the value itself: tiny logdetD must keep their own digits
         bar = tol * abs(w) if (prec == "fp64" or abs(w) < 1e-8) else tol * max(1.0, abs(w))
         assert abs(g - w) <= bar, (x, m, g, w)
+
+
+def test_free_energy_material_golden(cg, energy_golden):
+    """a tabulated material (set_material: material_init + material_epsilonm1) through
+    caps_free_energy against the reference library's free energy with the same file"""
+    d = energy_golden["material_RbyL10_ldim70_T300"]
+    c = cg.Caps(d["R"], d["L"], ldim=d["ldim"], detalg=cg.DETALG_LU)
+    c.set_material(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "material_synthetic.txt"))
+    E, info = c.free_energy(d["T"])
+    assert info["nxi"] == len(d["xi"])
+    assert abs(E - d["E"]) <= TOL * abs(d["E"]), (E, d["E"])
