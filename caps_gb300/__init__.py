@@ -53,6 +53,8 @@ def _load():
         "caps_integrate_plasma": (d, [vp, i, i, i, dp, dp]),
         "caps_free_energy": (d, [vp, d, d, d, C.POINTER(_EnergyInfo)]),
         "caps_free_energy_T0": (d, [vp, d, d, i, C.POINTER(_EnergyInfo)]),
+        "caps_logdetD2_batch": (i, [vp, dp, ip, i, dp, ip]),
+        "caps_sphere_sphere_T0": (d, [vp, d, d, C.POINTER(_EnergyInfo)]),
         "caps_free_energy_psd": (d, [vp, d, d, d, i, C.POINTER(_EnergyInfo)]),
         "caps_gpu_set_precision": (i, [vp, i]),
         "caps_gpu_last_error": (C.c_char_p, []),
@@ -284,6 +286,21 @@ class Caps:
         """free energy at T = 0, E (L+R)/(hbar c); method "qagi" (the reference's default) or "fcqs"."""
         m = {"qagi": 0, "fcqs": 1}[method]
         return self._energy(lambda info: lib.caps_free_energy_T0(self._h, float(cutoff), float(epsrel), m, info))
+
+    def logdetD2_batch(self, xi_, m):
+        """sphere-sphere: log det(1 - M^2) per (xi, m); make the object with L = d/2"""
+        xi_ = np.ascontiguousarray(xi_, dtype=np.float64)
+        m = np.ascontiguousarray(m, dtype=np.int32)
+        n = len(xi_)
+        out = np.empty(n)
+        st = np.empty(n, dtype=np.int32)
+        lib.caps_logdetD2_batch(self._h, xi_.ctypes.data_as(C.POINTER(C.c_double)), m.ctypes.data_as(C.POINTER(C.c_int)), n,
+                                out.ctypes.data_as(C.POINTER(C.c_double)), st.ctypes.data_as(C.POINTER(C.c_int)))
+        return out, st
+
+    def sphere_sphere_T0(self, cutoff=1e-10, epsrel=1e-6):
+        """two spheres of radius R at separation d = 2L, T = 0: E d/(hbar c)"""
+        return self._energy(lambda info: lib.caps_sphere_sphere_T0(self._h, float(cutoff), float(epsrel), info))
 
     def free_energy_psd(self, T, cutoff=1e-9, epsrel=1e-6, order=0):
         """free energy at T > 0 by Pade spectrum decomposition (order <= 0: automatic)"""

@@ -48,6 +48,9 @@ int itab_group_size();
 void launch_itab_grp(const Task *tasks, int ntask, const int4 *groups, int ngroups, int ldim, const sd *K, int nu_stride,
                      double4 *ptab, int pstride, ffe *KF, float4 *ptabf, const void *a12, void *Iout, bool ffe_out, int *status,
                      cudaStream_t st);
+// sphere-sphere: B = 1 - M^2 and (M^2)_ii from A = 1 - M and M_ii (square.cu)
+void launch_square(int ntask, int n, const double *A, size_t lda, size_t mstride, const double *mdiag, double *B,
+                   const int *status, double *mdiag2, cudaStream_t st);
 // a_0, a_1, a_2 per distinct m of a chunk (groups), shared by all frequencies
 void launch_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, cudaStream_t st);
 size_t a12_bytes(int ldim, int ngroup);

@@ -86,7 +86,7 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -358,6 +358,7 @@ struct BatchOpts {
     bool factor = true;      // false: stop after assembly (caps_M_init)
     double *M_out = nullptr; // host buffer for the dense M of a single task (row-major)
     double *mie_out_a = nullptr, *mie_out_b = nullptr; // Mie of task 0's window
+    bool square = false;     // sphere-sphere: log det(1 - M^2) (FP64, dense rules)
 };
 
 static void h2d(void *dst, const void *src, size_t bytes, cudaStream_t st)
@@ -439,15 +440,15 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     CK(cudaMemGetInfo(&freeb, &totb));
     // mixed precision without a dense-M request: elements go straight into the FP32 delta
     // matrix (no FP64 matrix)
-    const bool ff_elem = caps->precision == CAPS_PREC_MIXED && O.factor && !O.M_out;
-    const size_t mat_bytes = ff_elem ? 4 + 1 : (caps->precision == CAPS_PREC_MIXED ? 12 : 8);
+    const bool ff_elem = caps->precision == CAPS_PREC_MIXED && O.factor && !O.M_out && !O.square;
+    const size_t mat_bytes = O.square ? 16 : ff_elem ? 4 + 1 : (caps->precision == CAPS_PREC_MIXED ? 12 : 8);
     const size_t per_task = (size_t)dim * dim * mat_bytes + (size_t)2 * L * L * sizeof(sd) + (size_t)2 * nu_stride * sizeof(sd)
                           + (size_t)nu_stride * sizeof(double2) + (size_t)3 * L * sizeof(sd) + (size_t)dim * 8
                           + (size_t)2 * 256 * nu_stride * 12  // partial sums, up to 256 warps
                           + (size_t)(4 * (caps->ldim + 4096)) * sizeof(double4)  // p tables
                           + (size_t)L * (L + 1) / 2 * 32;                         // a_0..a_2 table (at most one row per task)
     size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes + g_eng.S32.bytes
-                                             + g_eng.a12.bytes + g_eng.part.bytes));
+                                             + g_eng.a12.bytes + g_eng.part.bytes + g_eng.B.bytes));
     int chunk = (int)std::max<size_t>(1, std::min<size_t>(budget / per_task, 65535));
     chunk = std::min(chunk, n);
 
@@ -557,6 +558,14 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             d_A = (double *)g_eng.A.get((size_t)nt * mstride * sizeof(double));
             d_dg = (double *)g_eng.diag.get((size_t)nt * dim * sizeof(double));
             launch_elem(d_tasks, nt, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, lda, mstride, d_dg, d_status, st);
+            if (O.square) {
+                // sphere-sphere: continue with B = 1 - M^2 in place of A
+                double *d_B = (double *)g_eng.B.get((size_t)nt * mstride * sizeof(double));
+                double *d_dg2 = (double *)g_eng.diag2.get((size_t)nt * dim * sizeof(double));
+                launch_square(nt, dim, d_A, lda, mstride, d_dg, d_B, d_status, d_dg2, st);
+                d_A = d_B;
+                d_dg = d_dg2;
+            }
             if (O.factor) launch_stats(d_tasks, nt, dim, d_A, lda, mstride, d_dg, O.mode, d_trace, d_res, d_status, st);
         }
         CK(cudaEventRecord(g_eng.ev[4], st));
@@ -565,7 +574,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         static const bool tc = getenv("CAPS_MIXED_SIMT") == nullptr;
         if (ff_elem) {
             launch_cholesky_mixed(nt, dim, nullptr, 0, 0, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, false);
-        } else if (O.factor && caps->precision == CAPS_PREC_MIXED) {
+        } else if (O.factor && caps->precision == CAPS_PREC_MIXED && !O.square) {
             d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
             launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc);
         } else if (O.factor) {
@@ -623,6 +632,18 @@ extern "C" int caps_logdetD_batch(caps_t *self, const double *xi_, const int *m,
     if (n <= 0) return 0;
     BatchOpts O;
     O.mode = detalg_mode(self);
+    return run_batch(self, xi_, m, n, out, status, O);
+}
+
+// sphere-sphere (cass.c:23-64): log det(1 - M^2) of the plane-sphere round trip M at
+// the caps object's L (half the sphere-sphere separation), dense rules, FP64
+extern "C" int caps_logdetD2_batch(caps_t *self, const double *xi_, const int *m, int n, double *out, int *status)
+{
+    if (n <= 0) return 0;
+    for (int i = 0; i < n; i++) TERMINATE(!(xi_[i] > 0), "Matsubara frequency must be positive");
+    BatchOpts O;
+    O.mode = 0;
+    O.square = true;
     return run_batch(self, xi_, m, n, out, status, O);
 }
 
@@ -905,7 +926,11 @@ static int m_chunk(const MState &s, double cutoff)
 // v_m == 0 or v_m / v_0 < cutoff, Kahan-summed in m order (caps.c:307-396), for n
 // frequencies at once: the m chunks of every unfinished frequency share one GPU batch
 // per round.  A non-finite term ends that frequency with F = NaN.
-void fxi_batch(caps_t *self, const double *xi, int n, double cutoff, double *out, int *ndet, int *nwasted)
+extern "C" int caps_logdetD2_batch(caps_t *self, const double *xi_, const int *m, int n, double *out, int *status);
+
+// kind 1: the sphere-sphere sum of cass.c:78-92 instead -- logdet(1 - M^2) terms and
+// 2 kahan(terms over 4096 slots) - term_0
+void fxi_batch(caps_t *self, const double *xi, int n, double cutoff, double *out, int *ndet, int *nwasted, int kind)
 {
     std::vector<MState> st(n);
     std::vector<char> bad(n, 0);
@@ -922,7 +947,8 @@ void fxi_batch(caps_t *self, const double *xi, int n, double cutoff, double *out
         }
         if (bx.empty()) break;
         std::vector<double> r(bx.size());
-        caps_logdetD_batch(self, bx.data(), bm.data(), (int)bx.size(), r.data(), NULL);
+        if (kind == 1) caps_logdetD2_batch(self, bx.data(), bm.data(), (int)bx.size(), r.data(), NULL);
+        else caps_logdetD_batch(self, bx.data(), bm.data(), (int)bx.size(), r.data(), NULL);
         if (ndet) *ndet += (int)bx.size();
         for (size_t k = 0; k < bx.size(); k++) st[who[k].first].v[who[k].second] = r[k];
         for (int i = 0; i < n; i++) {
@@ -939,6 +965,11 @@ void fxi_batch(caps_t *self, const double *xi, int n, double cutoff, double *out
         if (nwasted) *nwasted += s.next - (s.mstop + 1);
         if (bad[i]) { out[i] = NAN; continue; }
         std::vector<double> t(s.v.begin(), s.v.begin() + s.mstop + 1);
+        if (kind == 1) {
+            t.resize(4096, 0.0);
+            out[i] = 2 * kahan_sum(t.data(), t.size()) - t[0];
+            continue;
+        }
         t[0] /= 2;
         out[i] = kahan_sum(t.data(), t.size());
     }

@@ -476,7 +476,7 @@ static int psd(int N, double *xi, double *eta)
 } // namespace capsgpu
 
 // implemented in libcaps.cu
-void fxi_batch(caps_t *self, const double *xi, int n, double cutoff, double *out, int *ndet, int *nwasted);
+void fxi_batch(caps_t *self, const double *xi, int n, double cutoff, double *out, int *ndet, int *nwasted, int kind);
 double xi0_term(caps_t *self, double cutoff, int *ndet, int *nwasted);
 
 using namespace capsgpu;
@@ -525,7 +525,7 @@ extern "C" double caps_free_energy_T0(caps_t *self, double cutoff, double epsrel
             else { xs.push_back(xi_); where.push_back(k); }
         }
         std::vector<double> v(xs.size());
-        if (!xs.empty()) fxi_batch(self, xs.data(), (int)xs.size(), cutoff, v.data(), &ndet, &nwasted);
+        if (!xs.empty()) fxi_batch(self, xs.data(), (int)xs.size(), cutoff, v.data(), &ndet, &nwasted, 0);
         for (size_t k = 0; k < xs.size(); k++) y[where[k]] = v[k];
         for (int k = 0; k < n && info; k++, nrec++)
             if (nrec < 4096) {
@@ -564,7 +564,7 @@ extern "C" double caps_free_energy_psd(caps_t *self, double T, double cutoff, do
     qp::psd(order, pxi.data(), peta.data());
     for (int n = 0; n < order; n++) xs[n] = pxi[n] * Ts / (2 * M_PI);
     std::vector<double> Fv(order);
-    fxi_batch(self, xs.data(), order, cutoff, Fv.data(), &ndet, &nwasted);
+    fxi_batch(self, xs.data(), order, cutoff, Fv.data(), &ndet, &nwasted, 0);
     v[0] = v0 / 2;
     for (int n = 0; n < order; n++) v[n + 1] = peta[n] * Fv[n];
     double s = 0, c = 0;
@@ -580,4 +580,37 @@ extern "C" double caps_free_energy_psd(caps_t *self, double T, double cutoff, do
         }
     }
     return Ts / M_PI * s;
+}
+
+// ---- sphere-sphere at T = 0 (cass.c:66-223) ----
+// Two spheres of the caps object's radius R at separation d = 2L (the caps object is
+// made with L = d/2): E d/(hbar c) = 1/(2 pi) int_0^inf dy F2(y), y = xi d/c,
+// F2 = 2 sum_m logdet(1 - M^2) - the m = 0 term, m cut as the plane-sphere sum;
+// QUADPACK qagi with relative tolerance epsrel.
+extern "C" double caps_sphere_sphere_T0(caps_t *self, double cutoff, double epsrel, caps_energy_info_t *info)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    const double L = self->L, R = self->R;
+    int ndet = 0, nwasted = 0, nrec = 0;
+    const BatchFn F = [&](const double *x, int n, double *y) {
+        std::vector<double> xs(n);
+        for (int k = 0; k < n; k++) xs[k] = x[k] * (L + R) / (2 * L);
+        fxi_batch(self, xs.data(), n, cutoff, y, &ndet, &nwasted, 1);
+        for (int k = 0; k < n && info; k++, nrec++)
+            if (nrec < 4096) {
+                if (info->xi) info->xi[nrec] = xs[k];
+                if (info->logdetD) info->logdetD[nrec] = y[k];
+            }
+    };
+    double abserr = 0;
+    int neval = 0, ier = 0;
+    const double integral = qp::qagi(F, 0, 1, 0, epsrel, &abserr, &neval, &ier);
+    if (ier != 0) fprintf(stderr, "caps_sphere_sphere_T0: quadrature ier=%d\n", ier);
+    if (info) {
+        info->nxi = neval;
+        info->ndet = ndet;
+        info->nwasted = nwasted;
+        info->seconds = seconds_since(t0);
+    }
+    return integral / (2 * M_PI);
 }

@@ -211,6 +211,15 @@ double caps_free_energy_T0(caps_t *self, double cutoff, double epsrel, int metho
  * order (<= 0: the reference's automatic order, caps.c:635-639); all poles in one batch. */
 double caps_free_energy_psd(caps_t *self, double T, double cutoff, double epsrel, int order, caps_energy_info_t *info);
 
+/* Sphere-sphere geometry (the reference's cass program, src/cass.c): two spheres of radius
+ * R at separation d, for perfect reflectors as cass computes them.  Create the object with
+ * caps_init(R, d/2): the round trip is M^2 with M the plane-sphere round trip at L = d/2.
+ * caps_logdetD2_batch: log det(1 - M^2) per (xi, m) (cass.c:23-64: trace shortcut below
+ * 1e-8, dense Mercator rule, else factorisation; FP64).  caps_sphere_sphere_T0: the T = 0
+ * energy E d/(hbar c) (cass.c:66-92, 210-219: qagi over y = xi d/c of 2 sum_m - m=0 term). */
+int caps_logdetD2_batch(caps_t *self, const double *xi_, const int *m, int n, double *out, int *status);
+double caps_sphere_sphere_T0(caps_t *self, double cutoff, double epsrel, caps_energy_info_t *info);
+
 /* The quadratures and PSD poles behind these drivers, on a host callback: the same
  * algorithms as the reference's dqagi (cquadpack/src/dqagi.c:40), fcqs_semiinf
  * (src/fcqs.c:107) and psd (src/psd.c:80), with the same arguments and results. */

@@ -271,3 +271,29 @@ def test_free_energy_material_golden(cg, energy_golden):
     E, info = c.free_energy(d["T"])
     assert info["nxi"] == len(d["xi"])
     assert abs(E - d["E"]) <= TOL * abs(d["E"]), (E, d["E"])
+
+
+@pytest.fixture(scope="module")
+def cass_golden():
+    import json
+    return json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cass_golden.json")))
+
+
+def test_sphere_sphere_logdetD2_golden(cg, cass_golden):
+    """log det(1 - M^2) of the sphere-sphere round trip against the reference library run
+    through the steps of its cass program (matrix_mult, matrix_trace, matrix_logdet_dense)"""
+    g = cass_golden
+    c = cg.Caps(g["R"], g["d"] / 2, ldim=g["ldim"], detalg=cg.DETALG_LU)
+    out, st = c.logdetD2_batch([s["xi"] for s in g["samples"]], [s["m"] for s in g["samples"]])
+    for s, v, code in zip(g["samples"], out, st):
+        assert code < 16, (s, code)
+        assert abs(v - s["logdetD2"]) <= TOL * abs(s["logdetD2"]), (s, v)
+
+
+def test_sphere_sphere_T0_golden(cg, cass_golden):
+    """the T = 0 sphere-sphere energy (cass): same qagi abscissae, E to 1e-10"""
+    g = cass_golden
+    c = cg.Caps(g["R"], g["d"] / 2, ldim=g["ldim"], detalg=cg.DETALG_LU)
+    E, info = c.sphere_sphere_T0(g["cutoff"], g["epsrel"])
+    assert info["nxi"] == g["neval"]
+    assert abs(E - g["E"]) <= TOL * abs(g["E"]), (E, g["E"])
