@@ -127,6 +127,7 @@ enum : int {
     ST_ERR_PIVOT = 16,   // non-positive pivot in the Cholesky factorisation
     ST_ERR_NONFINITE = 32, // non-finite matrix element or integral
     ST_ERR_GRID = 64,      // quadrature grid did not fit the node budget
+    ST_ERR_WAIT = 128,     // a bounded wait for the tensor cores ran out
 };
 
 } // namespace capsgpu

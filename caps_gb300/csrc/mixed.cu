@@ -15,12 +15,16 @@
 // The pivot logarithms and every sum are FP64.  The result agrees with the
 // FP64 Cholesky to ~3e-9 absolute on the hardest matrices of the workload
 // (log det ~ -1) and to <1e-12 on the rest.
+#include <cstdlib>
+
 #include "common.cuh"
 #include "internal.h"
+#include "syrk_umma.cuh"
 
 namespace capsgpu {
 
 constexpr int MB = 64; // panel width
+static_assert(MB == UM_K, "the tcgen05 trailing update is built for the panel width");
 
 // S = A - I (lower triangle, FP32) for the tasks that need a factorisation
 __global__ void k_to_delta32(int ntask, int n, const double *A, size_t lda, size_t mstride, const int *status, float *S,
@@ -292,7 +296,15 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
                            const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc, bool convert)
 {
     // convert: A is the FP64 matrix 1 - M and S receives its delta form here; otherwise S
-    // already holds it.  mdiag: M_ii in FP64, n per task (tr(A - I) = -tr M)
+    // already holds it.  mdiag: M_ii in FP64, n per task (tr(A - I) = -tr M).
+    // Trailing update: tcgen05 (k_syrk_umma); CAPS_MIXED_MMASYNC=1 selects the mma.sync
+    // kernel, tc = false (CAPS_MIXED_SIMT=1) the FFMA one.
+    static const bool legacy_mma = getenv("CAPS_MIXED_MMASYNC") != nullptr;
+    static bool attr = false;
+    if (!attr) {
+        CK(cudaFuncSetAttribute(k_syrk_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
+        attr = true;
+    }
     if (convert) {
         dim3 g(256, ntask);
         k_to_delta32<<<g, 256, 0, st>>>(ntask, n, A, lda, mstride, status, S, sstride);
@@ -308,8 +320,13 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         COUNT_LAUNCH(1);
         const int nt = (rest + 63) / 64;
         dim3 gs(nt * (nt + 1) / 2, ntask);
-        if (tc) k_syrk_tc<<<gs, 128, 0, st>>>(ntask, n, k0, S, sstride, status);
-        else k_syrk_f<<<gs, 64, 0, st>>>(ntask, n, k0, S, sstride, status);
+        if (tc && !legacy_mma) {
+            const int nr = (rest + UM_M - 1) / UM_M;
+            k_syrk_umma<<<dim3(nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, S, sstride, status);
+        } else if (tc)
+            k_syrk_tc<<<gs, 128, 0, st>>>(ntask, n, k0, S, sstride, status);
+        else
+            k_syrk_f<<<gs, 64, 0, st>>>(ntask, n, k0, S, sstride, status);
         COUNT_LAUNCH(1);
     }
     k_final_mixed<<<ntask, 256, 0, st>>>(ntask, n, S, sstride, mdiag, trace, status, result, mode);

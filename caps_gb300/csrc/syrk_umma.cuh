@@ -1,0 +1,137 @@
+// syrk_umma.cuh -- trailing update of the FP32 delta-form Cholesky on the tcgen05 tensor
+// cores: S_tile -= P_rows P_cols^T over the current panel P (K = 64 columns), with the
+// split-TF32 product hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory.
+//
+// One CTA of 256 threads owns a 128 x 64 tile of the lower triangle.  The threads stage
+// the two panel slices into shared memory (8 independent loads in flight per thread),
+// already split into TF32 hi and lo parts and laid out as the tensor cores read them
+// (K-major, no swizzle: 8-row x 4-element core matrices of 128 B, 128 B apart along K
+// and 2048 B apart along the rows); one thread issues 8 k-steps x 3 MMAs (M = 128,
+// N = 64, K = 8) into a 64-column accumulator and commits them to an mbarrier; every
+// thread then waits (bounded) and the 8 warps subtract the accumulator from S: warp w
+// reads tensor-memory lanes 32 (w mod 4) .. +31 (tile rows) and columns 32 (w / 4) .. +31.
+#pragma once
+#include "common.cuh"
+#include "umma.cuh"
+
+namespace capsgpu {
+
+constexpr int UM_M = 128, UM_N = 64, UM_K = 64;
+constexpr int UM_SMEM = 2 * (UM_M + UM_N) * UM_K * 4; // hi and lo of both slices: 96 KB
+constexpr int UM_WAIT_ITERS = 1 << 20;
+constexpr int UM_THREADS = 256, UM_ILP = 8;
+
+// float offset of element (r, k) of a K-major slice with 16 core matrices along K
+__device__ __forceinline__ int um_off(int r, int k) { return (((r >> 3) * (UM_K / 4) + (k >> 2)) << 5) + ((r & 7) << 2) + (k & 3); }
+
+__device__ __forceinline__ void um_split(float x, float &hi, float &lo)
+{
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+    hi = __uint_as_float(h);
+    lo = x - hi;
+}
+
+// rows [row0, row0 + R) of the panel (columns k0 .. k0 + nb) into hi/lo slices
+template <int R>
+__device__ __forceinline__ void um_stage(const float *Sm, int n, int k0, int nb, int row0, float *hi_s, float *lo_s, int tid)
+{
+#pragma unroll 1
+    for (int base = 0; base < R * UM_K; base += UM_THREADS * UM_ILP) {
+        float x[UM_ILP];
+#pragma unroll
+        for (int u = 0; u < UM_ILP; u++) {
+            const int e = base + u * UM_THREADS + tid, r = e % R, k = e / R;
+            x[u] = (e < R * UM_K && row0 + r < n && k < nb) ? __ldg(Sm + (size_t)(k0 + k) * n + row0 + r) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < UM_ILP; u++) {
+            const int e = base + u * UM_THREADS + tid, r = e % R, k = e / R;
+            if (e < R * UM_K) {
+                float hi, lo;
+                um_split(x[u], hi, lo);
+                hi_s[um_off(r, k)] = hi;
+                lo_s[um_off(r, k)] = lo;
+            }
+        }
+    }
+}
+
+// grid (nr (nr + 1), ntask), nr = ceil(rest / 128); S column-major n x n per task
+__global__ void __launch_bounds__(UM_THREADS, 2) k_syrk_umma(int ntask, int n, int k0, float *S, size_t sstride, int *status)
+{
+    const int task = blockIdx.y;
+    if (task >= ntask || status[task] != ST_FACTOR) return;
+    const int nb = min(UM_K, n - k0);
+    const int t0 = k0 + nb;
+    // tile p -> (row block ri, column block cj <= 2 ri + 1)
+    const int p = blockIdx.x;
+    int ri = (int)((sqrtf(4.0f * p + 1.0f) - 1.0f) * 0.5f);
+    while ((ri + 1) * (ri + 2) <= p) ri++;
+    while (ri * (ri + 1) > p) ri--;
+    const int cj = p - ri * (ri + 1);
+    const int row0 = t0 + ri * UM_M, col0 = t0 + cj * UM_N;
+    if (row0 >= n || col0 >= n) return; // uniform per CTA
+
+    extern __shared__ __align__(128) float um_sm[];
+    float *Ahi = um_sm, *Alo = Ahi + UM_M * UM_K, *Bhi = Alo + UM_M * UM_K, *Blo = Bhi + UM_N * UM_K;
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    float *Sm = S + (size_t)task * sstride;
+
+    if (warp == 0) umma::alloc(&tslot, UM_N);
+    if (tid == 0) umma::mbar_init(&mbar, 1);
+    // stage both slices (coalesced along the rows), split into TF32 hi + lo
+    um_stage<UM_M>(Sm, n, k0, nb, row0, Ahi, Alo, tid);
+    um_stage<UM_N>(Sm, n, k0, nb, col0, Bhi, Blo, tid);
+    umma::fence_smem_async();
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = tslot;
+
+    if (tid == 0) {
+        constexpr uint32_t idesc = umma::idesc_tf32(UM_M, UM_N);
+        constexpr uint32_t LBO = 128, SBO = (UM_K / 4) * 128;
+        const uint32_t ah = umma::smem_u32(Ahi), al = umma::smem_u32(Alo), bh = umma::smem_u32(Bhi), bl = umma::smem_u32(Blo);
+        for (int ks = 0; ks < UM_K / 8; ks++) {
+            const uint32_t o = ks * 256; // two core matrices along K per k-step of 8
+            umma::mma_tf32(tmem, umma::desc_kmajor(al + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc, ks > 0);
+            umma::mma_tf32(tmem, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bl + o, LBO, SBO), idesc, 1);
+            umma::mma_tf32(tmem, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc, 1);
+        }
+        umma::commit(&mbar);
+    }
+    const bool ok = umma::mbar_wait(&mbar, 0, UM_WAIT_ITERS);
+    umma::fence_after();
+    if (ok) {
+        // this thread's 32 entries of C: all loads first (independent, in flight together),
+        // then the accumulator from tensor memory, then the stores
+        const int quad = warp & 3, half = warp >> 2;
+        const int R = row0 + quad * 32 + lane, cb = col0 + half * 32;
+        float c[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const int C = cb + j;
+            c[j] = (R < n && C < n && R >= C) ? Sm[(size_t)C * n + R] : 0.0f;
+        }
+        float v[32];
+        umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + half * 32, *reinterpret_cast<float(*)[16]>(v));
+        umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + half * 32 + 16, *reinterpret_cast<float(*)[16]>(v + 16));
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const int C = cb + j;
+            if (R < n && C < n && R >= C) Sm[(size_t)C * n + R] = c[j] - v[j];
+        }
+    } else if (tid == 0)
+        atomicOr(status + task, ST_ERR_WAIT);
+    umma::fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        umma::fence_after();
+        umma::dealloc(tmem, UM_N);
+    }
+}
+
+} // namespace capsgpu
