@@ -86,7 +86,7 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -573,10 +573,12 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         // CAPS_MIXED_SIMT=1 selects the FP32 FFMA trailing update instead of split-TF32 tensor cores
         static const bool tc = getenv("CAPS_MIXED_SIMT") == nullptr;
         if (ff_elem) {
-            launch_cholesky_mixed(nt, dim, nullptr, 0, 0, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, false);
+            void *d_work = g_eng.mwork.get(mixed_work_bytes(nt));
+            launch_cholesky_mixed(nt, dim, nullptr, 0, 0, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, false, d_work);
         } else if (O.factor && caps->precision == CAPS_PREC_MIXED && !O.square) {
             d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
-            launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc);
+            void *d_work = g_eng.mwork.get(mixed_work_bytes(nt));
+            launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, true, d_work);
         } else if (O.factor) {
             double *d_ld = (double *)g_eng.logdiag.get((size_t)nt * dim * sizeof(double));
             launch_cholesky(nt, dim, d_A, lda, mstride, d_status, d_ld, st);

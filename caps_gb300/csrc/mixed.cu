@@ -25,6 +25,7 @@ namespace capsgpu {
 
 constexpr int MB = 64; // panel width
 static_assert(MB == UM_K, "the tcgen05 trailing update is built for the panel width");
+constexpr int FROP = 32; // blocks per matrix of the Frobenius partial sums
 
 // S = A - I (lower triangle, FP32) for the tasks that need a factorisation
 __global__ void k_to_delta32(int ntask, int n, const double *A, size_t lda, size_t mstride, const int *status, float *S,
@@ -41,12 +42,14 @@ __global__ void k_to_delta32(int ntask, int n, const double *A, size_t lda, size
     }
 }
 
-// diagonal block in delta form: one CTA per task
-__global__ void __launch_bounds__(256) k_potf2_d(int ntask, int n, int k0, float *S, size_t sstride, int *status)
+// diagonal block in delta form: one CTA per task.  Also writes W = (I + Lam_kk)^{-1}
+// (lower triangular, row-major MB x MB per task) for the panel solve.
+__global__ void __launch_bounds__(256) k_potf2_d(int ntask, int n, int k0, float *S, size_t sstride, int *status, float *Winv)
 {
     const int task = blockIdx.x;
     if (task >= ntask || status[task] != ST_FACTOR) return;
     __shared__ float T[MB][MB + 1];
+    __shared__ float W[MB][MB + 1];
     __shared__ int bad;
     const int nb = min(MB, n - k0);
     float *Sm = S + (size_t)task * sstride + (size_t)k0 * n + k0;
@@ -77,40 +80,65 @@ __global__ void __launch_bounds__(256) k_potf2_d(int ntask, int n, int k0, float
         const int c = e / nb, r = e % nb;
         if (r >= c) Sm[(size_t)c * n + r] = T[r][c];
     }
+    // W = (I + Lam)^{-1} column by column (forward substitution, one column per thread)
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+        W[j][j] = 1.0f / (1.0f + T[j][j]);
+        for (int i = j + 1; i < nb; i++) {
+            float acc = 0.0f;
+            for (int k = j; k < i; k++) acc = fmaf(T[i][k], W[k][j], acc);
+            W[i][j] = -acc / (1.0f + T[i][i]);
+        }
+    }
+    __syncthreads();
+    float *Wt = Winv + (size_t)task * MB * MB;
+    for (int e = threadIdx.x; e < MB * MB; e += blockDim.x) {
+        const int r = e / MB, c = e % MB;
+        Wt[e] = (r < nb && c <= r) ? W[r][c] : 0.0f;
+    }
     if (threadIdx.x == 0 && bad) atomicOr(status + task, ST_ERR_PIVOT);
 }
 
-// panel: x (I+Lam_kk)^T = s for the rows below the diagonal block
+// panel: X (I + Lam_kk)^T = S for the rows below the diagonal block, as X = S W^T with
+// W = (I + Lam_kk)^{-1} from k_potf2_d (I + Lam_kk is within a few per cent of I, so the
+// product is as accurate as the substitution).  64 rows per CTA of 256 threads; thread t
+// takes row t mod 64 and the 16 columns c = t / 64 (mod 4), so a warp reads 32 distinct
+// rows of X (no bank conflict), one broadcast W entry, and stores 32 consecutive rows.
 constexpr int MT = 64;
-__global__ void __launch_bounds__(MT) k_trsm_d(int ntask, int n, int k0, float *S, size_t sstride, const int *status)
+__global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, const int *status,
+                                                  const float *Winv)
 {
     const int task = blockIdx.y;
     if (task >= ntask || status[task] != ST_FACTOR) return;
     const int nb = min(MB, n - k0);
     const int r0 = k0 + nb + blockIdx.x * MT;
     if (r0 >= n) return;
-    __shared__ float Lk[MB][MB + 1];
-    __shared__ float X[MT][MB + 1];
+    __shared__ float Wl[MB][MB + 1]; // W[c][k]
+    __shared__ float X[MT][MB + 1];  // S rows
     float *Sm = S + (size_t)task * sstride;
-    for (int e = threadIdx.x; e < nb * nb; e += MT) {
-        const int c = e / nb, r = e % nb;
-        Lk[r][c] = (r > c) ? Sm[(size_t)(k0 + c) * n + k0 + r] : (r == c ? 1.0f + Sm[(size_t)(k0 + c) * n + k0 + r] : 0.0f);
-    }
+    const float *Wt = Winv + (size_t)task * MB * MB;
+    for (int e = threadIdx.x; e < MB * MB; e += 256) Wl[e / MB][e % MB] = Wt[e];
     const int rows = min(MT, n - r0);
-    for (int c = 0; c < nb; c++)
-        for (int r = threadIdx.x; r < rows; r += MT) X[r][c] = Sm[(size_t)(k0 + c) * n + r0 + r];
+    for (int e = threadIdx.x; e < MT * MB; e += 256) {
+        const int c = e / MT, r = e % MT;
+        X[r][c] = (r < rows && c < nb) ? Sm[(size_t)(k0 + c) * n + r0 + r] : 0.0f;
+    }
     __syncthreads();
-    if (threadIdx.x < rows) {
-        float *x = X[threadIdx.x];
-        for (int c = 0; c < nb; c++) {
-            float v = x[c];
-            for (int cc = 0; cc < c; cc++) v = fmaf(-x[cc], Lk[c][cc], v);
-            x[c] = v / Lk[c][c];
+    const int r = threadIdx.x & (MT - 1), cq = threadIdx.x / MT;
+    float acc[MB / 4];
+#pragma unroll
+    for (int q = 0; q < MB / 4; q++) acc[q] = 0.0f;
+    for (int k = 0; k < nb; k++) {
+        const float a = X[r][k];
+#pragma unroll
+        for (int q = 0; q < MB / 4; q++) acc[q] = fmaf(a, Wl[cq + 4 * q][k], acc[q]);
+    }
+    if (r < rows) {
+#pragma unroll
+        for (int q = 0; q < MB / 4; q++) {
+            const int c = cq + 4 * q;
+            if (c < nb) Sm[(size_t)(k0 + c) * n + r0 + r] = acc[q];
         }
     }
-    __syncthreads();
-    for (int c = 0; c < nb; c++)
-        for (int r = threadIdx.x; r < rows; r += MT) Sm[(size_t)(k0 + c) * n + r0 + r] = X[r][c];
 }
 
 // trailing update S_ab -= sum_k Lam_ak Lam_bk over the panel, 64x64 tiles of the
@@ -253,10 +281,33 @@ __global__ void __launch_bounds__(128) k_syrk_tc(int ntask, int n, int k0, float
             }
 }
 
+// ||Lam||_F^2 in FROP partial sums per task: block b takes the columns c = b (mod FROP)
+__global__ void __launch_bounds__(256) k_fro_part(int ntask, int n, const float *S, size_t sstride, const int *status, double *part)
+{
+    const int task = blockIdx.y;
+    if (task >= ntask || status[task] != ST_FACTOR) return;
+    const float *Sm = S + (size_t)task * sstride;
+    __shared__ double red[256];
+    double fro = 0.0;
+    for (int c = blockIdx.x; c < n; c += FROP)
+        for (int r = c + threadIdx.x; r < n; r += blockDim.x) {
+            const double v = Sm[(size_t)c * n + r];
+            fro = fma(v, v, fro);
+        }
+    red[threadIdx.x] = fro;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[(size_t)task * FROP + blockIdx.x] = red[0];
+}
+
 // log det = 2 sum log1p(Lam_jj) + tr(A-I) - 2 tr Lam - ||Lam||_F^2, all sums FP64;
 // one CTA per task, fixed reduction order
 __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const float *S, size_t sstride, const double *mdiag,
-                                                     const double *trace, int *status, double *result, int mode)
+                                                     const double *trace, int *status, double *result, int mode,
+                                                     const double *part)
 {
     const int task = blockIdx.x;
     if (task >= ntask) return;
@@ -265,13 +316,7 @@ __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const flo
     if (st != ST_FACTOR) return;
     const float *Sm = S + (size_t)task * sstride;
     __shared__ double red[256];
-    double fro = 0.0;
-    for (int c = 0; c < n; c++)
-        for (int r = c + threadIdx.x; r < n; r += blockDim.x) {
-            const double v = Sm[(size_t)c * n + r];
-            fro = fma(v, v, fro);
-        }
-    red[threadIdx.x] = fro;
+    red[threadIdx.x] = threadIdx.x < FROP ? part[(size_t)task * FROP + threadIdx.x] : 0.0;
     __syncthreads();
     for (int w = 128; w > 0; w >>= 1) {
         if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
@@ -292,9 +337,15 @@ __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const flo
     result[task] = ld;
 }
 
+size_t mixed_work_bytes(int ntask) { return (size_t)ntask * (MB * MB * sizeof(float) + FROP * sizeof(double)); }
+
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
-                           const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc, bool convert)
+                           const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc, bool convert,
+                           void *work)
 {
+    // work: mixed_work_bytes(ntask) of scratch (diagonal-block inverses, Frobenius partials)
+    float *Winv = (float *)work;
+    double *part = (double *)((char *)work + (size_t)ntask * MB * MB * sizeof(float));
     // convert: A is the FP64 matrix 1 - M and S receives its delta form here; otherwise S
     // already holds it.  mdiag: M_ii in FP64, n per task (tr(A - I) = -tr M).
     // Trailing update: tcgen05 (k_syrk_umma); CAPS_MIXED_MMASYNC=1 selects the mma.sync
@@ -311,12 +362,12 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         COUNT_LAUNCH(1);
     }
     for (int k0 = 0; k0 < n; k0 += MB) {
-        k_potf2_d<<<ntask, 256, 0, st>>>(ntask, n, k0, S, sstride, status);
+        k_potf2_d<<<ntask, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv);
         COUNT_LAUNCH(1);
         const int rest = n - k0 - MB;
         if (rest <= 0) break;
         dim3 gt((rest + MT - 1) / MT, ntask);
-        k_trsm_d<<<gt, MT, 0, st>>>(ntask, n, k0, S, sstride, status);
+        k_trsm_inv<<<gt, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv);
         COUNT_LAUNCH(1);
         const int nt = (rest + 63) / 64;
         dim3 gs(nt * (nt + 1) / 2, ntask);
@@ -329,8 +380,10 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
             k_syrk_f<<<gs, 64, 0, st>>>(ntask, n, k0, S, sstride, status);
         COUNT_LAUNCH(1);
     }
-    k_final_mixed<<<ntask, 256, 0, st>>>(ntask, n, S, sstride, mdiag, trace, status, result, mode);
-    COUNT_LAUNCH(1);
+    dim3 gf(FROP, ntask);
+    k_fro_part<<<gf, 256, 0, st>>>(ntask, n, S, sstride, status, part);
+    k_final_mixed<<<ntask, 256, 0, st>>>(ntask, n, S, sstride, mdiag, trace, status, result, mode, part);
+    COUNT_LAUNCH(2);
     CK(cudaGetLastError());
 }
 
