@@ -75,6 +75,12 @@ def _load():
         "caps_mlp_proposal": (i, [vp, d, d, d, vp, i, ip]),
         "caps_free_energy_learned": (d, [vp, d, d, d, vp, C.POINTER(_EnergyInfo)]),
         "caps_noalloc_last_error": (C.c_char_p, []),
+        "caps_capc_lmax": (i, [d, d, d]), "caps_capc_pfa": (d, [d, d]),
+        "caps_capc_logdet": (d, [d, d, i, d, C.c_char, i]),
+        "caps_capc_logdet_batch": (i, [d, d, i, dp, i, C.c_char, i, dp]),
+        "caps_capc_energy_T0": (d, [d, d, i, C.c_char, d, i, ip, ip]),
+        "bessel_logI0": (d, [d]), "bessel_logI1": (d, [d]), "bessel_logK0": (d, [d]), "bessel_logK1": (d, [d]),
+        "bessel_logIn": (d, [i, d]), "bessel_logKn": (d, [i, d]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -363,3 +369,30 @@ class MLP:
         N = lib.caps_mlp_proposal(caps._h, float(T), float(cutoff), float(epsrel), self._h, nmax,
                                   ch.ctypes.data_as(C.POINTER(C.c_int)))
         return N, ch[:max(N, 0)]
+
+
+# ---- cylinder-plane geometry (the reference's capc program) ----
+
+_DETALG = {"HODLR": 0, "LU": 1, "QR": 2, "CHOLESKY": 3}
+
+
+def capc_lmax(R, d, eta=6.0):
+    """the capc program's dimension max(25, ceil(eta R/d))"""
+    return lib.caps_capc_lmax(float(R), float(d), float(eta))
+
+
+def capc_logdet(R, d, q, DN="D", lmax=0, detalg="HODLR"):
+    """CasimirCP::logdet for one wave number q or an array of them (one GPU batch)"""
+    qs = np.atleast_1d(np.ascontiguousarray(q, dtype=np.float64))
+    out = np.empty_like(qs)
+    lib.caps_capc_logdet_batch(float(R), float(d), int(lmax), qs.ctypes.data_as(C.POINTER(C.c_double)), len(qs),
+                               DN.encode()[:1], _DETALG[detalg.upper()], out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out if np.ndim(q) else float(out[0])
+
+
+def capc_energy_T0(R, d, p="D", lmax=0, epsrel=1e-8, detalg="HODLR"):
+    """CasimirCP::energy at T = 0: (E/(hbar c L), qagi neval, qagi ier)"""
+    ne, ier = C.c_int(0), C.c_int(0)
+    E = lib.caps_capc_energy_T0(float(R), float(d), int(lmax), p.encode()[:1], float(epsrel), _DETALG[detalg.upper()],
+                                C.byref(ne), C.byref(ier))
+    return E, ne.value, ier.value

@@ -2,6 +2,7 @@
 #pragma once
 #include <cstdio>
 #include <cstdlib>
+#include <functional>
 #include <cuda_runtime.h>
 #include "common.cuh"
 
@@ -71,5 +72,9 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
                            const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc,
                            bool convert, void *work);
 void launch_final(int ntask, int n, const double *logdiag, const double *trace, int *status, double *result, int mode, cudaStream_t st);
+
+// F for n abscissae at once; QUADPACK qagi with every node of a step in one call (tzero.cu)
+using BatchFn = std::function<void(const double *x, int n, double *y)>;
+double qagi_batched(const BatchFn &F, double bound, int inf, double epsabs, double epsrel, double *abserr, int *neval, int *ier);
 
 } // namespace capsgpu

@@ -24,8 +24,6 @@
 
 namespace capsgpu {
 
-// F for n abscissae at once
-using BatchFn = std::function<void(const double *x, int n, double *y)>;
 
 // ---------------------------------------------------------------------------
 // QUADPACK qagi (Piessens, de Doncker-Kapenga, Ueberhuber, Kahaner 1983), as the
@@ -473,6 +471,11 @@ static int psd(int N, double *xi, double *eta)
 }
 
 } // namespace qp
+
+double qagi_batched(const BatchFn &F, double bound, int inf, double epsabs, double epsrel, double *abserr, int *neval, int *ier)
+{
+    return qp::qagi(F, bound, inf, epsabs, epsrel, abserr, neval, ier);
+}
 } // namespace capsgpu
 
 // implemented in libcaps.cu

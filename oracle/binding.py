@@ -51,6 +51,13 @@ def _load():
         "oracle_logdetD_batch": (None, [gp, i, dp, C.POINTER(C.c_int), dp, i]),
         "oracle_free_energy": (d, [gp, d, d, d, i, dp, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "oracle_logdet_1mM": (d, [dp, i, C.POINTER(C.c_int)]),
+        "oracle_bessel_logI0": (d, [d]),
+        "oracle_bessel_logI1": (d, [d]),
+        "oracle_bessel_logK0": (d, [d]),
+        "oracle_bessel_logK1": (d, [d]),
+        "oracle_bessel_logIn": (d, [i, d]),
+        "oracle_bessel_logKn": (d, [i, d]),
+        "oracle_capc_logdet": (d, [d, d, i, d, C.c_char, i]),
     }
     for k, (r, a) in sig.items():
         f = getattr(lib, k)

@@ -1177,3 +1177,163 @@ double oracle_free_energy(const oracle_geom_t *g, double T, double cutoff, doubl
     v[0] /= 2;
     return Ts / M_PI * kahan(v, nv);
 }
+
+/* ------------------------------------------------------------------------- */
+/* integer-order modified Bessel functions (src/bessel.c:283-633)             */
+/*                                                                            */
+/* The branch structure of bessel_logIn / bessel_logKn is restated: series    */
+/* for x < 5 sqrt(n) (bessel.c:744), Miller's downward recurrence started     */
+/* from the continued-fraction ratio (bessel.c:608-620), upward recurrence of */
+/* K in the log domain (bessel.c:506-544), Debye asymptotics for n >= 100.    */
+/* Orders 0 and 1: the reference evaluates Cephes Chebyshev fits              */
+/* (bessel.c:283-461), which are not restated; here the power series for      */
+/* x < 8 as the reference's I_0/I_1, I_1 = I_0 / ratio above, and for I_0 and */
+/* K_0, K_1 the trapezoidal rule on the integral representations             */
+/* (DLMF 10.32.3, 10.32.9) or Hankel's expansion (DLMF 10.40.1) at large x.   */
+/* The values are pinned against the reference library's functions.         */
+/* ------------------------------------------------------------------------- */
+static double o_logInu_series(double nu, double x) /* bessel.c:744-759 */
+{
+    const double y = 0.25 * x * x;
+    double v = 1, sum = 0;
+    for (int m = 1; m < 2048; m++) {
+        v *= y / (m * (m + nu));
+        sum += v;
+        if (v < 1e-16 * sum) return 0.5 * nu * log(y) - lgamma(1 + nu) + log1p(sum);
+    }
+    return NAN;
+}
+
+double oracle_bessel_logI0(double x)
+{
+    if (x < 0) return NAN;
+    if (x == 0) return 0;
+    if (x < 8) return o_logInu_series(0, x);
+    if (x > 2000) {
+        double term = 1, sum = 1;
+        for (int k = 1; k < 60; k++) {
+            term *= (2.0 * k - 1) * (2.0 * k - 1) / (8.0 * k * x);
+            sum += term;
+            if (term < 1e-18 * sum) break;
+        }
+        return x - 0.5 * log(2 * M_PI * x) + log(sum);
+    }
+    /* (1/pi) int_0^pi exp(x (cos th - 1)) dth by the trapezoidal rule (aliasing I_{2N}) */
+    const int N = 20 + (int)ceil(sqrt(25 * x));
+    double s = 0.5 * (1 + exp(-2 * x));
+    for (int k = 1; k < N; k++) s += exp(x * (cos(M_PI * k / N) - 1));
+    return x + log(s / N);
+}
+
+double oracle_bessel_logI1(double x)
+{
+    if (x <= 0) return NAN;
+    if (x < 8) return o_logInu_series(1, x);
+    return oracle_bessel_logI0(x) - log(oracle_ratioI(0, x));
+}
+
+/* log K_nu(x), nu = 0 or 1: x + log int_0^inf exp(-x (cosh t - 1)) cosh(nu t) dt */
+static double o_logK01(int nu, double x)
+{
+    if (x <= 0) return NAN;
+    const double h = fmin(M_PI * M_PI / (42 + fmax(0, -log(x))), 0.6 / sqrt(x));
+    double s = 0.5, prev = 1;
+    for (int k = 1; k < 1000000; k++) {
+        const double t = k * h;
+        const double f = exp(-x * (cosh(t) - 1)) * (nu ? cosh(t) : 1.0);
+        s += f;
+        if (f < 1e-18 * s && f <= prev) break;
+        prev = f;
+    }
+    return -x + log(h * s);
+}
+double oracle_bessel_logK0(double x) { return o_logK01(0, x); }
+double oracle_bessel_logK1(double x) { return o_logK01(1, x); }
+
+double oracle_bessel_logKn(int n, double x) /* bessel.c:506-581 */
+{
+    if (n < 0) n = -n;
+    if (n == 0) return oracle_bessel_logK0(x);
+    if (n == 1) return oracle_bessel_logK1(x);
+    if (n >= 100) return oracle_logK_asymp(n, x);
+    double Km = oracle_bessel_logK0(x), K = oracle_bessel_logK1(x);
+    for (int j = 1; j < n; j++) {
+        const double k = 0.5 * x / j;
+        const double Kp = -log(k) + K + log1p(exp(Km - K) * k);
+        Km = K;
+        K = Kp;
+    }
+    return K;
+}
+
+double oracle_bessel_logIn(int n, double x) /* bessel.c:583-621 */
+{
+    if (n < 0) n = -n;
+    if (n == 0) return oracle_bessel_logI0(x);
+    if (n == 1) return oracle_bessel_logI1(x);
+    if (x == 0) return -INFINITY;
+    if (n >= 100) return oracle_logI_asymp(n, x);
+    if (x < 5 * sqrt(n)) return o_logInu_series(n, x);
+    double Ip = 1, I = oracle_ratioI(n - 1, x); /* I_n = 1, I_{n-1}/I_n */
+    for (int k = n - 1; k > 0; k--) {
+        const double Im = Ip + 2 * k / x * I;
+        Ip = I;
+        I = Im;
+    }
+    return oracle_bessel_logI0(x) - log(I);
+}
+
+/* ------------------------------------------------------------------------- */
+/* cylinder-plane round trip (src/capc.cpp:47-127 and the kernel :155-177)    */
+/* ------------------------------------------------------------------------- */
+
+/* kernel_logdet's rules for a symmetric M (matrix.c:57-149): hodlr = 1 keeps the HODLR
+ * branch's trace shortcut and final |tr| > |logdet| check around an exact LU */
+static double o_kernel_logdet(double *M, int n, int hodlr)
+{
+    if (!hodlr) return oracle_logdet_1mM(M, n, NULL);
+    double *d = malloc(n * sizeof(double));
+    for (int i = 0; i < n; i++) d[i] = M[(size_t)i * n + i];
+    const double tr = kahan(d, n);
+    free(d);
+    if (fabs(tr) < 1e-8) return -tr;
+    for (size_t i = 0; i < (size_t)n * n; i++) M[i] = -M[i];
+    for (int i = 0; i < n; i++) M[(size_t)i * n + i] += 1;
+    const double ld = oracle_logdet_lu(M, n);
+    return fabs(tr) > fabs(ld) ? -tr : ld;
+}
+
+double oracle_capc_logdet(double R, double d, int lmax, double q, char DN, int hodlr)
+{
+    const double calL = d + R, xr = R * q;
+    const int dn = (DN == 'D' || DN == 'd');
+    double *ratio = malloc((lmax + 1) * sizeof(double)), *K = malloc(2 * (lmax + 1) * sizeof(double));
+    for (int j = 0; j < 2 * (lmax + 1); j++) K[j] = oracle_bessel_logKn(j, 2 * calL * q);
+    if (dn) {
+        for (int j = 0; j <= lmax; j++) ratio[j] = oracle_bessel_logIn(j, xr) - oracle_bessel_logKn(j, xr);
+    } else {
+        /* I'_0/K'_0 = -I_1/K_1; I'_j/(-K'_j) = (I_{j-1} + I_{j+1}) / (K_{j-1} + K_{j+1}) */
+        ratio[0] = oracle_bessel_logI1(xr) - oracle_bessel_logK1(xr);
+        for (int j = 1; j <= lmax; j++) {
+            const double num = logadd(oracle_bessel_logIn(j - 1, xr), oracle_bessel_logIn(j + 1, xr));
+            const double den = logadd(oracle_bessel_logKn(j - 1, xr), oracle_bessel_logKn(j + 1, xr));
+            ratio[j] = num - den;
+        }
+    }
+    const double M00 = exp(ratio[0] + K[0]);
+    const double log_rho = log1p(-M00), alpha = 2 / (1 - M00);
+    double *M = malloc((size_t)lmax * lmax * sizeof(double));
+    double total = log_rho;
+    for (int type = 0; type < 2; type++) {
+        for (int i = 0; i < lmax; i++)
+            for (int j = 0; j < lmax; j++) {
+                const int mu1 = i + 1, mu2 = j + 1;
+                const double term1 = 0.5 * (ratio[mu1] + ratio[mu2]);
+                const double U = exp(term1 + K[mu1 + mu2]), V = exp(term1 + K[abs(mu1 - mu2)]);
+                M[(size_t)i * lmax + j] = type == 0 ? U - V : U + V + alpha * exp(term1 + ratio[0] + K[mu1] + K[mu2]);
+            }
+        total += o_kernel_logdet(M, lmax, hodlr);
+    }
+    free(M); free(ratio); free(K);
+    return total;
+}

@@ -49,6 +49,14 @@ double oracle_plasma_I(int nu, double omegap_);
 double oracle_logdetD0_MM_plasma(const oracle_geom_t *g, int m, double omegap);
 double oracle_ht_plasma(const oracle_geom_t *g, double omegap, double eps);
 
+double oracle_bessel_logI0(double x);
+double oracle_bessel_logI1(double x);
+double oracle_bessel_logK0(double x);
+double oracle_bessel_logK1(double x);
+double oracle_bessel_logIn(int n, double x);
+double oracle_bessel_logKn(int n, double x);
+double oracle_capc_logdet(double R, double d, int lmax, double q, char DN, int hodlr);
+
 void   oracle_logdetD_batch(const oracle_geom_t *g, int n, const double *xi, const int *m, double *out, int nthreads);
 double oracle_free_energy(const oracle_geom_t *g, double T, double cutoff, double epsrel, int nthreads,
                           double *xi_out, double *v_out, int *nxi, int *ndet);

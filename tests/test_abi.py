@@ -1,5 +1,5 @@
-"""The C-ABI library loads without a GPU and exports every symbol declared in
-include/libcaps.h.  No compute call is made here."""
+"""The C-ABI library loads without a GPU and exports every function declared in
+include/*.h.  No compute call is made here."""
 import ctypes as C
 import os
 import re
@@ -8,15 +8,20 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def declared_functions():
-    src = open(os.path.join(ROOT, "include", "libcaps.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"^[A-Za-z_][\w \*]*?\b(caps_\w+)\s*\(", src, flags=re.M)
-    return sorted(set(names))
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for h in sorted(os.listdir(inc)):
+        if not h.endswith(".h"):
+            continue
+        src = re.sub(r"/\*.*?\*/", "", open(os.path.join(inc, h)).read(), flags=re.S)
+        names.update(re.findall(r"^[A-Za-z_][\w \*]*?\b((?:caps|bessel|material)_\w+)\s*\(", src, flags=re.M))
+    return sorted(names)
 
 
 def test_header_parsed():
     names = declared_functions()
     assert "caps_logdetD" in names and "caps_logdetD_batch" in names and len(names) >= 38
+    assert "caps_capc_energy_T0" in names and "bessel_logKn" in names and "material_epsilonm1" in names
 
 
 def test_library_exports_all():
