@@ -3,13 +3,16 @@
 // split-TF32 product hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory.
 //
 // One CTA of 256 threads owns a 128 x 64 tile of the lower triangle.  The threads stage
-// the two panel slices into shared memory (8 independent loads in flight per thread),
+// the two panel slices into shared memory (16 independent loads in flight per thread),
 // already split into TF32 hi and lo parts and laid out as the tensor cores read them
 // (K-major, no swizzle: 8-row x 4-element core matrices of 128 B, 128 B apart along K
-// and 2048 B apart along the rows); one thread issues 8 k-steps x 3 MMAs (M = 128,
-// N = 64, K = 8) into a 64-column accumulator and commits them to an mbarrier; every
-// thread then waits (bounded) and the 8 warps subtract the accumulator from S: warp w
-// reads tensor-memory lanes 32 (w mod 4) .. +31 (tile rows) and columns 32 (w / 4) .. +31.
+// and 2048 B apart along the rows).  Element e of a slice is the e-th float of that
+// layout, so a warp writes one whole core matrix (conflict-free) and reads 8 consecutive
+// rows of 4 columns (four full 32-byte sectors).  One thread issues 8 k-steps x 3 MMAs
+// (M = 128, N = 64, K = 8) into a 64-column accumulator and commits them to an mbarrier;
+// meanwhile every thread loads its 32 entries of the tile of S, then waits (bounded) and
+// the 8 warps subtract the accumulator: warp w reads tensor-memory lanes 32 (w mod 4) ..
+// +31 (tile rows) and columns 32 (w / 4) .. +31.
 #pragma once
 #include "common.cuh"
 #include "umma.cuh"
@@ -19,7 +22,7 @@ namespace capsgpu {
 constexpr int UM_M = 128, UM_N = 64, UM_K = 64;
 constexpr int UM_SMEM = 2 * (UM_M + UM_N) * UM_K * 4; // hi and lo of both slices: 96 KB
 constexpr int UM_WAIT_ITERS = 1 << 20;
-constexpr int UM_THREADS = 256, UM_ILP = 8;
+constexpr int UM_THREADS = 256, UM_ILP = 16;
 
 // float offset of element (r, k) of a K-major slice with 16 core matrices along K
 __device__ __forceinline__ int um_off(int r, int k) { return (((r >> 3) * (UM_K / 4) + (k >> 2)) << 5) + ((r & 7) << 2) + (k & 3); }
@@ -32,27 +35,35 @@ __device__ __forceinline__ void um_split(float x, float &hi, float &lo)
     lo = x - hi;
 }
 
+// (r, k) of the e-th float of a slice in the layout of um_off
+__device__ __forceinline__ void um_coord(int e, int &r, int &k)
+{
+    const int cm = e >> 5, lane = e & 31;
+    r = (cm / (UM_K / 4)) * 8 + (lane >> 2);
+    k = (cm % (UM_K / 4)) * 4 + (lane & 3);
+}
+
 // rows [row0, row0 + R) of the panel (columns k0 .. k0 + nb) into hi/lo slices
 template <int R>
 __device__ __forceinline__ void um_stage(const float *Sm, int n, int k0, int nb, int row0, float *hi_s, float *lo_s, int tid)
 {
+    static_assert((R * UM_K) % (UM_THREADS * UM_ILP) == 0, "whole staging rounds");
 #pragma unroll 1
     for (int base = 0; base < R * UM_K; base += UM_THREADS * UM_ILP) {
         float x[UM_ILP];
 #pragma unroll
         for (int u = 0; u < UM_ILP; u++) {
-            const int e = base + u * UM_THREADS + tid, r = e % R, k = e / R;
-            x[u] = (e < R * UM_K && row0 + r < n && k < nb) ? __ldg(Sm + (size_t)(k0 + k) * n + row0 + r) : 0.0f;
+            int r, k;
+            um_coord(base + u * UM_THREADS + tid, r, k);
+            x[u] = (row0 + r < n && k < nb) ? __ldg(Sm + (size_t)(k0 + k) * n + row0 + r) : 0.0f;
         }
 #pragma unroll
         for (int u = 0; u < UM_ILP; u++) {
-            const int e = base + u * UM_THREADS + tid, r = e % R, k = e / R;
-            if (e < R * UM_K) {
-                float hi, lo;
-                um_split(x[u], hi, lo);
-                hi_s[um_off(r, k)] = hi;
-                lo_s[um_off(r, k)] = lo;
-            }
+            const int e = base + u * UM_THREADS + tid;
+            float hi, lo;
+            um_split(x[u], hi, lo);
+            hi_s[e] = hi;
+            lo_s[e] = lo;
         }
     }
 }
@@ -103,19 +114,19 @@ __global__ void __launch_bounds__(UM_THREADS, 2) k_syrk_umma(int ntask, int n, i
         }
         umma::commit(&mbar);
     }
+    // this thread's 32 entries of C, loaded while the MMAs run (the MMAs read only the
+    // staged slices, never S)
+    const int quad = warp & 3, half = warp >> 2;
+    const int R = row0 + quad * 32 + lane, cb = col0 + half * 32;
+    float c[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+        const int C = cb + j;
+        c[j] = (R < n && C < n && R >= C) ? Sm[(size_t)C * n + R] : 0.0f;
+    }
     const bool ok = umma::mbar_wait(&mbar, 0, UM_WAIT_ITERS);
     umma::fence_after();
     if (ok) {
-        // this thread's 32 entries of C: all loads first (independent, in flight together),
-        // then the accumulator from tensor memory, then the stores
-        const int quad = warp & 3, half = warp >> 2;
-        const int R = row0 + quad * 32 + lane, cb = col0 + half * 32;
-        float c[32];
-#pragma unroll
-        for (int j = 0; j < 32; j++) {
-            const int C = cb + j;
-            c[j] = (R < n && C < n && R >= C) ? Sm[(size_t)C * n + R] : 0.0f;
-        }
         float v[32];
         umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + half * 32, *reinterpret_cast<float(*)[16]>(v));
         umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + half * 32 + 16, *reinterpret_cast<float(*)[16]>(v + 16));
