@@ -337,6 +337,76 @@ __global__ void k_a12(const int *group_m, const int *group_lmin, int ngroup, int
     tab[(size_t)g * npair + pid] = r;
 }
 
+// Mixed form: the same a_0, a_1, a_2 from O(L) tables per m.  With m' = max(m, 1),
+// s = 2(l1 + l2), n4 = l1 + l2 - 2m',
+//   F1(l) = (m'-l)(m'-l+1)/(2l-1),   F2(l) = F1(l) (m'-l+2)(m'-l+3)/(2l-3),
+//   a_1 = (l1 + l2 - 3/2)(1 - (s-1)/(n4(n4-1)) (F1(l1) + F1(l2))),
+//   a_2 = (s-1)(s-7)/4 ((s-3)/(n4(n4-1)) ((s-5)/(2(n4-2)(n4-3)) (F2(l1) + 2 F1(l1) F1(l2) + F2(l2))
+//         - F1(l1) - F1(l2)) + 1/2),
+//   a_0 = e^G(l1) e^G(l2) e^H(l1+l2),  G(l) = lfac(2l) - lfac(l) - lfac(l-m'),
+//         H(j) = lfac(j) - lfac(2j) + lfac(j-2m'),
+// which is k_a12's expression regrouped: every division and the exponential move into
+// per-l and per-(l1+l2) tables, and a pair costs a few FP64 products.  The rounding
+// differs from the reference's at the ulp level, far below the mixed form's 2^-44; the
+// FP64 form keeps k_a12.
+struct A12L { double F1, F2; sd eG; };             // per l, index l - (lmin - 1)
+struct A12J { double h1, pa, pb, pc; sd eH; };     // per l1 + l2, index l1 + l2 - 2(lmin - 1)
+
+// grid (ceil((2L-1)/128), ngroup)
+__global__ void k_a12_tabs(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *__restrict__ lft,
+                           A12L *tl, A12J *tj)
+{
+    const int L = ldim + 2, NJ = 2 * L - 1;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, g = blockIdx.y;
+    if (g >= ngroup || i >= NJ) return;
+    const int mt = group_m[g], mm = mt > 0 ? mt : 1, l0 = group_lmin[g] - 1;
+    const double m = mm;
+    if (i < L) {
+        const int l = l0 + i;
+        const double dl = l, u = m - dl;
+        const double F1 = u * (u + 1) / (2 * dl - 1);
+        A12L r{F1, F1 * (u + 2) * (u + 3) / (2 * dl - 3), sd{0.0, 0}};
+        if (l >= mm) r.eG = sd_from_log(__ldg(lft + 2 * l) - __ldg(lft + l) - __ldg(lft + l - mm), 1);
+        tl[(size_t)g * L + i] = r;
+    }
+    const int j = 2 * l0 + i, n4 = j - 2 * mm;
+    const double s = 2.0 * j, q = (double)n4 * (n4 - 1);
+    A12J r{0.0, (s - 1) * (s - 7) / 4, 0.0, 0.0, sd{0.0, 0}};
+    if (n4 >= 2) { r.h1 = (s - 1) / q; r.pb = (s - 3) / q; }
+    if (n4 >= 4) r.pc = (s - 5) / (2.0 * (n4 - 2) * (n4 - 3));
+    if (n4 >= 0) r.eH = sd_from_log(__ldg(lft + j) - __ldg(lft + 2 * j) + __ldg(lft + n4), 1);
+    tj[(size_t)g * NJ + i] = r;
+}
+
+__global__ void k_a12_mix(const int *group_m, const int *group_lmin, int ngroup, int ldim, const A12L *__restrict__ tl,
+                          const A12J *__restrict__ tj, A012 *tab)
+{
+    const int L = ldim + 2, NJ = 2 * L - 1;
+    const long long npair = (long long)L * (L + 1) / 2;
+    const long long pid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = blockIdx.y;
+    if (pid >= npair || g >= ngroup) return;
+    int a1 = (int)((sqrtf(8.0f * (float)pid + 1.0f) - 1.0f) * 0.5f);
+    while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
+    while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
+    const int a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
+    const int mt = group_m[g], mm = mt > 0 ? mt : 1;
+    const int l1 = group_lmin[g] - 1 + a1, l2 = group_lmin[g] - 1 + a2;
+    A012 r{0.0, 0.0, 0.0, 0, 0};
+    if (!(l2 < mm || l2 < mt || l1 < 1)) {
+        const int qmax = min(min(l1, l2), (l1 + l2 - 2 * mm) / 2);
+        const A12L x = tl[(size_t)g * L + a1], y = tl[(size_t)g * L + a2];
+        const A12J z = tj[(size_t)g * NJ + a1 + a2];
+        const sd a0 = sd_mul(sd_mul(x.eG, y.eG), z.eH);
+        r.a0m = a0.m;
+        r.a0e = a0.e;
+        const double f = x.F1 + y.F1;
+        if (qmax >= 1) r.a1 = (l1 + l2 - 1.5) * (1 - z.h1 * f);
+        if (qmax >= 2) r.a2 = z.pa * (z.pb * (z.pc * (x.F2 + 2 * x.F1 * y.F1 + y.F2) - f) + 0.5);
+    }
+    tab[(size_t)g * npair + pid] = r;
+}
+
 __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride,
                                               const double *__restrict__ lft, const double2 *__restrict__ xtab,
                                               const double4 *__restrict__ ptab, int pstride, sd *I, int *status,
@@ -690,6 +760,26 @@ void launch_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim,
     dim3 g((unsigned)((npair + 127) / 128), ngroup);
     k_a12<<<g, 128, 0, st>>>(group_m, group_lmin, ngroup, ldim, lft, (A012 *)tab);
     COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
+}
+
+size_t a12_tab_bytes(int ldim, int ngroup)
+{
+    const size_t L = ldim + 2;
+    return (L * sizeof(A12L) + (2 * L - 1) * sizeof(A12J)) * ngroup;
+}
+
+void launch_a12_mixed(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, void *work,
+                      cudaStream_t st)
+{
+    const long long L = ldim + 2, npair = L * (L + 1) / 2;
+    A12L *tl = (A12L *)work;
+    A12J *tj = (A12J *)((char *)work + (size_t)L * ngroup * sizeof(A12L));
+    dim3 gt((unsigned)((2 * L - 1 + 127) / 128), ngroup);
+    k_a12_tabs<<<gt, 128, 0, st>>>(group_m, group_lmin, ngroup, ldim, lft, tl, tj);
+    dim3 g((unsigned)((npair + 127) / 128), ngroup);
+    k_a12_mix<<<g, 128, 0, st>>>(group_m, group_lmin, ngroup, ldim, tl, tj, (A012 *)tab);
+    COUNT_LAUNCH(2);
     CK(cudaGetLastError());
 }
 

@@ -55,6 +55,10 @@ void launch_square(int ntask, int n, const double *A, size_t lda, size_t mstride
 // a_0, a_1, a_2 per distinct m of a chunk (groups), shared by all frequencies
 void launch_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, cudaStream_t st);
 size_t a12_bytes(int ldim, int ngroup);
+// mixed form: the same from per-m tables (work: a12_tab_bytes of scratch)
+size_t a12_tab_bytes(int ldim, int ngroup);
+void launch_a12_mixed(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, void *work,
+                      cudaStream_t st);
 void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv, double *A,
                  size_t lda, size_t mat_stride, double *mdiag, int *status, cudaStream_t st);
 void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, const double *mdiag, int mode,

@@ -13,19 +13,25 @@
 // the FP64 pipe is touched only by per-pair set-up.
 //
 // The early stop is the reference's rule (three consecutive terms below a threshold
-// relative to the q = 0 term, integration.c:563-575) with the threshold e^-40 instead
-// of e^-60: float-float carries ~2^-48 of the q = 0 term, so smaller terms, and the
-// geometric tail after three of them, cannot change the sum.
+// relative to the q = 0 term, integration.c:563-575) with the threshold 2^-44 (about
+// e^-30.5) instead of e^-60, tested on exponents only.  The I values feed elements that
+// the mixed form stores in FP32 (2^-24), so terms below 2^-44 of the q = 0 term leave 20
+// bits of headroom for cancellation in the B, C, D combinations of the elements.  On
+// the R/L=150 free energy the result does not move between 2^-58 and 2^-38 (|dE/E|
+// 5.58e-11 throughout) while the term count falls by a quarter.
 #include "common.cuh"
 #include "ff.cuh"
 #include "internal.h"
 
 namespace capsgpu {
 
-// float-float quotient x / y (Dekker 1971: one correction of the leading quotient)
+// float-float quotient x / y (Dekker 1971: one correction of the leading quotient).  The
+// reciprocal is the hardware approximation (relative error ~2^-23): the correction
+// q2 = (x - q1 y) r then leaves a relative error ~2^-45, below the 2^-44 the q-sums keep.
 CAPS_DEV ff ff_div(ff x, ff y)
 {
-    const float r = __frcp_rn(y.h);
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y.h));
     const float q1 = x.h * r;
     const ff p = ff_mul(ff{q1, 0.0f}, y);
     const ff rem = ff_add(x, ff_neg(p));
@@ -35,17 +41,16 @@ CAPS_DEV ff ff_div(ff x, ff y)
 struct IAcc {
     float h, l; // running sum (h + l) 2^e
     int e;
-    int e0;     // exponent and mantissa of the q = 0 term
-    float m0;
+    int thr;    // a term t stops counting as significant once exponent(t) < thr
     int count;
     bool on;
 };
 
-// sum += t 2^et, keeping |h| within 2^+-40 by exact power-of-two shifts
+// sum += t 2^et, keeping |h| within 2^+-40 by exact power-of-two shifts.  A zero term
+// adds zero; a zero sum takes the term at the sum's exponent (or moves to the term's
+// exponent when that is more than 2^30 above).
 CAPS_DEV void iacc_add(IAcc &A, ff t, int et)
 {
-    if (t.h == 0.0f) return;
-    if (A.h == 0.0f) { A.h = t.h; A.l = t.l; A.e = et; return; }
     int d = et - A.e;
     if (d > 30) {
         const ff s = ff_shift(ff{A.h, A.l}, -d);
@@ -70,7 +75,7 @@ template <int G>
 __global__ void __launch_bounds__(128, 3) k_itab_grp(const Task *tasks, const int4 *groups, int ngroups, int ldim,
                                                   const ffe *__restrict__ KF, int nu_stride, const float4 *__restrict__ ptabf,
                                                   int pstride, const A012 *__restrict__ a12, void *Iout, bool ffe_out,
-                                                  int *status)
+                                                  int *status, int stop_bits)
 {
     const int L = ldim + 2;
     const long long npair = (long long)L * (L + 1) / 2;
@@ -118,10 +123,10 @@ __global__ void __launch_bounds__(128, 3) k_itab_grp(const Task *tasks, const in
     for (int j = 0; j < 2 * G; j++) {
         const bool live = (j >> 1) < ng && ((j & 1) == 0 || both);
         IAcc &A = acc[j];
-        A = IAcc{0.0f, 0.0f, 0, 0, 1.0f, 0, live};
+        A = IAcc{0.0f, 0.0f, 0, 0, 0, live};
         if (!live) continue;
         const ffe k0 = Kat(j, l12);
-        A.h = k0.h; A.l = k0.l; A.e = k0.e; A.e0 = k0.e; A.m0 = fabsf(k0.h);
+        A.h = k0.h; A.l = k0.l; A.e = k0.e; A.thr = fexpo(k0.h) + k0.e - stop_bits;
         if (qmax >= 1) { const ffe k = Kat(j, l12 - 2); iacc_add(A, ff_mul(ff_from_d(A12.a1), ff{k.h, k.l}), k.e); }
         if (qmax >= 2) { const ffe k = Kat(j, l12 - 4); iacc_add(A, ff_mul(ff_from_d(A12.a2), ff{k.h, k.l}), k.e); }
     }
@@ -185,15 +190,9 @@ __global__ void __launch_bounds__(128, 3) k_itab_grp(const Task *tasks, const in
                 const int et = ea + Kv.e;
                 iacc_add(A, t, et);
                 if (t.h != 0.0f) {
-                    // |term| / |q=0 term| = (mt / m0) 2^approx with mt, m0 in [1,2):
-                    // below e^-40 = 2^-57.708 for approx <= -59, above for approx >= -56
-                    const int kt = fexpo(t.h);
-                    const int approx = kt + et - A.e0;
-                    bool below;
-                    if (approx <= -59) below = true;
-                    else if (approx >= -56) below = false;
-                    else below = fabsf(fshift(t.h, -kt)) < (approx == -58 ? 1.2245047450284177f : 0.6122523725142088f) * A.m0;
-                    if (below) { if (++A.count >= 3) A.on = false; }
+                    // exponent(t) < exponent(q=0 term) - stop_bits: |t| below 2^-stop_bits of
+                    // the q = 0 term (and above 2^-stop_bits-2 of it when not)
+                    if (fexpo(t.h) + et < A.thr) { if (++A.count >= 3) A.on = false; }
                     else A.count = 0;
                 }
                 any |= A.on;
@@ -230,6 +229,7 @@ __global__ void __launch_bounds__(128, 3) k_itab_grp(const Task *tasks, const in
 // shared) and 4 (145 registers cost occupancy, and a subgroup runs to the term count of
 // its slowest frequency, which grows linearly with the Matsubara index)
 constexpr int IGRP = 2;
+constexpr int ITAB_STOP_BITS = 44; // early stop below 2^-44 of the q = 0 term
 int itab_group_size() { return IGRP; }
 
 void launch_itab_grp(const Task *tasks, int ntask, const int4 *groups, int ngroups, int ldim, const sd *K, int nu_stride,
@@ -240,7 +240,7 @@ void launch_itab_grp(const Task *tasks, int ntask, const int4 *groups, int ngrou
     const long long L = ldim + 2, npair = L * (L + 1) / 2;
     dim3 g((unsigned)((npair + 127) / 128), ngroups);
     k_itab_grp<IGRP><<<g, 128, 0, st>>>(tasks, groups, ngroups, (int)ldim, KF, nu_stride, ptabf, pstride, (const A012 *)a12, Iout,
-                                        ffe_out, status);
+                                        ffe_out, status, ITAB_STOP_BITS);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

@@ -86,7 +86,7 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -530,7 +530,10 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         sd *d_I = (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
         double4 *d_ptab = (double4 *)g_eng.ptab.get((size_t)nt * 2 * pstride * sizeof(double4));
         void *d_a12 = g_eng.a12.get(a12_bytes(ldim, ngroup));
-        launch_a12(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, st);
+        if (caps->precision == CAPS_PREC_MIXED)
+            launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, g_eng.a12t.get(a12_tab_bytes(ldim, ngroup)), st);
+        else
+            launch_a12(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, st);
         if (caps->precision == CAPS_PREC_MIXED) {
             // mixed form: the q-sums in float-float on the FP32 pipe
             ffe *d_KF = (ffe *)g_eng.KF.get((size_t)nt * 2 * nu_stride * 16);
