@@ -14,6 +14,8 @@
 // Formulas: elements as in libcaps.c:717-831 (caps_M_elem / caps_kernel_M) with A, B,
 // C, D from integration.c:762-888; shortcut decision as in matrix.c:57-119
 // (kernel_logdet) and matrix.c:489-505 (Mercator bound).
+#include <climits>
+
 #include "common.cuh"
 #include "ff.cuh"
 #include "internal.h"
@@ -36,17 +38,27 @@ CAPS_DEV fe fe_norm(ff x, int e)
 CAPS_DEV fe fe_ld(const ffe &v) { return fe{v.h, v.l, v.e}; }
 CAPS_DEV fe fe_neg(fe a) { return fe{-a.h, -a.l, a.e}; }
 CAPS_DEV fe fe_mul(fe a, fe b) { return fe_norm(ff_mul(ff{a.h, a.l}, ff{b.h, b.l}), a.e + b.e); }
-// c a for a float-float constant c of moderate size
-CAPS_DEV fe fe_scale(ff c, fe a) { return fe_norm(ff_mul(c, ff{a.h, a.l}), a.e); }
-CAPS_DEV fe fe_add(fe a, fe b)
+// sum_k c_k x_k for float-float coefficients c_k and fe values x_k: every x_k is rescaled
+// by an exact power of two to the largest exponent among them (terms more than 2^100
+// below it drop out), then float-float products and sums, one normalisation at the end
+template <int N>
+CAPS_DEV fe fe_lincomb(const ff (&c)[N], const fe (&x)[N])
 {
-    if (a.h == 0.0f) return b;
-    if (b.h == 0.0f) return a;
-    if (a.e < b.e) { const fe t = a; a = b; b = t; }
-    const int d = b.e - a.e;
-    const ff bs = d < -60 ? ff{0.0f, 0.0f} : ff_shift(ff{b.h, b.l}, d);
-    return fe_norm(ff_add(ff{a.h, a.l}, bs), a.e);
+    int emax = INT_MIN;
+#pragma unroll
+    for (int k = 0; k < N; k++)
+        if (x[k].h != 0.0f) emax = max(emax, x[k].e);
+    if (emax == INT_MIN) return fe{0.0f, 0.0f, 0};
+    ff s{0.0f, 0.0f};
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        const int d = x[k].e - emax;
+        const ff xs = (x[k].h == 0.0f || d < -100) ? ff{0.0f, 0.0f} : ff_shift(ff{x[k].h, x[k].l}, d);
+        s = ff_add(s, ff_mul(c[k], xs));
+    }
+    return fe_norm(s, emax);
 }
+
 // to FP32: values below 2^-120 flush to 0; non-finite or >= 2^126 set *bad
 CAPS_DEV float fe_to_float(fe a, bool &bad)
 {
@@ -115,24 +127,33 @@ __global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, int ntask, in
             const float4 w1 = uvf[so + i1], w2 = uvf[so + i2];
             const ff U1{w1.x, w1.y}, V1{w1.z, w1.w}, U2{w2.x, w2.y}, V2{w2.z, w2.w};
             const ff cUU = ff_mul(U1, U2), cVU = ff_mul(V1, U2), cUV = ff_mul(U1, V2), cVV = ff_mul(V1, V2);
+            const ff mU1 = ff_mul(m1, U1), mV1 = ff_mul(m1, V1), mU2 = ff_mul(m1, U2), mV2 = ff_mul(m1, V2);
             // B_p = u1 u2 I(l1-1,l2-1) - v1 u2 I(l1+1,l2-1) - u1 v2 I(l1-1,l2+1) + v1 v2 I(l1+1,l2+1)
-            auto Bv = [&](const ffe *t) {
-                fe r = fe_scale(cUU, Iv(t, i1 - 1, i2 - 1));
-                r = fe_add(r, fe_neg(fe_scale(cVU, Iv(t, i1 + 1, i2 - 1))));
-                r = fe_add(r, fe_neg(fe_scale(cUV, Iv(t, i1 - 1, i2 + 1))));
-                return fe_add(r, fe_scale(cVV, Iv(t, i1 + 1, i2 + 1)));
-            };
             // C_p(l1,l2) = m (v2 I(l1,l2+1) - u2 I(l1,l2-1)); D_p(l1,l2) = C_p(l2,l1)
-            auto Cv = [&](const ffe *t) {
-                return fe_scale(m1, fe_add(fe_scale(V2, Iv(t, i1, i2 + 1)), fe_neg(fe_scale(U2, Iv(t, i1, i2 - 1)))));
-            };
-            auto Dv = [&](const ffe *t) {
-                return fe_scale(m1, fe_add(fe_scale(V1, Iv(t, i1 + 1, i2)), fe_neg(fe_scale(U1, Iv(t, i1 - 1, i2)))));
-            };
-            EE = fe_mul(fe_mul(sa1, sa2), fe_add(Bv(ITM), fe_neg(fe_scale(m2, Iv(ITE, i1, i2)))));
-            MM = fe_mul(fe_mul(sb1, sb2), fe_add(fe_scale(m2, Iv(ITM, i1, i2)), fe_neg(Bv(ITE))));
-            EM = fe_mul(fe_mul(sa1, sb2), fe_add(Dv(ITM), fe_neg(Cv(ITE))));
-            ME = fe_mul(fe_mul(sb1, sa2), fe_add(Cv(ITM), fe_neg(Dv(ITE))));
+            // EE = B_TM - m^2 I_TE,  MM = m^2 I_TM - B_TE,  EM = D_TM - C_TE,  ME = C_TM - D_TE
+            // (times the scale factors), each one linear combination of the I values
+            {
+                const ff c[5] = {cUU, ff_neg(cVU), ff_neg(cUV), cVV, ff_neg(m2)};
+                const fe x[5] = {Iv(ITM, i1 - 1, i2 - 1), Iv(ITM, i1 + 1, i2 - 1), Iv(ITM, i1 - 1, i2 + 1), Iv(ITM, i1 + 1, i2 + 1),
+                                 Iv(ITE, i1, i2)};
+                EE = fe_mul(fe_mul(sa1, sa2), fe_lincomb(c, x));
+            }
+            {
+                const ff c[5] = {m2, ff_neg(cUU), cVU, cUV, ff_neg(cVV)};
+                const fe x[5] = {Iv(ITM, i1, i2), Iv(ITE, i1 - 1, i2 - 1), Iv(ITE, i1 + 1, i2 - 1), Iv(ITE, i1 - 1, i2 + 1),
+                                 Iv(ITE, i1 + 1, i2 + 1)};
+                MM = fe_mul(fe_mul(sb1, sb2), fe_lincomb(c, x));
+            }
+            {
+                const ff c[4] = {mV1, ff_neg(mU1), ff_neg(mV2), mU2};
+                const fe x[4] = {Iv(ITM, i1 + 1, i2), Iv(ITM, i1 - 1, i2), Iv(ITE, i1, i2 + 1), Iv(ITE, i1, i2 - 1)};
+                EM = fe_mul(fe_mul(sa1, sb2), fe_lincomb(c, x));
+            }
+            {
+                const ff c[4] = {mV2, ff_neg(mU2), ff_neg(mV1), mU1};
+                const fe x[4] = {Iv(ITM, i1, i2 + 1), Iv(ITM, i1, i2 - 1), Iv(ITE, i1 + 1, i2), Iv(ITE, i1 - 1, i2)};
+                ME = fe_mul(fe_mul(sb1, sa2), fe_lincomb(c, x));
+            }
         }
         bool bad = false;
         const float ee = fe_to_float(EE, bad), mm = fe_to_float(MM, bad);
