@@ -71,7 +71,7 @@ void launch_elem_ff(const Task *tasks, int ntask, int ldim, const sd *Sa, const 
 void launch_stats_ff(int ntask, int ldim, const double *diag, const float *part, int mode, double *trace, double *result,
                      int *status, cudaStream_t st);
 void launch_cholesky(int ntask, int n, double *A, size_t lda, size_t mstride, int *status, double *logdiag, cudaStream_t st);
-size_t mixed_work_bytes(int ntask);
+size_t mixed_work_bytes(int ntask, int n);
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
                            const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc,
                            bool convert, void *work);

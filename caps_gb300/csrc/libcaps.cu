@@ -576,11 +576,11 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         // CAPS_MIXED_SIMT=1 selects the FP32 FFMA trailing update instead of split-TF32 tensor cores
         static const bool tc = getenv("CAPS_MIXED_SIMT") == nullptr;
         if (ff_elem) {
-            void *d_work = g_eng.mwork.get(mixed_work_bytes(nt));
+            void *d_work = g_eng.mwork.get(mixed_work_bytes(nt, dim));
             launch_cholesky_mixed(nt, dim, nullptr, 0, 0, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, false, d_work);
         } else if (O.factor && caps->precision == CAPS_PREC_MIXED && !O.square) {
             d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
-            void *d_work = g_eng.mwork.get(mixed_work_bytes(nt));
+            void *d_work = g_eng.mwork.get(mixed_work_bytes(nt, dim));
             launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, true, d_work);
         } else if (O.factor) {
             double *d_ld = (double *)g_eng.logdiag.get((size_t)nt * dim * sizeof(double));

@@ -25,7 +25,23 @@ namespace capsgpu {
 
 constexpr int MB = 64; // panel width
 static_assert(MB == UM_K, "the tcgen05 trailing update is built for the panel width");
-constexpr int FROP = 32; // blocks per matrix of the Frobenius partial sums
+// ||Lam||_F^2 is summed where the final entries of Lam are written: one partial per
+// diagonal block (k_potf2_d) and per 64-row block of each panel solve (k_trsm_inv), in
+// slot p (NBR + 1) and p (NBR + 1) + 1 + b of a task's PS = NBR (NBR + 1) slots, NBR = ceil(n / 64)
+__host__ __device__ inline int fro_nbr(int n) { return (n + MB - 1) / MB; }
+__host__ __device__ inline int fro_slots(int n) { return fro_nbr(n) * (fro_nbr(n) + 1); }
+
+// sum over the 256 threads of a block, fixed order; the result is valid in thread 0
+__device__ __forceinline__ double block_sum256(double v, double *red8)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red8[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < 8; w++) s += red8[w];
+    return s;
+}
 
 // S = A - I (lower triangle, FP32) for the tasks that need a factorisation
 __global__ void k_to_delta32(int ntask, int n, const double *A, size_t lda, size_t mstride, const int *status, float *S,
@@ -44,12 +60,14 @@ __global__ void k_to_delta32(int ntask, int n, const double *A, size_t lda, size
 
 // diagonal block in delta form: one CTA per task.  Also writes W = (I + Lam_kk)^{-1}
 // (lower triangular, row-major MB x MB per task) for the panel solve.
-__global__ void __launch_bounds__(256) k_potf2_d(int ntask, int n, int k0, float *S, size_t sstride, int *status, float *Winv)
+__global__ void __launch_bounds__(256) k_potf2_d(int ntask, int n, int k0, float *S, size_t sstride, int *status, float *Winv,
+                                                 double *fro)
 {
     const int task = blockIdx.x;
     if (task >= ntask || status[task] != ST_FACTOR) return;
     __shared__ float T[MB][MB + 1];
     __shared__ float W[MB][MB + 1];
+    __shared__ double red8[8];
     __shared__ int bad;
     const int nb = min(MB, n - k0);
     float *Sm = S + (size_t)task * sstride + (size_t)k0 * n + k0;
@@ -76,10 +94,16 @@ __global__ void __launch_bounds__(256) k_potf2_d(int ntask, int n, int k0, float
         }
         __syncthreads();
     }
+    double sq = 0.0;
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
         const int c = e / nb, r = e % nb;
-        if (r >= c) Sm[(size_t)c * n + r] = T[r][c];
+        if (r >= c) {
+            Sm[(size_t)c * n + r] = T[r][c];
+            sq = fma((double)T[r][c], (double)T[r][c], sq);
+        }
     }
+    sq = block_sum256(sq, red8);
+    if (threadIdx.x == 0) fro[(size_t)task * fro_slots(n) + (size_t)(k0 / MB) * (fro_nbr(n) + 1)] = sq;
     // W = (I + Lam)^{-1} column by column (forward substitution, one column per thread)
     for (int j = threadIdx.x; j < nb; j += blockDim.x) {
         W[j][j] = 1.0f / (1.0f + T[j][j]);
@@ -105,7 +129,7 @@ __global__ void __launch_bounds__(256) k_potf2_d(int ntask, int n, int k0, float
 // rows of X (no bank conflict), one broadcast W entry, and stores 32 consecutive rows.
 constexpr int MT = 64;
 __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, const int *status,
-                                                  const float *Winv)
+                                                  const float *Winv, double *fro)
 {
     const int task = blockIdx.y;
     if (task >= ntask || status[task] != ST_FACTOR) return;
@@ -132,13 +156,20 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
 #pragma unroll
         for (int q = 0; q < MB / 4; q++) acc[q] = fmaf(a, Wl[cq + 4 * q][k], acc[q]);
     }
+    double sq = 0.0;
     if (r < rows) {
 #pragma unroll
         for (int q = 0; q < MB / 4; q++) {
             const int c = cq + 4 * q;
-            if (c < nb) Sm[(size_t)(k0 + c) * n + r0 + r] = acc[q];
+            if (c < nb) {
+                Sm[(size_t)(k0 + c) * n + r0 + r] = acc[q];
+                sq = fma((double)acc[q], (double)acc[q], sq);
+            }
         }
     }
+    __shared__ double red8[8];
+    sq = block_sum256(sq, red8);
+    if (threadIdx.x == 0) fro[(size_t)task * fro_slots(n) + (size_t)(k0 / MB) * (fro_nbr(n) + 1) + 1 + blockIdx.x] = sq;
 }
 
 // trailing update S_ab -= sum_k Lam_ak Lam_bk over the panel, 64x64 tiles of the
@@ -281,28 +312,6 @@ __global__ void __launch_bounds__(128) k_syrk_tc(int ntask, int n, int k0, float
             }
 }
 
-// ||Lam||_F^2 in FROP partial sums per task: block b takes the columns c = b (mod FROP)
-__global__ void __launch_bounds__(256) k_fro_part(int ntask, int n, const float *S, size_t sstride, const int *status, double *part)
-{
-    const int task = blockIdx.y;
-    if (task >= ntask || status[task] != ST_FACTOR) return;
-    const float *Sm = S + (size_t)task * sstride;
-    __shared__ double red[256];
-    double fro = 0.0;
-    for (int c = blockIdx.x; c < n; c += FROP)
-        for (int r = c + threadIdx.x; r < n; r += blockDim.x) {
-            const double v = Sm[(size_t)c * n + r];
-            fro = fma(v, v, fro);
-        }
-    red[threadIdx.x] = fro;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) part[(size_t)task * FROP + blockIdx.x] = red[0];
-}
-
 // log det = 2 sum log1p(Lam_jj) + tr(A-I) - 2 tr Lam - ||Lam||_F^2, all sums FP64;
 // one CTA per task, fixed reduction order
 __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const float *S, size_t sstride, const double *mdiag,
@@ -315,37 +324,42 @@ __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const flo
     if (st & ~0xF) { if (threadIdx.x == 0) result[task] = NAN; return; }
     if (st != ST_FACTOR) return;
     const float *Sm = S + (size_t)task * sstride;
-    __shared__ double red[256];
-    red[threadIdx.x] = threadIdx.x < FROP ? part[(size_t)task * FROP + threadIdx.x] : 0.0;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x != 0) return;
-    // Kahan sums in index order: pivot logs, tr(A-I), tr Lam
-    double sl = 0, cl = 0, sa = 0, ca = 0, st_ = 0, ct = 0;
-    for (int j = 0; j < n; j++) {
+    // per thread (strided j, fixed order): pivot logs, tr(A-I), tr Lam, and the Frobenius
+    // partials; then one fixed-order block sum of each
+    double sl = 0, sa = 0, st_ = 0, sf = 0;
+    for (int j = threadIdx.x; j < n; j += 256) {
         const double lam = Sm[(size_t)j * n + j];
-        const double y1 = log1p(lam) - cl; const double t1 = sl + y1; cl = (t1 - sl) - y1; sl = t1;
-        const double y2 = -mdiag[(size_t)task * n + j] - ca; const double t2 = sa + y2; ca = (t2 - sa) - y2; sa = t2;
-        const double y3 = lam - ct; const double t3 = st_ + y3; ct = (t3 - st_) - y3; st_ = t3;
+        sl += log1p(lam);
+        sa -= mdiag[(size_t)task * n + j];
+        st_ += lam;
     }
-    const double trDelta = sa - 2.0 * st_ - red[0];
+    const int PS = fro_slots(n);
+    for (int i = threadIdx.x; i < PS; i += 256) sf += part[(size_t)task * PS + i];
+    __shared__ double red8[8];
+    sl = block_sum256(sl, red8);
+    __syncthreads();
+    sa = block_sum256(sa, red8);
+    __syncthreads();
+    st_ = block_sum256(st_, red8);
+    __syncthreads();
+    sf = block_sum256(sf, red8);
+    if (threadIdx.x != 0) return;
+    const double trDelta = sa - 2.0 * st_ - sf;
     double ld = 2.0 * sl + trDelta;
     if (mode == 1 && fabs(trace[task]) > fabs(ld)) ld = -trace[task];
     result[task] = ld;
 }
 
-size_t mixed_work_bytes(int ntask) { return (size_t)ntask * (MB * MB * sizeof(float) + FROP * sizeof(double)); }
+size_t mixed_work_bytes(int ntask, int n) { return (size_t)ntask * (MB * MB * sizeof(float) + fro_slots(n) * sizeof(double)); }
 
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
                            const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc, bool convert,
                            void *work)
 {
-    // work: mixed_work_bytes(ntask) of scratch (diagonal-block inverses, Frobenius partials)
+    // work: mixed_work_bytes(ntask, n) of scratch (diagonal-block inverses, Frobenius partials)
     float *Winv = (float *)work;
     double *part = (double *)((char *)work + (size_t)ntask * MB * MB * sizeof(float));
+    CK(cudaMemsetAsync(part, 0, (size_t)ntask * fro_slots(n) * sizeof(double), st));
     // convert: A is the FP64 matrix 1 - M and S receives its delta form here; otherwise S
     // already holds it.  mdiag: M_ii in FP64, n per task (tr(A - I) = -tr M).
     // Trailing update: tcgen05 (k_syrk_umma); CAPS_MIXED_MMASYNC=1 selects the mma.sync
@@ -362,12 +376,12 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         COUNT_LAUNCH(1);
     }
     for (int k0 = 0; k0 < n; k0 += MB) {
-        k_potf2_d<<<ntask, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv);
+        k_potf2_d<<<ntask, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part);
         COUNT_LAUNCH(1);
         const int rest = n - k0 - MB;
         if (rest <= 0) break;
         dim3 gt((rest + MT - 1) / MT, ntask);
-        k_trsm_inv<<<gt, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv);
+        k_trsm_inv<<<gt, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part);
         COUNT_LAUNCH(1);
         const int nt = (rest + 63) / 64;
         dim3 gs(nt * (nt + 1) / 2, ntask);
@@ -380,10 +394,8 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
             k_syrk_f<<<gs, 64, 0, st>>>(ntask, n, k0, S, sstride, status);
         COUNT_LAUNCH(1);
     }
-    dim3 gf(FROP, ntask);
-    k_fro_part<<<gf, 256, 0, st>>>(ntask, n, S, sstride, status, part);
     k_final_mixed<<<ntask, 256, 0, st>>>(ntask, n, S, sstride, mdiag, trace, status, result, mode, part);
-    COUNT_LAUNCH(2);
+    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
