@@ -375,24 +375,44 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         k_to_delta32<<<g, 256, 0, st>>>(ntask, n, A, lda, mstride, status, S, sstride);
         COUNT_LAUNCH(1);
     }
-    for (int k0 = 0; k0 < n; k0 += MB) {
+    // diagonal block k0 and the panel solve below it; false when nothing lies below
+    auto factor_panel = [&](int k0) {
         k_potf2_d<<<ntask, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part);
         COUNT_LAUNCH(1);
         const int rest = n - k0 - MB;
-        if (rest <= 0) break;
+        if (rest <= 0) return false;
         dim3 gt((rest + MT - 1) / MT, ntask);
         k_trsm_inv<<<gt, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part);
         COUNT_LAUNCH(1);
-        const int nt = (rest + 63) / 64;
-        dim3 gs(nt * (nt + 1) / 2, ntask);
-        if (tc && !legacy_mma) {
-            const int nr = (rest + UM_M - 1) / UM_M;
-            k_syrk_umma<<<dim3(nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, S, sstride, status);
-        } else if (tc)
-            k_syrk_tc<<<gs, 128, 0, st>>>(ntask, n, k0, S, sstride, status);
-        else
-            k_syrk_f<<<gs, 64, 0, st>>>(ntask, n, k0, S, sstride, status);
-        COUNT_LAUNCH(1);
+        return true;
+    };
+    if (tc && !legacy_mma) {
+        // two-level panels of 2 MB columns: factor the first MB, update the second MB
+        // columns with it (one column block), factor the second MB, then one K = 2 MB
+        // trailing update, so the trailing matrix passes through DRAM once per 2 MB columns
+        for (int k0 = 0; k0 < n; k0 += 2 * MB) {
+            if (!factor_panel(k0)) break;
+            const int t1 = k0 + MB, r1 = n - t1;
+            k_syrk_umma<<<dim3((r1 + UM_M - 1) / UM_M, ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, MB, t1, t1 + MB, true, S,
+                                                                                          sstride, status);
+            COUNT_LAUNCH(1);
+            if (!factor_panel(t1)) break;
+            const int t2 = k0 + 2 * MB, nr = (n - t2 + UM_M - 1) / UM_M;
+            k_syrk_umma<<<dim3(nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, 2 * MB, t2, n, false, S, sstride,
+                                                                                 status);
+            COUNT_LAUNCH(1);
+        }
+    } else {
+        for (int k0 = 0; k0 < n; k0 += MB) {
+            if (!factor_panel(k0)) break;
+            const int rest = n - k0 - MB, nt = (rest + 63) / 64;
+            dim3 gs(nt * (nt + 1) / 2, ntask);
+            if (tc)
+                k_syrk_tc<<<gs, 128, 0, st>>>(ntask, n, k0, S, sstride, status);
+            else
+                k_syrk_f<<<gs, 64, 0, st>>>(ntask, n, k0, S, sstride, status);
+            COUNT_LAUNCH(1);
+        }
     }
     k_final_mixed<<<ntask, 256, 0, st>>>(ntask, n, S, sstride, mdiag, trace, status, result, mode, part);
     COUNT_LAUNCH(1);

@@ -1,6 +1,8 @@
 // syrk_umma.cuh -- trailing update of the FP32 delta-form Cholesky on the tcgen05 tensor
-// cores: S_tile -= P_rows P_cols^T over the current panel P (K = 64 columns), with the
-// split-TF32 product hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory.
+// cores: S_tile -= P_rows P_cols^T over a panel P of kw = 64 or 128 columns (chunks of
+// K = 64 accumulated in place), with the split-TF32 product hi*hi + hi*lo + lo*hi
+// accumulated in FP32 in tensor memory.  Each tile of S is read and written once per
+// call, so a 128-column panel halves the trailing matrix's DRAM traffic.
 //
 // One CTA of 256 threads owns a 128 x 64 tile of the lower triangle.  The threads stage
 // the two panel slices into shared memory (16 independent loads in flight per thread),
@@ -10,9 +12,10 @@
 // layout, so a warp writes one whole core matrix (conflict-free) and reads 8 consecutive
 // rows of 4 columns (four full 32-byte sectors).  One thread issues 8 k-steps x 3 MMAs
 // (M = 128, N = 64, K = 8) into a 64-column accumulator and commits them to an mbarrier;
-// meanwhile every thread loads its 32 entries of the tile of S, then waits (bounded) and
-// the 8 warps subtract the accumulator: warp w reads tensor-memory lanes 32 (w mod 4) ..
-// +31 (tile rows) and columns 32 (w / 4) .. +31.
+// before the next chunk overwrites the slices every thread waits (bounded) for that
+// commit.  While the last chunk's MMAs run every thread loads its 32 entries of the tile
+// of S, then waits and the 8 warps subtract the accumulator: warp w reads tensor-memory
+// lanes 32 (w mod 4) .. +31 (tile rows) and columns 32 (w / 4) .. +31.
 #pragma once
 #include "common.cuh"
 #include "umma.cuh"
@@ -68,21 +71,26 @@ __device__ __forceinline__ void um_stage(const float *Sm, int n, int k0, int nb,
     }
 }
 
-// grid (nr (nr + 1), ntask), nr = ceil(rest / 128); S column-major n x n per task
-__global__ void __launch_bounds__(UM_THREADS, 2) k_syrk_umma(int ntask, int n, int k0, float *S, size_t sstride, int *status)
+// S[t0.., t0..cmax) -= P P^T with P = columns k0 .. k0 + kw - 1 (rows >= t0), lower triangle.
+// grid (nr (nr + 1), ntask) with nr = ceil((n - t0) / 128), tile p -> (row block ri, column
+// block cj <= 2 ri + 1); with one_col, grid (nr, ntask) and tile p -> (p, 0), the single
+// column block [t0, t0 + 64).  S column-major n x n per task.
+__global__ void __launch_bounds__(UM_THREADS, 2) k_syrk_umma(int ntask, int n, int k0, int kw, int t0, int cmax, bool one_col,
+                                                            float *S, size_t sstride, int *status)
 {
     const int task = blockIdx.y;
     if (task >= ntask || status[task] != ST_FACTOR) return;
-    const int nb = min(UM_K, n - k0);
-    const int t0 = k0 + nb;
-    // tile p -> (row block ri, column block cj <= 2 ri + 1)
     const int p = blockIdx.x;
-    int ri = (int)((sqrtf(4.0f * p + 1.0f) - 1.0f) * 0.5f);
-    while ((ri + 1) * (ri + 2) <= p) ri++;
-    while (ri * (ri + 1) > p) ri--;
-    const int cj = p - ri * (ri + 1);
+    int ri = p, cj = 0;
+    if (!one_col) {
+        ri = (int)((sqrtf(4.0f * p + 1.0f) - 1.0f) * 0.5f);
+        while ((ri + 1) * (ri + 2) <= p) ri++;
+        while (ri * (ri + 1) > p) ri--;
+        cj = p - ri * (ri + 1);
+    }
+    const int cend = min(n, cmax);
     const int row0 = t0 + ri * UM_M, col0 = t0 + cj * UM_N;
-    if (row0 >= n || col0 >= n) return; // uniform per CTA
+    if (row0 >= n || col0 >= cend) return; // uniform per CTA
 
     extern __shared__ __align__(128) float um_sm[];
     float *Ahi = um_sm, *Alo = Ahi + UM_M * UM_K, *Bhi = Alo + UM_M * UM_K, *Blo = Bhi + UM_N * UM_K;
@@ -93,27 +101,40 @@ __global__ void __launch_bounds__(UM_THREADS, 2) k_syrk_umma(int ntask, int n, i
 
     if (warp == 0) umma::alloc(&tslot, UM_N);
     if (tid == 0) umma::mbar_init(&mbar, 1);
-    // stage both slices (coalesced along the rows), split into TF32 hi + lo
-    um_stage<UM_M>(Sm, n, k0, nb, row0, Ahi, Alo, tid);
-    um_stage<UM_N>(Sm, n, k0, nb, col0, Bhi, Blo, tid);
-    umma::fence_smem_async();
-    umma::fence_before();
-    __syncthreads();
-    umma::fence_after();
-    const uint32_t tmem = tslot;
-
-    if (tid == 0) {
-        constexpr uint32_t idesc = umma::idesc_tf32(UM_M, UM_N);
-        constexpr uint32_t LBO = 128, SBO = (UM_K / 4) * 128;
-        const uint32_t ah = umma::smem_u32(Ahi), al = umma::smem_u32(Alo), bh = umma::smem_u32(Bhi), bl = umma::smem_u32(Blo);
-        for (int ks = 0; ks < UM_K / 8; ks++) {
-            const uint32_t o = ks * 256; // two core matrices along K per k-step of 8
-            umma::mma_tf32(tmem, umma::desc_kmajor(al + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc, ks > 0);
-            umma::mma_tf32(tmem, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bl + o, LBO, SBO), idesc, 1);
-            umma::mma_tf32(tmem, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc, 1);
+    const int nchunk = (kw + UM_K - 1) / UM_K;
+    bool ok = true;
+    for (int ch = 0; ch < nchunk; ch++) {
+        if (ch > 0) {
+            // the previous chunk's MMAs read the slices: wait for their commit (phase ch-1)
+            // before overwriting; the decision to go on is taken by the whole CTA
+            const bool mine = umma::mbar_wait(&mbar, (ch - 1) & 1, UM_WAIT_ITERS);
+            if (!__syncthreads_and(mine)) { ok = false; break; }
+            umma::fence_after();
         }
-        umma::commit(&mbar);
+        const int kc = k0 + ch * UM_K, nb = min(UM_K, k0 + kw - kc);
+        // stage both slices (coalesced along the rows), split into TF32 hi + lo
+        um_stage<UM_M>(Sm, n, kc, nb, row0, Ahi, Alo, tid);
+        um_stage<UM_N>(Sm, n, kc, nb, col0, Bhi, Blo, tid);
+        umma::fence_smem_async();
+        umma::fence_before();
+        __syncthreads();
+        umma::fence_after();
+        if (tid == 0) {
+            const uint32_t tmem = tslot;
+            constexpr uint32_t idesc = umma::idesc_tf32(UM_M, UM_N);
+            constexpr uint32_t LBO = 128, SBO = (UM_K / 4) * 128;
+            const uint32_t ah = umma::smem_u32(Ahi), al = umma::smem_u32(Alo), bh = umma::smem_u32(Bhi), bl = umma::smem_u32(Blo);
+            for (int ks = 0; ks < UM_K / 8; ks++) {
+                const uint32_t o = ks * 256; // two core matrices along K per k-step of 8
+                umma::mma_tf32(tmem, umma::desc_kmajor(al + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc,
+                               ch > 0 || ks > 0);
+                umma::mma_tf32(tmem, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bl + o, LBO, SBO), idesc, 1);
+                umma::mma_tf32(tmem, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc, 1);
+            }
+            umma::commit(&mbar);
+        }
     }
+    const uint32_t tmem = tslot;
     // this thread's 32 entries of C, loaded while the MMAs run (the MMAs read only the
     // staged slices, never S)
     const int quad = warp & 3, half = warp >> 2;
@@ -122,9 +143,9 @@ __global__ void __launch_bounds__(UM_THREADS, 2) k_syrk_umma(int ntask, int n, i
 #pragma unroll
     for (int j = 0; j < 32; j++) {
         const int C = cb + j;
-        c[j] = (R < n && C < n && R >= C) ? Sm[(size_t)C * n + R] : 0.0f;
+        c[j] = (ok && R < n && C < cend && R >= C) ? Sm[(size_t)C * n + R] : 0.0f;
     }
-    const bool ok = umma::mbar_wait(&mbar, 0, UM_WAIT_ITERS);
+    if (ok) ok = umma::mbar_wait(&mbar, (nchunk - 1) & 1, UM_WAIT_ITERS);
     umma::fence_after();
     if (ok) {
         float v[32];
@@ -133,9 +154,9 @@ __global__ void __launch_bounds__(UM_THREADS, 2) k_syrk_umma(int ntask, int n, i
 #pragma unroll
         for (int j = 0; j < 32; j++) {
             const int C = cb + j;
-            if (R < n && C < n && R >= C) Sm[(size_t)C * n + R] = c[j] - v[j];
+            if (R < n && C < cend && R >= C) Sm[(size_t)C * n + R] = c[j] - v[j];
         }
-    } else if (tid == 0)
+    } else
         atomicOr(status + task, ST_ERR_WAIT);
     umma::fence_before();
     __syncthreads();
