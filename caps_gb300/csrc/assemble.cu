@@ -348,7 +348,8 @@ __global__ void k_a12(const int *group_m, const int *group_lmin, int ngroup, int
 // which is k_a12's expression regrouped: every division and the exponential move into
 // per-l and per-(l1+l2) tables, and a pair costs a few FP64 products.  The rounding
 // differs from the reference's at the ulp level, far below the mixed form's 2^-44; the
-// FP64 form keeps k_a12.
+// FP64 form keeps k_a12.  The mixed table is written as float-float (A012F), so the
+// q-sum kernel needs no FP64 instruction.
 struct A12L { double F1, F2; sd eG; };             // per l, index l - (lmin - 1)
 struct A12J { double h1, pa, pb, pc; sd eH; };     // per l1 + l2, index l1 + l2 - 2(lmin - 1)
 
@@ -379,7 +380,7 @@ __global__ void k_a12_tabs(const int *group_m, const int *group_lmin, int ngroup
 }
 
 __global__ void k_a12_mix(const int *group_m, const int *group_lmin, int ngroup, int ldim, const A12L *__restrict__ tl,
-                          const A12J *__restrict__ tj, A012 *tab)
+                          const A12J *__restrict__ tj, A012F *tab)
 {
     const int L = ldim + 2, NJ = 2 * L - 1;
     const long long npair = (long long)L * (L + 1) / 2;
@@ -392,17 +393,23 @@ __global__ void k_a12_mix(const int *group_m, const int *group_lmin, int ngroup,
     const int a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
     const int mt = group_m[g], mm = mt > 0 ? mt : 1;
     const int l1 = group_lmin[g] - 1 + a1, l2 = group_lmin[g] - 1 + a2;
-    A012 r{0.0, 0.0, 0.0, 0, 0};
+    A012F r{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0, 0};
     if (!(l2 < mm || l2 < mt || l1 < 1)) {
         const int qmax = min(min(l1, l2), (l1 + l2 - 2 * mm) / 2);
         const A12L x = tl[(size_t)g * L + a1], y = tl[(size_t)g * L + a2];
         const A12J z = tj[(size_t)g * NJ + a1 + a2];
         const sd a0 = sd_mul(sd_mul(x.eG, y.eG), z.eH);
-        r.a0m = a0.m;
+        const ff a0f = ff_from_d(a0.m);
+        r.a0h = a0f.h;
+        r.a0l = a0f.l;
         r.a0e = a0.e;
         const double f = x.F1 + y.F1;
-        if (qmax >= 1) r.a1 = (l1 + l2 - 1.5) * (1 - z.h1 * f);
-        if (qmax >= 2) r.a2 = z.pa * (z.pb * (z.pc * (x.F2 + 2 * x.F1 * y.F1 + y.F2) - f) + 0.5);
+        if (qmax >= 1) { const ff v = ff_from_d((l1 + l2 - 1.5) * (1 - z.h1 * f)); r.a1h = v.h; r.a1l = v.l; }
+        if (qmax >= 2) {
+            const ff v = ff_from_d(z.pa * (z.pb * (z.pc * (x.F2 + 2 * x.F1 * y.F1 + y.F2) - f) + 0.5));
+            r.a2h = v.h;
+            r.a2l = v.l;
+        }
     }
     tab[(size_t)g * npair + pid] = r;
 }
@@ -778,7 +785,7 @@ void launch_a12_mixed(const int *group_m, const int *group_lmin, int ngroup, int
     dim3 gt((unsigned)((2 * L - 1 + 127) / 128), ngroup);
     k_a12_tabs<<<gt, 128, 0, st>>>(group_m, group_lmin, ngroup, ldim, lft, tl, tj);
     dim3 g((unsigned)((npair + 127) / 128), ngroup);
-    k_a12_mix<<<g, 128, 0, st>>>(group_m, group_lmin, ngroup, ldim, tl, tj, (A012 *)tab);
+    k_a12_mix<<<g, 128, 0, st>>>(group_m, group_lmin, ngroup, ldim, tl, tj, (A012F *)tab);
     COUNT_LAUNCH(2);
     CK(cudaGetLastError());
 }

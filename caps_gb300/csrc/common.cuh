@@ -27,6 +27,8 @@ struct sd { double m; int e; };   // value = m * 2^e
 
 // per (m, l1 >= l2) pair: a_1, a_2 and a_0 = a0m 2^a0e of the I q-sum
 struct A012 { double a1, a2, a0m; int a0e, pad; };
+// the same for the mixed form, as float-float: a_1, a_2, and a_0 = (a0h + a0l) 2^a0e
+struct A012F { float a1h, a1l, a2h, a2l, a0h, a0l; int a0e, pad; };
 
 // 2^k as a double for -1022 <= k <= 1023
 CAPS_DEV double pow2i(int k) { return __longlong_as_double((long long)(k + 1023) << 52); }

@@ -74,7 +74,7 @@ CAPS_DEV void iacc_add(IAcc &A, ff t, int et)
 template <int G>
 __global__ void __launch_bounds__(128, 3) k_itab_grp(const Task *tasks, const int4 *groups, int ngroups, int ldim,
                                                   const ffe *__restrict__ KF, int nu_stride, const float4 *__restrict__ ptabf,
-                                                  int pstride, const A012 *__restrict__ a12, void *Iout, bool ffe_out,
+                                                  int pstride, const A012F *__restrict__ a12, void *Iout, bool ffe_out,
                                                   int *status, int stop_bits)
 {
     const int L = ldim + 2;
@@ -113,7 +113,8 @@ __global__ void __launch_bounds__(128, 3) k_itab_grp(const Task *tasks, const in
     const bool both = !T.is_pr;
     const int l12 = l1 + l2;
     const int qmax = min(min(l1, l2), (l12 - 2 * mm) / 2);
-    const A012 A12 = a12[(size_t)grp.z * npair + pid];
+    const A012F A12 = a12[(size_t)grp.z * npair + pid];
+    const ff a1f{A12.a1h, A12.a1l}, a2f{A12.a2h, A12.a2l};
 
     // accumulators: j = 2 g + (0: TM, 1: TE); K table of task t, polarisation p at
     // KF[(t*2 + p) nu_stride - mu + nu] with p = 1 for TM
@@ -127,8 +128,8 @@ __global__ void __launch_bounds__(128, 3) k_itab_grp(const Task *tasks, const in
         if (!live) continue;
         const ffe k0 = Kat(j, l12);
         A.h = k0.h; A.l = k0.l; A.e = k0.e; A.thr = fexpo(k0.h) + k0.e - stop_bits;
-        if (qmax >= 1) { const ffe k = Kat(j, l12 - 2); iacc_add(A, ff_mul(ff_from_d(A12.a1), ff{k.h, k.l}), k.e); }
-        if (qmax >= 2) { const ffe k = Kat(j, l12 - 4); iacc_add(A, ff_mul(ff_from_d(A12.a2), ff{k.h, k.l}), k.e); }
+        if (qmax >= 1) { const ffe k = Kat(j, l12 - 2); iacc_add(A, ff_mul(a1f, ff{k.h, k.l}), k.e); }
+        if (qmax >= 2) { const ffe k = Kat(j, l12 - 4); iacc_add(A, ff_mul(a2f, ff{k.h, k.l}), k.e); }
     }
 
     if (qmax >= 3) {
@@ -151,12 +152,15 @@ __global__ void __launch_bounds__(128, 3) k_itab_grp(const Task *tasks, const in
             return ff_mul(av, cv);
         };
         const bool diag = (l1 == l2);
-        const double Ap = -2.0 * mm * (double)(l1 - l2) * (double)(l1 + l2 + 1);
-        const ff Ap2 = diag ? ff{0.0f, 0.0f} : ff_from_d(Ap * Ap * ldexp(1.0, -30 - sig));
+        // Ap = -2 m (l1 - l2)(l1 + l2 + 1): 2m (l1 - l2) as an exact two-product of integers
+        // below 2^24, times l1 + l2 + 1 in float-float; Ap^2 lam to ~2^-48 (sign irrelevant)
+        const float m2f = 2.0f * mm, dlf = (float)(l1 - l2), pA = m2f * dlf;
+        const ff ApF = ff_mul(ff{pA, fmaf(m2f, dlf, -pA)}, ff{(float)(l1 + l2 + 1), 0.0f});
+        const ff Ap2 = diag ? ff{0.0f, 0.0f} : ff_shift(ff_mul(ApF, ApF), -30 - sig);
         const float4 *pt = ptabf + ((size_t)t0 * 2 + (diag ? 1 : 0)) * pstride * 2;
         // b_{q-2} = a_1, b_{q-1} = a_2, D_2 = 1, normalised by the exponent of a_2
-        const int e_b = expo(A12.a2);
-        ff bm2 = ff_from_d(shift2(A12.a1, -e_b)), bm1 = ff_from_d(shift2(A12.a2, -e_b));
+        const int e_b = fexpo(A12.a2h);
+        ff bm2 = ff_shift(a1f, -e_b), bm1 = ff_shift(a2f, -e_b);
         int eb = e_b, eD = 0;
         ff Dq{1.0f, 0.0f}, Zprev{1.0f, 0.0f};
         float fx = (float)(ip + 1);
@@ -201,7 +205,7 @@ __global__ void __launch_bounds__(128, 3) k_itab_grp(const Task *tasks, const in
     }
 
     // I = a_0 sum; TE of a perfect reflector is -TM
-    const ff a0f = ff_from_d(A12.a0m);
+    const ff a0f{A12.a0h, A12.a0l};
 #pragma unroll
     for (int g = 0; g < G; g++) {
         if (g >= ng) break;
@@ -239,7 +243,7 @@ void launch_itab_grp(const Task *tasks, int ntask, const int4 *groups, int ngrou
     launch_ptab_kff(tasks, ntask, K, nu_stride, ptab, ptabf, pstride, KF, st);
     const long long L = ldim + 2, npair = L * (L + 1) / 2;
     dim3 g((unsigned)((npair + 127) / 128), ngroups);
-    k_itab_grp<IGRP><<<g, 128, 0, st>>>(tasks, groups, ngroups, (int)ldim, KF, nu_stride, ptabf, pstride, (const A012 *)a12, Iout,
+    k_itab_grp<IGRP><<<g, 128, 0, st>>>(tasks, groups, ngroups, (int)ldim, KF, nu_stride, ptabf, pstride, (const A012F *)a12, Iout,
                                         ffe_out, status, ITAB_STOP_BITS);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
