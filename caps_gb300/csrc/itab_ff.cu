@@ -71,10 +71,10 @@ CAPS_DEV void iacc_add(IAcc &A, ff t, int et)
 // The tasks of a group are consecutive, share m (hence lmin, mu, the p table and the
 // a_0..a_2 row) and the material.  Output: I tables as float-float (ffe) or, with
 // ffe_out false, as scaled doubles.  The kernel is bound by FP32/ALU issue and the latency
-// of float-float dependency chains, so occupancy pays: seven blocks of 128 per SM (72
-// registers) ran the R/L=150 free energy's q-sums in 124 ms against 137 ms at five (94).
+// of float-float dependency chains, so occupancy pays: at G = 3, six blocks of 128 per SM
+// (80 registers).
 template <int G>
-__global__ void __launch_bounds__(128, 7) k_itab_grp(const Task *tasks, const int4 *groups, int ngroups, int ldim,
+__global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const int4 *groups, int ngroups, int ldim,
                                                   const ffe *__restrict__ KF, int nu_stride, const float4 *__restrict__ ptabf,
                                                   int pstride, const A012F *__restrict__ a12, void *Iout, bool ffe_out,
                                                   int *status, int stop_bits)
@@ -231,10 +231,11 @@ __global__ void __launch_bounds__(128, 7) k_itab_grp(const Task *tasks, const in
     }
 }
 
-// tasks per subgroup.  Measured on the R/L=150 free energy: 2 beats 1 (the recurrence is
-// shared) and 4 (145 registers cost occupancy, and a subgroup runs to the term count of
-// its slowest frequency, which grows linearly with the Matsubara index)
-constexpr int IGRP = 2;
+// tasks per subgroup.  q-sums of the R/L=150 free energy (ms): G = 3 at six blocks per
+// SM 119.7, at five 123.8, at seven 122.3; G = 2 at seven 124.1, at five 136.6; G = 4
+// at five 134.6, at six 137.9.  More tasks share the recurrence, but the registers
+// cost occupancy and a subgroup runs to the term count of its slowest frequency.
+constexpr int IGRP = 3;
 constexpr int ITAB_STOP_BITS = 44; // early stop below 2^-44 of the q = 0 term
 int itab_group_size() { return IGRP; }
 
