@@ -188,6 +188,156 @@ k_ktab(const Task *tasks, const double *edges, int max_panels, const double2 *co
 }
 
 // fold the per-warp partials into K_{nu,p} (scaled doubles)
+// Mixed form of k_ktab: the same grid, node weights and row normalisation, with the
+// Legendre recurrence and the 32-node dot products in float-float (~2^-48) on the FP32
+// pipe.  P_nu^mu(x) > 0 for x >= 1 and every weight of one polarisation has one sign, so
+// the sums do not cancel; the upward recurrence (dominant solution) loses at most a bit
+// per step to its subtraction.  The node weights are still formed once per node in FP64.
+// Partials: float-float (h, l) times 2^partE.
+__global__ void k_coef_ff(int ntask, int nu_stride, const double2 *coefAB, float4 *coefF)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, task = blockIdx.y;
+    if (i >= nu_stride || task >= ntask) return;
+    const double2 c = coefAB[(size_t)task * nu_stride + i];
+    const ff a = ff_from_d(c.x), b = ff_from_d(c.y);
+    coefF[(size_t)task * nu_stride + i] = make_float4(a.h, a.l, b.h, b.l);
+}
+
+template <bool PR>
+__global__ void __launch_bounds__(KT_WARPS * 32)
+k_ktab_ff(const Task *tasks, const double *edges, int max_panels, const float4 *coefF, int nu_stride, const double *lfac_tab,
+          float2 *partF, int *partE, int max_warps)
+{
+    extern __shared__ double smem[];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2 *buf = reinterpret_cast<float2 *>(smem + wib * (32 * 33));      // [32][33]
+    float2 *wTM = reinterpret_cast<float2 *>(smem + KT_WARPS * 32 * 33 + wib * 64); // [32]
+    float2 *wTE = wTM + 32;                                                          // [32]
+    int *rowE = (int *)(smem + KT_WARPS * (32 * 33 + 64)) + wib * 32;
+
+    const int task = blockIdx.y;
+    const Task T = tasks[task];
+    const int warp = blockIdx.x * KT_WARPS + wib;
+    const int nwarp = (T.npanel + 1) / 2;
+    if (warp >= nwarp) return;
+
+    const int panel = warp * 2 + (lane >> 4), j = lane & 15;
+    const bool valid = panel < T.npanel;
+    ff x{1.0f, 0.0f}, WTM{0.0f, 0.0f}, WTE{0.0f, 0.0f};
+    int E = -(1 << 29);
+    if (valid) {
+        const double *ed = edges + (size_t)task * (max_panels + 1);
+        const double a = ed[panel], b = ed[panel + 1];
+        const double h = 0.5 * (b - a), c = 0.5 * (a + b);
+        const double t = c + h * c_glx[j], w = h * c_glw[j];
+        const double sh = sinh(t), xd = cosh(t);
+        const double ldf = lfac(lfac_tab, 2 * T.mu) - T.mu * LN2 - lfac(lfac_tab, T.mu);
+        const double lc = log(w) - T.alpha * xd + (T.mu + 1 - 2 * T.s) * log(sh) + ldf;
+        const double fl = floor(lc * INV_LN2);
+        const double f = exp(lc - fl * LN2);
+        E = (int)fl;
+        double rTE = -1.0, rTM = 1.0;
+        if (!PR) { // Fresnel at k = xi_ sinh t  (libcaps.c:616)
+            const double eps = T.epsm1_plate;
+            const double y = eps / (xd * xd);
+            const double bm1 = y / (sqrt(1 + y) + 1);
+            rTE = -bm1 / (2 + bm1);
+            rTM = (eps - bm1) / (eps + 2 + bm1);
+        }
+        x = ff_from_d(xd);
+        WTM = ff_from_d(f * rTM);
+        WTE = ff_from_d(f * rTE);
+    }
+    wTM[lane] = make_float2(WTM.h, WTM.l);
+    wTE[lane] = make_float2(WTE.h, WTE.l);
+
+    ff pp{0.0f, 0.0f}, pc{valid ? 1.0f : 0.0f, 0.0f};
+    const int nnu = T.nu_max - T.mu + 1;
+    const float4 *ab = coefF + (size_t)task * nu_stride;
+    const size_t pTM = ((size_t)(task * 2 + 1) * max_warps + warp) * nu_stride;
+    const size_t pTE = ((size_t)(task * 2 + 0) * max_warps + warp) * nu_stride;
+
+    for (int base = 0; base < nnu; base += 32) {
+        const int rows = min(32, nnu - base);
+        for (int r = 0; r < rows; r++) {
+            const int e = (pc.h != 0.0f) ? fexpo(pc.h) + E : -(1 << 29);
+            const int emax = __reduce_max_sync(0xffffffffu, e);
+            const int d = E - emax;
+            const ff v = (pc.h != 0.0f && d > -100) ? ff_shift(pc, d) : ff{0.0f, 0.0f};
+            buf[r * 33 + lane] = make_float2(v.h, v.l);
+            if (lane == 0) rowE[r] = emax;
+            const float4 c = __ldg(ab + base + r);
+            const ff pn = ff_add(ff_mul(ff_mul(ff{c.x, c.y}, x), pc), ff_neg(ff_mul(ff{c.z, c.w}, pp)));
+            pp = pc;
+            pc = pn;
+            if (fabsf(pc.h) > 0x1p40f) { pc = ff_shift(pc, -40); pp = ff_shift(pp, -40); E += 40; }
+        }
+        __syncwarp();
+        if (lane < rows) {
+            ff sTM{0.0f, 0.0f}, sTE{0.0f, 0.0f};
+            const float2 *row = buf + lane * 33;
+#pragma unroll 8
+            for (int l = 0; l < 32; l++) {
+                const float2 v = row[l];
+                const float2 wm = wTM[l];
+                sTM = ff_add(sTM, ff_mul(ff{v.x, v.y}, ff{wm.x, wm.y}));
+                if (!PR) {
+                    const float2 we = wTE[l];
+                    sTE = ff_add(sTE, ff_mul(ff{v.x, v.y}, ff{we.x, we.y}));
+                }
+            }
+            partF[pTM + base + lane] = make_float2(sTM.h, sTM.l);
+            partE[pTM + base + lane] = rowE[lane];
+            if (!PR) {
+                partF[pTE + base + lane] = make_float2(sTE.h, sTE.l);
+                partE[pTE + base + lane] = rowE[lane];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Mixed form of k_kred: the warps' float-float partials aligned to the largest exponent
+// and summed in float-float, written as the float-float K table (h in [1, 2)) that the
+// q-sums read
+__global__ void k_kred_ff(const Task *tasks, int ntask, const float2 *partF, const int *partE, int max_warps, int nu_stride,
+                          ffe *KF, int *status)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int task = blockIdx.y;
+    if (task >= ntask) return;
+    const Task &T = tasks[task];
+    const int nnu = T.nu_max - T.mu + 1;
+    if (i >= nnu) return;
+    const int nwarp = (T.npanel + 1) / 2;
+    for (int p = 1; p >= 0; p--) {
+        ffe *out = KF + (size_t)(task * 2 + p) * nu_stride + i;
+        if (p == 0 && T.is_pr) { // K_TE = -K_TM for perfect reflectors (integration.c:638)
+            const ffe k = KF[(size_t)(task * 2 + 1) * nu_stride + i];
+            *out = ffe{-k.h, -k.l, k.e, 0};
+            continue;
+        }
+        const size_t base = (size_t)(task * 2 + p) * max_warps * nu_stride + i;
+        int emax = -(1 << 29);
+        for (int w = 0; w < nwarp; w++) {
+            const float2 m = partF[base + (size_t)w * nu_stride];
+            if (m.x != 0.0f) emax = max(emax, partE[base + (size_t)w * nu_stride]);
+        }
+        ff s{0.0f, 0.0f};
+        for (int w = 0; w < nwarp; w++) {
+            const float2 m = partF[base + (size_t)w * nu_stride];
+            const int d = partE[base + (size_t)w * nu_stride] - emax;
+            if (m.x != 0.0f && d > -100) s = ff_add(s, ff_shift(ff{m.x, m.y}, d));
+        }
+        const int k = fexpo(s.h);
+        if (s.h == 0.0f || k == 128) {
+            atomicOr(status + task, ST_ERR_NONFINITE);
+            *out = ffe{s.h, 0.0f, 0, 0};
+        } else
+            *out = ffe{fshift(s.h, -k), fshift(s.l, -k), emax + k, 0};
+    }
+}
+
 __global__ void k_kred(const Task *tasks, int ntask, const double *partM, const int *partE, int max_warps, int nu_stride,
                        sd *K, int *status)
 {
@@ -802,8 +952,38 @@ void launch_ptab_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, d
     dim3 gp((pstride + 127) / 128, ntask);
     k_ptab<<<gp, 128, 0, st>>>(tasks, ntask, ptab, ptabf, pstride);
     COUNT_LAUNCH(1);
-    dim3 gk((nu_stride + 127) / 128, ntask);
-    k_kff<<<gk, 128, 0, st>>>(tasks, ntask, K, nu_stride, KF);
+    if (K) { // K == nullptr: KF already holds the float-float table (k_kred_ff)
+        dim3 gk((nu_stride + 127) / 128, ntask);
+        k_kff<<<gk, 128, 0, st>>>(tasks, ntask, K, nu_stride, KF);
+        COUNT_LAUNCH(1);
+    }
+    CK(cudaGetLastError());
+}
+
+void launch_ktab_ff(bool pr, const Task *tasks, int ntask, int max_warps, const double *edges, int max_panels, const double2 *coefAB,
+                    float4 *coefF, int nu_stride, const double *lfac_tab, float2 *partF, int *partE, cudaStream_t st)
+{
+    static bool attr_set = false;
+    const size_t sm = ktab_smem_bytes();
+    if (!attr_set) {
+        CK(cudaFuncSetAttribute(k_ktab_ff<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        CK(cudaFuncSetAttribute(k_ktab_ff<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr_set = true;
+    }
+    dim3 gc((nu_stride + 127) / 128, ntask);
+    k_coef_ff<<<gc, 128, 0, st>>>(ntask, nu_stride, coefAB, coefF);
+    dim3 g((max_warps + KT_WARPS - 1) / KT_WARPS, ntask);
+    if (pr) k_ktab_ff<true><<<g, KT_WARPS * 32, sm, st>>>(tasks, edges, max_panels, coefF, nu_stride, lfac_tab, partF, partE, max_warps);
+    else k_ktab_ff<false><<<g, KT_WARPS * 32, sm, st>>>(tasks, edges, max_panels, coefF, nu_stride, lfac_tab, partF, partE, max_warps);
+    COUNT_LAUNCH(2);
+    CK(cudaGetLastError());
+}
+
+void launch_kred_ff(const Task *tasks, int ntask, int max_nnu, const float2 *partF, const int *partE, int max_warps, int nu_stride,
+                    ffe *KF, int *status, cudaStream_t st)
+{
+    dim3 g((max_nnu + 127) / 128, ntask);
+    k_kred_ff<<<g, 128, 0, st>>>(tasks, ntask, partF, partE, max_warps, nu_stride, KF, status);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

@@ -38,6 +38,12 @@ void launch_ktab(bool pr, const Task *tasks, int ntask, int max_warps, const dou
                  int nu_stride, const double *lfac_tab, double *partM, int *partE, cudaStream_t st);
 void launch_kred(const Task *tasks, int ntask, int max_nnu, const double *partM, const int *partE, int max_warps, int nu_stride,
                  sd *K, int *status, cudaStream_t st);
+// mixed form: the K integrals in float-float straight into the float-float K table
+struct ffe;
+void launch_ktab_ff(bool pr, const Task *tasks, int ntask, int max_warps, const double *edges, int max_panels, const double2 *coefAB,
+                    float4 *coefF, int nu_stride, const double *lfac_tab, float2 *partF, int *partE, cudaStream_t st);
+void launch_kred_ff(const Task *tasks, int ntask, int max_nnu, const float2 *partF, const int *partE, int max_warps, int nu_stride,
+                    ffe *KF, int *status, cudaStream_t st);
 void launch_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, int nx, cudaStream_t st);
 struct ffe;
 void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,

@@ -86,7 +86,7 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -522,9 +522,21 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
 
         double *d_pM = (double *)g_eng.partM.get((size_t)nt * 2 * max_warps * nu_stride * sizeof(double));
         int *d_pE = (int *)g_eng.partE.get((size_t)nt * 2 * max_warps * nu_stride * sizeof(int));
-        sd *d_K = (sd *)g_eng.K.get((size_t)nt * 2 * nu_stride * sizeof(sd));
-        launch_ktab(is_pr, d_tasks, nt, max_warps, d_edges, MAX_PANELS, d_coef, nu_stride, g_eng.d_lfac, d_pM, d_pE, st);
-        launch_kred(d_tasks, nt, nnu_max, d_pM, d_pE, max_warps, nu_stride, d_K, d_status, st);
+        const bool mixed = caps->precision == CAPS_PREC_MIXED;
+        sd *d_K = nullptr;
+        ffe *d_KF = nullptr;
+        if (mixed) {
+            // mixed form: float-float K straight into the table the q-sums read
+            d_KF = (ffe *)g_eng.KF.get((size_t)nt * 2 * nu_stride * 16);
+            float4 *d_coefF = (float4 *)g_eng.coefF.get((size_t)nt * nu_stride * sizeof(float4));
+            launch_ktab_ff(is_pr, d_tasks, nt, max_warps, d_edges, MAX_PANELS, d_coef, d_coefF, nu_stride, g_eng.d_lfac,
+                           (float2 *)d_pM, d_pE, st);
+            launch_kred_ff(d_tasks, nt, nnu_max, (const float2 *)d_pM, d_pE, max_warps, nu_stride, d_KF, d_status, st);
+        } else {
+            d_K = (sd *)g_eng.K.get((size_t)nt * 2 * nu_stride * sizeof(sd));
+            launch_ktab(is_pr, d_tasks, nt, max_warps, d_edges, MAX_PANELS, d_coef, nu_stride, g_eng.d_lfac, d_pM, d_pE, st);
+            launch_kred(d_tasks, nt, nnu_max, d_pM, d_pE, max_warps, nu_stride, d_K, d_status, st);
+        }
         CK(cudaEventRecord(g_eng.ev[2], st));
 
         sd *d_I = (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
@@ -536,7 +548,6 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             launch_a12(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, st);
         if (caps->precision == CAPS_PREC_MIXED) {
             // mixed form: the q-sums in float-float on the FP32 pipe
-            ffe *d_KF = (ffe *)g_eng.KF.get((size_t)nt * 2 * nu_stride * 16);
             float4 *d_ptabf = (float4 *)g_eng.ptabf.get((size_t)nt * 2 * pstride * 2 * sizeof(float4));
             launch_itab_grp(d_tasks, nt, d_sub, nsub, ldim, d_K, nu_stride, d_ptab, pstride, d_KF, d_ptabf, d_a12, d_I, ff_elem,
                             d_status, st);
