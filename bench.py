@@ -168,6 +168,22 @@ def run_reference(args, dist, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# DRAM bytes per algorithmic byte of k_syrk_umma, from the ncu capture summarised in
+# profiles/k_syrk_umma_c3_small.md
+SYRK_DRAM_PER_ALGORITHMIC = 0.92
+
+
+def measured_hbm_peak():
+    """HBM copy bandwidth of the GB300s (GB/s) from MEASURED_PEAKS.json, else the fallback"""
+    p = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            v = json.load(f)["hbm_gbs"]
+        return float(v), "of measured (MEASURED_PEAKS.json hbm_gbs: STREAM-style copy)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "of fallback (6.8 TB/s, one earlier GB300 measurement)"
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -183,6 +199,9 @@ def main():
                     help="skip the side measurement of the plain FP64 form")
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: one batch of 8 matrices of the workload (n in {1,5}, m in {0,20,40,60})")
+    ap.add_argument("--ncu-matrices", type=int, default=8,
+                    help="matrices in the profiling case; other than 8: n = 1..4, m = 0, 4, 8, ... (all factored), "
+                         "e.g. 48 for a trailing-matrix working set above L2")
     args = ap.parse_args()
     if args.ncu_case:
         import caps_gb300 as cg
@@ -190,8 +209,13 @@ def main():
         caps = cg.Caps(R, L, ldim=LDIM)
         caps.set_drude(OMEGAP_EV, GAMMA_EV)
         caps.set_precision(cg.PREC_MIXED if args.precision == "mixed" else cg.PREC_FP64)
-        xi = [n * Ts for n in (1, 5) for m in (0, 20, 40, 60)]
-        ms = [m for n in (1, 5) for m in (0, 20, 40, 60)]
+        if args.ncu_matrices == 8:
+            xi = [n * Ts for n in (1, 5) for m in (0, 20, 40, 60)]
+            ms = [m for n in (1, 5) for m in (0, 20, 40, 60)]
+        else:  # n = 1..4, m = 0, 4, 8, ...: every matrix large enough to be factored
+            per = (args.ncu_matrices + 3) // 4
+            xi = [n * Ts for n in (1, 2, 3, 4) for k in range(per)][:args.ncu_matrices]
+            ms = [4 * k for n in (1, 2, 3, 4) for k in range(per)][:args.ncu_matrices]
         out, st = caps.logdetD_batch(xi, ms)
         print(json.dumps({"logdetD": list(out), "status": [int(s) for s in st], "phases_ms": cg.timings()}))
         return
@@ -234,6 +258,7 @@ def main():
     barrier(dist)
     cg.counters(reset=True)
     cg.reset_timings()
+    cg.kernel_timing(True)
     clocks.start()
     t0 = time.time()
     infos = []
@@ -246,6 +271,8 @@ def main():
     ctr = cg.counters()
     wk = cg.work()
     ph = cg.timings(cumulative=True)   # device ms per phase, summed over the timed steps
+    syrk_ms, syrk_bytes, syrk_n = cg.kernel_stats()
+    cg.kernel_timing(False)
 
     ndet = sum(i["ndet"] for i in infos)
     dev_s = ph[5] * 1e-3
@@ -276,6 +303,8 @@ def main():
     e2e = ndet_all / wall_max           # wall time of the public API call, host work and copies included
     fac_s = ph[4] * 1e-3
     achieved = wk["factor_flops"] / fac_s / 1e12 if fac_s > 0 else None
+    hbm_peak, hbm_src = measured_hbm_peak()
+    syrk_gbs = syrk_bytes / (syrk_ms * 1e-3) / 1e9 if syrk_ms > 0 else None
     ref = load_reference_energy()
     err = abs(E - ref["E"]) / abs(ref["E"]) if ref else None
 
@@ -306,11 +335,23 @@ def main():
                       "frac": achieved / fp64_peak if achieved else None,
                       "peak_source": "measured live: DFMA-chain probe kernel (caps_gpu_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
                       "traffic": None} if args.precision == "fp64" else
-                     {"bound": "fp32", "kernel": "FP32 delta-form Cholesky (potf2_d+trsm_d+syrk_f), n^3/3 flops per factored matrix",
-                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                      "frac": achieved / fp32_peak if achieved else None,
-                      "peak_source": "measured live: FFMA-chain probe kernel (caps_gpu_fp32_peak); MEASURED_PEAKS.json has no FP32 SIMT figure",
-                      "traffic": None}),
+                     {"bound": "hbm",
+                      "kernel": "k_syrk_umma: tcgen05 trailing update of the FP32 delta-form Cholesky (128-column panels, "
+                                "split TF32, TMEM accumulator); algorithmic bytes = trailing triangle read + written once "
+                                "and the panel rows read once, per factored matrix",
+                      "achieved": syrk_gbs, "peak": hbm_peak, "unit": "GB/s",
+                      "frac": syrk_gbs / hbm_peak if syrk_gbs else None,
+                      "traffic": syrk_bytes / syrk_n * SYRK_DRAM_PER_ALGORITHMIC if syrk_n else None,
+                      "peak_source": hbm_src,
+                      "launches": syrk_n, "avg_launch_ms": syrk_ms / syrk_n if syrk_n else None,
+                      "algorithmic_bytes_per_launch": syrk_bytes / syrk_n if syrk_n else None,
+                      "traffic_source": "DRAM bytes per algorithmic byte of the same kernel from one ncu capture "
+                                        "(profiles/k_syrk_umma_c3_small.md), times this run's algorithmic bytes per launch",
+                      "fp32_accurate_tflops_factorisation": achieved}),
+        "dominant_kernel": None if args.precision == "fp64" else {
+            "kernel": "k_itab_grp<3> (float-float q-sums)", "phase_share_of_step": ph[2] / ph[5] if ph[5] else None,
+            "bound": "FP32/ALU instruction issue; no HBM or tensor roofline applies (DRAM idle)",
+            "evidence": "profiles/k_itab_grp_c3_small.md"},
         "cpu_baseline": cpu,
         "learned_training": train_info,
         "fp64_plain_form": fp64,

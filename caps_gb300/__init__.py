@@ -63,6 +63,8 @@ def _load():
         "caps_gpu_reset_timings": (None, []),
         "caps_gpu_counters": (None, [C.POINTER(C.c_longlong)] * 3 + [i]),
         "caps_gpu_fp64_peak": (d, []),
+        "caps_gpu_kernel_timing": (None, [i]),
+        "caps_gpu_kernel_stats": (None, [dp, dp, C.POINTER(C.c_longlong)]),
         "caps_gpu_fp32_peak": (d, []),
         "caps_gpu_work": (None, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
         "caps_logdetD_noalloc": (i, [vp, d, i, dp]),
@@ -99,6 +101,18 @@ def last_error():
 def set_stream(handle):
     """Run subsequent GPU work on the given cudaStream_t handle (int) or None."""
     lib.caps_gpu_set_stream(C.c_void_p(handle) if handle else None)
+
+
+def kernel_timing(enable):
+    """live CUDA-event timing of the tcgen05 trailing update on/off (resets the totals)"""
+    lib.caps_gpu_kernel_timing(1 if enable else 0)
+
+
+def kernel_stats():
+    """(device ms, algorithmic bytes, launches) of the tcgen05 trailing update since kernel_timing(True)"""
+    ms, by, n = C.c_double(0), C.c_double(0), C.c_longlong(0)
+    lib.caps_gpu_kernel_stats(C.byref(ms), C.byref(by), C.byref(n))
+    return ms.value, by.value, n.value
 
 
 def timings(cumulative=False):

@@ -78,6 +78,10 @@ void launch_stats_ff(int ntask, int ldim, const double *diag, const float *part,
                      int *status, cudaStream_t st);
 void launch_cholesky(int ntask, int n, double *A, size_t lda, size_t mstride, int *status, double *logdiag, cudaStream_t st);
 size_t mixed_work_bytes(int ntask, int n);
+// live CUDA-event timing of the tcgen05 trailing update (mixed.cu)
+void kernel_timer_enable(bool on);
+void kernel_timer_collect(long long nfactored);
+void kernel_timer_stats(double *ms, double *bytes, long long *launches);
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
                            const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc,
                            bool convert, void *work);

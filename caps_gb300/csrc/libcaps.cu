@@ -146,6 +146,17 @@ extern "C" void caps_gpu_counters(long long *launches, long long *h2d_bytes, lon
     if (reset) g_counters = Counters();
 }
 
+extern "C" void caps_gpu_kernel_timing(int enable)
+{
+    std::lock_guard<std::mutex> lk(g_eng.mu);
+    kernel_timer_enable(enable != 0);
+}
+
+extern "C" void caps_gpu_kernel_stats(double *ms, double *bytes, long long *launches)
+{
+    kernel_timer_stats(ms, bytes, launches);
+}
+
 extern "C" void caps_gpu_work(long long *nmat, long long *nfactor, double *factor_flops)
 {
     if (nmat) *nmat = g_counters.nmat;
@@ -626,6 +637,9 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         for (int k = 0; k < 5; k++) { CK(cudaEventElapsedTime(&f, g_eng.ev[k], g_eng.ev[k + 1])); tsum[k] += f; }
         CK(cudaEventElapsedTime(&f, g_eng.ev[0], g_eng.ev[5])); tsum[5] += f;
         g_counters.nmat += nt;
+        long long nfac = 0;
+        for (int i = 0; i < nt; i++) nfac += hst[i] == ST_FACTOR;
+        kernel_timer_collect(nfac);
         for (int i = 0; i < nt; i++) {
             const int dst = order[c0 + i];
             if (O.factor) out[dst] = hres[i];

@@ -17,6 +17,8 @@
 // (log det ~ -1) and to <1e-12 on the rest.
 #include <cstdlib>
 
+#include <vector>
+
 #include "common.cuh"
 #include "internal.h"
 #include "syrk_umma.cuh"
@@ -350,6 +352,62 @@ __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const flo
     result[task] = ld;
 }
 
+// live timing of the tcgen05 trailing update (off unless caps_gpu_kernel_timing(1)):
+// CUDA events on the launching stream around every k_syrk_umma launch, and the
+// launch's algorithmic bytes per factored matrix (the trailing triangle read and
+// written once, the panel rows read once); kernel_timer_collect() resolves the events of
+// a finished batch and scales the bytes by the number of matrices it factored
+namespace {
+struct KernelTimer {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    std::vector<double> per_matrix_bytes; // one per pending launch
+    double ms = 0, bytes = 0;
+    long long launches = 0;
+    cudaEvent_t next()
+    {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+};
+KernelTimer g_kt;
+} // namespace
+
+void kernel_timer_enable(bool on)
+{
+    g_kt.on = on;
+    g_kt.used = 0;
+    g_kt.per_matrix_bytes.clear();
+    g_kt.ms = g_kt.bytes = 0;
+    g_kt.launches = 0;
+}
+
+void kernel_timer_collect(long long nfactored)
+{
+    if (!g_kt.on) return;
+    for (size_t i = 0; i < g_kt.per_matrix_bytes.size(); i++) {
+        float f;
+        CK(cudaEventElapsedTime(&f, g_kt.pool[2 * i], g_kt.pool[2 * i + 1]));
+        g_kt.ms += f;
+        g_kt.bytes += g_kt.per_matrix_bytes[i] * (double)nfactored;
+        g_kt.launches++;
+    }
+    g_kt.used = 0;
+    g_kt.per_matrix_bytes.clear();
+}
+
+void kernel_timer_stats(double *ms, double *bytes, long long *launches)
+{
+    if (ms) *ms = g_kt.ms;
+    if (bytes) *bytes = g_kt.bytes;
+    if (launches) *launches = g_kt.launches;
+}
+
 size_t mixed_work_bytes(int ntask, int n) { return (size_t)ntask * (MB * MB * sizeof(float) + fro_slots(n) * sizeof(double)); }
 
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
@@ -393,14 +451,25 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         for (int k0 = 0; k0 < n; k0 += 2 * MB) {
             if (!factor_panel(k0)) break;
             const int t1 = k0 + MB, r1 = n - t1;
+            if (g_kt.on) CK(cudaEventRecord(g_kt.next(), st));
             k_syrk_umma<<<dim3((r1 + UM_M - 1) / UM_M, ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, MB, t1, t1 + MB, true, S,
                                                                                           sstride, status);
             COUNT_LAUNCH(1);
+            if (g_kt.on) {
+                CK(cudaEventRecord(g_kt.next(), st));
+                const double cb = (double)(r1 - MB) * MB + MB * (MB + 1) / 2; // column block, lower part
+                g_kt.per_matrix_bytes.push_back(8.0 * cb + 4.0 * r1 * MB);
+            }
             if (!factor_panel(t1)) break;
-            const int t2 = k0 + 2 * MB, nr = (n - t2 + UM_M - 1) / UM_M;
+            const int t2 = k0 + 2 * MB, r2 = n - t2, nr = (r2 + UM_M - 1) / UM_M;
+            if (g_kt.on) CK(cudaEventRecord(g_kt.next(), st));
             k_syrk_umma<<<dim3(nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, 2 * MB, t2, n, false, S, sstride,
                                                                                  status);
             COUNT_LAUNCH(1);
+            if (g_kt.on) {
+                CK(cudaEventRecord(g_kt.next(), st));
+                g_kt.per_matrix_bytes.push_back(4.0 * r2 * (r2 + 1.0) + 4.0 * r2 * 2 * MB);
+            }
         }
     } else {
         for (int k0 = 0; k0 < n; k0 += MB) {
