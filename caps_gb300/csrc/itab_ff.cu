@@ -195,12 +195,11 @@ __global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const in
                 const ff t = ff_mul(aq, ff{Kv.h, Kv.l});
                 const int et = ea + Kv.e;
                 iacc_add(A, t, et);
-                if (t.h != 0.0f) {
-                    // exponent(t) < exponent(q=0 term) - stop_bits: |t| below 2^-stop_bits of
-                    // the q = 0 term (and above 2^-stop_bits-2 of it when not)
-                    if (fexpo(t.h) + et < A.thr) { if (++A.count >= 3) A.on = false; }
-                    else A.count = 0;
-                }
+                // exponent(t) < exponent(q=0 term) - stop_bits: |t| below 2^-stop_bits of the
+                // q = 0 term (and above 2^-stop_bits-2 of it when not); a zero term counts as
+                // below, as log 0 = -inf does in the reference's test
+                if (fexpo(t.h) + et < A.thr) { if (++A.count >= 3) A.on = false; }
+                else A.count = 0;
                 any |= A.on;
             }
         }
