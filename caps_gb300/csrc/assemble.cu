@@ -688,11 +688,13 @@ __global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int 
                 A.S = fma(Z, A.S, shift2(t, d));
                 const int ks = expo(A.S);
                 if (ks > 300 || (ks < -300 && ks > -1023)) { A.S = shift2(A.S, -ks); A.eS += ks; }
-                // early stop on |a_q K_q| / |K_0| < e^-60, i.e. log2 ratio < -86.5617
-                if (eb1 != -1023) {
+                // early stop on |a_q K_q| / |K_0| < e^-60, i.e. log2 ratio < -86.5617; a zero
+                // term counts as below, as log 0 = -inf does in the reference's test
+                {
                     const int approx = eb1 + eb + Kv.e - eDq - A.e0; // true log2 ratio in (approx-2, approx+2)
                     bool below;
-                    if (approx <= -89) below = true;
+                    if (eb1 == -1023) below = true;
+                    else if (approx <= -89) below = true;
                     else if (approx >= -84) below = false;
                     else {
                         // exact test without logarithms: with mantissas in [1,2),
