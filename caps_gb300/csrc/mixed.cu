@@ -17,11 +17,13 @@
 // (log det ~ -1) and to <1e-12 on the rest.
 #include <cstdlib>
 
+#include <algorithm>
 #include <vector>
 
 #include "common.cuh"
 #include "internal.h"
 #include "syrk_umma.cuh"
+#include "syrk_pipe.cuh"
 
 namespace capsgpu {
 
@@ -423,11 +425,28 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     // Trailing update: tcgen05 (k_syrk_umma); CAPS_MIXED_MMASYNC=1 selects the mma.sync
     // kernel, tc = false (CAPS_MIXED_SIMT=1) the FFMA one.
     static const bool legacy_mma = getenv("CAPS_MIXED_MMASYNC") != nullptr;
+    static const bool no_pipe = getenv("CAPS_MIXED_NOPIPE") != nullptr;
     static bool attr = false;
+    static int nsm = 1;
     if (!attr) {
         CK(cudaFuncSetAttribute(k_syrk_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
+        CK(cudaFuncSetAttribute(k_syrk_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM));
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
         attr = true;
     }
+    // trailing update of S[t0.., t0..cmax) by the panel columns k0 .. k0 + kw - 1: the
+    // persistent pipelined kernel (one CTA per SM), or with CAPS_MIXED_NOPIPE=1 one CTA per tile
+    auto syrk = [&](int k0, int kw, int t0, int cmax, bool one_col) {
+        const int nr = (n - t0 + UM_M - 1) / UM_M, tpt = one_col ? nr : nr * (nr + 1);
+        if (no_pipe)
+            k_syrk_umma<<<dim3(tpt, ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, one_col, S, sstride, status);
+        else
+            k_syrk_pipe<<<std::min(ntask * tpt, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, one_col, S, sstride,
+                                                                                     status);
+        COUNT_LAUNCH(1);
+    };
     if (convert) {
         dim3 g(256, ntask);
         k_to_delta32<<<g, 256, 0, st>>>(ntask, n, A, lda, mstride, status, S, sstride);
@@ -452,20 +471,16 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
             if (!factor_panel(k0)) break;
             const int t1 = k0 + MB, r1 = n - t1;
             if (g_kt.on) CK(cudaEventRecord(g_kt.next(), st));
-            k_syrk_umma<<<dim3((r1 + UM_M - 1) / UM_M, ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, MB, t1, t1 + MB, true, S,
-                                                                                          sstride, status);
-            COUNT_LAUNCH(1);
+            syrk(k0, MB, t1, t1 + MB, true);
             if (g_kt.on) {
                 CK(cudaEventRecord(g_kt.next(), st));
                 const double cb = (double)(r1 - MB) * MB + MB * (MB + 1) / 2; // column block, lower part
                 g_kt.per_matrix_bytes.push_back(8.0 * cb + 4.0 * r1 * MB);
             }
             if (!factor_panel(t1)) break;
-            const int t2 = k0 + 2 * MB, r2 = n - t2, nr = (r2 + UM_M - 1) / UM_M;
+            const int t2 = k0 + 2 * MB, r2 = n - t2;
             if (g_kt.on) CK(cudaEventRecord(g_kt.next(), st));
-            k_syrk_umma<<<dim3(nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, 2 * MB, t2, n, false, S, sstride,
-                                                                                 status);
-            COUNT_LAUNCH(1);
+            syrk(k0, 2 * MB, t2, n, false);
             if (g_kt.on) {
                 CK(cudaEventRecord(g_kt.next(), st));
                 g_kt.per_matrix_bytes.push_back(4.0 * r2 * (r2 + 1.0) + 4.0 * r2 * 2 * MB);
