@@ -43,28 +43,34 @@ constexpr int PIPE_A = UM_M * UM_K, PIPE_B = UM_N * UM_K;
 
 // rows [row0, row0 + R) of the panel (columns kc .. kc + nb) into hi/lo slices, by the
 // PIPE_PRODUCERS producer threads (ptid), 8 loads in flight per thread (measured: 12 loads
-// over both slices at once ran slower under the 80-register budget of 800 threads)
+// over both slices at once ran slower under the 80-register budget of 800 threads, and
+// 4-byte cp.async copies with an in-place split pass slower still).
+// Element e = base + u PIPE_PRODUCERS + ptid of a round sits in core matrix e / 32 =
+// (base + ptid) / 32 + 16 u: a thread keeps its column k through the round and its row
+// steps by 8, so the loads and stores are one base address with immediate offsets.
 template <int R>
 __device__ __forceinline__ void pipe_stage(const float *Sm, int n, int kc, int nb, int row0, float *hi_s, float *lo_s, int ptid)
 {
-    constexpr int ILP = 8;
+    constexpr int ILP = 8, CPR = UM_K / 4; // core matrices per 8-row group
     static_assert((R * UM_K) % (PIPE_PRODUCERS * ILP) == 0, "whole staging rounds");
+    static_assert(PIPE_PRODUCERS / 32 == CPR, "a round advances one 8-row group per load");
+    const int lane = ptid & 31;
 #pragma unroll 1
     for (int base = 0; base < R * UM_K; base += PIPE_PRODUCERS * ILP) {
+        const int cm0 = (base + ptid) >> 5;
+        const int k = (cm0 % CPR) * 4 + (lane & 3), r0 = row0 + (cm0 / CPR) * 8 + (lane >> 2);
+        const float *src = Sm + (size_t)(kc + k) * n + r0;
+        const bool kok = k < nb;
         float x[ILP];
 #pragma unroll
-        for (int u = 0; u < ILP; u++) {
-            int r, k;
-            um_coord(base + u * PIPE_PRODUCERS + ptid, r, k);
-            x[u] = (row0 + r < n && k < nb) ? __ldg(Sm + (size_t)(kc + k) * n + row0 + r) : 0.0f;
-        }
+        for (int u = 0; u < ILP; u++) x[u] = (kok && r0 + 8 * u < n) ? __ldg(src + 8 * u) : 0.0f;
+        float *hd = hi_s + base + ptid, *ld = lo_s + base + ptid;
 #pragma unroll
         for (int u = 0; u < ILP; u++) {
-            const int e = base + u * PIPE_PRODUCERS + ptid;
             float hi, lo;
             um_split(x[u], hi, lo);
-            hi_s[e] = hi;
-            lo_s[e] = lo;
+            hd[u * PIPE_PRODUCERS] = hi;
+            ld[u * PIPE_PRODUCERS] = lo;
         }
     }
 }
