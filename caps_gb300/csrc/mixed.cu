@@ -438,14 +438,23 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     }
     // trailing update of S[t0.., t0..cmax) by the panel columns k0 .. k0 + kw - 1: the
     // persistent pipelined kernel (one CTA per SM), or with CAPS_MIXED_NOPIPE=1 one CTA per tile
-    auto syrk = [&](int k0, int kw, int t0, int cmax, bool one_col) {
-        const int nr = (n - t0 + UM_M - 1) / UM_M, tpt = one_col ? nr : nr * (nr + 1);
+    // ncb > 0: only the first ncb column blocks (the rest of the current outer panel)
+    auto syrk = [&](int k0, int kw, int t0, int cmax, int ncb) {
+        const int nr = (n - t0 + UM_M - 1) / UM_M, tpt = ncb > 0 ? nr * ncb : nr * (nr + 1);
+        if (g_kt.on) CK(cudaEventRecord(g_kt.next(), st));
         if (no_pipe)
-            k_syrk_umma<<<dim3(tpt, ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, one_col, S, sstride, status);
+            k_syrk_umma<<<dim3(ncb == 1 ? nr : nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb == 1,
+                                                                                                 S, sstride, status);
         else
-            k_syrk_pipe<<<std::min(ntask * tpt, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, one_col, S, sstride,
+            k_syrk_pipe<<<std::min(ntask * tpt, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb, S, sstride,
                                                                                      status);
         COUNT_LAUNCH(1);
+        if (g_kt.on) {
+            CK(cudaEventRecord(g_kt.next(), st));
+            // lower part of the target block read and written in FP32, panel rows read once
+            const double r = n - t0, w = std::min(cmax, n) - t0;
+            g_kt.per_matrix_bytes.push_back(8.0 * (w * r - w * (w - 1) / 2) + 4.0 * r * kw);
+        }
     };
     if (convert) {
         dim3 g(256, ntask);
@@ -464,27 +473,21 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         return true;
     };
     if (tc && !legacy_mma) {
-        // two-level panels of 2 MB columns: factor the first MB, update the second MB
-        // columns with it (one column block), factor the second MB, then one K = 2 MB
-        // trailing update, so the trailing matrix passes through DRAM once per 2 MB columns
-        for (int k0 = 0; k0 < n; k0 += 2 * MB) {
-            if (!factor_panel(k0)) break;
-            const int t1 = k0 + MB, r1 = n - t1;
-            if (g_kt.on) CK(cudaEventRecord(g_kt.next(), st));
-            syrk(k0, MB, t1, t1 + MB, true);
-            if (g_kt.on) {
-                CK(cudaEventRecord(g_kt.next(), st));
-                const double cb = (double)(r1 - MB) * MB + MB * (MB + 1) / 2; // column block, lower part
-                g_kt.per_matrix_bytes.push_back(8.0 * cb + 4.0 * r1 * MB);
+        // two-level panels of OUTER columns: factor 64 columns at a time and update the rest of
+        // the outer panel with them, then one K = OUTER trailing update, so the trailing
+        // matrix passes through DRAM once per OUTER columns
+        constexpr int OUTER = 4 * MB;
+        bool more = true; // columns remain below the last factored panel
+        for (int k0 = 0; k0 < n && more; k0 += OUTER) {
+            // inner steps: factor 64 columns, update the rest of the outer panel with them
+            for (int kj = k0; kj < k0 + OUTER; kj += MB) {
+                if (!factor_panel(kj)) { more = false; break; }
+                const int t1 = kj + MB, cmax = std::min(k0 + OUTER, n);
+                if (t1 < cmax) syrk(kj, MB, t1, cmax, (cmax - t1 + UM_N - 1) / UM_N);
             }
-            if (!factor_panel(t1)) break;
-            const int t2 = k0 + 2 * MB, r2 = n - t2;
-            if (g_kt.on) CK(cudaEventRecord(g_kt.next(), st));
-            syrk(k0, 2 * MB, t2, n, false);
-            if (g_kt.on) {
-                CK(cudaEventRecord(g_kt.next(), st));
-                g_kt.per_matrix_bytes.push_back(4.0 * r2 * (r2 + 1.0) + 4.0 * r2 * 2 * MB);
-            }
+            const int t2 = k0 + OUTER;
+            if (!more || t2 >= n) break;
+            syrk(k0, OUTER, t2, n, 0);
         }
     } else {
         for (int k0 = 0; k0 < n; k0 += MB) {

@@ -80,14 +80,18 @@ struct PipeTile {
     bool valid;
 };
 
-// tile t of the launch: tpt tiles per matrix; one_col: tile p -> (p, 0), else p -> (ri, cj <= 2 ri + 1)
-__device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, bool one_col, int n, int t0, int cend, const int *status)
+// tile t of the launch: tpt tiles per matrix; ncb > 0: tile p -> (p / ncb, p mod ncb), the
+// first ncb column blocks; ncb = 0: p -> (ri, cj <= 2 ri + 1), the whole lower triangle
+__device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, int ncb, int n, int t0, int cend, const int *status)
 {
     PipeTile T;
     T.task = t / tpt;
     const int p = t - T.task * tpt;
     int ri = p, cj = 0;
-    if (!one_col) {
+    if (ncb > 0) {
+        ri = p / ncb;
+        cj = p - ri * ncb;
+    } else {
         ri = (int)((sqrtf(4.0f * p + 1.0f) - 1.0f) * 0.5f);
         while ((ri + 1) * (ri + 2) <= p) ri++;
         while (ri * (ri + 1) > p) ri--;
@@ -98,12 +102,12 @@ __device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, bool one_col, int 
     // skip matrices that are not being factored or failed before this launch; a wait
     // error set during this launch (ST_ERR_WAIT) does not change the walk
     const int st = status[T.task] & ~ST_ERR_WAIT;
-    T.valid = st == ST_FACTOR && T.row0 < n && T.col0 < cend;
+    T.valid = st == ST_FACTOR && T.row0 < n && T.col0 < cend && T.col0 < T.row0 + UM_M;
     return T;
 }
 
 // S[t0.., t0..cmax) -= P P^T, P = columns k0 .. k0 + kw - 1; grid = min(tiles, SMs), 800 threads
-__global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n, int k0, int kw, int t0, int cmax, bool one_col,
+__global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n, int k0, int kw, int t0, int cmax, int ncb,
                                                                float *S, size_t sstride, int *status)
 {
     extern __shared__ __align__(1024) float pipe_sm[];
@@ -112,7 +116,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int cend = min(n, cmax);
     const int nr = (n - t0 + UM_M - 1) / UM_M;
-    const int tpt = one_col ? nr : nr * (nr + 1);
+    const int tpt = ncb > 0 ? nr * ncb : nr * (nr + 1);
     const int ntile = ntask * tpt;
     const int nchunk = (kw + UM_K - 1) / UM_K;
 
@@ -135,7 +139,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
         const int ptid = tid;
         int it = 0; // chunk counter (stage ring)
         for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
-            const PipeTile T = pipe_tile(t, tpt, one_col, n, t0, cend, status);
+            const PipeTile T = pipe_tile(t, tpt, ncb, n, t0, cend, status);
             if (!T.valid) continue;
             const float *Sm = S + (size_t)T.task * sstride;
             bool ok = true;
@@ -159,7 +163,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
             constexpr uint32_t idesc = umma::idesc_tf32(UM_M, UM_N);
             constexpr uint32_t LBO = 128, SBO = (UM_K / 4) * 128;
             for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
-                const PipeTile T = pipe_tile(t, tpt, one_col, n, t0, cend, status);
+                const PipeTile T = pipe_tile(t, tpt, ncb, n, t0, cend, status);
                 if (!T.valid) continue;
                 const int b = tt & 1, ub = tt >> 1;
                 bool ok = ub == 0 || umma::mbar_wait(&tempty[b], (ub - 1) & 1, PIPE_WAIT_ITERS);
@@ -190,7 +194,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
         const int quad = warp & 3, half = (warp - PIPE_PRODUCER_WARPS - 1) >> 2;
         int tt = 0;
         for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
-            const PipeTile T = pipe_tile(t, tpt, one_col, n, t0, cend, status);
+            const PipeTile T = pipe_tile(t, tpt, ncb, n, t0, cend, status);
             if (!T.valid) continue;
             float *Sm = S + (size_t)T.task * sstride;
             const int b = tt & 1, ub = tt >> 1;
