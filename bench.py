@@ -144,7 +144,7 @@ def cpu_baseline(nmat, threads):
 
 def run_reference(args, dist, rank, world):
     threads = os.cpu_count() or 1
-    per_step = threads  # one matrix per host thread per step
+    per_step = args.cpu_sample or threads  # default: one matrix per host thread per step
     if rank != 0:
         return
     for _ in range(args.warmup):
