@@ -26,6 +26,18 @@ def test_mixed_unit_vectors_RbyL100(cg, unit_vectors):
         assert abs(got - v["logdetD"]) <= TOL_MIXED * max(1.0, abs(v["logdetD"])), (v, got)
 
 
+def test_mixed_unit_vectors_RbyL1000(cg, unit_vectors):
+    """test_logdetD.c:77-102 in the mixed form: R/L=1000, ldim=10000 (matrices of dimension
+    20000, degrees up to ~21000 in the float-float K recurrence)"""
+    cases = [v for v in unit_vectors["test_logdetD"]["cases"] if v["ldim"] == 10000]
+    c = cg.Caps(1.0, 0.001, ldim=10000)
+    c.set_precision(cg.PREC_MIXED)
+    out, st = c.logdetD_batch([v["xi"] for v in cases], [v["m"] for v in cases])
+    for v, got, s in zip(cases, out, st):
+        assert s < 16, (v, s)
+        assert abs(got - v["logdetD"]) <= TOL_MIXED * max(1.0, abs(v["logdetD"])), (v, got)
+
+
 @pytest.mark.parametrize("name", ["drude_RbyL150_ldim1050", "pr_RbyL50_ldim350", "drude_RbyL20_ldim140"])
 def test_mixed_vs_reference_fixtures(cg, ref_values, name):
     if name not in ref_values:
