@@ -46,9 +46,12 @@ struct IAcc {
     bool on;
 };
 
-// sum += t 2^et, keeping |h| within 2^+-40 by exact power-of-two shifts.  A zero term
-// adds zero; a zero sum takes the term at the sum's exponent (or moves to the term's
-// exponent when that is more than 2^30 above).
+// sum += t 2^et.  The sum's exponent frame moves up (an exact power-of-two shift of the
+// sum) only when a term lies more than 2^30 above it; otherwise the term is aligned to the
+// frame by one exact multiply.  No renormalisation is needed for range: a term adds at most
+// ~2^32 in frame units, so |h| stays below 2^32 times the number of terms, far inside float
+// range, and float-float precision does not depend on the binary scale.  A zero term adds
+// zero; a zero sum takes the term at the frame's exponent.
 CAPS_DEV void iacc_add(IAcc &A, ff t, int et)
 {
     int d = et - A.e;
@@ -60,11 +63,6 @@ CAPS_DEV void iacc_add(IAcc &A, ff t, int et)
     const float p2 = __uint_as_float((unsigned)(127 + d) << 23);
     const ff s = ff_add(ff{A.h, A.l}, d < -100 ? ff{0.0f, 0.0f} : ff{t.h * p2, t.l * p2});
     A.h = s.h; A.l = s.l;
-    const int ks = fexpo(A.h);
-    if (ks > 40 || (ks < -40 && ks > -127)) {
-        const ff r = ff_shift(ff{A.h, A.l}, -ks);
-        A.h = r.h; A.l = r.l; A.e += ks;
-    }
 }
 
 // grid (ceil(npair/128), ngroups); groups[g] = {first task, count <= G, a_0..a_2 row}.
