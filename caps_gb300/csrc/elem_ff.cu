@@ -39,7 +39,7 @@ CAPS_DEV fe fe_ld(const ffe &v) { return fe{v.h, v.l, v.e}; }
 CAPS_DEV fe fe_neg(fe a) { return fe{-a.h, -a.l, a.e}; }
 CAPS_DEV fe fe_mul(fe a, fe b) { return fe_norm(ff_mul(ff{a.h, a.l}, ff{b.h, b.l}), a.e + b.e); }
 // sum_k c_k x_k for float-float coefficients c_k and fe values x_k: every x_k is rescaled
-// by an exact power of two to the largest exponent among them (terms more than 2^100
+// to the largest exponent among them by one exact multiply with 2^d (terms more than 2^100
 // below it drop out), then float-float products and sums, one normalisation at the end
 template <int N>
 CAPS_DEV fe fe_lincomb(const ff (&c)[N], const fe (&x)[N])
@@ -52,8 +52,9 @@ CAPS_DEV fe fe_lincomb(const ff (&c)[N], const fe (&x)[N])
     ff s{0.0f, 0.0f};
 #pragma unroll
     for (int k = 0; k < N; k++) {
-        const int d = x[k].e - emax;
-        const ff xs = (x[k].h == 0.0f || d < -100) ? ff{0.0f, 0.0f} : ff_shift(ff{x[k].h, x[k].l}, d);
+        const int d = x[k].e - emax; // <= 0 for every nonzero x_k
+        const float p2 = __uint_as_float((unsigned)(127 + max(d, -126)) << 23);
+        const ff xs = (x[k].h == 0.0f || d < -100) ? ff{0.0f, 0.0f} : ff{x[k].h * p2, x[k].l * p2};
         s = ff_add(s, ff_mul(c[k], xs));
     }
     return fe_norm(s, emax);
