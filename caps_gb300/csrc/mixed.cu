@@ -30,7 +30,7 @@ namespace capsgpu {
 constexpr int MB = 64; // panel width
 static_assert(MB == UM_K, "the tcgen05 trailing update is built for the panel width");
 // ||Lam||_F^2 is summed where the final entries of Lam are written: one partial per
-// diagonal block (k_potf2_d) and per 64-row block of each panel solve (k_trsm_inv), in
+// diagonal block (k_potf2_w) and per 64-row block of each panel solve (k_trsm_inv), in
 // slot p (NBR + 1) and p (NBR + 1) + 1 + b of a task's PS = NBR (NBR + 1) slots, NBR = ceil(n / 64)
 __host__ __device__ inline int fro_nbr(int n) { return (n + MB - 1) / MB; }
 __host__ __device__ inline int fro_slots(int n) { return fro_nbr(n) * (fro_nbr(n) + 1); }
@@ -62,54 +62,63 @@ __global__ void k_to_delta32(int ntask, int n, const double *A, size_t lda, size
     }
 }
 
-// diagonal block in delta form: one CTA per task.  Also writes W = (I + Lam_kk)^{-1}
-// (lower triangular, row-major MB x MB per task) for the panel solve.
-__global__ void __launch_bounds__(256) k_potf2_d(int ntask, int n, int k0, float *S, size_t sstride, int *status, float *Winv,
-                                                 double *fro)
+// diagonal block in delta form, one warp per matrix (no block-wide barriers, only
+// __syncwarp); also writes W = (I + Lam_kk)^{-1} (lower triangular, row-major MB x MB per
+// task) for the panel solve and the block's share of ||Lam||_F^2.
+// Lane l owns rows l and l + 32 of the block (shared-memory rows 65 floats apart, so a warp's
+// accesses to one column fall into 32 distinct banks): per column j every lane forms the
+// pivot from T[j][j], scales its rows' entries of column j and subtracts their rank-1
+// update; W = (I + Lam)^{-1} follows column-parallel (two columns per lane).
+__global__ void __launch_bounds__(32) k_potf2_w(int ntask, int n, int k0, float *S, size_t sstride, int *status, float *Winv,
+                                                double *fro)
 {
     const int task = blockIdx.x;
     if (task >= ntask || status[task] != ST_FACTOR) return;
     __shared__ float T[MB][MB + 1];
     __shared__ float W[MB][MB + 1];
-    __shared__ double red8[8];
-    __shared__ int bad;
+    const int lane = threadIdx.x;
     const int nb = min(MB, n - k0);
     float *Sm = S + (size_t)task * sstride + (size_t)k0 * n + k0;
-    if (threadIdx.x == 0) bad = 0;
-    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-        const int c = e / nb, r = e % nb;
-        if (r >= c) T[r][c] = Sm[(size_t)c * n + r];
-    }
-    __syncthreads();
+    for (int c = 0; c < nb; c++)
+        for (int r = c + lane; r < nb; r += 32) T[r][c] = Sm[(size_t)c * n + r];
+    __syncwarp();
+    bool bad = false;
     for (int j = 0; j < nb; j++) {
-        const float d = T[j][j];            // pivot - 1
+        const float d = T[j][j]; // pivot - 1
         const float one_d = 1.0f + d;
-        if (!(one_d > 0.0f) && threadIdx.x == 0) bad = 1;
+        bad |= !(one_d > 0.0f);
         const float lam = d / (sqrtf(fmaxf(one_d, 1e-30f)) + 1.0f);
         const float inv = 1.0f / (1.0f + lam);
-        __syncthreads();
-        if (threadIdx.x == 0) T[j][j] = lam;
-        for (int i = j + 1 + threadIdx.x; i < nb; i += blockDim.x) T[i][j] *= inv;
-        __syncthreads();
-        const int m = nb - j - 1;
-        for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-            const int i = j + 1 + e / m, c = j + 1 + e % m;
-            if (i >= c) T[i][c] -= T[i][j] * T[c][j];
+        __syncwarp();
+        float cj[2] = {0.0f, 0.0f};
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int i = lane + 32 * h;
+            if (i > j && i < nb) { cj[h] = T[i][j] * inv; T[i][j] = cj[h]; }
         }
-        __syncthreads();
+        if (lane == 0) T[j][j] = lam;
+        __syncwarp();
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int i = lane + 32 * h;
+            if (i > j && i < nb)
+                for (int c = j + 1; c <= i; c++) T[i][c] -= cj[h] * T[c][j];
+        }
+        __syncwarp();
     }
     double sq = 0.0;
-    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-        const int c = e / nb, r = e % nb;
-        if (r >= c) {
+    for (int c = 0; c < nb; c++)
+        for (int r = c + lane; r < nb; r += 32) {
             Sm[(size_t)c * n + r] = T[r][c];
             sq = fma((double)T[r][c], (double)T[r][c], sq);
         }
-    }
-    sq = block_sum256(sq, red8);
-    if (threadIdx.x == 0) fro[(size_t)task * fro_slots(n) + (size_t)(k0 / MB) * (fro_nbr(n) + 1)] = sq;
-    // W = (I + Lam)^{-1} column by column (forward substitution, one column per thread)
-    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+    for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    if (lane == 0) fro[(size_t)task * fro_slots(n) + (size_t)(k0 / MB) * (fro_nbr(n) + 1)] = sq;
+    // W = (I + Lam)^{-1} column by column (forward substitution, columns lane and lane + 32)
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int j = lane + 32 * h;
+        if (j >= nb) continue;
         W[j][j] = 1.0f / (1.0f + T[j][j]);
         for (int i = j + 1; i < nb; i++) {
             float acc = 0.0f;
@@ -117,17 +126,18 @@ __global__ void __launch_bounds__(256) k_potf2_d(int ntask, int n, int k0, float
             W[i][j] = -acc / (1.0f + T[i][i]);
         }
     }
-    __syncthreads();
+    __syncwarp();
     float *Wt = Winv + (size_t)task * MB * MB;
-    for (int e = threadIdx.x; e < MB * MB; e += blockDim.x) {
+    for (int e = lane; e < MB * MB; e += 32) {
         const int r = e / MB, c = e % MB;
         Wt[e] = (r < nb && c <= r) ? W[r][c] : 0.0f;
     }
-    if (threadIdx.x == 0 && bad) atomicOr(status + task, ST_ERR_PIVOT);
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0 && bad) atomicOr(status + task, ST_ERR_PIVOT);
 }
 
 // panel: X (I + Lam_kk)^T = S for the rows below the diagonal block, as X = S W^T with
-// W = (I + Lam_kk)^{-1} from k_potf2_d (I + Lam_kk is within a few per cent of I, so the
+// W = (I + Lam_kk)^{-1} from k_potf2_w (I + Lam_kk is within a few per cent of I, so the
 // product is as accurate as the substitution).  64 rows per CTA of 256 threads; thread t
 // takes row t mod 64 and the 16 columns c = t / 64 (mod 4), so a warp reads 32 distinct
 // rows of X (no bank conflict), one broadcast W entry, and stores 32 consecutive rows.
@@ -463,7 +473,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     }
     // diagonal block k0 and the panel solve below it; false when nothing lies below
     auto factor_panel = [&](int k0) {
-        k_potf2_d<<<ntask, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part);
+        k_potf2_w<<<ntask, 32, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part);
         COUNT_LAUNCH(1);
         const int rest = n - k0 - MB;
         if (rest <= 0) return false;
