@@ -139,8 +139,9 @@ __global__ void __launch_bounds__(32) k_potf2_w(int ntask, int n, int k0, float 
 // panel: X (I + Lam_kk)^T = S for the rows below the diagonal block, as X = S W^T with
 // W = (I + Lam_kk)^{-1} from k_potf2_w (I + Lam_kk is within a few per cent of I, so the
 // product is as accurate as the substitution).  64 rows per CTA of 256 threads; thread t
-// takes row t mod 64 and the 16 columns c = t / 64 (mod 4), so a warp reads 32 distinct
-// rows of X (no bank conflict), one broadcast W entry, and stores 32 consecutive rows.
+// computes a 4 x 4 tile, rows t mod 16 + 16 i and columns t / 16 + 16 j, so per k it loads
+// 4 entries of X (16 distinct rows per warp, no bank conflict) and 4 of W (broadcast) for
+// 16 FMAs, and a warp stores 16 consecutive rows of each of its columns.
 constexpr int MT = 64;
 __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, const int *status,
                                                   const float *Winv, double *fro)
@@ -161,23 +162,35 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
         X[r][c] = (r < rows && c < nb) ? Sm[(size_t)(k0 + c) * n + r0 + r] : 0.0f;
     }
     __syncthreads();
-    const int r = threadIdx.x & (MT - 1), cq = threadIdx.x / MT;
-    float acc[MB / 4];
+    // 4 x 4 register tile per thread: rows rg + 16 i, columns cg + 16 j
+    const int rg = threadIdx.x & 15, cg = threadIdx.x >> 4;
+    float acc[4][4];
 #pragma unroll
-    for (int q = 0; q < MB / 4; q++) acc[q] = 0.0f;
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = 0.0f;
     for (int k = 0; k < nb; k++) {
-        const float a = X[r][k];
+        float a[4], w[4];
 #pragma unroll
-        for (int q = 0; q < MB / 4; q++) acc[q] = fmaf(a, Wl[cq + 4 * q][k], acc[q]);
+        for (int i = 0; i < 4; i++) a[i] = X[rg + 16 * i][k];
+#pragma unroll
+        for (int j = 0; j < 4; j++) w[j] = Wl[cg + 16 * j][k];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], w[j], acc[i][j]);
     }
     double sq = 0.0;
-    if (r < rows) {
 #pragma unroll
-        for (int q = 0; q < MB / 4; q++) {
-            const int c = cq + 4 * q;
-            if (c < nb) {
-                Sm[(size_t)(k0 + c) * n + r0 + r] = acc[q];
-                sq = fma((double)acc[q], (double)acc[q], sq);
+    for (int j = 0; j < 4; j++) {
+        const int c = cg + 16 * j;
+        if (c >= nb) continue;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int r = rg + 16 * i;
+            if (r < rows) {
+                Sm[(size_t)(k0 + c) * n + r0 + r] = acc[i][j];
+                sq = fma((double)acc[i][j], (double)acc[i][j], sq);
             }
         }
     }
