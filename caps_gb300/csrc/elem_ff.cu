@@ -24,23 +24,23 @@ namespace capsgpu {
 
 constexpr int EB = 128; // threads per element block (one 2x2 block of M each)
 
-struct fe { float h, l; int e; }; // (h + l) 2^e with |h| in [1,2], or h == 0
+// (h + l) 2^e.  Table values (I, scale factors) arrive with |h| in [1,2); products and
+// combinations are left unnormalised -- a product of three such mantissas stays below 8,
+// a combination of a few terms with float-float coefficients below 2^30 -- and only the
+// final conversion to FP32 / FP64 applies the exponent, so no renormalisation is spent in
+// between (float-float precision does not depend on the binary scale).
+struct fe { float h, l; int e; };
 
-// normalise |h| into [1,2); zero (or a result below 2^-126 after cancellation) is 0,
-// inf / NaN are kept so that the element check sees them
-CAPS_DEV fe fe_norm(ff x, int e)
-{
-    const int k = fexpo(x.h);
-    if (k == -127) return fe{0.0f, 0.0f, 0};
-    if (k == 128) return fe{x.h, 0.0f, 0};
-    return fe{fshift(x.h, -k), fshift(x.l, -k), e + k};
-}
 CAPS_DEV fe fe_ld(const ffe &v) { return fe{v.h, v.l, v.e}; }
 CAPS_DEV fe fe_neg(fe a) { return fe{-a.h, -a.l, a.e}; }
-CAPS_DEV fe fe_mul(fe a, fe b) { return fe_norm(ff_mul(ff{a.h, a.l}, ff{b.h, b.l}), a.e + b.e); }
-// sum_k c_k x_k for float-float coefficients c_k and fe values x_k: every x_k is rescaled
-// to the largest exponent among them by one exact multiply with 2^d (terms more than 2^100
-// below it drop out), then float-float products and sums, one normalisation at the end
+CAPS_DEV fe fe_mul(fe a, fe b)
+{
+    const ff p = ff_mul(ff{a.h, a.l}, ff{b.h, b.l});
+    return fe{p.h, p.l, a.e + b.e};
+}
+// sum_k c_k x_k for float-float coefficients c_k and table values x_k (|h| in [1,2)): every
+// x_k is rescaled to the largest exponent among them by one exact multiply with 2^d (terms
+// more than 2^100 below it drop out), then float-float products and sums
 template <int N>
 CAPS_DEV fe fe_lincomb(const ff (&c)[N], const fe (&x)[N])
 {
@@ -57,15 +57,17 @@ CAPS_DEV fe fe_lincomb(const ff (&c)[N], const fe (&x)[N])
         const ff xs = (x[k].h == 0.0f || d < -100) ? ff{0.0f, 0.0f} : ff{x[k].h * p2, x[k].l * p2};
         s = ff_add(s, ff_mul(c[k], xs));
     }
-    return fe_norm(s, emax);
+    return fe{s.h, s.l, emax};
 }
 
-// to FP32: values below 2^-120 flush to 0; non-finite or >= 2^126 set *bad
+// to FP32: values below 2^-120 flush to 0 (as do subnormal mantissas left by cancellation);
+// non-finite or >= 2^126 set *bad
 CAPS_DEV float fe_to_float(fe a, bool &bad)
 {
-    if (a.h == 0.0f) return 0.0f;
-    if (fexpo(a.h) == 128 || a.e > 125) { bad = true; return a.h; }
-    if (a.e < -120) return 0.0f;
+    const int k = fexpo(a.h);
+    if (k == -127) return 0.0f;
+    if (k == 128 || a.e + k > 125) { bad = true; return a.h; }
+    if (a.e + k < -120) return 0.0f;
     return fshift(a.h + a.l, a.e);
 }
 CAPS_DEV double fe_to_double(fe a)
