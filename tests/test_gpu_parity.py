@@ -290,6 +290,21 @@ def test_sphere_sphere_logdetD2_golden(cg, cass_golden):
         assert abs(v - s["logdetD2"]) <= TOL * abs(s["logdetD2"]), (s, v)
 
 
+def test_sphere_sphere_logdetD2_mixed(cg, cass_golden):
+    """the same log det(1 - M^2) values in the mixed form (float-float q-sums, FP64 elements
+    and square, FP32 delta-form Cholesky with the FP64 correction): 5e-8 max(1, |x|), and
+    relative below 1e-8"""
+    g = cass_golden
+    c = cg.Caps(g["R"], g["d"] / 2, ldim=g["ldim"], detalg=cg.DETALG_LU)
+    c.set_precision(cg.PREC_MIXED)
+    out, st = c.logdetD2_batch([s["xi"] for s in g["samples"]], [s["m"] for s in g["samples"]])
+    for s, v, code in zip(g["samples"], out, st):
+        w = s["logdetD2"]
+        assert code < 16, (s, code)
+        bar = 5e-8 * (abs(w) if abs(w) < 1e-8 else max(1.0, abs(w)))
+        assert abs(v - w) <= bar, (s, v)
+
+
 def test_sphere_sphere_T0_golden(cg, cass_golden):
     """the T = 0 sphere-sphere energy (cass): same qagi abscissae, E to 1e-10"""
     g = cass_golden
