@@ -453,7 +453,8 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     static int nsm = 1;
     if (!attr) {
         CK(cudaFuncSetAttribute(k_syrk_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
-        CK(cudaFuncSetAttribute(k_syrk_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM));
+        CK(cudaFuncSetAttribute(k_syrk_pipe<64, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM));
+        CK(cudaFuncSetAttribute(k_syrk_pipe<128, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM_WIDE));
         int dev = 0;
         CK(cudaGetDevice(&dev));
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -468,9 +469,14 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         if (no_pipe)
             k_syrk_umma<<<dim3(ncb == 1 ? nr : nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb == 1,
                                                                                                  S, sstride, status);
-        else
-            k_syrk_pipe<<<std::min(ntask * tpt, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb, S, sstride,
-                                                                                     status);
+        else if (ncb > 0) // the rest of an outer panel: 128 x 64 tiles, 64-column chunks
+            k_syrk_pipe<64, 64><<<std::min(ntask * tpt, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb, S,
+                                                                                             sstride, status);
+        else { // the whole trailing matrix: 128 x 128 tiles (a third less staging per entry), 32-column chunks
+            const int tw = ntask * pipe_tiles<128>(nr, 0);
+            k_syrk_pipe<128, 32><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_WIDE, st>>>(ntask, n, k0, kw, t0, cmax, 0, S, sstride,
+                                                                                          status);
+        }
         COUNT_LAUNCH(1);
         if (g_kt.on) {
             CK(cudaEventRecord(g_kt.next(), st));

@@ -28,8 +28,14 @@ namespace capsgpu {
 
 constexpr int PIPE_PRODUCER_WARPS = 16, PIPE_EPI_WARPS = 8;
 constexpr int PIPE_THREADS = (PIPE_PRODUCER_WARPS + 1 + PIPE_EPI_WARPS) * 32; // 800
-constexpr int PIPE_STAGE_FLOATS = 2 * (UM_M + UM_N) * UM_K;                  // hi + lo of both slices
-constexpr int PIPE_SMEM = 2 * PIPE_STAGE_FLOATS * 4;                         // two stages: 192 KB
+// tile width TN (columns of S per tile) and chunk depth TK (panel columns per stage): a
+// stage holds hi + lo of the 128-row and the TN-row slice; two stages
+template <int TN, int TK> struct PipeShape {
+    static constexpr int STAGE = 2 * (UM_M + TN) * TK; // floats
+    static constexpr int SMEM = 2 * STAGE * 4;         // bytes
+};
+constexpr int PIPE_SMEM = PipeShape<64, 64>::SMEM;   // 192 KB
+constexpr int PIPE_SMEM_WIDE = PipeShape<128, 32>::SMEM; // 128 KB
 constexpr int PIPE_WAIT_ITERS = 1 << 22;
 constexpr int PIPE_PRODUCERS = PIPE_PRODUCER_WARPS * 32;
 
@@ -38,32 +44,34 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *mbar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma::smem_u32(mbar)) : "memory");
 }
 
-// Stage layout: Ahi (128 x 64), Alo, Bhi (64 x 64), Blo, each slice in the layout of um_off.
-constexpr int PIPE_A = UM_M * UM_K, PIPE_B = UM_N * UM_K;
+// Stage layout: Ahi (128 x TK), Alo, Bhi (TN x TK), Blo, each slice K-major in 8-row x
+// 4-column core matrices (core matrix (r / 8) (TK / 4) + k / 4, 32 floats each).
 
-// rows [row0, row0 + R) of the panel (columns kc .. kc + nb) into hi/lo slices, by the
-// PIPE_PRODUCERS producer threads (ptid), 8 loads in flight per thread (measured: 12 loads
-// over both slices at once ran slower under the 80-register budget of 800 threads, and
-// 4-byte cp.async copies with an in-place split pass slower still).
+// rows [row0, row0 + R) of the panel (columns kc .. kc + nb, nb <= TK) into hi/lo slices,
+// by the PIPE_PRODUCERS producer threads (ptid), 8 loads in flight per thread (measured:
+// 12 loads over both slices at once ran slower under the 80-register budget of 800
+// threads, and 4-byte cp.async copies with an in-place split pass slower still).
 // Element e = base + u PIPE_PRODUCERS + ptid of a round sits in core matrix e / 32 =
 // (base + ptid) / 32 + 16 u: a thread keeps its column k through the round and its row
-// steps by 8, so the loads and stores are one base address with immediate offsets.
-template <int R>
+// steps by 8 x 16 / (TK / 4), so the loads and stores are one base address with immediate
+// offsets.
+template <int R, int TK>
 __device__ __forceinline__ void pipe_stage(const float *Sm, int n, int kc, int nb, int row0, float *hi_s, float *lo_s, int ptid)
 {
-    constexpr int ILP = 8, CPR = UM_K / 4; // core matrices per 8-row group
-    static_assert((R * UM_K) % (PIPE_PRODUCERS * ILP) == 0, "whole staging rounds");
-    static_assert(PIPE_PRODUCERS / 32 == CPR, "a round advances one 8-row group per load");
+    constexpr int ILP = 8, CPR = TK / 4; // core matrices per 8-row group
+    constexpr int STEP = 8 * (PIPE_PRODUCERS / 32) / CPR;
+    static_assert((R * TK) % (PIPE_PRODUCERS * ILP) == 0, "whole staging rounds");
+    static_assert((PIPE_PRODUCERS / 32) % CPR == 0, "a thread keeps its column through a round");
     const int lane = ptid & 31;
 #pragma unroll 1
-    for (int base = 0; base < R * UM_K; base += PIPE_PRODUCERS * ILP) {
+    for (int base = 0; base < R * TK; base += PIPE_PRODUCERS * ILP) {
         const int cm0 = (base + ptid) >> 5;
         const int k = (cm0 % CPR) * 4 + (lane & 3), r0 = row0 + (cm0 / CPR) * 8 + (lane >> 2);
         const float *src = Sm + (size_t)(kc + k) * n + r0;
         const bool kok = k < nb;
         float x[ILP];
 #pragma unroll
-        for (int u = 0; u < ILP; u++) x[u] = (kok && r0 + 8 * u < n) ? __ldg(src + 8 * u) : 0.0f;
+        for (int u = 0; u < ILP; u++) x[u] = (kok && r0 + STEP * u < n) ? __ldg(src + STEP * u) : 0.0f;
         float *hd = hi_s + base + ptid, *ld = lo_s + base + ptid;
 #pragma unroll
         for (int u = 0; u < ILP; u++) {
@@ -80,10 +88,19 @@ struct PipeTile {
     bool valid;
 };
 
-// tile t of the launch: tpt tiles per matrix; ncb > 0: tile p -> (p / ncb, p mod ncb), the
-// first ncb column blocks; ncb = 0: p -> (ri, cj <= 2 ri + 1), the whole lower triangle
+// tiles per matrix: ncb > 0 the first ncb column blocks of every row block, else the whole
+// lower triangle (128 / TN column blocks per row block)
+template <int TN> __host__ __device__ inline int pipe_tiles(int nr, int ncb)
+{
+    return ncb > 0 ? nr * ncb : (TN == UM_M ? nr * (nr + 1) / 2 : nr * (nr + 1));
+}
+
+// tile t of the launch: tpt tiles per matrix; ncb > 0: tile p -> (p / ncb, p mod ncb); ncb =
+// 0: p -> (ri, cj) over the lower triangle (cj <= 2 ri + 1 for TN = 64, cj <= ri for TN = 128)
+template <int TN>
 __device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, int ncb, int n, int t0, int cend, const int *status)
 {
+    static_assert(TN == UM_M || 2 * TN == UM_M, "tile width 64 or 128");
     PipeTile T;
     T.task = t / tpt;
     const int p = t - T.task * tpt;
@@ -91,6 +108,11 @@ __device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, int ncb, int n, in
     if (ncb > 0) {
         ri = p / ncb;
         cj = p - ri * ncb;
+    } else if (TN == UM_M) {
+        ri = (int)((sqrtf(8.0f * p + 1.0f) - 1.0f) * 0.5f);
+        while ((ri + 1) * (ri + 2) / 2 <= p) ri++;
+        while (ri * (ri + 1) / 2 > p) ri--;
+        cj = p - ri * (ri + 1) / 2;
     } else {
         ri = (int)((sqrtf(4.0f * p + 1.0f) - 1.0f) * 0.5f);
         while ((ri + 1) * (ri + 2) <= p) ri++;
@@ -98,7 +120,7 @@ __device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, int ncb, int n, in
         cj = p - ri * (ri + 1);
     }
     T.row0 = t0 + ri * UM_M;
-    T.col0 = t0 + cj * UM_N;
+    T.col0 = t0 + cj * TN;
     // skip matrices that are not being factored or failed before this launch; a wait
     // error set during this launch (ST_ERR_WAIT) does not change the walk
     const int st = status[T.task] & ~ST_ERR_WAIT;
@@ -106,21 +128,25 @@ __device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, int ncb, int n, in
     return T;
 }
 
-// S[t0.., t0..cmax) -= P P^T, P = columns k0 .. k0 + kw - 1; grid = min(tiles, SMs), 800 threads
+// S[t0.., t0..cmax) -= P P^T, P = columns k0 .. k0 + kw - 1, in 128 x TN tiles and TK-column
+// chunks; grid = min(tiles, SMs), 800 threads
+template <int TN, int TK>
 __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n, int k0, int kw, int t0, int cmax, int ncb,
                                                                float *S, size_t sstride, int *status)
 {
+    using Shape = PipeShape<TN, TK>;
+    constexpr int PA = UM_M * TK, PB = TN * TK;
     extern __shared__ __align__(1024) float pipe_sm[];
     __shared__ uint64_t full[2], empty[2], tfull[2], tempty[2];
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int cend = min(n, cmax);
     const int nr = (n - t0 + UM_M - 1) / UM_M;
-    const int tpt = ncb > 0 ? nr * ncb : nr * (nr + 1);
+    const int tpt = pipe_tiles<TN>(nr, ncb);
     const int ntile = ntask * tpt;
-    const int nchunk = (kw + UM_K - 1) / UM_K;
+    const int nchunk = (kw + TK - 1) / TK;
 
-    if (warp == 0) umma::alloc(&tslot, 2 * UM_N);
+    if (warp == 0) umma::alloc(&tslot, 2 * TN);
     if (tid == 0) {
         for (int i = 0; i < 2; i++) {
             umma::mbar_init(&full[i], PIPE_PRODUCERS);
@@ -139,18 +165,18 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
         const int ptid = tid;
         int it = 0; // chunk counter (stage ring)
         for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
-            const PipeTile T = pipe_tile(t, tpt, ncb, n, t0, cend, status);
+            const PipeTile T = pipe_tile<TN>(t, tpt, ncb, n, t0, cend, status);
             if (!T.valid) continue;
             const float *Sm = S + (size_t)T.task * sstride;
             bool ok = true;
             for (int ch = 0; ch < nchunk; ch++, it++) {
                 const int s = it & 1, use = it >> 1;
                 if (use > 0 && !umma::mbar_wait(&empty[s], (use - 1) & 1, PIPE_WAIT_ITERS)) { ok = false; break; }
-                float *st = pipe_sm + s * PIPE_STAGE_FLOATS;
-                float *Ahi = st, *Alo = Ahi + PIPE_A, *Bhi = Alo + PIPE_A, *Blo = Bhi + PIPE_B;
-                const int kc = k0 + ch * UM_K, nb = min(UM_K, k0 + kw - kc);
-                pipe_stage<UM_M>(Sm, n, kc, nb, T.row0, Ahi, Alo, ptid);
-                pipe_stage<UM_N>(Sm, n, kc, nb, T.col0, Bhi, Blo, ptid);
+                float *st = pipe_sm + s * Shape::STAGE;
+                float *Ahi = st, *Alo = Ahi + PA, *Bhi = Alo + PA, *Blo = Bhi + PB;
+                const int kc = k0 + ch * TK, nb = min(TK, k0 + kw - kc);
+                pipe_stage<UM_M, TK>(Sm, n, kc, nb, T.row0, Ahi, Alo, ptid);
+                pipe_stage<TN, TK>(Sm, n, kc, nb, T.col0, Bhi, Blo, ptid);
                 umma::fence_smem_async();
                 mbar_arrive(&full[s]);
             }
@@ -160,22 +186,22 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
         // ---- MMA issue (one thread) ----
         if (lane == 0) {
             int it = 0, tt = 0;
-            constexpr uint32_t idesc = umma::idesc_tf32(UM_M, UM_N);
-            constexpr uint32_t LBO = 128, SBO = (UM_K / 4) * 128;
+            constexpr uint32_t idesc = umma::idesc_tf32(UM_M, TN);
+            constexpr uint32_t LBO = 128, SBO = (TK / 4) * 128;
             for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
-                const PipeTile T = pipe_tile(t, tpt, ncb, n, t0, cend, status);
+                const PipeTile T = pipe_tile<TN>(t, tpt, ncb, n, t0, cend, status);
                 if (!T.valid) continue;
                 const int b = tt & 1, ub = tt >> 1;
                 bool ok = ub == 0 || umma::mbar_wait(&tempty[b], (ub - 1) & 1, PIPE_WAIT_ITERS);
                 umma::fence_after();
-                const uint32_t acc = tmem + b * UM_N;
+                const uint32_t acc = tmem + b * TN;
                 for (int ch = 0; ok && ch < nchunk; ch++, it++) {
                     const int s = it & 1, use = it >> 1;
                     if (!umma::mbar_wait(&full[s], use & 1, PIPE_WAIT_ITERS)) { ok = false; break; }
                     umma::fence_after();
-                    const float *st = pipe_sm + s * PIPE_STAGE_FLOATS;
-                    const uint32_t ah = umma::smem_u32(st), al = ah + PIPE_A * 4, bh = al + PIPE_A * 4, bl = bh + PIPE_B * 4;
-                    for (int ks = 0; ks < UM_K / 8; ks++) {
+                    const float *st = pipe_sm + s * Shape::STAGE;
+                    const uint32_t ah = umma::smem_u32(st), al = ah + PA * 4, bh = al + PA * 4, bl = bh + PB * 4;
+                    for (int ks = 0; ks < TK / 8; ks++) {
                         const uint32_t o = ks * 256;
                         umma::mma_tf32(acc, umma::desc_kmajor(al + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc,
                                        ch > 0 || ks > 0);
@@ -191,17 +217,18 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
         }
     } else {
         // ---- epilogue: warp w reads lane quadrant w mod 4 and column half (w - 17) / 4 ----
+        constexpr int HW = TN / 2; // columns per warp
         const int quad = warp & 3, half = (warp - PIPE_PRODUCER_WARPS - 1) >> 2;
         int tt = 0;
         for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
-            const PipeTile T = pipe_tile(t, tpt, ncb, n, t0, cend, status);
+            const PipeTile T = pipe_tile<TN>(t, tpt, ncb, n, t0, cend, status);
             if (!T.valid) continue;
             float *Sm = S + (size_t)T.task * sstride;
             const int b = tt & 1, ub = tt >> 1;
             const int R = T.row0 + quad * 32 + lane;
             bool ok = true;
-            for (int part = 0; part < 2; part++) {
-                const int cb = T.col0 + half * 32 + part * 16;
+            for (int part = 0; part < HW / 16; part++) {
+                const int cb = T.col0 + half * HW + part * 16;
                 float c[16];
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
@@ -214,7 +241,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
                     if (!ok) break;
                 }
                 float v[16];
-                umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * UM_N + half * 32 + part * 16, v);
+                umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * TN + half * HW + part * 16, v);
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
                     const int C = cb + j;
@@ -231,7 +258,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
     __syncthreads();
     if (warp == 0) {
         umma::fence_after();
-        umma::dealloc(tmem, 2 * UM_N);
+        umma::dealloc(tmem, 2 * TN);
     }
 }
 
