@@ -61,3 +61,31 @@ def test_learned_free_energy_equals_plain_with_fewer_matrices(cg, trained):
         assert E1 == E0, (E1, E0)            # same terms, same values: the reference rules decide
         assert i1["ndet"] <= i0["ndet"], (i1, i0)
         assert i1["nwasted"] < i0["nwasted"] or i0["nwasted"] == 0, (i1, i0)
+
+
+def test_learned_sweep_random_geometries(cg, trained):
+    """the learned-truncation sweep over random geometries (fixed seed; log-uniform R/L,
+    T in (0, 350] K, Drude omega_p in [7, 10] eV, gamma in [0.02, 0.05] eV, ldim = 7 R/L;
+    R/L <= 30 here to keep the plain runs short): in both precisions the learned E equals
+    the plain E exactly -- the reference's rules decide which terms enter -- and the matrices
+    beyond the cutoffs stay a small share of those needed"""
+    import math
+    net = trained[0]
+    rng = np.random.default_rng(1)
+    done = 0
+    while done < 4:
+        RbyL = math.exp(rng.uniform(math.log(10), math.log(500)))
+        T, wp, ga = rng.uniform(0, 350), rng.uniform(7, 10), rng.uniform(0.02, 0.05)
+        if RbyL > 30 or T < 1:
+            continue
+        L = 1e-6
+        for prec in (cg.PREC_FP64, cg.PREC_MIXED):
+            c = cg.Caps(RbyL * L, L, ldim=int(math.ceil(7 * RbyL)))
+            c.set_drude(wp, ga)
+            c.set_precision(prec)
+            E0, i0 = c.free_energy(T)
+            E1, i1 = c.free_energy(T, mlp=net)
+            assert E1 == E0, (RbyL, T, prec, E1, E0)
+            needed = i0["ndet"] - i0["nwasted"]
+            assert i1["nwasted"] <= max(8, 0.5 * needed), (RbyL, T, prec, i1, i0)
+        done += 1
