@@ -28,7 +28,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "logdetD/s and time-to-E at R/L=150: mixed+learned vs FP64 GPU, |ΔE/E|≤1e-6"
 UNIT = "logdetD/s"
-# workload (BASELINE config: Drude gold, R/L=150, L=1um, T=300K, ldim=1050)
+# workload: Drude gold, R/L=150, L=1um, T=300K, ldim=1050
 R, L, T, LDIM = 150e-6, 1e-6, 300.0, 1050
 OMEGAP_EV, GAMMA_EV = 9.0, 0.035
 CUTOFF, EPSREL = 1e-9, 1e-6

@@ -5,7 +5,7 @@ one nvcc process per translation unit (run in parallel) and a final link.
 The oracle (test infrastructure) goes to oracle/_build/liboracle.so.  When the
 CaPS source tree is available (CAPS_REFERENCE_SRC or ../reference next to the
 checkout), its unmodified library is also built into oracle/_ref/ as a second
-checker.
+parity reference.
 """
 import os
 import subprocess

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
 
 Test infrastructure only: imported by tests/, by __graft_entry__.smoke() and by
-bench.py's CPU-baseline leg, always as the checker or the timed baseline.
+bench.py's CPU-baseline leg, always as the parity reference or the timed baseline.
 """
 import ctypes as C
 import os

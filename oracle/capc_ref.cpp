@@ -1,4 +1,4 @@
-// capc_ref.cpp -- checker only.  Compiles the reference's cylinder-plane program
+// capc_ref.cpp -- test infrastructure only.  Compiles the reference's cylinder-plane program
 // (src/capc.cpp) unmodified from the reference tree, with its main() renamed, and
 // exports its CasimirCP methods with C linkage so that tests/golden/make_golden_capc.py
 // can record golden values.  Built by Makefile.ref into oracle/_ref/libcapc_ref.so;

@@ -1,6 +1,6 @@
 /*
  * caps_oracle.h -- CPU restatement of the CaPS v0.5 logdetD path.
- * TEST INFRASTRUCTURE ONLY: the parity checker and the CPU baseline.
+ * TEST INFRASTRUCTURE ONLY: the parity reference and the CPU baseline.
  */
 #ifndef CAPS_ORACLE_H
 #define CAPS_ORACLE_H

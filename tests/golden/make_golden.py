@@ -11,7 +11,7 @@ Two sources:
  2. values computed by the unmodified reference library (libcaps_ref.so):
     logdetD per (xi,m) for the benchmark geometries (LU and HODLR), Mie
     coefficients, K and I integrals, and dense round-trip matrices.
-The GPU machine has no reference tree: the tests read only the JSON written here.
+The machines that run the tests need no reference tree: the tests read only the JSON written here.
 """
 import argparse
 import ctypes as C

@@ -1,4 +1,4 @@
-"""Randomised geometries (the survey's fifth configuration): 64 draws from a fixed seed --
+"""Randomised geometries: 64 draws from a fixed seed --
 log-uniform R/L in [10, 500], T uniform in [0, 350] K, omega_p uniform in [7, 10] eV,
 gamma uniform in [0.02, 0.05] eV, ldim = ceil(7 R/L) -- of which those with R/L <= 40 are
 compared with the oracle at several (xi, m): FP64 to 1e-10, the mixed form to 5e-8."""

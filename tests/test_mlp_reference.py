@@ -1,5 +1,5 @@
 """The NumPy reference of the network, checked by central finite differences
-(it is the CPU checker of the GPU gradients in test_gpu_mlp.py)."""
+(it is the CPU reference for the GPU gradients in test_gpu_mlp.py)."""
 import numpy as np
 
 import mlp_reference as ref
