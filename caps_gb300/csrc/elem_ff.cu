@@ -92,20 +92,76 @@ __global__ void k_scale_ff(int ntask, int L, const sd *Sa, const sd *Sb, const d
     uvf[o] = make_float4(u.h, u.l, v.h, v.l);
 }
 
-// grid (ceil(ldim/EB), ldim, ntask); thread (a, b) with a >= b owns rows 2a, 2a+1 and
+// EE and MM (with OFFD also EM and ME) of the 2x2 block of M at rows lmin + i1 - 1 and
+// columns lmin + i2 - 1 (i1, i2 index [lmin-1, lmin+ldim]); each is one linear combination
+// of I values times the scale factors.  One routine for the full assembly and for the
+// diagonal that the trace shortcut reads, so that both give the same numbers.
+template <bool OFFD>
+CAPS_DEV void elem_block(const Task &T, int L, const ffe *ITM, const ffe *ITE, int i1, int i2, size_t so, const ffe *__restrict__ Saf,
+                         const ffe *__restrict__ Sbf, const float4 *__restrict__ uvf, fe &EE, fe &MM, fe &EM, fe &ME)
+{
+    const fe sa1 = fe_ld(Saf[so + i1]), sa2 = fe_ld(Saf[so + i2]);
+    const fe sb1 = fe_ld(Sbf[so + i1]), sb2 = fe_ld(Sbf[so + i2]);
+    // the table is symmetric; I(x, y) is read at t[y L + x] so that consecutive
+    // threads (consecutive x) read consecutive entries
+    auto Iv = [&](const ffe *t, int x, int y) { return fe_ld(t[(size_t)y * L + x]); };
+    EM = fe{0.0f, 0.0f, 0};
+    ME = fe{0.0f, 0.0f, 0};
+    if (T.m == 0) {
+        EE = fe_mul(fe_mul(sa1, sa2), Iv(ITM, i1, i2));          // B_TM, A = 0
+        MM = fe_neg(fe_mul(fe_mul(sb1, sb2), Iv(ITE, i1, i2)));  // -B_TE
+        return;
+    }
+    const float mf = (float)T.m, m2h = mf * mf;
+    const ff m1{mf, 0.0f}, m2{m2h, fmaf(mf, mf, -m2h)};
+    const float4 w1 = uvf[so + i1], w2 = uvf[so + i2];
+    const ff U1{w1.x, w1.y}, V1{w1.z, w1.w}, U2{w2.x, w2.y}, V2{w2.z, w2.w};
+    const ff cUU = ff_mul(U1, U2), cVU = ff_mul(V1, U2), cUV = ff_mul(U1, V2), cVV = ff_mul(V1, V2);
+    // B_p = u1 u2 I(l1-1,l2-1) - v1 u2 I(l1+1,l2-1) - u1 v2 I(l1-1,l2+1) + v1 v2 I(l1+1,l2+1)
+    // C_p(l1,l2) = m (v2 I(l1,l2+1) - u2 I(l1,l2-1)); D_p(l1,l2) = C_p(l2,l1)
+    // EE = B_TM - m^2 I_TE,  MM = m^2 I_TM - B_TE,  EM = D_TM - C_TE,  ME = C_TM - D_TE
+    // (times the scale factors), each one linear combination of the I values
+    {
+        const ff c[5] = {cUU, ff_neg(cVU), ff_neg(cUV), cVV, ff_neg(m2)};
+        const fe x[5] = {Iv(ITM, i1 - 1, i2 - 1), Iv(ITM, i1 + 1, i2 - 1), Iv(ITM, i1 - 1, i2 + 1), Iv(ITM, i1 + 1, i2 + 1),
+                         Iv(ITE, i1, i2)};
+        EE = fe_mul(fe_mul(sa1, sa2), fe_lincomb(c, x));
+    }
+    {
+        const ff c[5] = {m2, ff_neg(cUU), cVU, cUV, ff_neg(cVV)};
+        const fe x[5] = {Iv(ITM, i1, i2), Iv(ITE, i1 - 1, i2 - 1), Iv(ITE, i1 + 1, i2 - 1), Iv(ITE, i1 - 1, i2 + 1),
+                         Iv(ITE, i1 + 1, i2 + 1)};
+        MM = fe_mul(fe_mul(sb1, sb2), fe_lincomb(c, x));
+    }
+    if (!OFFD) return;
+    const ff mU1 = ff_mul(m1, U1), mV1 = ff_mul(m1, V1), mU2 = ff_mul(m1, U2), mV2 = ff_mul(m1, V2);
+    {
+        const ff c[4] = {mV1, ff_neg(mU1), ff_neg(mV2), mU2};
+        const fe x[4] = {Iv(ITM, i1 + 1, i2), Iv(ITM, i1 - 1, i2), Iv(ITE, i1, i2 + 1), Iv(ITE, i1, i2 - 1)};
+        EM = fe_mul(fe_mul(sa1, sb2), fe_lincomb(c, x));
+    }
+    {
+        const ff c[4] = {mV2, ff_neg(mU2), ff_neg(mV1), mU1};
+        const fe x[4] = {Iv(ITM, i1, i2 + 1), Iv(ITM, i1, i2 - 1), Iv(ITE, i1 + 1, i2), Iv(ITE, i1 - 1, i2)};
+        ME = fe_mul(fe_mul(sb1, sa2), fe_lincomb(c, x));
+    }
+}
+
+// grid (ceil(ldim/EB), ldim, nlist); block z handles task tlist[z] (tlist == nullptr: task
+// z); thread (a, b) with a >= b owns rows 2a, 2a+1 and
 // columns 2b, 2b+1 of M.  S receives -M (the delta form of A = 1 - M), lower triangle,
 // column-major with leading dimension n; diag receives M_ii in FP64; part
 // receives, per warp, the sum of squares of M over the warp's blocks (strict lower
 // entries twice).  Blocks entirely above the diagonal exit before doing anything.
-__global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, int ntask, int ldim, const ffe *__restrict__ I,
+__global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, const int *tlist, int nlist, int ldim, const ffe *__restrict__ I,
                                                 const ffe *__restrict__ Saf, const ffe *__restrict__ Sbf,
                                                 const float4 *__restrict__ uvf, float *S, size_t sstride, double *diag,
                                                 float *part, int *status)
 {
     const int L = ldim + 2, n = 2 * ldim;
     const int b = blockIdx.y;
-    const int task = blockIdx.z;
-    if (task >= ntask || (int)blockIdx.x < b / EB) return; // uniform per block
+    if ((int)blockIdx.z >= nlist || (int)blockIdx.x < b / EB) return; // uniform per block
+    const int task = tlist ? tlist[blockIdx.z] : (int)blockIdx.z;
     const int a = blockIdx.x * EB + threadIdx.x;
     const bool valid = a < ldim && b <= a;
     float wsum = 0.0f;
@@ -113,51 +169,8 @@ __global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, int ntask, in
         const Task &T = tasks[task];
         const ffe *ITM = I + (size_t)(task * 2 + 1) * L * L;
         const ffe *ITE = I + (size_t)(task * 2 + 0) * L * L;
-        const int i1 = a + 1, i2 = b + 1; // index into [lmin-1, lmin+ldim]
-        const size_t so = (size_t)task * L;
-        const fe sa1 = fe_ld(Saf[so + i1]), sa2 = fe_ld(Saf[so + i2]);
-        const fe sb1 = fe_ld(Sbf[so + i1]), sb2 = fe_ld(Sbf[so + i2]);
-        // the table is symmetric; I(x, y) is read at t[y L + x] so that consecutive
-        // threads (consecutive x) read consecutive entries
-        auto Iv = [&](const ffe *t, int x, int y) { return fe_ld(t[(size_t)y * L + x]); };
-        fe EE, MM, EM{0.0f, 0.0f, 0}, ME{0.0f, 0.0f, 0};
-        if (T.m == 0) {
-            EE = fe_mul(fe_mul(sa1, sa2), Iv(ITM, i1, i2));          // B_TM, A = 0
-            MM = fe_neg(fe_mul(fe_mul(sb1, sb2), Iv(ITE, i1, i2)));  // -B_TE
-        } else {
-            const float mf = (float)T.m, m2h = mf * mf;
-            const ff m1{mf, 0.0f}, m2{m2h, fmaf(mf, mf, -m2h)};
-            const float4 w1 = uvf[so + i1], w2 = uvf[so + i2];
-            const ff U1{w1.x, w1.y}, V1{w1.z, w1.w}, U2{w2.x, w2.y}, V2{w2.z, w2.w};
-            const ff cUU = ff_mul(U1, U2), cVU = ff_mul(V1, U2), cUV = ff_mul(U1, V2), cVV = ff_mul(V1, V2);
-            const ff mU1 = ff_mul(m1, U1), mV1 = ff_mul(m1, V1), mU2 = ff_mul(m1, U2), mV2 = ff_mul(m1, V2);
-            // B_p = u1 u2 I(l1-1,l2-1) - v1 u2 I(l1+1,l2-1) - u1 v2 I(l1-1,l2+1) + v1 v2 I(l1+1,l2+1)
-            // C_p(l1,l2) = m (v2 I(l1,l2+1) - u2 I(l1,l2-1)); D_p(l1,l2) = C_p(l2,l1)
-            // EE = B_TM - m^2 I_TE,  MM = m^2 I_TM - B_TE,  EM = D_TM - C_TE,  ME = C_TM - D_TE
-            // (times the scale factors), each one linear combination of the I values
-            {
-                const ff c[5] = {cUU, ff_neg(cVU), ff_neg(cUV), cVV, ff_neg(m2)};
-                const fe x[5] = {Iv(ITM, i1 - 1, i2 - 1), Iv(ITM, i1 + 1, i2 - 1), Iv(ITM, i1 - 1, i2 + 1), Iv(ITM, i1 + 1, i2 + 1),
-                                 Iv(ITE, i1, i2)};
-                EE = fe_mul(fe_mul(sa1, sa2), fe_lincomb(c, x));
-            }
-            {
-                const ff c[5] = {m2, ff_neg(cUU), cVU, cUV, ff_neg(cVV)};
-                const fe x[5] = {Iv(ITM, i1, i2), Iv(ITE, i1 - 1, i2 - 1), Iv(ITE, i1 + 1, i2 - 1), Iv(ITE, i1 - 1, i2 + 1),
-                                 Iv(ITE, i1 + 1, i2 + 1)};
-                MM = fe_mul(fe_mul(sb1, sb2), fe_lincomb(c, x));
-            }
-            {
-                const ff c[4] = {mV1, ff_neg(mU1), ff_neg(mV2), mU2};
-                const fe x[4] = {Iv(ITM, i1 + 1, i2), Iv(ITM, i1 - 1, i2), Iv(ITE, i1, i2 + 1), Iv(ITE, i1, i2 - 1)};
-                EM = fe_mul(fe_mul(sa1, sb2), fe_lincomb(c, x));
-            }
-            {
-                const ff c[4] = {mV2, ff_neg(mU2), ff_neg(mV1), mU1};
-                const fe x[4] = {Iv(ITM, i1, i2 + 1), Iv(ITM, i1, i2 - 1), Iv(ITE, i1 + 1, i2), Iv(ITE, i1 - 1, i2)};
-                ME = fe_mul(fe_mul(sb1, sa2), fe_lincomb(c, x));
-            }
-        }
+        fe EE, MM, EM, ME;
+        elem_block<true>(T, L, ITM, ITE, a + 1, b + 1, (size_t)task * L, Saf, Sbf, uvf, EE, MM, EM, ME);
         bool bad = false;
         const float ee = fe_to_float(EE, bad), mm = fe_to_float(MM, bad);
         const float em = fe_to_float(EM, bad), me = fe_to_float(ME, bad);
@@ -181,28 +194,56 @@ __global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, int ntask, in
         part[(((size_t)task * ldim + b) * gridDim.x + blockIdx.x) * (EB / 32) + threadIdx.x / 32] = wsum;
 }
 
-// per task: Kahan trace of M over its FP64 diagonal (index order, misc.c:26), the
-// Frobenius norm from the element partials (fixed order), and the reference's
-// shortcut decision: |tr| < 1e-8 -> -tr; dense modes: Mercator when its error bound is
-// below 1e-8 relative; otherwise factorise.
-__global__ void k_stats_ff(int ntask, int ldim, const double *diag, const float *part, int nbx, int mode, double *trace_out,
-                           double *result, int *status)
+// the diagonal of M alone (kernel_logdet computes it first, matrix.c:62-66): grid
+// (ceil(ldim/EB), ntask), thread a writes M_ii of the diagonal block (a, a) in FP64, from
+// the band of I values that k_itab_grp's band mode leaves
+__global__ void __launch_bounds__(EB) k_diag_ff(const Task *tasks, int ntask, int ldim, const ffe *__restrict__ I,
+                                                const ffe *__restrict__ Saf, const ffe *__restrict__ Sbf,
+                                                const float4 *__restrict__ uvf, double *diag, int *status)
 {
-    const int task = blockIdx.x;
-    if (task >= ntask) return;
+    const int L = ldim + 2, n = 2 * ldim;
+    const int task = blockIdx.y;
+    const int a = blockIdx.x * EB + threadIdx.x;
+    if (task >= ntask || a >= ldim) return;
+    const Task &T = tasks[task];
+    const ffe *ITM = I + (size_t)(task * 2 + 1) * L * L;
+    const ffe *ITE = I + (size_t)(task * 2 + 0) * L * L;
+    fe EE, MM, EM, ME;
+    elem_block<false>(T, L, ITM, ITE, a + 1, a + 1, (size_t)task * L, Saf, Sbf, uvf, EE, MM, EM, ME);
+    bool bad = false;
+    fe_to_float(EE, bad);
+    fe_to_float(MM, bad);
+    if (bad) atomicOr(status + task, ST_ERR_NONFINITE);
+    diag[(size_t)task * n + 2 * a] = fe_to_double(EE);
+    diag[(size_t)task * n + 2 * a + 1] = fe_to_double(MM);
+}
+
+// per task (tlist[blockIdx.x], or blockIdx.x without a list): Kahan trace of M over its
+// FP64 diagonal (index order, misc.c:26), the Frobenius norm from the element partials
+// (fixed order), and the reference's shortcut decision: |tr| < 1e-8 -> -tr; dense modes:
+// Mercator when its error bound is below 1e-8 relative; otherwise factorise.  Without
+// partials (part == nullptr) only the trace rule is applied: a matrix it does not decide
+// keeps status 0, to be assembled in full.
+__global__ void k_stats_ff(const int *tlist, int nlist, int ldim, const double *diag, const float *part, int nbx, int mode,
+                           double *trace_out, double *result, int *status)
+{
+    if ((int)blockIdx.x >= nlist) return;
+    const int task = tlist ? tlist[blockIdx.x] : (int)blockIdx.x;
     const int n = 2 * ldim, per_b = nbx * (EB / 32);
-    const float *p = part + (size_t)task * ldim * per_b;
     __shared__ double red[256];
-    double s = 0.0;
-    for (int i = threadIdx.x; i < ldim * per_b; i += blockDim.x) {
-        const int b = i / per_b, x = (i % per_b) / (EB / 32);
-        if (x >= b / EB) s += p[i];
-    }
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    if (part) {
+        const float *p = part + (size_t)task * ldim * per_b;
+        double s = 0.0;
+        for (int i = threadIdx.x; i < ldim * per_b; i += blockDim.x) {
+            const int b = i / per_b, x = (i % per_b) / (EB / 32);
+            if (x >= b / EB) s += p[i];
+        }
+        red[threadIdx.x] = s;
         __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
     }
     if (threadIdx.x != 0) return;
     const double *dg = diag + (size_t)task * n;
@@ -216,6 +257,7 @@ __global__ void k_stats_ff(int ntask, int ldim, const double *diag, const float 
     trace_out[task] = tr;
     if (status[task] & ~0xF) { result[task] = NAN; return; }
     if (fabs(tr) < 1e-8) { result[task] = -tr; status[task] = ST_TRACE; return; }
+    if (!part) return;
     const double fro2 = red[0], fro = sqrt(fro2);
     if (mode == 0 && fro < 1) {
         const double merc = -tr - fro2 / 2;
@@ -227,25 +269,41 @@ __global__ void k_stats_ff(int ntask, int ldim, const double *diag, const float 
 
 size_t elem_ff_part_floats(int ldim) { return (size_t)ldim * ((ldim + EB - 1) / EB) * (EB / 32); }
 
-void launch_elem_ff(const Task *tasks, int ntask, int ldim, const sd *Sa, const sd *Sb, const double2 *uv, void *Saf, void *Sbf,
-                    float4 *uvf, const void *I, float *S, size_t sstride, double *diag, float *part, int *status,
-                    cudaStream_t st)
+void launch_scale_ff(int ntask, int ldim, const sd *Sa, const sd *Sb, const double2 *uv, void *Saf, void *Sbf, float4 *uvf,
+                     cudaStream_t st)
 {
     const int L = ldim + 2;
     dim3 gs((L + 127) / 128, ntask);
     k_scale_ff<<<gs, 128, 0, st>>>(ntask, L, Sa, Sb, uv, (ffe *)Saf, (ffe *)Sbf, uvf);
     COUNT_LAUNCH(1);
-    dim3 g((ldim + EB - 1) / EB, ldim, ntask);
-    k_elem_ff<<<g, EB, 0, st>>>(tasks, ntask, ldim, (const ffe *)I, (const ffe *)Saf, (const ffe *)Sbf, uvf, S, sstride, diag,
-                                part, status);
+    CK(cudaGetLastError());
+}
+
+void launch_diag_ff(const Task *tasks, int ntask, int ldim, const void *I, const void *Saf, const void *Sbf, const float4 *uvf,
+                    double *diag, int *status, cudaStream_t st)
+{
+    dim3 g((ldim + EB - 1) / EB, ntask);
+    k_diag_ff<<<g, EB, 0, st>>>(tasks, ntask, ldim, (const ffe *)I, (const ffe *)Saf, (const ffe *)Sbf, uvf, diag, status);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
-void launch_stats_ff(int ntask, int ldim, const double *diag, const float *part, int mode, double *trace, double *result,
-                     int *status, cudaStream_t st)
+void launch_elem_ff(const Task *tasks, const int *tlist, int nlist, int ldim, const void *Saf, const void *Sbf, const float4 *uvf,
+                    const void *I, float *S, size_t sstride, double *diag, float *part, int *status, cudaStream_t st)
 {
-    k_stats_ff<<<ntask, 256, 0, st>>>(ntask, ldim, diag, part, (ldim + EB - 1) / EB, mode, trace, result, status);
+    if (nlist <= 0) return;
+    dim3 g((ldim + EB - 1) / EB, ldim, nlist);
+    k_elem_ff<<<g, EB, 0, st>>>(tasks, tlist, nlist, ldim, (const ffe *)I, (const ffe *)Saf, (const ffe *)Sbf, uvf, S, sstride,
+                                diag, part, status);
+    COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
+}
+
+void launch_stats_ff(const int *tlist, int nlist, int ldim, const double *diag, const float *part, int mode, double *trace,
+                     double *result, int *status, cudaStream_t st)
+{
+    if (nlist <= 0) return;
+    k_stats_ff<<<nlist, 256, 0, st>>>(tlist, nlist, ldim, diag, part, (ldim + EB - 1) / EB, mode, trace, result, status);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

@@ -50,10 +50,12 @@ void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_str
                  double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, const void *a12);
 void launch_ptab_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, double4 *ptab, float4 *ptabf, int pstride, ffe *KF,
                      cudaStream_t st);
-// mixed form: q-sums with one a_q recurrence per (pair, subgroup of same-m tasks) (itab_ff.cu)
+// mixed form: q-sums with one a_q recurrence per (pair, subgroup of same-m tasks) (itab_ff.cu);
+// groups index tlist (nullptr: the tasks themselves); band: only the pairs the diagonal reads.
+// The p tables and the float-float K table come first (launch_ptab_kff).
 int itab_group_size();
-void launch_itab_grp(const Task *tasks, int ntask, const int4 *groups, int ngroups, int ldim, const sd *K, int nu_stride,
-                     double4 *ptab, int pstride, ffe *KF, float4 *ptabf, const void *a12, void *Iout, bool ffe_out, int *status,
+void launch_itab_grp(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim, const ffe *KF, int nu_stride,
+                     const float4 *ptabf, int pstride, const void *a12, void *Iout, bool ffe_out, bool band, int *status,
                      cudaStream_t st);
 // sphere-sphere: B = 1 - M^2 and (M^2)_ii from A = 1 - M and M_ii (square.cu)
 void launch_square(int ntask, int n, const double *A, size_t lda, size_t mstride, const double *mdiag, double *B,
@@ -71,11 +73,18 @@ void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t l
                   double *trace, double *result, int *status, cudaStream_t st);
 // mixed form: elements in float-float straight into the FP32 delta matrix (elem_ff.cu)
 size_t elem_ff_part_floats(int ldim);
-void launch_elem_ff(const Task *tasks, int ntask, int ldim, const sd *Sa, const sd *Sb, const double2 *uv, void *Saf, void *Sbf,
-                    float4 *uvf, const void *I, float *S, size_t sstride, double *diag, float *part, int *status,
-                    cudaStream_t st);
-void launch_stats_ff(int ntask, int ldim, const double *diag, const float *part, int mode, double *trace, double *result,
-                     int *status, cudaStream_t st);
+// float-float copies of the scale factors (Saf, Sbf: L ffe per task; uvf: L float4 per task)
+void launch_scale_ff(int ntask, int ldim, const sd *Sa, const sd *Sb, const double2 *uv, void *Saf, void *Sbf, float4 *uvf,
+                     cudaStream_t st);
+// the diagonal of M alone, from the band of the I table
+void launch_diag_ff(const Task *tasks, int ntask, int ldim, const void *I, const void *Saf, const void *Sbf, const float4 *uvf,
+                    double *diag, int *status, cudaStream_t st);
+// the listed tasks (tlist, nlist; tlist == nullptr: tasks 0..nlist-1)
+void launch_elem_ff(const Task *tasks, const int *tlist, int nlist, int ldim, const void *Saf, const void *Sbf, const float4 *uvf,
+                    const void *I, float *S, size_t sstride, double *diag, float *part, int *status, cudaStream_t st);
+// part == nullptr: the trace rule alone, undecided tasks keep status 0
+void launch_stats_ff(const int *tlist, int nlist, int ldim, const double *diag, const float *part, int mode, double *trace,
+                     double *result, int *status, cudaStream_t st);
 void launch_cholesky(int ntask, int n, double *A, size_t lda, size_t mstride, int *status, double *logdiag, cudaStream_t st);
 size_t mixed_work_bytes(int ntask, int n);
 // live CUDA-event timing of the tcgen05 trailing update (mixed.cu)

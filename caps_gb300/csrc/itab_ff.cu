@@ -65,30 +65,50 @@ CAPS_DEV void iacc_add(IAcc &A, ff t, int et)
     A.h = s.h; A.l = s.l;
 }
 
-// grid (ceil(npair/128), ngroups); groups[g] = {first task, count <= G, a_0..a_2 row}.
-// The tasks of a group are consecutive, share m (hence lmin, mu, the p table and the
-// a_0..a_2 row) and the material.  Output: I tables as float-float (ffe) or, with
-// ffe_out false, as scaled doubles.  The kernel is bound by FP32/ALU issue and the latency
-// of float-float dependency chains, so occupancy pays: at G = 3, six blocks of 128 per SM
-// (80 registers).
-template <int G>
-__global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const int4 *groups, int ngroups, int ldim,
+// grid (ceil(npair/128), ngroups) or, for the band, (ceil(2L/128), ngroups);
+// groups[g] = {first list position, count <= G, a_0..a_2 row}: the group's tasks are
+// tlist[x], ..., tlist[x + count - 1] (tlist == nullptr: tasks x, ..., x + count - 1).
+// They share m (hence lmin, mu, the p table and the a_0..a_2 row) and the material.
+// BAND computes only the pairs that the diagonal of M reads, l1 - l2 in {0, 2} (the EE and
+// MM entries of a diagonal 2x2 block, integration.c:762-888); each pair's sum is the one
+// the full kernel forms.  Output: I tables as float-float (ffe) or, with ffe_out false, as
+// scaled doubles.  The kernel is bound by FP32/ALU issue and the latency of float-float
+// dependency chains, so occupancy pays: at G = 3, six blocks of 128 per SM (80 registers).
+template <int G, bool BAND>
+__global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim,
                                                   const ffe *__restrict__ KF, int nu_stride, const float4 *__restrict__ ptabf,
                                                   int pstride, const A012F *__restrict__ a12, void *Iout, bool ffe_out,
                                                   int *status, int stop_bits)
 {
     const int L = ldim + 2;
     const long long npair = (long long)L * (L + 1) / 2;
-    const long long pid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int gi = blockIdx.y;
-    if (pid >= npair || gi >= ngroups) return;
+    if (gi >= ngroups) return;
+    long long pid;
+    int a1, a2;
+    if (BAND) {
+        // thread 2 a2 + d owns the pair (a2 + 2 d, a2)
+        if (tid >= 2LL * L) return;
+        a2 = (int)(tid >> 1);
+        a1 = a2 + 2 * (int)(tid & 1);
+        if (a1 >= L) return;
+        pid = (long long)a1 * (a1 + 1) / 2 + a2;
+    } else {
+        if (tid >= npair) return;
+        pid = tid;
+        // pair index -> (a1 >= a2); the float root is exact to +-1 and corrected in integers
+        a1 = (int)((sqrtf(8.0f * (float)pid + 1.0f) - 1.0f) * 0.5f);
+        while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
+        while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
+        a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
+    }
     const int4 grp = groups[gi];
-    const int t0 = grp.x, ng = grp.y;
-    // pair index -> (a1 >= a2); the float root is exact to +-1 and corrected in integers
-    int a1 = (int)((sqrtf(8.0f * (float)pid + 1.0f) - 1.0f) * 0.5f);
-    while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
-    while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
-    const int a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
+    const int ng = grp.y;
+    int tk[G]; // task index of each member
+#pragma unroll
+    for (int g = 0; g < G; g++) tk[g] = g < ng ? (tlist ? tlist[grp.x + g] : grp.x + g) : 0;
+    const int t0 = tk[0];
 
     const Task &T = tasks[t0];
     const int l1 = T.lmin - 1 + a1, l2 = T.lmin - 1 + a2;
@@ -96,7 +116,7 @@ __global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const in
     const size_t o12 = (size_t)a1 * L + a2, o21 = (size_t)a2 * L + a1;
     const size_t LL = (size_t)L * L;
     auto store = [&](int g, int pol, float h, float l, int e) { // pol 1 = TM, 0 = TE (table order of K and I)
-        const size_t base = (size_t)((t0 + g) * 2 + pol) * LL;
+        const size_t base = (size_t)(tk[g] * 2 + pol) * LL;
         if (ffe_out) {
             ffe *F = reinterpret_cast<ffe *>(Iout) + base;
             F[o12] = F[o21] = ffe{h, l, e, 0};
@@ -119,7 +139,7 @@ __global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const in
     // accumulators: j = 2 g + (0: TM, 1: TE); K table of task t, polarisation p at
     // KF[(t*2 + p) nu_stride - mu + nu] with p = 1 for TM
     IAcc acc[2 * G];
-    auto Kat = [&](int j, int nu) { return KF[(size_t)((t0 + (j >> 1)) * 2 + ((j & 1) ? 0 : 1)) * nu_stride + (nu - T.mu)]; };
+    auto Kat = [&](int j, int nu) { return KF[(size_t)(tk[j >> 1] * 2 + ((j & 1) ? 0 : 1)) * nu_stride + (nu - T.mu)]; };
 #pragma unroll
     for (int j = 0; j < 2 * G; j++) {
         const bool live = (j >> 1) < ng && ((j & 1) == 0 || both);
@@ -211,7 +231,7 @@ __global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const in
         const IAcc &AT = acc[2 * g];
         ff r = ff_mul(a0f, ff{AT.h, AT.l});
         int k = fexpo(r.h);
-        if (k == -127 || k == 128) atomicOr(status + t0 + g, ST_ERR_NONFINITE);
+        if (k == -127 || k == 128) atomicOr(status + tk[g], ST_ERR_NONFINITE);
         if (k == 128 || k == -127) k = 0;
         r = ff_shift(r, -k);
         const int eT = AT.e + A12.a0e + k;
@@ -236,15 +256,19 @@ constexpr int IGRP = 3;
 constexpr int ITAB_STOP_BITS = 44; // early stop below 2^-44 of the q = 0 term
 int itab_group_size() { return IGRP; }
 
-void launch_itab_grp(const Task *tasks, int ntask, const int4 *groups, int ngroups, int ldim, const sd *K, int nu_stride,
-                     double4 *ptab, int pstride, ffe *KF, float4 *ptabf, const void *a12, void *Iout, bool ffe_out, int *status,
+void launch_itab_grp(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim, const ffe *KF, int nu_stride,
+                     const float4 *ptabf, int pstride, const void *a12, void *Iout, bool ffe_out, bool band, int *status,
                      cudaStream_t st)
 {
-    launch_ptab_kff(tasks, ntask, K, nu_stride, ptab, ptabf, pstride, KF, st);
+    if (ngroups <= 0) return;
     const long long L = ldim + 2, npair = L * (L + 1) / 2;
-    dim3 g((unsigned)((npair + 127) / 128), ngroups);
-    k_itab_grp<IGRP><<<g, 128, 0, st>>>(tasks, groups, ngroups, (int)ldim, KF, nu_stride, ptabf, pstride, (const A012F *)a12, Iout,
-                                        ffe_out, status, ITAB_STOP_BITS);
+    dim3 g((unsigned)(((band ? 2 * L : npair) + 127) / 128), ngroups);
+    if (band)
+        k_itab_grp<IGRP, true><<<g, 128, 0, st>>>(tasks, tlist, groups, ngroups, (int)ldim, KF, nu_stride, ptabf, pstride,
+                                                  (const A012F *)a12, Iout, ffe_out, status, ITAB_STOP_BITS);
+    else
+        k_itab_grp<IGRP, false><<<g, 128, 0, st>>>(tasks, tlist, groups, ngroups, (int)ldim, KF, nu_stride, ptabf, pstride,
+                                                   (const A012F *)a12, Iout, ffe_out, status, ITAB_STOP_BITS);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

@@ -86,11 +86,12 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF, tlist, groups2;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
-    cudaEvent_t ev[7];
+    static constexpr int NEV = 9;
+    cudaEvent_t ev[NEV];
     std::mutex mu;
     cudaStream_t stream() const { return user ? user : own; }
 };
@@ -127,7 +128,7 @@ static void engine_init()
         w[i] = 2 / ((1 - z * z) * pp * pp);
     }
     upload_gauss_legendre(x, w);
-    for (int i = 0; i < 7; i++) CK(cudaEventCreate(&g_eng.ev[i]));
+    for (int i = 0; i < Engine::NEV; i++) CK(cudaEventCreate(&g_eng.ev[i]));
     g_eng.ready = true;
 }
 
@@ -557,31 +558,75 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, g_eng.a12t.get(a12_tab_bytes(ldim, ngroup)), st);
         else
             launch_a12(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, st);
-        if (caps->precision == CAPS_PREC_MIXED) {
-            // mixed form: the q-sums in float-float on the FP32 pipe
-            float4 *d_ptabf = (float4 *)g_eng.ptabf.get((size_t)nt * 2 * pstride * 2 * sizeof(float4));
-            launch_itab_grp(d_tasks, nt, d_sub, nsub, ldim, d_K, nu_stride, d_ptab, pstride, d_KF, d_ptabf, d_a12, d_I, ff_elem,
-                            d_status, st);
-        } else
-            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_a12);
-        CK(cudaEventRecord(g_eng.ev[3], st));
-
         const size_t lda = dim, mstride = (size_t)dim * dim;
         double *d_trace = (double *)g_eng.trace.get(nt * sizeof(double));
         double *d_res = (double *)g_eng.result.get(nt * sizeof(double));
-        double *d_A = nullptr, *d_dg = nullptr;
+        double *d_dg = (double *)g_eng.diag.get((size_t)nt * dim * sizeof(double));
+        void *d_Saf = nullptr, *d_Sbf = nullptr;
+        float4 *d_uvf = nullptr;
+        int nlist = nt;            // matrices assembled in full
+        const int *d_list = nullptr; // their chunk indices (nullptr: all of them)
+        if (caps->precision == CAPS_PREC_MIXED) {
+            // mixed form: the q-sums in float-float on the FP32 pipe
+            float4 *d_ptabf = (float4 *)g_eng.ptabf.get((size_t)nt * 2 * pstride * 2 * sizeof(float4));
+            launch_ptab_kff(d_tasks, nt, d_K, nu_stride, d_ptab, d_ptabf, pstride, d_KF, st);
+            if (ff_elem) {
+                // the diagonal first, as kernel_logdet does (matrix.c:62-82): the band of the
+                // q-sums that M_ii reads, M_ii, and the trace rule.  Only the matrices that the
+                // rule leaves undecided are summed and assembled in full.
+                d_Saf = g_eng.Saf.get((size_t)nt * L * 16);
+                d_Sbf = g_eng.Sbf.get((size_t)nt * L * 16);
+                d_uvf = (float4 *)g_eng.uvf.get((size_t)nt * L * sizeof(float4));
+                launch_scale_ff(nt, ldim, d_Sa, d_Sb, d_uv, d_Saf, d_Sbf, d_uvf, st);
+                launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KF, nu_stride, d_ptabf, pstride, d_a12, d_I, true, true,
+                                d_status, st);
+                CK(cudaEventRecord(g_eng.ev[3], st));
+                launch_diag_ff(d_tasks, nt, ldim, d_I, d_Saf, d_Sbf, d_uvf, d_dg, d_status, st);
+                launch_stats_ff(nullptr, nt, ldim, d_dg, nullptr, O.mode, d_trace, d_res, d_status, st);
+                CK(cudaEventRecord(g_eng.ev[4], st));
+                std::vector<int> hs(nt), list;
+                std::vector<int4> sub2;
+                d2h(hs.data(), d_status, nt * sizeof(int), st);
+                CK(cudaStreamSynchronize(st));
+                for (int i = 0; i < nt; i++) {
+                    if (hs[i] != 0) continue;
+                    if (sub2.empty() || tasks[c0 + i].m != tasks[c0 + list[sub2.back().x]].m || sub2.back().y == itab_group_size())
+                        sub2.push_back(make_int4((int)list.size(), 0, tasks[c0 + i].mgroup, 0));
+                    sub2.back().y++;
+                    list.push_back(i);
+                }
+                nlist = (int)list.size();
+                if (nlist > 0) {
+                    int *dl = (int *)g_eng.tlist.get(nlist * sizeof(int));
+                    int4 *dg2 = (int4 *)g_eng.groups2.get(sub2.size() * sizeof(int4));
+                    h2d(dl, list.data(), nlist * sizeof(int), st);
+                    h2d(dg2, sub2.data(), sub2.size() * sizeof(int4), st);
+                    d_list = dl;
+                    CK(cudaEventRecord(g_eng.ev[5], st));
+                    launch_itab_grp(d_tasks, d_list, dg2, (int)sub2.size(), ldim, d_KF, nu_stride, d_ptabf, pstride, d_a12, d_I, true,
+                                    false, d_status, st);
+                } else
+                    CK(cudaEventRecord(g_eng.ev[5], st));
+            } else {
+                for (int k = 3; k <= 5; k++) CK(cudaEventRecord(g_eng.ev[k], st));
+                launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KF, nu_stride, d_ptabf, pstride, d_a12, d_I, false, false,
+                                d_status, st);
+            }
+        } else {
+            for (int k = 3; k <= 5; k++) CK(cudaEventRecord(g_eng.ev[k], st));
+            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_a12);
+        }
+        CK(cudaEventRecord(g_eng.ev[6], st));
+
+        double *d_A = nullptr;
         float *d_S = nullptr;
         if (ff_elem) {
             d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
-            d_dg = (double *)g_eng.diag.get((size_t)nt * dim * sizeof(double));
             float *d_part = (float *)g_eng.part.get((size_t)nt * elem_ff_part_floats(ldim) * sizeof(float));
-            void *d_Saf = g_eng.Saf.get((size_t)nt * L * 16), *d_Sbf = g_eng.Sbf.get((size_t)nt * L * 16);
-            float4 *d_uvf = (float4 *)g_eng.uvf.get((size_t)nt * L * sizeof(float4));
-            launch_elem_ff(d_tasks, nt, ldim, d_Sa, d_Sb, d_uv, d_Saf, d_Sbf, d_uvf, d_I, d_S, mstride, d_dg, d_part, d_status, st);
-            launch_stats_ff(nt, ldim, d_dg, d_part, O.mode, d_trace, d_res, d_status, st);
+            launch_elem_ff(d_tasks, d_list, nlist, ldim, d_Saf, d_Sbf, d_uvf, d_I, d_S, mstride, d_dg, d_part, d_status, st);
+            launch_stats_ff(d_list, nlist, ldim, d_dg, d_part, O.mode, d_trace, d_res, d_status, st);
         } else {
             d_A = (double *)g_eng.A.get((size_t)nt * mstride * sizeof(double));
-            d_dg = (double *)g_eng.diag.get((size_t)nt * dim * sizeof(double));
             launch_elem(d_tasks, nt, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, lda, mstride, d_dg, d_status, st);
             if (O.square) {
                 // sphere-sphere: continue with B = 1 - M^2 in place of A
@@ -593,7 +638,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             }
             if (O.factor) launch_stats(d_tasks, nt, dim, d_A, lda, mstride, d_dg, O.mode, d_trace, d_res, d_status, st);
         }
-        CK(cudaEventRecord(g_eng.ev[4], st));
+        CK(cudaEventRecord(g_eng.ev[7], st));
 
         // CAPS_MIXED_SIMT=1 selects the FP32 FFMA trailing update instead of split-TF32 tensor cores
         static const bool tc = getenv("CAPS_MIXED_SIMT") == nullptr;
@@ -609,7 +654,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             launch_cholesky(nt, dim, d_A, lda, mstride, d_status, d_ld, st);
             launch_final(nt, dim, d_ld, d_trace, d_status, d_res, O.mode, st);
         }
-        CK(cudaEventRecord(g_eng.ev[5], st));
+        CK(cudaEventRecord(g_eng.ev[8], st));
 
         std::vector<int> hst(nt);
         std::vector<double> hres(nt);
@@ -633,9 +678,15 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             d2h(O.mie_out_b, d_lnb + (size_t)T.xi_index * (lmax_mie + 1) + T.lmin, ldim * sizeof(double), st);
         }
         CK(cudaStreamSynchronize(st));
-        float f;
-        for (int k = 0; k < 5; k++) { CK(cudaEventElapsedTime(&f, g_eng.ev[k], g_eng.ev[k + 1])); tsum[k] += f; }
-        CK(cudaEventElapsedTime(&f, g_eng.ev[0], g_eng.ev[5])); tsum[5] += f;
+        // phases: setup+Mie, K, I (band, the host's look at the trace rule, the rest), elements
+        // (diagonal, then the undecided matrices in full), factorisation, total
+        auto el = [](int a, int b) { float f; CK(cudaEventElapsedTime(&f, g_eng.ev[a], g_eng.ev[b])); return (double)f; };
+        tsum[0] += el(0, 1);
+        tsum[1] += el(1, 2);
+        tsum[2] += el(2, 3) + el(4, 6);
+        tsum[3] += el(3, 4) + el(6, 7);
+        tsum[4] += el(7, 8);
+        tsum[5] += el(0, 8);
         g_counters.nmat += nt;
         long long nfac = 0;
         for (int i = 0; i < nt; i++) nfac += hst[i] == ST_FACTOR;

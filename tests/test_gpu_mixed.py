@@ -101,3 +101,30 @@ def test_batch_order_and_grouping_independent(cg, prec, drude):
     for k, i in enumerate(perm):
         alone = c.logdetD(xis[i], ms[i])
         assert out[k] == alone, (xis[i], ms[i], out[k], alone)
+
+
+def test_mixed_trace_rule_first(cg):
+    """The mixed form applies the trace rule (matrix.c:62-82) to the diagonal before it
+    assembles anything else, and assembles in full only the matrices that the rule leaves
+    undecided.  The decision and the values must be those of the FP64 form, which
+    assembles every matrix; each result must also be bitwise the one of the matrix
+    computed alone (the full q-sums then group a different set of frequencies)."""
+    import numpy as np
+    xis = [1.0, 30.0, 150.0, 400.0]
+    ms = [0, 3, 60, 130]
+    X = [x for x in xis for _ in ms]
+    M = [m for _ in xis for m in ms]
+    c = cg.Caps(20e-6, 1e-6, ldim=140)
+    c.set_drude(9.0, 0.035)
+    ref, st_ref = c.logdetD_batch(X, M)
+    c.set_precision(cg.PREC_MIXED)
+    out, st = c.logdetD_batch(X, M)
+    assert list(st) == list(st_ref)
+    assert 1 in set(st) and 3 in set(st), st   # both trace-rule and factored matrices
+    for x, m, a, b, s in zip(X, M, out, ref, st):
+        if s == 1:  # -tr M: float-float elements, relative error far below the FP32 bar
+            assert abs(a - b) <= 1e-6 * abs(b), (x, m, a, b)
+        else:
+            assert abs(a - b) <= TOL_MIXED * max(1.0, abs(b)), (x, m, a, b)
+    for k in np.random.default_rng(5).permutation(len(X))[:6]:
+        assert out[k] == c.logdetD(X[k], M[k]), (X[k], M[k])
