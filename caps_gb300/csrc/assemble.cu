@@ -564,21 +564,38 @@ __global__ void k_a12_mix(const int *group_m, const int *group_lmin, int ngroup,
     tab[(size_t)g * npair + pid] = r;
 }
 
-__global__ void __launch_bounds__(128) k_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride,
+// grid (ceil(npair/128), nlist) or, for the band, (ceil(2L/128), nlist); block row y handles
+// task tlist[y] (tlist == nullptr: task y).  BAND computes only the pairs that the
+// diagonal of M reads (l1 - l2 in {0, 2}), each with the sum the full kernel forms.
+template <bool BAND>
+__global__ void __launch_bounds__(128) k_itab(const Task *tasks, const int *tlist, int nlist, int ldim, const sd *K, int nu_stride,
                                               const double *__restrict__ lft, const double2 *__restrict__ xtab,
                                               const double4 *__restrict__ ptab, int pstride, sd *I, int *status,
                                               const A012 *__restrict__ a12)
 {
     const int L = ldim + 2;
     const long long npair = (long long)L * (L + 1) / 2;
-    const long long pid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int task = blockIdx.y;
-    if (pid >= npair || task >= ntask) return;
-    // pair index -> (a1 >= a2)
-    int a1 = (int)((sqrt(8.0 * (double)pid + 1.0) - 1.0) * 0.5);
-    while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
-    while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
-    const int a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((int)blockIdx.y >= nlist) return;
+    const int task = tlist ? tlist[blockIdx.y] : (int)blockIdx.y;
+    long long pid;
+    int a1, a2;
+    if (BAND) {
+        // thread 2 a2 + d owns the pair (a2 + 2 d, a2)
+        if (tid >= 2LL * L) return;
+        a2 = (int)(tid >> 1);
+        a1 = a2 + 2 * (int)(tid & 1);
+        if (a1 >= L) return;
+        pid = (long long)a1 * (a1 + 1) / 2 + a2;
+    } else {
+        if (tid >= npair) return;
+        pid = tid;
+        // pair index -> (a1 >= a2)
+        a1 = (int)((sqrt(8.0 * (double)pid + 1.0) - 1.0) * 0.5);
+        while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
+        while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
+        a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
+    }
 
     const Task &T = tasks[task];
     const int l1 = T.lmin - 1 + a1, l2 = T.lmin - 1 + a2;
@@ -742,15 +759,19 @@ CAPS_DEV sd sdx(double c, sd a) { return sd_norm(c * a.m, a.e); }
 CAPS_DEV sd sd_neg(sd a) { return sd{-a.m, a.e}; }
 
 // A = 1 - M (lower triangle); mdiag receives M_ii itself, so that the trace keeps its
-// relative precision when M_ii is far below the unit diagonal of A
-__global__ void k_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv,
-                       double *A, size_t lda, size_t mat_stride, double *mdiag, int *status)
+// relative precision when M_ii is far below the unit diagonal of A.  Grid (ceil(ldim/128),
+// ldim, nlist), block z on task tlist[z] (tlist == nullptr: task z).  DIAG: grid
+// (ceil(ldim/128), 1, nlist), M_ii alone into mdiag (A untouched), from the band of I
+// values that k_itab<true> leaves; the same arithmetic as the full assembly.
+template <bool DIAG>
+__global__ void k_elem(const Task *tasks, const int *tlist, int nlist, int ldim, const sd *I, const sd *Sa, const sd *Sb,
+                       const double2 *uv, double *A, size_t lda, size_t mat_stride, double *mdiag, int *status)
 {
     const int L = ldim + 2;
     const int a = blockIdx.x * blockDim.x + threadIdx.x; // row block
-    const int b = blockIdx.y;                            // column block
-    const int task = blockIdx.z;
-    if (a >= ldim || b > a || task >= ntask) return;
+    const int b = DIAG ? a : (int)blockIdx.y;           // column block
+    if (a >= ldim || b > a || (int)blockIdx.z >= nlist) return;
+    const int task = tlist ? tlist[blockIdx.z] : (int)blockIdx.z;
     const Task &T = tasks[task];
     const sd *ITM = I + (size_t)(task * 2 + 1) * L * L;
     const sd *ITE = I + (size_t)(task * 2 + 0) * L * L;
@@ -781,8 +802,17 @@ __global__ void k_elem(const Task *tasks, int ntask, int ldim, const sd *I, cons
         auto Dv = [&](const sd *t) { return sdx(m, sd_add(sdx(uv1.y, Iv(t, i1 + 1, i2)), sdx(-uv1.x, Iv(t, i1 - 1, i2)))); };
         EE = sd_mul(sd_mul(sa1, sa2), sd_add(Bv(ITM), sdx(-m2, Iv(ITE, i1, i2))));
         MM = sd_mul(sd_mul(sb1, sb2), sd_add(sdx(m2, Iv(ITM, i1, i2)), sd_neg(Bv(ITE))));
-        EM = sd_mul(sd_mul(sa1, sb2), sd_add(Dv(ITM), sd_neg(Cv(ITE))));
-        ME = sd_mul(sd_mul(sb1, sa2), sd_add(Cv(ITM), sd_neg(Dv(ITE))));
+        if (!DIAG) {
+            EM = sd_mul(sd_mul(sa1, sb2), sd_add(Dv(ITM), sd_neg(Cv(ITE))));
+            ME = sd_mul(sd_mul(sb1, sa2), sd_add(Cv(ITM), sd_neg(Dv(ITE))));
+        }
+    }
+    if (DIAG) {
+        const double ee = sd_to_double(EE), mm = sd_to_double(MM);
+        if (!isfinite(ee) || !isfinite(mm)) atomicOr(status + task, ST_ERR_NONFINITE);
+        mdiag[(size_t)task * 2 * ldim + 2 * a] = ee;
+        mdiag[(size_t)task * 2 * ldim + 2 * a + 1] = mm;
+        return;
     }
     double *Am = A + (size_t)task * mat_stride;
     const int r0 = 2 * a, c0 = 2 * b;
@@ -806,27 +836,31 @@ __global__ void k_elem(const Task *tasks, int ntask, int ldim, const sd *I, cons
 // trace and Frobenius norm of M from its strict lower triangle (-A) and its diagonal
 // M_ii (mdiag, n per task), as the reference takes them from the elements of M
 // (matrix.c:57-119): 1 - A_ii would lose every M_ii below the rounding of 1
-__global__ void k_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, int mode,
+// One block per listed task (tlist[x], or x without a list).  A == nullptr: the trace rule
+// alone; a task it does not decide keeps status 0, to be assembled in full.
+__global__ void k_stats(const int *tlist, int nlist, int n, const double *A, size_t lda, size_t mat_stride, int mode,
                         const double *mdiag, double *trace_out, double *result, int *status)
 {
-    const int task = blockIdx.x;
-    if (task >= ntask) return;
-    const double *Am = A + (size_t)task * mat_stride;
+    if ((int)blockIdx.x >= nlist) return;
+    const int task = tlist ? tlist[blockIdx.x] : (int)blockIdx.x;
     __shared__ double red[256];
-    double s = 0.0;
-    // sum of squares of M: diagonal once, strict lower twice (M is symmetric)
-    for (int j = 0; j < n; j++) {
-        const double *col = Am + (size_t)j * lda;
-        for (int i = j + threadIdx.x; i < n; i += blockDim.x) {
-            const double v = (i == j) ? mdiag[(size_t)task * n + i] : -col[i];
-            s += (i == j ? 1.0 : 2.0) * v * v;
+    if (A) {
+        const double *Am = A + (size_t)task * mat_stride;
+        double s = 0.0;
+        // sum of squares of M: diagonal once, strict lower twice (M is symmetric)
+        for (int j = 0; j < n; j++) {
+            const double *col = Am + (size_t)j * lda;
+            for (int i = j + threadIdx.x; i < n; i += blockDim.x) {
+                const double v = (i == j) ? mdiag[(size_t)task * n + i] : -col[i];
+                s += (i == j ? 1.0 : 2.0) * v * v;
+            }
         }
-    }
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        red[threadIdx.x] = s;
         __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
     }
     if (threadIdx.x != 0) return;
     // Kahan trace in index order (misc.c:26)
@@ -840,6 +874,7 @@ __global__ void k_stats(const Task *tasks, int ntask, int n, const double *A, si
     trace_out[task] = tr;
     if (status[task] & ~0xF) { result[task] = NAN; return; }
     if (fabs(tr) < 1e-8) { result[task] = -tr; status[task] = ST_TRACE; return; }
+    if (!A) return;
     const double fro2 = red[0], fro = sqrt(fro2);
     if (mode == 0 && fro < 1) {
         const double merc = -tr - fro2 / 2;
@@ -990,32 +1025,51 @@ void launch_kred_ff(const Task *tasks, int ntask, int max_nnu, const float2 *par
     CK(cudaGetLastError());
 }
 
-void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
-                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, const void *a12)
+void launch_ptab(const Task *tasks, int ntask, double4 *ptab, int pstride, cudaStream_t st)
 {
     dim3 gp((pstride + 127) / 128, ntask);
     k_ptab<<<gp, 128, 0, st>>>(tasks, ntask, ptab, nullptr, pstride);
     COUNT_LAUNCH(1);
-    const long long L = ldim + 2, npair = L * (L + 1) / 2;
-    dim3 g((unsigned)((npair + 127) / 128), ntask);
-    k_itab<<<g, 128, 0, st>>>(tasks, ntask, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status, (const A012 *)a12);
-    COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
-void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv, double *A,
-                 size_t lda, size_t mat_stride, double *mdiag, int *status, cudaStream_t st)
+void launch_itab(const Task *tasks, const int *tlist, int nlist, int ldim, const sd *K, int nu_stride, const double *lft,
+                 const double2 *xtab, const double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, const void *a12,
+                 bool band)
 {
-    dim3 g((ldim + 127) / 128, ldim, ntask);
-    k_elem<<<g, 128, 0, st>>>(tasks, ntask, ldim, I, Sa, Sb, uv, A, lda, mat_stride, mdiag, status);
+    if (nlist <= 0) return;
+    const long long L = ldim + 2, npair = L * (L + 1) / 2;
+    dim3 g((unsigned)(((band ? 2 * L : npair) + 127) / 128), nlist);
+    if (band)
+        k_itab<true><<<g, 128, 0, st>>>(tasks, tlist, nlist, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status,
+                                        (const A012 *)a12);
+    else
+        k_itab<false><<<g, 128, 0, st>>>(tasks, tlist, nlist, ldim, K, nu_stride, lft, xtab, ptab, pstride, I, status,
+                                         (const A012 *)a12);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
 
-void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, const double *mdiag, int mode,
+void launch_elem(const Task *tasks, const int *tlist, int nlist, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv,
+                 double *A, size_t lda, size_t mat_stride, double *mdiag, int *status, cudaStream_t st, bool diag_only)
+{
+    if (nlist <= 0) return;
+    if (diag_only) {
+        dim3 g((ldim + 127) / 128, 1, nlist);
+        k_elem<true><<<g, 128, 0, st>>>(tasks, tlist, nlist, ldim, I, Sa, Sb, uv, A, lda, mat_stride, mdiag, status);
+    } else {
+        dim3 g((ldim + 127) / 128, ldim, nlist);
+        k_elem<false><<<g, 128, 0, st>>>(tasks, tlist, nlist, ldim, I, Sa, Sb, uv, A, lda, mat_stride, mdiag, status);
+    }
+    COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
+}
+
+void launch_stats(const int *tlist, int nlist, int n, const double *A, size_t lda, size_t mat_stride, const double *mdiag, int mode,
                   double *trace, double *result, int *status, cudaStream_t st)
 {
-    k_stats<<<ntask, 256, 0, st>>>(tasks, ntask, n, A, lda, mat_stride, mode, mdiag, trace, result, status);
+    if (nlist <= 0) return;
+    k_stats<<<nlist, 256, 0, st>>>(tlist, nlist, n, A, lda, mat_stride, mode, mdiag, trace, result, status);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

@@ -46,8 +46,12 @@ void launch_kred_ff(const Task *tasks, int ntask, int max_nnu, const float2 *par
                     ffe *KF, int *status, cudaStream_t st);
 void launch_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, int nx, cudaStream_t st);
 struct ffe;
-void launch_itab(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double *lft, const double2 *xtab,
-                 double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, const void *a12);
+// FP64 q-sums of the listed tasks (tlist, nlist; tlist == nullptr: tasks 0..nlist-1); band:
+// only the pairs the diagonal reads.  The p tables come first (launch_ptab).
+void launch_ptab(const Task *tasks, int ntask, double4 *ptab, int pstride, cudaStream_t st);
+void launch_itab(const Task *tasks, const int *tlist, int nlist, int ldim, const sd *K, int nu_stride, const double *lft,
+                 const double2 *xtab, const double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, const void *a12,
+                 bool band);
 void launch_ptab_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, double4 *ptab, float4 *ptabf, int pstride, ffe *KF,
                      cudaStream_t st);
 // mixed form: q-sums with one a_q recurrence per (pair, subgroup of same-m tasks) (itab_ff.cu);
@@ -67,9 +71,11 @@ size_t a12_bytes(int ldim, int ngroup);
 size_t a12_tab_bytes(int ldim, int ngroup);
 void launch_a12_mixed(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, void *work,
                       cudaStream_t st);
-void launch_elem(const Task *tasks, int ntask, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv, double *A,
-                 size_t lda, size_t mat_stride, double *mdiag, int *status, cudaStream_t st);
-void launch_stats(const Task *tasks, int ntask, int n, const double *A, size_t lda, size_t mat_stride, const double *mdiag, int mode,
+// elements of the listed tasks into A = 1 - M and M_ii; diag_only: M_ii alone (from the band)
+void launch_elem(const Task *tasks, const int *tlist, int nlist, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv,
+                 double *A, size_t lda, size_t mat_stride, double *mdiag, int *status, cudaStream_t st, bool diag_only);
+// shortcut decision of the listed tasks; A == nullptr: the trace rule alone, undecided tasks keep status 0
+void launch_stats(const int *tlist, int nlist, int n, const double *A, size_t lda, size_t mat_stride, const double *mdiag, int mode,
                   double *trace, double *result, int *status, cudaStream_t st);
 // mixed form: elements in float-float straight into the FP32 delta matrix (elem_ff.cu)
 size_t elem_ff_part_floats(int ldim);

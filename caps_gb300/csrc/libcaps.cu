@@ -566,14 +566,36 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         float4 *d_uvf = nullptr;
         int nlist = nt;            // matrices assembled in full
         const int *d_list = nullptr; // their chunk indices (nullptr: all of them)
+        std::vector<int> list;
+        std::vector<int4> sub2;      // mixed form: q-sum subgroups of the listed matrices
+        // A factorising request whose M is not wanted in full applies the trace rule to the
+        // diagonal first, as kernel_logdet does (matrix.c:62-82): the band of the q-sums that
+        // M_ii reads, M_ii, and the rule.  Only the matrices it leaves undecided are summed
+        // and assembled in full.
+        const bool diag_first = O.factor && !O.square && !O.M_out && (ff_elem || caps->precision != CAPS_PREC_MIXED);
+        auto undecided = [&]() {
+            std::vector<int> hs(nt);
+            d2h(hs.data(), d_status, nt * sizeof(int), st);
+            CK(cudaStreamSynchronize(st));
+            for (int i = 0; i < nt; i++) {
+                if (hs[i] != 0) continue;
+                if (sub2.empty() || tasks[c0 + i].m != tasks[c0 + list[sub2.back().x]].m || sub2.back().y == itab_group_size())
+                    sub2.push_back(make_int4((int)list.size(), 0, tasks[c0 + i].mgroup, 0));
+                sub2.back().y++;
+                list.push_back(i);
+            }
+            nlist = (int)list.size();
+            if (nlist > 0) {
+                int *dl = (int *)g_eng.tlist.get(nlist * sizeof(int));
+                h2d(dl, list.data(), nlist * sizeof(int), st);
+                d_list = dl;
+            }
+        };
         if (caps->precision == CAPS_PREC_MIXED) {
             // mixed form: the q-sums in float-float on the FP32 pipe
             float4 *d_ptabf = (float4 *)g_eng.ptabf.get((size_t)nt * 2 * pstride * 2 * sizeof(float4));
             launch_ptab_kff(d_tasks, nt, d_K, nu_stride, d_ptab, d_ptabf, pstride, d_KF, st);
-            if (ff_elem) {
-                // the diagonal first, as kernel_logdet does (matrix.c:62-82): the band of the
-                // q-sums that M_ii reads, M_ii, and the trace rule.  Only the matrices that the
-                // rule leaves undecided are summed and assembled in full.
+            if (diag_first) {
                 d_Saf = g_eng.Saf.get((size_t)nt * L * 16);
                 d_Sbf = g_eng.Sbf.get((size_t)nt * L * 16);
                 d_uvf = (float4 *)g_eng.uvf.get((size_t)nt * L * sizeof(float4));
@@ -584,37 +606,33 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
                 launch_diag_ff(d_tasks, nt, ldim, d_I, d_Saf, d_Sbf, d_uvf, d_dg, d_status, st);
                 launch_stats_ff(nullptr, nt, ldim, d_dg, nullptr, O.mode, d_trace, d_res, d_status, st);
                 CK(cudaEventRecord(g_eng.ev[4], st));
-                std::vector<int> hs(nt), list;
-                std::vector<int4> sub2;
-                d2h(hs.data(), d_status, nt * sizeof(int), st);
-                CK(cudaStreamSynchronize(st));
-                for (int i = 0; i < nt; i++) {
-                    if (hs[i] != 0) continue;
-                    if (sub2.empty() || tasks[c0 + i].m != tasks[c0 + list[sub2.back().x]].m || sub2.back().y == itab_group_size())
-                        sub2.push_back(make_int4((int)list.size(), 0, tasks[c0 + i].mgroup, 0));
-                    sub2.back().y++;
-                    list.push_back(i);
-                }
-                nlist = (int)list.size();
+                undecided();
+                int4 *dg2 = nullptr;
                 if (nlist > 0) {
-                    int *dl = (int *)g_eng.tlist.get(nlist * sizeof(int));
-                    int4 *dg2 = (int4 *)g_eng.groups2.get(sub2.size() * sizeof(int4));
-                    h2d(dl, list.data(), nlist * sizeof(int), st);
+                    dg2 = (int4 *)g_eng.groups2.get(sub2.size() * sizeof(int4));
                     h2d(dg2, sub2.data(), sub2.size() * sizeof(int4), st);
-                    d_list = dl;
-                    CK(cudaEventRecord(g_eng.ev[5], st));
-                    launch_itab_grp(d_tasks, d_list, dg2, (int)sub2.size(), ldim, d_KF, nu_stride, d_ptabf, pstride, d_a12, d_I, true,
-                                    false, d_status, st);
-                } else
-                    CK(cudaEventRecord(g_eng.ev[5], st));
+                }
+                CK(cudaEventRecord(g_eng.ev[5], st));
+                launch_itab_grp(d_tasks, d_list, dg2, nlist > 0 ? (int)sub2.size() : 0, ldim, d_KF, nu_stride, d_ptabf, pstride, d_a12,
+                                d_I, true, false, d_status, st);
             } else {
                 for (int k = 3; k <= 5; k++) CK(cudaEventRecord(g_eng.ev[k], st));
-                launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KF, nu_stride, d_ptabf, pstride, d_a12, d_I, false, false,
+                launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KF, nu_stride, d_ptabf, pstride, d_a12, d_I, ff_elem, false,
                                 d_status, st);
             }
         } else {
-            for (int k = 3; k <= 5; k++) CK(cudaEventRecord(g_eng.ev[k], st));
-            launch_itab(d_tasks, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_a12);
+            launch_ptab(d_tasks, nt, d_ptab, pstride, st);
+            if (diag_first) {
+                launch_itab(d_tasks, nullptr, nt, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_a12, true);
+                CK(cudaEventRecord(g_eng.ev[3], st));
+                launch_elem(d_tasks, nullptr, nt, ldim, d_I, d_Sa, d_Sb, d_uv, nullptr, lda, mstride, d_dg, d_status, st, true);
+                launch_stats(nullptr, nt, dim, nullptr, lda, mstride, d_dg, O.mode, d_trace, d_res, d_status, st);
+                CK(cudaEventRecord(g_eng.ev[4], st));
+                undecided();
+                CK(cudaEventRecord(g_eng.ev[5], st));
+            } else
+                for (int k = 3; k <= 5; k++) CK(cudaEventRecord(g_eng.ev[k], st));
+            launch_itab(d_tasks, d_list, nlist, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_a12, false);
         }
         CK(cudaEventRecord(g_eng.ev[6], st));
 
@@ -627,7 +645,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             launch_stats_ff(d_list, nlist, ldim, d_dg, d_part, O.mode, d_trace, d_res, d_status, st);
         } else {
             d_A = (double *)g_eng.A.get((size_t)nt * mstride * sizeof(double));
-            launch_elem(d_tasks, nt, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, lda, mstride, d_dg, d_status, st);
+            launch_elem(d_tasks, d_list, nlist, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, lda, mstride, d_dg, d_status, st, false);
             if (O.square) {
                 // sphere-sphere: continue with B = 1 - M^2 in place of A
                 double *d_B = (double *)g_eng.B.get((size_t)nt * mstride * sizeof(double));
@@ -636,7 +654,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
                 d_A = d_B;
                 d_dg = d_dg2;
             }
-            if (O.factor) launch_stats(d_tasks, nt, dim, d_A, lda, mstride, d_dg, O.mode, d_trace, d_res, d_status, st);
+            if (O.factor) launch_stats(d_list, nlist, dim, d_A, lda, mstride, d_dg, O.mode, d_trace, d_res, d_status, st);
         }
         CK(cudaEventRecord(g_eng.ev[7], st));
 

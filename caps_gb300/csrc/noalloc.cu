@@ -199,10 +199,11 @@ extern "C" int caps_logdetD_noalloc(caps_t *self, double xi_, int m, double *log
     NA_CK(cudaMemcpyAsync(d_gm, &gm_h[0], sizeof(int), cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(d_glm, &gm_h[1], sizeof(int), cudaMemcpyHostToDevice, st));
     launch_a12(d_gm, d_glm, 1, ldim, d_lft, d_a12, st);
-    launch_itab(d_task, 1, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_a12);
-    launch_elem(d_task, 1, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, dim, (size_t)dim * dim, d_md, d_status, st);
+    launch_ptab(d_task, 1, d_ptab, pstride, st);
+    launch_itab(d_task, nullptr, 1, ldim, d_K, nu_stride, d_lft, d_xtab, d_ptab, pstride, d_I, d_status, st, d_a12, false);
+    launch_elem(d_task, nullptr, 1, ldim, d_I, d_Sa, d_Sb, d_uv, d_A, dim, (size_t)dim * dim, d_md, d_status, st, false);
     const int mode = self->detalg == DETALG_HODLR ? 1 : 0;
-    launch_stats(d_task, 1, dim, d_A, dim, (size_t)dim * dim, d_md, mode, d_trace, d_res, d_status, st);
+    launch_stats(nullptr, 1, dim, d_A, dim, (size_t)dim * dim, d_md, mode, d_trace, d_res, d_status, st);
     launch_cholesky(1, dim, d_A, dim, (size_t)dim * dim, d_status, d_ld, st);
     launch_final(1, dim, d_ld, d_trace, d_status, d_res, mode, st);
     int status = 0;
