@@ -433,15 +433,23 @@ void kernel_timer_stats(double *ms, double *bytes, long long *launches)
     if (launches) *launches = g_kt.launches;
 }
 
-size_t mixed_work_bytes(int ntask, int n) { return (size_t)ntask * (MB * MB * sizeof(float) + fro_slots(n) * sizeof(double)); }
+// scratch: diagonal-block inverses, Frobenius partials, then (256-byte aligned) the panel
+// images of the trailing update
+static size_t mixed_img_offset(int ntask, int n)
+{
+    return ((size_t)ntask * (MB * MB * sizeof(float) + fro_slots(n) * sizeof(double)) + 255) / 256 * 256;
+}
+size_t mixed_work_bytes(int ntask, int n) { return mixed_img_offset(ntask, n) + (size_t)ntask * pipe_img_bytes(n); }
 
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
                            const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc, bool convert,
                            void *work)
 {
-    // work: mixed_work_bytes(ntask, n) of scratch (diagonal-block inverses, Frobenius partials)
+    // work: mixed_work_bytes(ntask, n) of scratch (diagonal-block inverses, Frobenius partials,
+    // panel images)
     float *Winv = (float *)work;
     double *part = (double *)((char *)work + (size_t)ntask * MB * MB * sizeof(float));
+    float *img = (float *)((char *)work + mixed_img_offset(ntask, n));
     CK(cudaMemsetAsync(part, 0, (size_t)ntask * fro_slots(n) * sizeof(double), st));
     // convert: A is the FP64 matrix 1 - M and S receives its delta form here; otherwise S
     // already holds it.  mdiag: M_ii in FP64, n per task (tr(A - I) = -tr M).
@@ -449,12 +457,16 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     // kernel, tc = false (CAPS_MIXED_SIMT=1) the FFMA one.
     static const bool legacy_mma = getenv("CAPS_MIXED_MMASYNC") != nullptr;
     static const bool no_pipe = getenv("CAPS_MIXED_NOPIPE") != nullptr;
+    // CAPS_MIXED_REGSTAGE=1: the whole-trailing-matrix update stages the panel through
+    // registers (16 producer warps) instead of copying prepared images
+    static const bool reg_stage = getenv("CAPS_MIXED_REGSTAGE") != nullptr;
     static bool attr = false;
     static int nsm = 1;
     if (!attr) {
         CK(cudaFuncSetAttribute(k_syrk_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
         CK(cudaFuncSetAttribute(k_syrk_pipe<64, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM));
         CK(cudaFuncSetAttribute(k_syrk_pipe<128, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM_WIDE));
+        CK(cudaFuncSetAttribute(k_syrk_pipe<128, 32, PIPE_IMG_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM_IMG));
         int dev = 0;
         CK(cudaGetDevice(&dev));
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -471,11 +483,18 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
                                                                                                  S, sstride, status);
         else if (ncb > 0) // the rest of an outer panel: 128 x 64 tiles, 64-column chunks
             k_syrk_pipe<64, 64><<<std::min(ntask * tpt, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb, S,
-                                                                                             sstride, status);
+                                                                                             sstride, status, nullptr);
         else { // the whole trailing matrix: 128 x 128 tiles (a third less staging per entry), 32-column chunks
             const int tw = ntask * pipe_tiles<128>(nr, 0);
-            k_syrk_pipe<128, 32><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_WIDE, st>>>(ntask, n, k0, kw, t0, cmax, 0, S, sstride,
-                                                                                          status);
+            if (!reg_stage && kw <= PIPE_IMG_CH * PIPE_IMG_TK) {
+                // the panel once as split TF32 images; the update copies them in bulk
+                k_panel_img<<<dim3(nr * PIPE_IMG_CH, ntask), 256, 0, st>>>(ntask, n, k0, kw, t0, S, sstride, status, img);
+                COUNT_LAUNCH(1);
+                k_syrk_pipe<128, 32, PIPE_IMG_STAGES><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_IMG, st>>>(
+                    ntask, n, k0, kw, t0, cmax, 0, S, sstride, status, img);
+            } else
+                k_syrk_pipe<128, 32><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_WIDE, st>>>(ntask, n, k0, kw, t0, cmax, 0, S,
+                                                                                              sstride, status, nullptr);
         }
         COUNT_LAUNCH(1);
         if (g_kt.on) {

@@ -30,12 +30,15 @@ constexpr int PIPE_PRODUCER_WARPS = 16, PIPE_EPI_WARPS = 8;
 constexpr int PIPE_THREADS = (PIPE_PRODUCER_WARPS + 1 + PIPE_EPI_WARPS) * 32; // 800
 // tile width TN (columns of S per tile) and chunk depth TK (panel columns per stage): a
 // stage holds hi + lo of the 128-row and the TN-row slice; two stages
-template <int TN, int TK> struct PipeShape {
+// stage; NS stages
+template <int TN, int TK, int NS = 2> struct PipeShape {
     static constexpr int STAGE = 2 * (UM_M + TN) * TK; // floats
-    static constexpr int SMEM = 2 * STAGE * 4;         // bytes
+    static constexpr int SMEM = NS * STAGE * 4;        // bytes
 };
 constexpr int PIPE_SMEM = PipeShape<64, 64>::SMEM;   // 192 KB
 constexpr int PIPE_SMEM_WIDE = PipeShape<128, 32>::SMEM; // 128 KB
+constexpr int PIPE_IMG_STAGES = 3;                       // stages of the image-fed update
+constexpr int PIPE_SMEM_IMG = PipeShape<128, 32, PIPE_IMG_STAGES>::SMEM; // 192 KB
 constexpr int PIPE_WAIT_ITERS = 1 << 22;
 constexpr int PIPE_PRODUCERS = PIPE_PRODUCER_WARPS * 32;
 
@@ -80,6 +83,40 @@ __device__ __forceinline__ void pipe_stage(const float *Sm, int n, int kc, int n
             hd[u * PIPE_PRODUCERS] = hi;
             ld[u * PIPE_PRODUCERS] = lo;
         }
+    }
+}
+
+// Panel images for the whole-trailing-matrix update (128 x 128 tiles, 32-column chunks):
+// the panel P = S[t0 .., k0 .. k0 + kw) cut into 128-row blocks and 32-column chunks, each
+// chunk split into TF32 hi and lo and stored as the 16 KB image of a shared-memory slice
+// (the layout above), so that a stage is filled by four bulk copies:
+// img[(((task nrb + rb) PIPE_IMG_CH + ch) 2 + part) PIPE_IMG_FLOATS + e], nrb = ceil((n - t0) / 128).
+constexpr int PIPE_IMG_TK = 32, PIPE_IMG_CH = 8, PIPE_IMG_FLOATS = UM_M * PIPE_IMG_TK, PIPE_IMG_BYTES = PIPE_IMG_FLOATS * 4;
+// bytes of image space per matrix of dimension n
+__host__ __device__ inline size_t pipe_img_bytes(int n) { return (size_t)((n + UM_M - 1) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_BYTES; }
+
+// grid (nrb PIPE_IMG_CH, ntask), 256 threads: one chunk image (hi and lo) per block, rows
+// beyond n and columns beyond kw as zeros; matrices not being factored are skipped, as the
+// update skips them
+__global__ void __launch_bounds__(256) k_panel_img(int ntask, int n, int k0, int kw, int t0, const float *S, size_t sstride,
+                                                   const int *status, float *img)
+{
+    const int nrb = (n - t0 + UM_M - 1) / UM_M;
+    const int rb = blockIdx.x / PIPE_IMG_CH, ch = blockIdx.x % PIPE_IMG_CH;
+    const int task = blockIdx.y;
+    if (rb >= nrb || task >= ntask || (status[task] & ~ST_ERR_WAIT) != ST_FACTOR) return;
+    const float *Sm = S + (size_t)task * sstride;
+    float *hi = img + (((size_t)task * nrb + rb) * PIPE_IMG_CH + ch) * 2 * PIPE_IMG_FLOATS, *lo = hi + PIPE_IMG_FLOATS;
+    constexpr int CPR = PIPE_IMG_TK / 4;
+#pragma unroll 4
+    for (int e = threadIdx.x; e < PIPE_IMG_FLOATS; e += 256) {
+        const int cm = e >> 5, w = e & 31;
+        const int row = t0 + rb * UM_M + (cm / CPR) * 8 + (w >> 2), kk = ch * PIPE_IMG_TK + (cm % CPR) * 4 + (w & 3);
+        const float x = (row < n && kk < kw) ? Sm[(size_t)(k0 + kk) * n + row] : 0.0f;
+        float h, l;
+        um_split(x, h, l);
+        hi[e] = h;
+        lo[e] = l;
     }
 }
 
@@ -129,15 +166,17 @@ __device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, int ncb, int n, in
 }
 
 // S[t0.., t0..cmax) -= P P^T, P = columns k0 .. k0 + kw - 1, in 128 x TN tiles and TK-column
-// chunks; grid = min(tiles, SMs), 800 threads
-template <int TN, int TK>
+// chunks; grid = min(tiles, SMs), 800 threads.  img != nullptr (128 x 128 tiles, 32-column
+// chunks only): the panel comes from its images (k_panel_img), one thread of warp 0 fills
+// each stage with four bulk copies and the other producer warps stay idle.
+template <int TN, int TK, int NS = 2>
 __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n, int k0, int kw, int t0, int cmax, int ncb,
-                                                               float *S, size_t sstride, int *status)
+                                                               float *S, size_t sstride, int *status, const float *img)
 {
-    using Shape = PipeShape<TN, TK>;
+    using Shape = PipeShape<TN, TK, NS>;
     constexpr int PA = UM_M * TK, PB = TN * TK;
     extern __shared__ __align__(1024) float pipe_sm[];
-    __shared__ uint64_t full[2], empty[2], tfull[2], tempty[2];
+    __shared__ uint64_t full[NS], empty[NS], tfull[2], tempty[2];
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int cend = min(n, cmax);
@@ -148,9 +187,11 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
 
     if (warp == 0) umma::alloc(&tslot, 2 * TN);
     if (tid == 0) {
-        for (int i = 0; i < 2; i++) {
-            umma::mbar_init(&full[i], PIPE_PRODUCERS);
+        for (int i = 0; i < NS; i++) {
+            umma::mbar_init(&full[i], img ? 1 : PIPE_PRODUCERS);
             umma::mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; i++) {
             umma::mbar_init(&tfull[i], 1);
             umma::mbar_init(&tempty[i], PIPE_EPI_WARPS * 32);
         }
@@ -160,7 +201,42 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
     umma::fence_after();
     const uint32_t tmem = tslot;
 
-    if (warp < PIPE_PRODUCER_WARPS) {
+    if (warp < PIPE_PRODUCER_WARPS && img) {
+        // ---- producer: bulk copies of the panel images (one thread) ----
+        if constexpr (TN == UM_M && TK == PIPE_IMG_TK) {
+            if (tid == 0) {
+                int it = 0, last[NS];
+                for (int s = 0; s < NS; s++) last[s] = -1;
+                bool ok = true;
+                for (int t = blockIdx.x; ok && t < ntile; t += gridDim.x) {
+                    const PipeTile T = pipe_tile<TN>(t, tpt, ncb, n, t0, cend, status);
+                    if (!T.valid) continue;
+                    const float *ia = img + ((size_t)T.task * nr + (T.row0 - t0) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_FLOATS;
+                    const float *ib = img + ((size_t)T.task * nr + (T.col0 - t0) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_FLOATS;
+                    for (int ch = 0; ch < nchunk; ch++, it++) {
+                        const int s = it % NS, use = it / NS;
+                        if (use > 0 && !umma::mbar_wait(&empty[s], (use - 1) & 1, PIPE_WAIT_ITERS)) {
+                            ok = false;
+                            atomicOr(status + T.task, ST_ERR_WAIT);
+                            break;
+                        }
+                        float *st = pipe_sm + s * Shape::STAGE;
+                        const size_t o = (size_t)ch * 2 * PIPE_IMG_FLOATS;
+                        umma::mbar_arrive_tx(&full[s], 4 * PIPE_IMG_BYTES);
+                        umma::bulk_g2s(st, ia + o, PIPE_IMG_BYTES, &full[s]);
+                        umma::bulk_g2s(st + PA, ia + o + PIPE_IMG_FLOATS, PIPE_IMG_BYTES, &full[s]);
+                        umma::bulk_g2s(st + 2 * PA, ib + o, PIPE_IMG_BYTES, &full[s]);
+                        umma::bulk_g2s(st + 2 * PA + PB, ib + o + PIPE_IMG_FLOATS, PIPE_IMG_BYTES, &full[s]);
+                        last[s] = use;
+                    }
+                }
+                // the copies complete whatever the other roles do: wait (bounded) for the
+                // last fill of each stage, so that none is in flight when the CTA leaves
+                for (int s = 0; s < NS; s++)
+                    if (last[s] >= 0) umma::mbar_wait(&full[s], last[s] & 1, PIPE_WAIT_ITERS);
+            }
+        }
+    } else if (warp < PIPE_PRODUCER_WARPS) {
         // ---- producers ----
         const int ptid = tid;
         int it = 0; // chunk counter (stage ring)
@@ -170,7 +246,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
             const float *Sm = S + (size_t)T.task * sstride;
             bool ok = true;
             for (int ch = 0; ch < nchunk; ch++, it++) {
-                const int s = it & 1, use = it >> 1;
+                const int s = it % NS, use = it / NS;
                 if (use > 0 && !umma::mbar_wait(&empty[s], (use - 1) & 1, PIPE_WAIT_ITERS)) { ok = false; break; }
                 float *st = pipe_sm + s * Shape::STAGE;
                 float *Ahi = st, *Alo = Ahi + PA, *Bhi = Alo + PA, *Blo = Bhi + PB;
@@ -196,7 +272,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
                 umma::fence_after();
                 const uint32_t acc = tmem + b * TN;
                 for (int ch = 0; ok && ch < nchunk; ch++, it++) {
-                    const int s = it & 1, use = it >> 1;
+                    const int s = it % NS, use = it / NS;
                     if (!umma::mbar_wait(&full[s], use & 1, PIPE_WAIT_ITERS)) { ok = false; break; }
                     umma::fence_after();
                     const float *st = pipe_sm + s * Shape::STAGE;

@@ -72,6 +72,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, int m
     return done != 0;
 }
 
+// arrive on the mbarrier and add `bytes` to the transaction count its phase waits for
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t *mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+}
+// asynchronous bulk copy global -> shared memory of this CTA; completion counts `bytes` off
+// the mbarrier's transaction count.  Both addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+                 "l"((uint64_t)__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_u32(mbar))
+                 : "memory");
+}
+
 // 16 consecutive FP32 columns of this warp's 32 lanes (lane = thread)
 __device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16])
 {
