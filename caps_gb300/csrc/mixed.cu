@@ -79,8 +79,25 @@ __global__ void __launch_bounds__(32) k_potf2_w(int ntask, int n, int k0, float 
     const int lane = threadIdx.x;
     const int nb = min(MB, n - k0);
     float *Sm = S + (size_t)task * sstride + (size_t)k0 * n + k0;
-    for (int c = 0; c < nb; c++)
-        for (int r = c + lane; r < nb; r += 32) T[r][c] = Sm[(size_t)c * n + r];
+    // the block's lower triangle, 16 loads in flight per lane (read-only path, so that the
+    // loads are not ordered behind the shared-memory stores)
+    for (int c0 = 0; c0 < nb; c0 += 8) {
+        float v[8][2];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int c = c0 + u, r = lane + 32 * h;
+                v[u][h] = (c < nb && r >= c && r < nb) ? __ldg(Sm + (size_t)c * n + r) : 0.0f;
+            }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int c = c0 + u, r = lane + 32 * h;
+                if (c < nb && r >= c && r < nb) T[r][c] = v[u][h];
+            }
+    }
     __syncwarp();
     bool bad = false;
     for (int j = 0; j < nb; j++) {
@@ -139,9 +156,9 @@ __global__ void __launch_bounds__(32) k_potf2_w(int ntask, int n, int k0, float 
 // panel: X (I + Lam_kk)^T = S for the rows below the diagonal block, as X = S W^T with
 // W = (I + Lam_kk)^{-1} from k_potf2_w (I + Lam_kk is within a few per cent of I, so the
 // product is as accurate as the substitution).  64 rows per CTA of 256 threads; thread t
-// computes a 4 x 4 tile, rows t mod 16 + 16 i and columns t / 16 + 16 j, so per k it loads
-// 4 entries of X (16 distinct rows per warp, no bank conflict) and 4 of W (broadcast) for
-// 16 FMAs, and a warp stores 16 consecutive rows of each of its columns.
+// computes a 4 x 4 tile, rows t mod 16 + 16 i and columns 4 (t / 16) + j.  The rows are kept
+// in shared memory k-major with row r at position 4 (r mod 16) + r / 16 and W k-major, so
+// per k a thread reads its four rows and its four columns as one float4 each for 16 FMAs.
 constexpr int MT = 64;
 __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, const int *status,
                                                   const float *Winv, double *fro)
@@ -151,18 +168,32 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
     const int nb = min(MB, n - k0);
     const int r0 = k0 + nb + blockIdx.x * MT;
     if (r0 >= n) return;
-    __shared__ float Wl[MB][MB + 1]; // W[c][k]
-    __shared__ float X[MT][MB + 1];  // S rows
+    __shared__ __align__(16) float Wk[MB][MB + 4]; // W[c][k] at Wk[k][c]
+    __shared__ __align__(16) float Xk[MB][MT + 4]; // S[r0 + r][k0 + k] at Xk[k][4 (r mod 16) + r / 16]
     float *Sm = S + (size_t)task * sstride;
     const float *Wt = Winv + (size_t)task * MB * MB;
-    for (int e = threadIdx.x; e < MB * MB; e += 256) Wl[e / MB][e % MB] = Wt[e];
     const int rows = min(MT, n - r0);
-    for (int e = threadIdx.x; e < MT * MB; e += 256) {
-        const int c = e / MT, r = e % MT;
-        X[r][c] = (r < rows && c < nb) ? Sm[(size_t)(k0 + c) * n + r0 + r] : 0.0f;
+    {
+        float w[MB * MB / 256], x[MT * MB / 256];
+#pragma unroll
+        for (int u = 0; u < MB * MB / 256; u++) w[u] = __ldg(Wt + threadIdx.x + 256 * u);
+#pragma unroll
+        for (int u = 0; u < MT * MB / 256; u++) {
+            const int e = threadIdx.x + 256 * u, c = e / MT, r = e % MT;
+            x[u] = (r < rows && c < nb) ? __ldg(Sm + (size_t)(k0 + c) * n + r0 + r) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < MB * MB / 256; u++) {
+            const int e = threadIdx.x + 256 * u; // W row-major: e = c MB + k
+            Wk[e % MB][e / MB] = w[u];
+        }
+#pragma unroll
+        for (int u = 0; u < MT * MB / 256; u++) {
+            const int e = threadIdx.x + 256 * u, c = e / MT, r = e % MT;
+            Xk[c][4 * (r & 15) + (r >> 4)] = x[u];
+        }
     }
     __syncthreads();
-    // 4 x 4 register tile per thread: rows rg + 16 i, columns cg + 16 j
     const int rg = threadIdx.x & 15, cg = threadIdx.x >> 4;
     float acc[4][4];
 #pragma unroll
@@ -170,20 +201,18 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
 #pragma unroll
         for (int j = 0; j < 4; j++) acc[i][j] = 0.0f;
     for (int k = 0; k < nb; k++) {
-        float a[4], w[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) a[i] = X[rg + 16 * i][k];
-#pragma unroll
-        for (int j = 0; j < 4; j++) w[j] = Wl[cg + 16 * j][k];
+        const float4 a = *reinterpret_cast<const float4 *>(&Xk[k][4 * rg]);
+        const float4 w = *reinterpret_cast<const float4 *>(&Wk[k][4 * cg]);
+        const float av[4] = {a.x, a.y, a.z, a.w}, wv[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
         for (int i = 0; i < 4; i++)
 #pragma unroll
-            for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], w[j], acc[i][j]);
+            for (int j = 0; j < 4; j++) acc[i][j] = fmaf(av[i], wv[j], acc[i][j]);
     }
     double sq = 0.0;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-        const int c = cg + 16 * j;
+        const int c = 4 * cg + j;
         if (c >= nb) continue;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
