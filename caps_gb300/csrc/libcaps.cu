@@ -1244,27 +1244,44 @@ extern "C" int caps_mlp_proposal(caps_t *self, double T, double cutoff, double e
     double wp, ga;
     if (!material_features(self, &wp, &ga)) return -1;
     const double Ts = 2 * PI * CAPS_kB * (self->R + self->L) * T / (CAPS_hbar * CAPS_c);
-    const int MCAP = 1024, NPROBE = std::min(nmax, 256);
-    std::vector<float> X((size_t)NPROBE * MCAP * 5), Y((size_t)NPROBE * MCAP);
-    for (int n = 1; n <= NPROBE; n++)
-        for (int m = 0; m < MCAP; m++)
-            caps_mlp_features(1.0 / self->LbyR, n * Ts, m, wp, ga, &X[(((size_t)(n - 1) * MCAP) + m) * 5]);
-    caps_mlp_predict(mlp, X.data(), NPROBE * MCAP, Y.data());
+    const int MCAP = 1024, NPROBE = std::min(nmax, 256), NB = 16;
     // the xi = 0 term (analytic for Drude; drude term as the scale for other materials)
     const double v0 = fabs(caps_ht_drude(self));
     const double lc = log(cutoff);
-    int N = NPROBE;
-    for (int n = 1; n <= NPROBE; n++) {
-        const float *y = &Y[(size_t)(n - 1) * MCAP];
-        int mstop = MCAP - 1;
-        for (int m = 1; m < MCAP; m++)
-            if (y[m] - y[0] < lc) { mstop = m; break; }
-        mchunk[n - 1] = mstop + 1 + 2; // two extra m beyond the predicted cutoff
-        double v = 0.5 * exp((double)y[0]);
-        for (int m = 1; m <= mstop; m++) v += exp((double)y[m]);
-        if (v / v0 < epsrel) { N = n; break; }
+    // frequencies in blocks of NB, stopping at the first block that reaches the Matsubara
+    // cutoff; features as caps_mlp_features forms them, the frequency-independent ones
+    // once (a prediction depends on its own features only)
+    float xm[5];
+    caps_mlp_features(1.0 / self->LbyR, Ts, 0, wp, ga, xm);
+    std::vector<float> X((size_t)NB * MCAP * 5), Y((size_t)NB * MCAP);
+    for (int n0 = 1; n0 <= NPROBE; n0 += NB) {
+        const int nb = std::min(NB, NPROBE - n0 + 1);
+        for (int k = 0; k < nb; k++) {
+            float xn[5];
+            caps_mlp_features(1.0 / self->LbyR, (n0 + k) * Ts, 0, wp, ga, xn);
+            for (int m = 0; m < MCAP; m++) {
+                float *x = &X[((size_t)k * MCAP + m) * 5];
+                x[0] = xm[0];
+                x[1] = xn[1];
+                x[2] = (float)(m / 200.0);
+                x[3] = xm[3];
+                x[4] = xm[4];
+            }
+        }
+        caps_mlp_predict(mlp, X.data(), nb * MCAP, Y.data());
+        for (int k = 0; k < nb; k++) {
+            const int n = n0 + k;
+            const float *y = &Y[(size_t)k * MCAP];
+            int mstop = MCAP - 1;
+            for (int m = 1; m < MCAP; m++)
+                if (y[m] - y[0] < lc) { mstop = m; break; }
+            mchunk[n - 1] = mstop + 1 + 2; // two extra m beyond the predicted cutoff
+            double v = 0.5 * exp((double)y[0]);
+            for (int m = 1; m <= mstop; m++) v += exp((double)y[m]);
+            if (v / v0 < epsrel) return n;
+        }
     }
-    return N;
+    return NPROBE;
 }
 
 extern "C" double caps_free_energy_learned(caps_t *self, double T, double cutoff, double epsrel, caps_mlp_t *mlp,
