@@ -69,8 +69,10 @@ void launch_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim,
 size_t a12_bytes(int ldim, int ngroup);
 // mixed form: the same from per-m tables (work: a12_tab_bytes of scratch)
 size_t a12_tab_bytes(int ldim, int ngroup);
+// tabs: the per-m tables first; then the pairs of the listed groups (glist == nullptr: groups
+// 0..nlist-1, nlist < 0: all), band: only the pairs the diagonal reads
 void launch_a12_mixed(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, void *work,
-                      cudaStream_t st);
+                      cudaStream_t st, bool tabs = true, const int *glist = nullptr, int nlist = -1, bool band = false);
 // elements of the listed tasks into A = 1 - M and M_ii; diag_only: M_ii alone (from the band)
 void launch_elem(const Task *tasks, const int *tlist, int nlist, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv,
                  double *A, size_t lda, size_t mat_stride, double *mdiag, int *status, cudaStream_t st, bool diag_only);

@@ -86,7 +86,7 @@ struct Engine {
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF, tlist, groups2;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF, tlist, groups2, glist2;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -554,9 +554,12 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         sd *d_I = (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
         double4 *d_ptab = (double4 *)g_eng.ptab.get((size_t)nt * 2 * pstride * sizeof(double4));
         void *d_a12 = g_eng.a12.get(a12_bytes(ldim, ngroup));
-        if (caps->precision == CAPS_PREC_MIXED)
-            launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, g_eng.a12t.get(a12_tab_bytes(ldim, ngroup)), st);
-        else
+        // a_0..a_2 per m; the mixed form's trace rule first needs only the band of each m
+        void *d_a12t = nullptr;
+        if (caps->precision == CAPS_PREC_MIXED) {
+            d_a12t = g_eng.a12t.get(a12_tab_bytes(ldim, ngroup));
+            launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, d_a12t, st, true, nullptr, -1, ff_elem);
+        } else
             launch_a12(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, st);
         const size_t lda = dim, mstride = (size_t)dim * dim;
         double *d_trace = (double *)g_eng.trace.get(nt * sizeof(double));
@@ -611,6 +614,13 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
                 if (nlist > 0) {
                     dg2 = (int4 *)g_eng.groups2.get(sub2.size() * sizeof(int4));
                     h2d(dg2, sub2.data(), sub2.size() * sizeof(int4), st);
+                    // all pairs of the a_0..a_2 rows of the m that still need them
+                    std::vector<int> gl;
+                    for (const int4 &g : sub2)
+                        if (gl.empty() || gl.back() != g.z) gl.push_back(g.z);
+                    int *dgl = (int *)g_eng.glist2.get(gl.size() * sizeof(int));
+                    h2d(dgl, gl.data(), gl.size() * sizeof(int), st);
+                    launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, d_a12t, st, false, dgl, (int)gl.size(), false);
                 }
                 CK(cudaEventRecord(g_eng.ev[5], st));
                 launch_itab_grp(d_tasks, d_list, dg2, nlist > 0 ? (int)sub2.size() : 0, ldim, d_KF, nu_stride, d_ptabf, pstride, d_a12,

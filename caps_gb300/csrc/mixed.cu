@@ -62,95 +62,89 @@ __global__ void k_to_delta32(int ntask, int n, const double *A, size_t lda, size
     }
 }
 
-// diagonal block in delta form, one warp per matrix (no block-wide barriers, only
-// __syncwarp); also writes W = (I + Lam_kk)^{-1} (lower triangular, row-major MB x MB per
-// task) for the panel solve and the block's share of ||Lam||_F^2.
-// Lane l owns rows l and l + 32 of the block (shared-memory rows 65 floats apart, so a warp's
-// accesses to one column fall into 32 distinct banks): per column j every lane forms the
-// pivot from T[j][j], scales its rows' entries of column j and subtracts their rank-1
-// update; W = (I + Lam)^{-1} follows column-parallel (two columns per lane).
-__global__ void __launch_bounds__(32) k_potf2_w(int ntask, int n, int k0, float *S, size_t sstride, int *status, float *Winv,
-                                                double *fro)
+// diagonal block in delta form, one CTA of 256 threads per matrix; also writes W =
+// (I + Lam_kk)^{-1} (lower triangular, row-major MB x MB per task) for the panel solve and
+// the block's share of ||Lam||_F^2.  Per column j every thread forms the pivot from
+// T[j][j]; threads 0..63 scale row tid of column j into colj; the rank-1 update of the
+// trailing triangle is spread over rows (tid mod 64) and every fourth column from
+// j + 1 + tid / 64 (a warp covers 32 rows of one column: T rows 65 floats apart, distinct
+// banks).  W follows column-parallel, one column per thread, by forward substitution.
+__global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float *S, size_t sstride, int *status, float *Winv,
+                                                 double *fro)
 {
     const int task = blockIdx.x;
     if (task >= ntask || status[task] != ST_FACTOR) return;
     __shared__ float T[MB][MB + 1];
     __shared__ float W[MB][MB + 1];
-    const int lane = threadIdx.x;
+    __shared__ float colj[MB];
+    __shared__ double red8[8];
+    const int tid = threadIdx.x;
     const int nb = min(MB, n - k0);
     float *Sm = S + (size_t)task * sstride + (size_t)k0 * n + k0;
-    // the block's lower triangle, 16 loads in flight per lane (read-only path, so that the
-    // loads are not ordered behind the shared-memory stores)
-    for (int c0 = 0; c0 < nb; c0 += 8) {
-        float v[8][2];
+    {
+        // the block's lower triangle, 16 loads in flight per thread
+        float v[MB * MB / 256];
 #pragma unroll
-        for (int u = 0; u < 8; u++)
+        for (int u = 0; u < MB * MB / 256; u++) {
+            const int e = tid + 256 * u, c = e / MB, r = e % MB;
+            v[u] = (c < nb && r >= c && r < nb) ? __ldg(Sm + (size_t)c * n + r) : 0.0f;
+        }
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int c = c0 + u, r = lane + 32 * h;
-                v[u][h] = (c < nb && r >= c && r < nb) ? __ldg(Sm + (size_t)c * n + r) : 0.0f;
-            }
-#pragma unroll
-        for (int u = 0; u < 8; u++)
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int c = c0 + u, r = lane + 32 * h;
-                if (c < nb && r >= c && r < nb) T[r][c] = v[u][h];
-            }
+        for (int u = 0; u < MB * MB / 256; u++) {
+            const int e = tid + 256 * u, c = e / MB, r = e % MB;
+            if (c < nb && r >= c && r < nb) T[r][c] = v[u];
+        }
     }
-    __syncwarp();
+    __syncthreads();
     bool bad = false;
+    const int i = tid & (MB - 1), cs = tid / MB;
     for (int j = 0; j < nb; j++) {
         const float d = T[j][j]; // pivot - 1
         const float one_d = 1.0f + d;
         bad |= !(one_d > 0.0f);
         const float lam = d / (sqrtf(fmaxf(one_d, 1e-30f)) + 1.0f);
         const float inv = 1.0f / (1.0f + lam);
-        __syncwarp();
-        float cj[2] = {0.0f, 0.0f};
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int i = lane + 32 * h;
-            if (i > j && i < nb) { cj[h] = T[i][j] * inv; T[i][j] = cj[h]; }
+        __syncthreads();
+        if (tid > j && tid < nb) {
+            const float cj = T[tid][j] * inv;
+            T[tid][j] = cj;
+            colj[tid] = cj;
         }
-        if (lane == 0) T[j][j] = lam;
-        __syncwarp();
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int i = lane + 32 * h;
-            if (i > j && i < nb)
-                for (int c = j + 1; c <= i; c++) T[i][c] -= cj[h] * T[c][j];
+        if (tid == 0) T[j][j] = lam;
+        __syncthreads();
+        if (i > j && i < nb) {
+            const float ci = colj[i];
+            for (int c = j + 1 + cs; c <= i; c += 4) T[i][c] -= ci * colj[c];
         }
-        __syncwarp();
+        __syncthreads();
     }
     double sq = 0.0;
-    for (int c = 0; c < nb; c++)
-        for (int r = c + lane; r < nb; r += 32) {
+    for (int e = tid; e < MB * MB; e += 256) {
+        const int c = e / MB, r = e % MB;
+        if (c < nb && r >= c && r < nb) {
             Sm[(size_t)c * n + r] = T[r][c];
             sq = fma((double)T[r][c], (double)T[r][c], sq);
         }
-    for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-    if (lane == 0) fro[(size_t)task * fro_slots(n) + (size_t)(k0 / MB) * (fro_nbr(n) + 1)] = sq;
-    // W = (I + Lam)^{-1} column by column (forward substitution, columns lane and lane + 32)
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const int j = lane + 32 * h;
-        if (j >= nb) continue;
-        W[j][j] = 1.0f / (1.0f + T[j][j]);
-        for (int i = j + 1; i < nb; i++) {
+    }
+    sq = block_sum256(sq, red8);
+    if (tid == 0) fro[(size_t)task * fro_slots(n) + (size_t)(k0 / MB) * (fro_nbr(n) + 1)] = sq;
+    // W = (I + Lam)^{-1} column by column (forward substitution, column tid)
+    if (tid < nb) {
+        const int jc = tid;
+        W[jc][jc] = 1.0f / (1.0f + T[jc][jc]);
+        for (int r = jc + 1; r < nb; r++) {
             float acc = 0.0f;
-            for (int k = j; k < i; k++) acc = fmaf(T[i][k], W[k][j], acc);
-            W[i][j] = -acc / (1.0f + T[i][i]);
+            for (int k = jc; k < r; k++) acc = fmaf(T[r][k], W[k][jc], acc);
+            W[r][jc] = -acc / (1.0f + T[r][r]);
         }
     }
-    __syncwarp();
+    __syncthreads();
     float *Wt = Winv + (size_t)task * MB * MB;
-    for (int e = lane; e < MB * MB; e += 32) {
+    for (int e = tid; e < MB * MB; e += 256) {
         const int r = e / MB, c = e % MB;
         Wt[e] = (r < nb && c <= r) ? W[r][c] : 0.0f;
     }
-    bad = __any_sync(0xffffffffu, bad);
-    if (lane == 0 && bad) atomicOr(status + task, ST_ERR_PIVOT);
+    if (__syncthreads_or(bad) && tid == 0) atomicOr(status + task, ST_ERR_PIVOT);
 }
 
 // panel: X (I + Lam_kk)^T = S for the rows below the diagonal block, as X = S W^T with
@@ -540,7 +534,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     }
     // diagonal block k0 and the panel solve below it; false when nothing lies below
     auto factor_panel = [&](int k0) {
-        k_potf2_w<<<ntask, 32, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part);
+        k_potf2_w<<<ntask, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part);
         COUNT_LAUNCH(1);
         const int rest = n - k0 - MB;
         if (rest <= 0) return false;
