@@ -170,7 +170,7 @@ def run_reference(args, dist, rank, world):
 
 # DRAM bytes per algorithmic byte of the trailing update (k_syrk_pipe, all four launch kinds
 # of a 256-column panel), from the ncu capture summarised in profiles/k_syrk_pipe_c3.md
-SYRK_DRAM_PER_ALGORITHMIC = 0.86
+SYRK_DRAM_PER_ALGORITHMIC = 0.95
 
 
 def measured_hbm_peak():
@@ -337,16 +337,19 @@ def main():
                       "traffic": None} if args.precision == "fp64" else
                      {"bound": "hbm",
                       "kernel": "k_syrk_pipe: persistent warp-specialised tcgen05 trailing update of the FP32 delta-form "
-                                "Cholesky (256-column panels, split TF32, TMEM accumulators); algorithmic bytes = target "
-                                "block read + written once and the panel rows read once, per factored matrix",
+                                "Cholesky (256-column panels, split TF32, TMEM accumulators; the whole-trailing-matrix "
+                                "launches fed by bulk copies of split-TF32 panel images, whose k_panel_img pass is "
+                                "inside the timed interval); algorithmic bytes = target block read + written once and "
+                                "the panel rows read once, per factored matrix",
                       "achieved": syrk_gbs, "peak": hbm_peak, "unit": "GB/s",
                       "frac": syrk_gbs / hbm_peak if syrk_gbs else None,
                       "traffic": syrk_bytes / syrk_n * SYRK_DRAM_PER_ALGORITHMIC if syrk_n else None,
                       "peak_source": hbm_src,
                       "launches": syrk_n, "avg_launch_ms": syrk_ms / syrk_n if syrk_n else None,
                       "algorithmic_bytes_per_launch": syrk_bytes / syrk_n if syrk_n else None,
-                      "traffic_source": "DRAM bytes per algorithmic byte of the same kernel from one ncu capture "
-                                        "(profiles/k_syrk_pipe_c3.md), times this run's algorithmic bytes per launch",
+                      "traffic_source": "DRAM bytes per algorithmic byte of the k_syrk_pipe launches from one ncu "
+                                        "capture (profiles/k_syrk_pipe_c3.md), times this run's algorithmic bytes per "
+                                        "launch; the panel-image pass (12 bytes per panel entry) is not included",
                       "fp32_accurate_tflops_factorisation": achieved}),
         "dominant_kernel": None if args.precision == "fp64" else {
             "kernel": "k_itab_grp<3> (float-float q-sums)", "phase_share_of_step": ph[2] / ph[5] if ph[5] else None,

@@ -5,7 +5,7 @@
 // survive on the way is the cancellation inside the B, C, D combinations (up to ~1e5
 // for m = 0).  The combinations are therefore formed in float-float with a separate
 // power-of-two exponent ("fe" below, ~48-bit mantissa) from the float-float I table
-// that k_itab<true> writes, and the result goes straight into the FP32 delta matrix:
+// that k_itab_grp writes, and the result goes straight into the FP32 delta matrix:
 // no FP64 matrix is formed, and the FP64 pipe is used only for the diagonal, which
 // the logdet correction needs in FP64.  Per element block the kernel also leaves a
 // per-warp sum of squares, from which k_stats_ff takes the Frobenius norm for the
