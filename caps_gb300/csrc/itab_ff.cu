@@ -59,9 +59,10 @@ CAPS_DEV void iacc_add(IAcc &A, ff t, int et)
         const ff s = ff_shift(ff{A.h, A.l}, -d);
         A.h = s.h; A.l = s.l; A.e = et; d = 0;
     }
-    // 2^d for -100 <= d <= 30 is a normal float: the alignment is one exact multiply
-    const float p2 = __uint_as_float((unsigned)(127 + d) << 23);
-    const ff s = ff_add(ff{A.h, A.l}, d < -100 ? ff{0.0f, 0.0f} : ff{t.h * p2, t.l * p2});
+    // 2^d for -126 <= d <= 30 is a normal float: the alignment is one exact multiply; below,
+    // where the term lies more than 2^126 under the sum's frame, p2 = 0 drops it
+    const float p2 = __uint_as_float((unsigned)max(127 + d, 0) << 23);
+    const ff s = ff_add(ff{A.h, A.l}, ff{t.h * p2, t.l * p2});
     A.h = s.h; A.l = s.l;
 }
 
