@@ -14,8 +14,6 @@
 // Formulas: elements as in libcaps.c:717-831 (caps_M_elem / caps_kernel_M) with A, B,
 // C, D from integration.c:762-888; shortcut decision as in matrix.c:57-119
 // (kernel_logdet) and matrix.c:489-505 (Mercator bound).
-#include <climits>
-
 #include "common.cuh"
 #include "ff.cuh"
 #include "internal.h"
@@ -38,24 +36,22 @@ CAPS_DEV fe fe_mul(fe a, fe b)
     const ff p = ff_mul(ff{a.h, a.l}, ff{b.h, b.l});
     return fe{p.h, p.l, a.e + b.e};
 }
-// sum_k c_k x_k for float-float coefficients c_k and table values x_k (|h| in [1,2)): every
-// x_k is rescaled to the largest exponent among them by one exact multiply with 2^d (terms
-// more than 2^100 below it drop out), then float-float products and sums
+// sum_k c_k x_k for float-float coefficients c_k and table values x_k (|h| in [1,2), zeros
+// with exponent FFE_ZERO_E): every x_k is rescaled to the largest exponent among them by one
+// exact multiply with 2^d, d <= 0 (terms more than 2^126 below it, zeros among them, scale
+// to 0), then float-float products and sums
 template <int N>
 CAPS_DEV fe fe_lincomb(const ff (&c)[N], const fe (&x)[N])
 {
-    int emax = INT_MIN;
+    int emax = x[0].e;
 #pragma unroll
-    for (int k = 0; k < N; k++)
-        if (x[k].h != 0.0f) emax = max(emax, x[k].e);
-    if (emax == INT_MIN) return fe{0.0f, 0.0f, 0};
+    for (int k = 1; k < N; k++) emax = max(emax, x[k].e);
     ff s{0.0f, 0.0f};
 #pragma unroll
     for (int k = 0; k < N; k++) {
-        const int d = x[k].e - emax; // <= 0 for every nonzero x_k
-        const float p2 = __uint_as_float((unsigned)(127 + max(d, -126)) << 23);
-        const ff xs = (x[k].h == 0.0f || d < -100) ? ff{0.0f, 0.0f} : ff{x[k].h * p2, x[k].l * p2};
-        s = ff_add(s, ff_mul(c[k], xs));
+        const int d = x[k].e - emax;
+        const float p2 = __uint_as_float((unsigned)max(127 + d, 0) << 23);
+        s = ff_add(s, ff_mul(c[k], ff{x[k].h * p2, x[k].l * p2}));
     }
     return fe{s.h, s.l, emax};
 }

@@ -8,6 +8,9 @@ namespace capsgpu {
 
 struct ff { float h, l; };
 struct ffe { float h, l; int e, pad; }; // (h + l) * 2^e
+// exponent carried by a zero table value, far below any nonzero one, so that a maximum over
+// exponents needs no zero test and a zero aligned to it scales to 0
+constexpr int FFE_ZERO_E = -(1 << 20);
 CAPS_DEV ff ff_fast2(float a, float b) { const float s = a + b; return ff{s, b - (s - a)}; }
 CAPS_DEV ff ff_mul(ff x, ff y)
 {

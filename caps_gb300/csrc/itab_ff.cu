@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const in
         }
     };
     if (l2 < mm || l2 < T.m || l1 < 1) { // I = 0 for l < m (integration.c:631)
-        for (int g = 0; g < ng; g++) { store(g, 1, 0.0f, 0.0f, 0); store(g, 0, 0.0f, 0.0f, 0); }
+        for (int g = 0; g < ng; g++) { store(g, 1, 0.0f, 0.0f, FFE_ZERO_E); store(g, 0, 0.0f, 0.0f, FFE_ZERO_E); }
         return;
     }
     const bool both = !T.is_pr;
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const in
         if (k == -127 || k == 128) atomicOr(status + tk[g], ST_ERR_NONFINITE);
         if (k == 128 || k == -127) k = 0;
         r = ff_shift(r, -k);
-        const int eT = AT.e + A12.a0e + k;
+        const int eT = r.h == 0.0f ? FFE_ZERO_E : AT.e + A12.a0e + k;
         store(g, 1, r.h, r.l, eT);
         if (both) {
             const IAcc &AE = acc[2 * g + 1];
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const in
             int ke = fexpo(s.h);
             if (ke == 128 || ke == -127) ke = 0;
             s = ff_shift(s, -ke);
-            store(g, 0, s.h, s.l, AE.e + A12.a0e + ke);
+            store(g, 0, s.h, s.l, s.h == 0.0f ? FFE_ZERO_E : AE.e + A12.a0e + ke);
         } else
             store(g, 0, -r.h, -r.l, eT);
     }
