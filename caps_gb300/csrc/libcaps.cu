@@ -85,6 +85,8 @@ struct Engine {
     bool ready = false;
     int device = 0;
     cudaStream_t own = nullptr, user = nullptr;
+    cudaStream_t side = nullptr;          // Mie coefficients and scale factors, beside setup and K
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double *d_lfac = nullptr;
     DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF, tlist, groups2, glist2;
     std::vector<double> host_pinned_dummy;
@@ -109,6 +111,9 @@ static void engine_init()
     }
     CK(cudaGetDevice(&g_eng.device));
     CK(cudaStreamCreateWithFlags(&g_eng.own, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&g_eng.side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&g_eng.ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&g_eng.ev_join, cudaEventDisableTiming));
     std::call_once(g_tab_once, init_host_tables);
     CK(cudaMalloc(&g_eng.d_lfac, 1024 * sizeof(double)));
     CK(cudaMemcpy(g_eng.d_lfac, h_lfac_tab, 1024 * sizeof(double), cudaMemcpyHostToDevice));
@@ -485,7 +490,13 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     for (int c0 = 0; c0 < n; c0 += chunk) {
         const int nt = std::min(chunk, n - c0);
         CK(cudaEventRecord(g_eng.ev[0], st));
-        if (c0 == 0) launch_mie(d_xi, d_eps, nxi, caps->LbyR, lmax_mie, d_lna, d_lnb, st);
+        // the Mie coefficients (first chunk) and the scale factors do not feed the quadrature
+        // set-up or the K integrals: they run on a side stream beside them
+        if (c0 == 0) {
+            CK(cudaEventRecord(g_eng.ev_fork, st));
+            CK(cudaStreamWaitEvent(g_eng.side, g_eng.ev_fork, 0));
+            launch_mie(d_xi, d_eps, nxi, caps->LbyR, lmax_mie, d_lna, d_lnb, g_eng.side);
+        }
         // group the chunk's tasks by m: a_0, a_1, a_2 of the q-sums depend on (l1, l2, m) only
         std::map<int, int> gidx;
         std::vector<int> gm, glm;
@@ -529,7 +540,10 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         sd *d_Sa = (sd *)g_eng.Sa.get((size_t)nt * L * sizeof(sd));
         sd *d_Sb = (sd *)g_eng.Sb.get((size_t)nt * L * sizeof(sd));
         double2 *d_uv = (double2 *)g_eng.uv.get((size_t)nt * L * sizeof(double2));
-        launch_scale(d_tasks, nt, ldim, d_lna, d_lnb, lmax_mie, g_eng.d_lfac, d_Sa, d_Sb, d_uv, st);
+        CK(cudaEventRecord(g_eng.ev_fork, st)); // the chunk's task table is on the device
+        CK(cudaStreamWaitEvent(g_eng.side, g_eng.ev_fork, 0));
+        launch_scale(d_tasks, nt, ldim, d_lna, d_lnb, lmax_mie, g_eng.d_lfac, d_Sa, d_Sb, d_uv, g_eng.side);
+        CK(cudaEventRecord(g_eng.ev_join, g_eng.side));
         CK(cudaEventRecord(g_eng.ev[1], st));
 
         double *d_pM = (double *)g_eng.partM.get((size_t)nt * 2 * max_warps * nu_stride * sizeof(double));
@@ -550,6 +564,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             launch_kred(d_tasks, nt, nnu_max, d_pM, d_pE, max_warps, nu_stride, d_K, d_status, st);
         }
         CK(cudaEventRecord(g_eng.ev[2], st));
+        CK(cudaStreamWaitEvent(st, g_eng.ev_join, 0)); // Mie and scale factors from here on
 
         sd *d_I = (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
         double4 *d_ptab = (double4 *)g_eng.ptab.get((size_t)nt * 2 * pstride * sizeof(double4));
