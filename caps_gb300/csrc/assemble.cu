@@ -36,12 +36,14 @@ __global__ void k_setup(Task *tasks, int ntask, double *edges, int max_panels, d
     const int task = blockIdx.x;
     if (task >= ntask) return;
     Task &T = tasks[task];
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) { // warp 0 builds the grid
         KGridParams P = kgrid_default();
         P.c_width = c_width;
-        const int np = kgrid_build(T.alpha, T.mu, T.s, T.nu_max, P, edges + (size_t)task * (max_panels + 1), max_panels);
-        if (np < 0) { T.npanel = 0; status[task] |= ST_ERR_GRID; }
-        else T.npanel = np;
+        const int np = kgrid_build_warp(T.alpha, T.mu, T.s, T.nu_max, P, edges + (size_t)task * (max_panels + 1), max_panels);
+        if (threadIdx.x == 0) {
+            if (np < 0) { T.npanel = 0; status[task] |= ST_ERR_GRID; }
+            else T.npanel = np;
+        }
     }
     // A_nu = (2nu+1)/(nu-mu+1), B_nu = (nu+mu)/(nu-mu+1): P_{nu+1} = A x P_nu - B P_{nu-1}
     const int nnu = T.nu_max - T.mu + 1;

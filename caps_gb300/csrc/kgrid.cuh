@@ -120,4 +120,80 @@ KG_HD int kgrid_build(double alpha, int mu, int s, int nu_max, const KGridParams
     return -1;
 }
 
+#ifdef __CUDACC__
+// [lo, hi] brackets the point where a monotone predicate `below` turns from true to false;
+// each round the 32 lanes of the warp test the 32 inner points of 33 equal sub-intervals
+// and all lanes keep the sub-interval that holds the turn (5 bits per round against a
+// bisection's 1).  Every lane returns the same bracket.
+template <class F> __device__ inline void kg_warp_section(double &lo, double &hi, int rounds, F below)
+{
+    const int lane = threadIdx.x & 31;
+    for (int r = 0; r < rounds; r++) {
+        const double x = lo + (hi - lo) * (double)(lane + 1) * (1.0 / 33.0);
+        const int c = __popc(__ballot_sync(0xffffffffu, below(x)));
+        const double xl = __shfl_sync(0xffffffffu, x, c > 0 ? c - 1 : 0);
+        const double xh = __shfl_sync(0xffffffffu, x, c < 32 ? c : 31);
+        if (c > 0) lo = xl;
+        if (c < 32) hi = xh;
+    }
+}
+
+// kgrid_build for one warp (all 32 lanes call it and get the same result; lane 0 writes
+// the edges): the same grid rules, with the three root searches as warp multisections
+__device__ inline int kgrid_build_warp(double alpha, int mu, int s, int nu_max, const KGridParams &P, double *edges, int max_panels)
+{
+    const bool writer = (threadIdx.x & 31) == 0;
+    const int k = mu + 1 - 2 * s;
+    const double keff = (k <= P.kpoly) ? 0.0 : (double)(mu + 1);
+    const double r = (double)k / alpha;
+    const double u = 0.5 * (r * r + sqrt(r * r * r * r + 4 * r * r));
+    const double tp0 = asinh(sqrt(u));
+
+    double t0 = 0.0;
+    if (k > P.kpoly) {
+        // left edge: g0(t) = g0(tp0) - neg_left, in log t
+        const double gt = kg_g0(tp0, k, alpha) - P.neg_left;
+        double lo = log(tp0) - 80.0, hi = log(tp0);
+        kg_warp_section(lo, hi, 12, [&](double x) { return kg_g0(exp(x), k, alpha) < gt; });
+        t0 = exp(lo);
+    }
+
+    // peak of the highest degree: dlog = 0 (dlog decreases in t)
+    double tlo = 1e-6, thi = 1.0;
+    while (kg_dlog(thi, nu_max, mu, s, alpha) > 0 && thi < 700) thi *= 2;
+    if (kg_dlog(tlo, nu_max, mu, s, alpha) < 0) tlo = 1e-12;
+    kg_warp_section(tlo, thi, 16, [&](double x) { return kg_dlog(x, nu_max, mu, s, alpha) > 0; });
+    const double tpk = 0.5 * (tlo + thi);
+
+    int np = 0;
+    double t = t0;
+    if (writer) edges[0] = t0;
+    double drop = 0.0;
+    bool past = false;
+    while (np < max_panels) {
+        double h1 = P.c_width / sqrt(kg_kappa(t > 0 ? t : 1e-300, alpha, keff));
+        if (t == 0.0) h1 = P.c_width / sqrt(alpha);
+        const double h2 = P.c_width / sqrt(kg_kappa(t + h1, alpha, keff));
+        double h = h1 < h2 ? h1 : h2;
+        if (h2 < 0.25 * h1) {
+            // self-consistent width h = c / sqrt(kappa(t + h)) (see kgrid_build)
+            double lo = 0.0, hi = h1;
+            kg_warp_section(lo, hi, 12, [&](double x) { return x < P.c_width / sqrt(kg_kappa(t + x, alpha, keff)); });
+            if (lo > h) h = lo;
+        }
+        const double tn = t + h;
+        if (past || tn > tpk) {
+            const double a = past ? t : tpk;
+            if (tn > a) drop += 0.5 * (tn - a) * (kg_dlog(a, nu_max, mu, s, alpha) + kg_dlog(tn, nu_max, mu, s, alpha));
+            past = true;
+        }
+        t = tn;
+        ++np;
+        if (writer) edges[np] = t;
+        if (past && drop < -P.neg_right) return np;
+    }
+    return -1;
+}
+#endif
+
 } // namespace capsgpu
