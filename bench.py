@@ -338,9 +338,9 @@ def main():
                      {"bound": "hbm",
                       "kernel": "k_syrk_pipe: persistent warp-specialised tcgen05 trailing update of the FP32 delta-form "
                                 "Cholesky (256-column panels, split TF32, TMEM accumulators; the whole-trailing-matrix "
-                                "launches fed by bulk copies of split-TF32 panel images, whose k_panel_img pass is "
-                                "inside the timed interval); algorithmic bytes = target block read + written once and "
-                                "the panel rows read once, per factored matrix",
+                                "launches fed by bulk copies of split-TF32 panel images that the panel solves write); "
+                                "algorithmic bytes = target block read + written once and the panel rows read once, "
+                                "per factored matrix",
                       "achieved": syrk_gbs, "peak": hbm_peak, "unit": "GB/s",
                       "frac": syrk_gbs / hbm_peak if syrk_gbs else None,
                       "traffic": syrk_bytes / syrk_n * SYRK_DRAM_PER_ALGORITHMIC if syrk_n else None,
@@ -349,7 +349,7 @@ def main():
                       "algorithmic_bytes_per_launch": syrk_bytes / syrk_n if syrk_n else None,
                       "traffic_source": "DRAM bytes per algorithmic byte of the k_syrk_pipe launches from one ncu "
                                         "capture (profiles/k_syrk_pipe_c3.md), times this run's algorithmic bytes per "
-                                        "launch; the panel-image pass (12 bytes per panel entry) is not included",
+                                        "launch (the images are written by the panel solves, outside these launches)",
                       "fp32_accurate_tflops_factorisation": achieved}),
         "dominant_kernel": None if args.precision == "fp64" else {
             "kernel": "k_itab_grp<3> (float-float q-sums)", "phase_share_of_step": ph[2] / ph[5] if ph[5] else None,

@@ -99,19 +99,22 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
     bool bad = false;
     const int i = tid & (MB - 1), cs = tid / MB;
     for (int j = 0; j < nb; j++) {
+        // phase 1: every thread forms the pivot from T[j][j], threads j+1..nb-1 scale their
+        // entry of column j (T[j][j] itself is rewritten only in phase 2, which reads
+        // neither it nor column j of T)
         const float d = T[j][j]; // pivot - 1
         const float one_d = 1.0f + d;
         bad |= !(one_d > 0.0f);
         const float lam = d / (sqrtf(fmaxf(one_d, 1e-30f)) + 1.0f);
         const float inv = 1.0f / (1.0f + lam);
-        __syncthreads();
         if (tid > j && tid < nb) {
             const float cj = T[tid][j] * inv;
             T[tid][j] = cj;
             colj[tid] = cj;
         }
-        if (tid == 0) T[j][j] = lam;
         __syncthreads();
+        // phase 2: rank-1 update of the trailing triangle from colj
+        if (tid == 0) T[j][j] = lam;
         if (i > j && i < nb) {
             const float ci = colj[i];
             for (int c = j + 1 + cs; c <= i; c += 4) T[i][c] -= ci * colj[c];
@@ -154,8 +157,12 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
 // in shared memory k-major with row r at position 4 (r mod 16) + r / 16 and W k-major, so
 // per k a thread reads its four rows and its four columns as one float4 each for 16 FMAs.
 constexpr int MT = 64;
+// img != nullptr: rows at or below t2 (the first row of the trailing matrix of this 256-column
+// panel) also go to the panel's split-TF32 images for the whole-trailing-matrix update
+// (layout of syrk_pipe.cuh, nrb 128-row blocks per matrix); rows past n are left unwritten
+// there, they only reach accumulator rows and columns that are never stored.
 __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, const int *status,
-                                                  const float *Winv, double *fro)
+                                                  const float *Winv, double *fro, float *img, int t2, int nrb)
 {
     const int task = blockIdx.y;
     if (task >= ntask || status[task] != ST_FACTOR) return;
@@ -214,6 +221,25 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
             if (r < rows) {
                 Sm[(size_t)(k0 + c) * n + r0 + r] = acc[i][j];
                 sq = fma((double)acc[i][j], (double)acc[i][j], sq);
+            }
+        }
+    }
+    if (img) {
+        // columns 4 cg .. 4 cg + 3 of this block are one 16-byte row of a core matrix
+        const int kk = k0 % (PIPE_IMG_CH * PIPE_IMG_TK) + 4 * cg; // column within the panel
+        const int ch = kk / PIPE_IMG_TK, kq = (kk % PIPE_IMG_TK) / 4;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int r = rg + 16 * i, R = r0 + r;
+            if (r < rows && R >= t2) {
+                const int rr = R - t2, rb = rr / UM_M, q = rr % UM_M;
+                float *hi = img + (((size_t)task * nrb + rb) * PIPE_IMG_CH + ch) * 2 * PIPE_IMG_FLOATS;
+                const int e = ((q / 8) * (PIPE_IMG_TK / 4) + kq) * 32 + (q % 8) * 4;
+                float h[4], l[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) um_split(acc[i][j], h[j], l[j]);
+                *reinterpret_cast<float4 *>(hi + e) = make_float4(h[0], h[1], h[2], h[3]);
+                *reinterpret_cast<float4 *>(hi + PIPE_IMG_FLOATS + e) = make_float4(l[0], l[1], l[2], l[3]);
             }
         }
     }
@@ -509,13 +535,10 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
                                                                                              sstride, status, nullptr);
         else { // the whole trailing matrix: 128 x 128 tiles (a third less staging per entry), 32-column chunks
             const int tw = ntask * pipe_tiles<128>(nr, 0);
-            if (!reg_stage && kw <= PIPE_IMG_CH * PIPE_IMG_TK) {
-                // the panel once as split TF32 images; the update copies them in bulk
-                k_panel_img<<<dim3(nr * PIPE_IMG_CH, ntask), 256, 0, st>>>(ntask, n, k0, kw, t0, S, sstride, status, img);
-                COUNT_LAUNCH(1);
+            if (!reg_stage && kw == PIPE_IMG_CH * PIPE_IMG_TK) // the panel solves left the panel's images
                 k_syrk_pipe<128, 32, PIPE_IMG_STAGES><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_IMG, st>>>(
                     ntask, n, k0, kw, t0, cmax, 0, S, sstride, status, img);
-            } else
+            else
                 k_syrk_pipe<128, 32><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_WIDE, st>>>(ntask, n, k0, kw, t0, cmax, 0, S,
                                                                                               sstride, status, nullptr);
         }
@@ -532,14 +555,20 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         k_to_delta32<<<g, 256, 0, st>>>(ntask, n, A, lda, mstride, status, S, sstride);
         COUNT_LAUNCH(1);
     }
-    // diagonal block k0 and the panel solve below it; false when nothing lies below
-    auto factor_panel = [&](int k0) {
+    // diagonal block k0 and the panel solve below it; false when nothing lies below.  With
+    // images, the solve also writes the split-TF32 images of the rows below the 256-column
+    // panel for its whole-trailing-matrix update.
+    constexpr int PANEL = PIPE_IMG_CH * PIPE_IMG_TK; // outer panel width, 256
+    auto factor_panel = [&](int k0, bool images) {
         k_potf2_w<<<ntask, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part);
         COUNT_LAUNCH(1);
         const int rest = n - k0 - MB;
         if (rest <= 0) return false;
+        const int t2 = k0 / PANEL * PANEL + PANEL;
+        const bool im = images && t2 < n;
         dim3 gt((rest + MT - 1) / MT, ntask);
-        k_trsm_inv<<<gt, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part);
+        k_trsm_inv<<<gt, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part, im ? img : nullptr, t2,
+                                      im ? (n - t2 + UM_M - 1) / UM_M : 0);
         COUNT_LAUNCH(1);
         return true;
     };
@@ -548,11 +577,12 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         // the outer panel with them, then one K = OUTER trailing update, so the trailing
         // matrix passes through DRAM once per OUTER columns
         constexpr int OUTER = 4 * MB;
+        static_assert(OUTER == PANEL, "outer panel = image panel");
         bool more = true; // columns remain below the last factored panel
         for (int k0 = 0; k0 < n && more; k0 += OUTER) {
             // inner steps: factor 64 columns, update the rest of the outer panel with them
             for (int kj = k0; kj < k0 + OUTER; kj += MB) {
-                if (!factor_panel(kj)) { more = false; break; }
+                if (!factor_panel(kj, !reg_stage)) { more = false; break; }
                 const int t1 = kj + MB, cmax = std::min(k0 + OUTER, n);
                 if (t1 < cmax) syrk(kj, MB, t1, cmax, (cmax - t1 + UM_N - 1) / UM_N);
             }
@@ -562,7 +592,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         }
     } else {
         for (int k0 = 0; k0 < n; k0 += MB) {
-            if (!factor_panel(k0)) break;
+            if (!factor_panel(k0, false)) break;
             const int rest = n - k0 - MB, nt = (rest + 63) / 64;
             dim3 gs(nt * (nt + 1) / 2, ntask);
             if (tc)

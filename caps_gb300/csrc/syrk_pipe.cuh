@@ -87,38 +87,14 @@ __device__ __forceinline__ void pipe_stage(const float *Sm, int n, int kc, int n
 }
 
 // Panel images for the whole-trailing-matrix update (128 x 128 tiles, 32-column chunks):
-// the panel P = S[t0 .., k0 .. k0 + kw) cut into 128-row blocks and 32-column chunks, each
+// the panel P = S[t0 .., k0 .. k0 + 256) cut into 128-row blocks and 32-column chunks, each
 // chunk split into TF32 hi and lo and stored as the 16 KB image of a shared-memory slice
 // (the layout above), so that a stage is filled by four bulk copies:
 // img[(((task nrb + rb) PIPE_IMG_CH + ch) 2 + part) PIPE_IMG_FLOATS + e], nrb = ceil((n - t0) / 128).
+// The panel solves that produce P write them (k_trsm_inv in mixed.cu).
 constexpr int PIPE_IMG_TK = 32, PIPE_IMG_CH = 8, PIPE_IMG_FLOATS = UM_M * PIPE_IMG_TK, PIPE_IMG_BYTES = PIPE_IMG_FLOATS * 4;
 // bytes of image space per matrix of dimension n
 __host__ __device__ inline size_t pipe_img_bytes(int n) { return (size_t)((n + UM_M - 1) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_BYTES; }
-
-// grid (nrb PIPE_IMG_CH, ntask), 256 threads: one chunk image (hi and lo) per block, rows
-// beyond n and columns beyond kw as zeros; matrices not being factored are skipped, as the
-// update skips them
-__global__ void __launch_bounds__(256) k_panel_img(int ntask, int n, int k0, int kw, int t0, const float *S, size_t sstride,
-                                                   const int *status, float *img)
-{
-    const int nrb = (n - t0 + UM_M - 1) / UM_M;
-    const int rb = blockIdx.x / PIPE_IMG_CH, ch = blockIdx.x % PIPE_IMG_CH;
-    const int task = blockIdx.y;
-    if (rb >= nrb || task >= ntask || (status[task] & ~ST_ERR_WAIT) != ST_FACTOR) return;
-    const float *Sm = S + (size_t)task * sstride;
-    float *hi = img + (((size_t)task * nrb + rb) * PIPE_IMG_CH + ch) * 2 * PIPE_IMG_FLOATS, *lo = hi + PIPE_IMG_FLOATS;
-    constexpr int CPR = PIPE_IMG_TK / 4;
-#pragma unroll 4
-    for (int e = threadIdx.x; e < PIPE_IMG_FLOATS; e += 256) {
-        const int cm = e >> 5, w = e & 31;
-        const int row = t0 + rb * UM_M + (cm / CPR) * 8 + (w >> 2), kk = ch * PIPE_IMG_TK + (cm % CPR) * 4 + (w & 3);
-        const float x = (row < n && kk < kw) ? Sm[(size_t)(k0 + kk) * n + row] : 0.0f;
-        float h, l;
-        um_split(x, h, l);
-        hi[e] = h;
-        lo[e] = l;
-    }
-}
 
 struct PipeTile {
     int task, row0, col0;
@@ -167,7 +143,7 @@ __device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, int ncb, int n, in
 
 // S[t0.., t0..cmax) -= P P^T, P = columns k0 .. k0 + kw - 1, in 128 x TN tiles and TK-column
 // chunks; grid = min(tiles, SMs), 800 threads.  img != nullptr (128 x 128 tiles, 32-column
-// chunks only): the panel comes from its images (k_panel_img), one thread of warp 0 fills
+// chunks only): the panel comes from its images (written by the panel solves), one thread of warp 0 fills
 // each stage with four bulk copies and the other producer warps stay idle.
 template <int TN, int TK, int NS = 2>
 __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n, int k0, int kw, int t0, int cmax, int ncb,
