@@ -41,9 +41,8 @@ CAPS_DEV ff ff_div(ff x, ff y)
 struct IAcc {
     float h, l; // running sum (h + l) 2^e
     int e;
-    int thr;    // a term t stops counting as significant once exponent(t) < thr
-    int count;
-    bool on;
+    int st; // 8 thr + 2 count + on: a term t stops counting as significant once exponent(t) < thr;
+            // count = consecutive such terms, on = still summing
 };
 
 // sum += t 2^et.  The sum's exponent frame moves up (an exact power-of-two shift of the
@@ -74,9 +73,10 @@ CAPS_DEV void iacc_add(IAcc &A, ff t, int et)
 // MM entries of a diagonal 2x2 block, integration.c:762-888); each pair's sum is the one
 // the full kernel forms.  Output: I tables as float-float (ffe) or, with ffe_out false, as
 // scaled doubles.  The kernel is bound by FP32/ALU issue and the latency of float-float
-// dependency chains, so occupancy pays: at G = 3, six blocks of 128 per SM (80 registers).
+// dependency chains, so occupancy pays: at G = 3, seven blocks of 128 per SM (72 registers;
+// the stop state of an accumulator packed into one register).
 template <int G, bool BAND>
-__global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim,
+__global__ void __launch_bounds__(128, 7) k_itab_grp(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim,
                                                   const ffe *__restrict__ KF, int nu_stride, const float4 *__restrict__ ptabf,
                                                   int pstride, const A012F *__restrict__ a12, void *Iout, bool ffe_out,
                                                   int *status, int stop_bits)
@@ -145,10 +145,10 @@ __global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const in
     for (int j = 0; j < 2 * G; j++) {
         const bool live = (j >> 1) < ng && ((j & 1) == 0 || both);
         IAcc &A = acc[j];
-        A = IAcc{0.0f, 0.0f, 0, 0, 0, live};
+        A = IAcc{0.0f, 0.0f, 0, 0};
         if (!live) continue;
         const ffe k0 = Kat(j, l12);
-        A.h = k0.h; A.l = k0.l; A.e = k0.e; A.thr = fexpo(k0.h) + k0.e - stop_bits;
+        A.h = k0.h; A.l = k0.l; A.e = k0.e; A.st = (fexpo(k0.h) + k0.e - stop_bits) * 8 + 1;
         if (qmax >= 1) { const ffe k = Kat(j, l12 - 2); iacc_add(A, ff_mul(a1f, ff{k.h, k.l}), k.e); }
         if (qmax >= 2) { const ffe k = Kat(j, l12 - 4); iacc_add(A, ff_mul(a2f, ff{k.h, k.l}), k.e); }
     }
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const in
 #pragma unroll
             for (int j = 0; j < 2 * G; j++) {
                 IAcc &A = acc[j];
-                if (!A.on) continue;
+                if (!(A.st & 1)) continue;
                 const ffe Kv = Kat(j, ip);
                 const ff t = ff_mul(aq, ff{Kv.h, Kv.l});
                 const int et = ea + Kv.e;
@@ -217,9 +217,9 @@ __global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const in
                 // exponent(t) < exponent(q=0 term) - stop_bits: |t| below 2^-stop_bits of the
                 // q = 0 term (and above 2^-stop_bits-2 of it when not); a zero term counts as
                 // below, as log 0 = -inf does in the reference's test
-                if (fexpo(t.h) + et < A.thr) { if (++A.count >= 3) A.on = false; }
-                else A.count = 0;
-                any |= A.on;
+                const int cnt = fexpo(t.h) + et < (A.st >> 3) ? ((A.st >> 1) & 3) + 1 : 0;
+                A.st = (A.st & ~7) | (cnt << 1) | (cnt < 3 ? 1 : 0);
+                any |= (A.st & 1) != 0;
             }
         }
     }
@@ -249,10 +249,13 @@ __global__ void __launch_bounds__(128, 6) k_itab_grp(const Task *tasks, const in
     }
 }
 
-// tasks per subgroup.  q-sums of the R/L=150 free energy (ms): G = 3 at six blocks per
-// SM 119.7, at five 123.8, at seven 122.3; G = 2 at seven 124.1, at five 136.6; G = 4
-// at five 134.6, at six 137.9.  More tasks share the recurrence, but the registers
-// cost occupancy and a subgroup runs to the term count of its slowest frequency.
+// tasks per subgroup.  q-sums of the R/L=150 free energy (ms), first float-float version:
+// G = 3 at six blocks per SM 119.7, at five 123.8, at seven 122.3; G = 2 at seven 124.1, at
+// five 136.6; G = 4 at five 134.6, at six 137.9.  With the packed stop state and the trace
+// rule first (q-sum phase of the undecided matrices): G = 3 at seven 57.1, at six 59.3, at
+// eight 57.7; G = 4 at six 61.0, at five 62.9; G = 2 at seven 62.0, at eight 62.3.  More
+// tasks share the recurrence, but the registers cost occupancy and a subgroup runs to the
+// term count of its slowest frequency.
 constexpr int IGRP = 3;
 constexpr int ITAB_STOP_BITS = 44; // early stop below 2^-44 of the q = 0 term
 int itab_group_size() { return IGRP; }
