@@ -241,15 +241,28 @@ __global__ void k_stats_ff(const int *tlist, int nlist, int ldim, const double *
             __syncthreads();
         }
     }
-    if (threadIdx.x != 0) return;
+    if (threadIdx.x >= 32) return;
+    // Kahan trace (misc.c:26) over the diagonal, split across the 32 lanes of warp 0: lane l
+    // sums the l-th contiguous chunk, lane 0 then adds the 32 compensated partials in order
     const double *dg = diag + (size_t)task * n;
+    const int lane = threadIdx.x, per = (n + 31) / 32;
     double tr = 0.0, c = 0.0;
-    for (int i = 0; i < n; i++) {
+    for (int i = lane * per; i < min(n, (lane + 1) * per); i++) {
         const double y = dg[i] - c;
         const double t = tr + y;
         c = (t - tr) - y;
         tr = t;
     }
+    const double partial = tr - c;
+    tr = 0.0;
+    c = 0.0;
+    for (int l = 0; l < 32; l++) {
+        const double y = __shfl_sync(0xffffffffu, partial, l) - c;
+        const double t = tr + y;
+        c = (t - tr) - y;
+        tr = t;
+    }
+    if (lane != 0) return;
     trace_out[task] = tr;
     if (status[task] & ~0xF) { result[task] = NAN; return; }
     if (fabs(tr) < 1e-8) { result[task] = -tr; status[task] = ST_TRACE; return; }
