@@ -264,8 +264,10 @@ k_ktab_ff(const Task *tasks, const double *edges, int max_panels, const float4 *
         for (int r = 0; r < rows; r++) {
             const int e = (pc.h != 0.0f) ? fexpo(pc.h) + E : -(1 << 29);
             const int emax = __reduce_max_sync(0xffffffffu, e);
-            const int d = E - emax;
-            const ff v = (pc.h != 0.0f && d > -100) ? ff_shift(pc, d) : ff{0.0f, 0.0f};
+            // align to the warp maximum by one multiply with 2^(E - emax) (0 below 2^-126; the
+            // clamp at 2^127 only matters for a zero value, which stays zero)
+            const float p2 = __uint_as_float((unsigned)min(max(127 + E - emax, 0), 254) << 23);
+            const ff v{pc.h * p2, pc.l * p2};
             buf[r * 33 + lane] = make_float2(v.h, v.l);
             if (lane == 0) rowE[r] = emax;
             const float4 c = __ldg(ab + base + r);
