@@ -159,10 +159,13 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
 constexpr int MT = 64;
 // img != nullptr: rows at or below t2 (the first row of the trailing matrix of this 256-column
 // panel) also go to the panel's split-TF32 images for the whole-trailing-matrix update
-// (layout of syrk_pipe.cuh, nrb 128-row blocks per matrix); rows past n are left unwritten
-// there, they only reach accumulator rows and columns that are never stored.
+// (layout of syrk_pipe.cuh, nrb 128-row blocks per matrix); img64 != nullptr: every row goes
+// to the 64-column images for the update of the rest of the panel (nrb64 64-row blocks).
+// Rows past n are left unwritten there; they only reach accumulator rows and columns that
+// are never stored.
 __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, const int *status,
-                                                  const float *Winv, double *fro, float *img, int t2, int nrb)
+                                                  const float *Winv, double *fro, float *img, int t2, int nrb, float *img64,
+                                                  int nrb64)
 {
     const int task = blockIdx.y;
     if (task >= ntask || status[task] != ST_FACTOR) return;
@@ -240,6 +243,22 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
                 for (int j = 0; j < 4; j++) um_split(acc[i][j], h[j], l[j]);
                 *reinterpret_cast<float4 *>(hi + e) = make_float4(h[0], h[1], h[2], h[3]);
                 *reinterpret_cast<float4 *>(hi + PIPE_IMG_FLOATS + e) = make_float4(l[0], l[1], l[2], l[3]);
+            }
+        }
+    }
+    if (img64) {
+        // this block's 64 rows are 64-row block blockIdx.x of the image (rows from k0 + 64)
+        float *hi = img64 + ((size_t)task * 2 * nrb64 + blockIdx.x) * PIPE_IMG64_FLOATS;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int r = rg + 16 * i;
+            if (r < rows) {
+                const int e = ((r / 8) * 16 + cg) * 32 + (r % 8) * 4;
+                float h[4], l[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) um_split(acc[i][j], h[j], l[j]);
+                *reinterpret_cast<float4 *>(hi + e) = make_float4(h[0], h[1], h[2], h[3]);
+                *reinterpret_cast<float4 *>(hi + (size_t)nrb64 * PIPE_IMG64_FLOATS + e) = make_float4(l[0], l[1], l[2], l[3]);
             }
         }
     }
@@ -488,7 +507,10 @@ static size_t mixed_img_offset(int ntask, int n)
 {
     return ((size_t)ntask * (MB * MB * sizeof(float) + fro_slots(n) * sizeof(double)) + 255) / 256 * 256;
 }
-size_t mixed_work_bytes(int ntask, int n) { return mixed_img_offset(ntask, n) + (size_t)ntask * pipe_img_bytes(n); }
+size_t mixed_work_bytes(int ntask, int n)
+{
+    return mixed_img_offset(ntask, n) + (size_t)ntask * (pipe_img_bytes(n) + pipe_img64_bytes(n));
+}
 
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
                            const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc, bool convert,
@@ -499,6 +521,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     float *Winv = (float *)work;
     double *part = (double *)((char *)work + (size_t)ntask * MB * MB * sizeof(float));
     float *img = (float *)((char *)work + mixed_img_offset(ntask, n));
+    float *img64 = img + (size_t)ntask * pipe_img_bytes(n) / 4;
     CK(cudaMemsetAsync(part, 0, (size_t)ntask * fro_slots(n) * sizeof(double), st));
     // convert: A is the FP64 matrix 1 - M and S receives its delta form here; otherwise S
     // already holds it.  mdiag: M_ii in FP64, n per task (tr(A - I) = -tr M).
@@ -530,9 +553,9 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         if (no_pipe)
             k_syrk_umma<<<dim3(ncb == 1 ? nr : nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb == 1,
                                                                                                  S, sstride, status);
-        else if (ncb > 0) // the rest of an outer panel: 128 x 64 tiles, 64-column chunks
+        else if (ncb > 0) // the rest of an outer panel: 128 x 64 tiles, 64-column chunks (images of the panel solve)
             k_syrk_pipe<64, 64><<<std::min(ntask * tpt, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb, S,
-                                                                                             sstride, status, nullptr);
+                                                                                             sstride, status, reg_stage ? nullptr : img64);
         else { // the whole trailing matrix: 128 x 128 tiles (a third less staging per entry), 32-column chunks
             const int tw = ntask * pipe_tiles<128>(nr, 0);
             if (!reg_stage && kw == PIPE_IMG_CH * PIPE_IMG_TK) // the panel solves left the panel's images
@@ -566,9 +589,12 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         if (rest <= 0) return false;
         const int t2 = k0 / PANEL * PANEL + PANEL;
         const bool im = images && t2 < n;
+        // the rest of the panel is updated after this step when columns remain before t2
+        const bool im64 = images && k0 + MB < std::min(t2, n);
         dim3 gt((rest + MT - 1) / MT, ntask);
         k_trsm_inv<<<gt, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part, im ? img : nullptr, t2,
-                                      im ? (n - t2 + UM_M - 1) / UM_M : 0);
+                                      im ? (n - t2 + UM_M - 1) / UM_M : 0, im64 ? img64 : nullptr,
+                                      2 * ((rest + UM_M - 1) / UM_M));
         COUNT_LAUNCH(1);
         return true;
     };

@@ -95,6 +95,12 @@ __device__ __forceinline__ void pipe_stage(const float *Sm, int n, int kc, int n
 constexpr int PIPE_IMG_TK = 32, PIPE_IMG_CH = 8, PIPE_IMG_FLOATS = UM_M * PIPE_IMG_TK, PIPE_IMG_BYTES = PIPE_IMG_FLOATS * 4;
 // bytes of image space per matrix of dimension n
 __host__ __device__ inline size_t pipe_img_bytes(int n) { return (size_t)((n + UM_M - 1) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_BYTES; }
+// Images for the update of the rest of a 256-column panel (128 x 64 tiles, one 64-column
+// chunk): the 64-column panel of one step, rows t0 .., cut into 64-row blocks of 16 KB, all
+// hi blocks of a matrix and then all lo blocks, so that a 128-row slice is two consecutive
+// blocks: img[((task 2 + part) nrb64 + rb) PIPE_IMG64_FLOATS + e], nrb64 = 2 ceil((n - t0) / 128).
+constexpr int PIPE_IMG64_FLOATS = 64 * 64;
+__host__ __device__ inline size_t pipe_img64_bytes(int n) { return (size_t)2 * 2 * ((n + UM_M - 1) / UM_M) * PIPE_IMG64_FLOATS * 4; }
 
 struct PipeTile {
     int task, row0, col0;
@@ -142,9 +148,10 @@ __device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, int ncb, int n, in
 }
 
 // S[t0.., t0..cmax) -= P P^T, P = columns k0 .. k0 + kw - 1, in 128 x TN tiles and TK-column
-// chunks; grid = min(tiles, SMs), 800 threads.  img != nullptr (128 x 128 tiles, 32-column
-// chunks only): the panel comes from its images (written by the panel solves), one thread of warp 0 fills
-// each stage with four bulk copies and the other producer warps stay idle.
+// chunks; grid = min(tiles, SMs), 800 threads.  img != nullptr (128 x 128 tiles with 32-column
+// chunks, or 128 x 64 tiles with one 64-column chunk): the panel comes from its images
+// (written by the panel solves), one thread of warp 0 fills each stage with four bulk copies
+// and the other producer warps stay idle.
 template <int TN, int TK, int NS = 2>
 __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n, int k0, int kw, int t0, int cmax, int ncb,
                                                                float *S, size_t sstride, int *status, const float *img)
@@ -179,7 +186,9 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
 
     if (warp < PIPE_PRODUCER_WARPS && img) {
         // ---- producer: bulk copies of the panel images (one thread) ----
-        if constexpr (TN == UM_M && TK == PIPE_IMG_TK) {
+        constexpr bool WIDE = TN == UM_M && TK == PIPE_IMG_TK; // whole trailing matrix
+        constexpr bool REST = TN == 64 && TK == 64;            // rest of a 256-column panel
+        if constexpr (WIDE || REST) {
             if (tid == 0) {
                 int it = 0, last[NS];
                 for (int s = 0; s < NS; s++) last[s] = -1;
@@ -187,9 +196,22 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
                 for (int t = blockIdx.x; ok && t < ntile; t += gridDim.x) {
                     const PipeTile T = pipe_tile<TN>(t, tpt, ncb, n, t0, cend, status);
                     if (!T.valid) continue;
-                    const float *ia = img + ((size_t)T.task * nr + (T.row0 - t0) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_FLOATS;
-                    const float *ib = img + ((size_t)T.task * nr + (T.col0 - t0) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_FLOATS;
                     for (int ch = 0; ch < nchunk; ch++, it++) {
+                        const float *ahi, *alo, *bhi, *blo;
+                        if constexpr (WIDE) {
+                            const size_t o = (size_t)ch * 2 * PIPE_IMG_FLOATS;
+                            ahi = img + ((size_t)T.task * nr + (T.row0 - t0) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_FLOATS + o;
+                            bhi = img + ((size_t)T.task * nr + (T.col0 - t0) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_FLOATS + o;
+                            alo = ahi + PIPE_IMG_FLOATS;
+                            blo = bhi + PIPE_IMG_FLOATS;
+                        } else {
+                            const size_t nrb64 = 2 * (size_t)nr;
+                            const float *hi0 = img + (size_t)T.task * 2 * nrb64 * PIPE_IMG64_FLOATS;
+                            ahi = hi0 + (size_t)((T.row0 - t0) / 64) * PIPE_IMG64_FLOATS;
+                            bhi = hi0 + (size_t)((T.col0 - t0) / 64) * PIPE_IMG64_FLOATS;
+                            alo = ahi + nrb64 * PIPE_IMG64_FLOATS;
+                            blo = bhi + nrb64 * PIPE_IMG64_FLOATS;
+                        }
                         const int s = it % NS, use = it / NS;
                         if (use > 0 && !umma::mbar_wait(&empty[s], (use - 1) & 1, PIPE_WAIT_ITERS)) {
                             ok = false;
@@ -197,12 +219,11 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
                             break;
                         }
                         float *st = pipe_sm + s * Shape::STAGE;
-                        const size_t o = (size_t)ch * 2 * PIPE_IMG_FLOATS;
-                        umma::mbar_arrive_tx(&full[s], 4 * PIPE_IMG_BYTES);
-                        umma::bulk_g2s(st, ia + o, PIPE_IMG_BYTES, &full[s]);
-                        umma::bulk_g2s(st + PA, ia + o + PIPE_IMG_FLOATS, PIPE_IMG_BYTES, &full[s]);
-                        umma::bulk_g2s(st + 2 * PA, ib + o, PIPE_IMG_BYTES, &full[s]);
-                        umma::bulk_g2s(st + 2 * PA + PB, ib + o + PIPE_IMG_FLOATS, PIPE_IMG_BYTES, &full[s]);
+                        umma::mbar_arrive_tx(&full[s], 2 * (PA + PB) * 4);
+                        umma::bulk_g2s(st, ahi, PA * 4, &full[s]);
+                        umma::bulk_g2s(st + PA, alo, PA * 4, &full[s]);
+                        umma::bulk_g2s(st + 2 * PA, bhi, PB * 4, &full[s]);
+                        umma::bulk_g2s(st + 2 * PA + PB, blo, PB * 4, &full[s]);
                         last[s] = use;
                     }
                 }
