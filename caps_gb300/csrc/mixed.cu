@@ -162,10 +162,12 @@ constexpr int MT = 64;
 // (layout of syrk_pipe.cuh, nrb 128-row blocks per matrix); img64 != nullptr: every row goes
 // to the 64-column images for the update of the rest of the panel (nrb64 64-row blocks).
 // Rows past n are left unwritten there; they only reach accumulator rows and columns that
-// are never stored.
+// are never stored.  store_x false: X is not written back to S (with both images, nothing
+// reads it there again: later steps read S only in their own columns, the final sums only
+// its diagonal).
 __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, const int *status,
                                                   const float *Winv, double *fro, float *img, int t2, int nrb, float *img64,
-                                                  int nrb64)
+                                                  int nrb64, bool store_x)
 {
     const int task = blockIdx.y;
     if (task >= ntask || status[task] != ST_FACTOR) return;
@@ -222,7 +224,7 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
         for (int i = 0; i < 4; i++) {
             const int r = rg + 16 * i;
             if (r < rows) {
-                Sm[(size_t)(k0 + c) * n + r0 + r] = acc[i][j];
+                if (store_x) Sm[(size_t)(k0 + c) * n + r0 + r] = acc[i][j];
                 sq = fma((double)acc[i][j], (double)acc[i][j], sq);
             }
         }
@@ -532,6 +534,9 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     // CAPS_MIXED_REGSTAGE=1: the whole-trailing-matrix update stages the panel through
     // registers (16 producer warps) instead of copying prepared images
     static const bool reg_stage = getenv("CAPS_MIXED_REGSTAGE") != nullptr;
+    // the persistent updates read the panel from images that the panel solves write (and X
+    // then stays out of S); the register-staged and one-CTA-per-tile updates read S
+    const bool use_img = !reg_stage && !no_pipe;
     static bool attr = false;
     static int nsm = 1;
     if (!attr) {
@@ -555,10 +560,10 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
                                                                                                  S, sstride, status);
         else if (ncb > 0) // the rest of an outer panel: 128 x 64 tiles, 64-column chunks (images of the panel solve)
             k_syrk_pipe<64, 64><<<std::min(ntask * tpt, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb, S,
-                                                                                             sstride, status, reg_stage ? nullptr : img64);
+                                                                                             sstride, status, use_img ? img64 : nullptr);
         else { // the whole trailing matrix: 128 x 128 tiles (a third less staging per entry), 32-column chunks
             const int tw = ntask * pipe_tiles<128>(nr, 0);
-            if (!reg_stage && kw == PIPE_IMG_CH * PIPE_IMG_TK) // the panel solves left the panel's images
+            if (use_img && kw == PIPE_IMG_CH * PIPE_IMG_TK) // the panel solves left the panel's images
                 k_syrk_pipe<128, 32, PIPE_IMG_STAGES><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_IMG, st>>>(
                     ntask, n, k0, kw, t0, cmax, 0, S, sstride, status, img);
             else
@@ -594,7 +599,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         dim3 gt((rest + MT - 1) / MT, ntask);
         k_trsm_inv<<<gt, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part, im ? img : nullptr, t2,
                                       im ? (n - t2 + UM_M - 1) / UM_M : 0, im64 ? img64 : nullptr,
-                                      2 * ((rest + UM_M - 1) / UM_M));
+                                      2 * ((rest + UM_M - 1) / UM_M), !images);
         COUNT_LAUNCH(1);
         return true;
     };
@@ -608,7 +613,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         for (int k0 = 0; k0 < n && more; k0 += OUTER) {
             // inner steps: factor 64 columns, update the rest of the outer panel with them
             for (int kj = k0; kj < k0 + OUTER; kj += MB) {
-                if (!factor_panel(kj, !reg_stage)) { more = false; break; }
+                if (!factor_panel(kj, use_img)) { more = false; break; }
                 const int t1 = kj + MB, cmax = std::min(k0 + OUTER, n);
                 if (t1 < cmax) syrk(kj, MB, t1, cmax, (cmax - t1 + UM_N - 1) / UM_N);
             }

@@ -128,3 +128,37 @@ def test_mixed_trace_rule_first(cg):
             assert abs(a - b) <= TOL_MIXED * max(1.0, abs(b)), (x, m, a, b)
     for k in np.random.default_rng(5).permutation(len(X))[:6]:
         assert out[k] == c.logdetD(X[k], M[k]), (X[k], M[k])
+
+
+@pytest.mark.parametrize("variant", ["", "CAPS_MIXED_REGSTAGE", "CAPS_MIXED_NOPIPE", "CAPS_MIXED_MMASYNC", "CAPS_MIXED_SIMT"])
+def test_mixed_update_variants(variant):
+    """Every trailing-update variant of the mixed factorisation (image-fed persistent
+    kernels by default; register staging, one CTA per tile, the single-level mma.sync and
+    FFMA forms behind environment switches, read once per process) against the FP64 form,
+    on matrices of dimension 700 (two 256-column panels and a partial third)."""
+    import json
+    import os
+    import subprocess
+    import sys
+    code = (
+        "import json, caps_gb300 as cg\n"
+        "c = cg.Caps(50e-6, 1e-6, ldim=350)\n"
+        "c.set_drude(9.0, 0.035)\n"
+        "x = [0.8, 3.0, 3.0, 12.0]; m = [0, 0, 7, 2]\n"
+        "ref, _ = c.logdetD_batch(x, m)\n"
+        "c.set_precision(cg.PREC_MIXED)\n"
+        "out, st = c.logdetD_batch(x, m)\n"
+        "print(json.dumps({'ref': list(ref), 'out': list(out), 'st': [int(s) for s in st]}))\n")
+    env = dict(os.environ)
+    for k in ["CAPS_MIXED_REGSTAGE", "CAPS_MIXED_NOPIPE", "CAPS_MIXED_MMASYNC", "CAPS_MIXED_SIMT"]:
+        env.pop(k, None)
+    if variant:
+        env[variant] = "1"
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env["PYTHONPATH"] = root + os.pathsep + env.get("PYTHONPATH", "")
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert all(s == 3 for s in d["st"]), d["st"]  # all factored
+    for a, b in zip(d["out"], d["ref"]):
+        assert abs(a - b) <= TOL_MIXED * max(1.0, abs(b)), (variant, a, b)
