@@ -160,14 +160,15 @@ constexpr int MT = 64;
 // img != nullptr: rows at or below t2 (the first row of the trailing matrix of this 256-column
 // panel) also go to the panel's split-TF32 images for the whole-trailing-matrix update
 // (layout of syrk_pipe.cuh, nrb 128-row blocks per matrix); img64 != nullptr: every row goes
-// to the 64-column images for the update of the rest of the panel (nrb64 64-row blocks).
+// to the image of 64-column block blk64 of the panel for the left-looking updates of the
+// later blocks (layout of syrk_pipe.cuh).
 // Rows past n are left unwritten there; they only reach accumulator rows and columns that
 // are never stored.  store_x false: X is not written back to S (with both images, nothing
 // reads it there again: later steps read S only in their own columns, the final sums only
 // its diagonal).
 __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, const int *status,
                                                   const float *Winv, double *fro, float *img, int t2, int nrb, float *img64,
-                                                  int nrb64, bool store_x)
+                                                  int blk64, bool store_x)
 {
     const int task = blockIdx.y;
     if (task >= ntask || status[task] != ST_FACTOR) return;
@@ -250,7 +251,8 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
     }
     if (img64) {
         // this block's 64 rows are 64-row block blockIdx.x of the image (rows from k0 + 64)
-        float *hi = img64 + ((size_t)task * 2 * nrb64 + blockIdx.x) * PIPE_IMG64_FLOATS;
+        const int nrb64 = pipe_img64_nrb(n);
+        float *hi = img64 + (((size_t)blk64 * ntask + task) * 2 * nrb64 + blockIdx.x) * PIPE_IMG64_FLOATS;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const int r = rg + 16 * i;
@@ -558,7 +560,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         if (no_pipe)
             k_syrk_umma<<<dim3(ncb == 1 ? nr : nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb == 1,
                                                                                                  S, sstride, status);
-        else if (ncb > 0) // the rest of an outer panel: 128 x 64 tiles, 64-column chunks (images of the panel solve)
+        else if (ncb > 0) // one 64-column block from the panel's earlier blocks: 128 x 64 tiles, 64-column chunks
             k_syrk_pipe<64, 64><<<std::min(ntask * tpt, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb, S,
                                                                                              sstride, status, use_img ? img64 : nullptr);
         else { // the whole trailing matrix: 128 x 128 tiles (a third less staging per entry), 32-column chunks
@@ -594,28 +596,27 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         if (rest <= 0) return false;
         const int t2 = k0 / PANEL * PANEL + PANEL;
         const bool im = images && t2 < n;
-        // the rest of the panel is updated after this step when columns remain before t2
-        const bool im64 = images && k0 + MB < std::min(t2, n);
+        // later blocks of this panel are updated with this one when columns remain before t2
+        const int blk = (k0 % PANEL) / MB;
+        const bool im64 = images && blk < PIPE_IMG64_BLOCKS && k0 + MB < std::min(t2, n);
         dim3 gt((rest + MT - 1) / MT, ntask);
         k_trsm_inv<<<gt, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part, im ? img : nullptr, t2,
-                                      im ? (n - t2 + UM_M - 1) / UM_M : 0, im64 ? img64 : nullptr,
-                                      2 * ((rest + UM_M - 1) / UM_M), !images);
+                                      im ? (n - t2 + UM_M - 1) / UM_M : 0, im64 ? img64 : nullptr, blk, !images);
         COUNT_LAUNCH(1);
         return true;
     };
     if (tc && !legacy_mma) {
-        // two-level panels of OUTER columns: factor 64 columns at a time and update the rest of
-        // the outer panel with them, then one K = OUTER trailing update, so the trailing
+        // two-level panels of OUTER columns: factor 64 columns at a time, each first updated
+        // with the panel's earlier blocks (left-looking, so every column block of S passes
+        // through the update once), then one K = OUTER trailing update, so the trailing
         // matrix passes through DRAM once per OUTER columns
         constexpr int OUTER = 4 * MB;
-        static_assert(OUTER == PANEL, "outer panel = image panel");
+        static_assert(OUTER == PANEL && OUTER / MB - 1 == PIPE_IMG64_BLOCKS, "outer panel = image panel");
         bool more = true; // columns remain below the last factored panel
         for (int k0 = 0; k0 < n && more; k0 += OUTER) {
-            // inner steps: factor 64 columns, update the rest of the outer panel with them
             for (int kj = k0; kj < k0 + OUTER; kj += MB) {
+                if (kj > k0) syrk(k0, kj - k0, kj, std::min(kj + MB, n), 1);
                 if (!factor_panel(kj, use_img)) { more = false; break; }
-                const int t1 = kj + MB, cmax = std::min(k0 + OUTER, n);
-                if (t1 < cmax) syrk(kj, MB, t1, cmax, (cmax - t1 + UM_N - 1) / UM_N);
             }
             const int t2 = k0 + OUTER;
             if (!more || t2 >= n) break;

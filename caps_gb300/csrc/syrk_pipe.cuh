@@ -95,12 +95,18 @@ __device__ __forceinline__ void pipe_stage(const float *Sm, int n, int kc, int n
 constexpr int PIPE_IMG_TK = 32, PIPE_IMG_CH = 8, PIPE_IMG_FLOATS = UM_M * PIPE_IMG_TK, PIPE_IMG_BYTES = PIPE_IMG_FLOATS * 4;
 // bytes of image space per matrix of dimension n
 __host__ __device__ inline size_t pipe_img_bytes(int n) { return (size_t)((n + UM_M - 1) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_BYTES; }
-// Images for the update of the rest of a 256-column panel (128 x 64 tiles, one 64-column
-// chunk): the 64-column panel of one step, rows t0 .., cut into 64-row blocks of 16 KB, all
-// hi blocks of a matrix and then all lo blocks, so that a 128-row slice is two consecutive
-// blocks: img[((task 2 + part) nrb64 + rb) PIPE_IMG64_FLOATS + e], nrb64 = 2 ceil((n - t0) / 128).
-constexpr int PIPE_IMG64_FLOATS = 64 * 64;
-__host__ __device__ inline size_t pipe_img64_bytes(int n) { return (size_t)2 * 2 * ((n + UM_M - 1) / UM_M) * PIPE_IMG64_FLOATS * 4; }
+// Images for the left-looking updates inside a 256-column panel (128 x 64 tiles, 64-column
+// chunks): 64-column block b = 0, 1, 2 of the panel (columns k0 + 64 b ..), rows from
+// t1 = k0 + 64 (b + 1), cut into 64-row blocks of 16 KB, all hi blocks of a matrix and then
+// all lo blocks, so that a 128-row slice is two consecutive blocks:
+// img[(((b ntask + task) 2 + part) PIPE_IMG64_NRB(n) + rb) PIPE_IMG64_FLOATS + e].  The update of
+// block j reads chunk b < j from block b's image.
+constexpr int PIPE_IMG64_FLOATS = 64 * 64, PIPE_IMG64_BLOCKS = 3;
+__host__ __device__ inline int pipe_img64_nrb(int n) { return 2 * ((n + UM_M - 1) / UM_M) + 2; }
+__host__ __device__ inline size_t pipe_img64_bytes(int n)
+{
+    return (size_t)PIPE_IMG64_BLOCKS * 2 * pipe_img64_nrb(n) * PIPE_IMG64_FLOATS * 4;
+}
 
 struct PipeTile {
     int task, row0, col0;
@@ -205,10 +211,12 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
                             alo = ahi + PIPE_IMG_FLOATS;
                             blo = bhi + PIPE_IMG_FLOATS;
                         } else {
-                            const size_t nrb64 = 2 * (size_t)nr;
-                            const float *hi0 = img + (size_t)T.task * 2 * nrb64 * PIPE_IMG64_FLOATS;
-                            ahi = hi0 + (size_t)((T.row0 - t0) / 64) * PIPE_IMG64_FLOATS;
-                            bhi = hi0 + (size_t)((T.col0 - t0) / 64) * PIPE_IMG64_FLOATS;
+                            // chunk ch is panel block ch, its image rows counted from k0 + 64 (ch + 1)
+                            const size_t nrb64 = pipe_img64_nrb(n);
+                            const int t1 = k0 + 64 * (ch + 1);
+                            const float *hi0 = img + ((size_t)ch * ntask + T.task) * 2 * nrb64 * PIPE_IMG64_FLOATS;
+                            ahi = hi0 + (size_t)((T.row0 - t1) / 64) * PIPE_IMG64_FLOATS;
+                            bhi = hi0 + (size_t)((T.col0 - t1) / 64) * PIPE_IMG64_FLOATS;
                             alo = ahi + nrb64 * PIPE_IMG64_FLOATS;
                             blo = bhi + nrb64 * PIPE_IMG64_FLOATS;
                         }
