@@ -504,8 +504,15 @@ __global__ void k_a12(const int *group_m, const int *group_lmin, int ngroup, int
 // differs from the reference's at the ulp level, far below the mixed form's 2^-44; the
 // FP64 form keeps k_a12.  The mixed table is written as float-float (A012F), so the
 // q-sum kernel needs no FP64 instruction.
-struct A12L { double F1, F2; sd eG; };             // per l, index l - (lmin - 1)
-struct A12J { double h1, pa, pb, pc; sd eH; };     // per l1 + l2, index l1 + l2 - 2(lmin - 1)
+// per-m tables of the mixed form, formed in FP64 and stored as float-float
+struct A12L { ff F1, F2; ffe eG; };         // per l, index l - (lmin - 1)
+struct A12J { ff h1, pa, pb, pc; ffe eH; }; // per l1 + l2, index l1 + l2 - 2(lmin - 1)
+CAPS_DEV ffe ffe_from_sd(sd v)
+{
+    if (v.m == 0.0) return ffe{0.0f, 0.0f, FFE_ZERO_E, 0};
+    const ff x = ff_from_d(v.m);
+    return ffe{x.h, x.l, v.e, 0};
+}
 
 // grid (ceil((2L-1)/128), ngroup)
 __global__ void k_a12_tabs(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *__restrict__ lft,
@@ -520,17 +527,18 @@ __global__ void k_a12_tabs(const int *group_m, const int *group_lmin, int ngroup
         const int l = l0 + i;
         const double dl = l, u = m - dl;
         const double F1 = u * (u + 1) / (2 * dl - 1);
-        A12L r{F1, F1 * (u + 2) * (u + 3) / (2 * dl - 3), sd{0.0, 0}};
-        if (l >= mm) r.eG = sd_from_log(__ldg(lft + 2 * l) - __ldg(lft + l) - __ldg(lft + l - mm), 1);
-        tl[(size_t)g * L + i] = r;
+        sd eG{0.0, 0};
+        if (l >= mm) eG = sd_from_log(__ldg(lft + 2 * l) - __ldg(lft + l) - __ldg(lft + l - mm), 1);
+        tl[(size_t)g * L + i] = A12L{ff_from_d(F1), ff_from_d(F1 * (u + 2) * (u + 3) / (2 * dl - 3)), ffe_from_sd(eG)};
     }
     const int j = 2 * l0 + i, n4 = j - 2 * mm;
     const double s = 2.0 * j, q = (double)n4 * (n4 - 1);
-    A12J r{0.0, (s - 1) * (s - 7) / 4, 0.0, 0.0, sd{0.0, 0}};
-    if (n4 >= 2) { r.h1 = (s - 1) / q; r.pb = (s - 3) / q; }
-    if (n4 >= 4) r.pc = (s - 5) / (2.0 * (n4 - 2) * (n4 - 3));
-    if (n4 >= 0) r.eH = sd_from_log(__ldg(lft + j) - __ldg(lft + 2 * j) + __ldg(lft + n4), 1);
-    tj[(size_t)g * NJ + i] = r;
+    double h1 = 0.0, pb = 0.0, pc = 0.0;
+    sd eH{0.0, 0};
+    if (n4 >= 2) { h1 = (s - 1) / q; pb = (s - 3) / q; }
+    if (n4 >= 4) pc = (s - 5) / (2.0 * (n4 - 2) * (n4 - 3));
+    if (n4 >= 0) eH = sd_from_log(__ldg(lft + j) - __ldg(lft + 2 * j) + __ldg(lft + n4), 1);
+    tj[(size_t)g * NJ + i] = A12J{ff_from_d(h1), ff_from_d((s - 1) * (s - 7) / 4), ff_from_d(pb), ff_from_d(pc), ffe_from_sd(eH)};
 }
 
 // grid (ceil(npair/128), nlist) or, for the band (l1 - l2 in {0, 2}, the pairs the diagonal
@@ -565,17 +573,25 @@ __global__ void k_a12_mix(const int *group_m, const int *group_lmin, const int *
     A012F r{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0, 0};
     if (!(l2 < mm || l2 < mt || l1 < 1)) {
         const int qmax = min(min(l1, l2), (l1 + l2 - 2 * mm) / 2);
+        // the closed forms of a_0, a_1, a_2 in float-float (FP32 pipe) from the per-m tables
         const A12L x = tl[(size_t)g * L + a1], y = tl[(size_t)g * L + a2];
         const A12J z = tj[(size_t)g * NJ + a1 + a2];
-        const sd a0 = sd_mul(sd_mul(x.eG, y.eG), z.eH);
-        const ff a0f = ff_from_d(a0.m);
-        r.a0h = a0f.h;
-        r.a0l = a0f.l;
-        r.a0e = a0.e;
-        const double f = x.F1 + y.F1;
-        if (qmax >= 1) { const ff v = ff_from_d((l1 + l2 - 1.5) * (1 - z.h1 * f)); r.a1h = v.h; r.a1l = v.l; }
+        ff p = ff_mul(ff_mul(ff{x.eG.h, x.eG.l}, ff{y.eG.h, y.eG.l}), ff{z.eH.h, z.eH.l});
+        int e = x.eG.e + y.eG.e + z.eH.e;
+        const int k = fexpo(p.h);
+        if (k > -127) { p = ff_shift(p, -k); e += k; }
+        r.a0h = p.h;
+        r.a0l = p.l;
+        r.a0e = e;
+        const ff f = ff_add(x.F1, y.F1);
+        if (qmax >= 1) {
+            const ff v = ff_mul(ff{(float)(l1 + l2) - 1.5f, 0.0f}, ff_add(ff{1.0f, 0.0f}, ff_neg(ff_mul(z.h1, f))));
+            r.a1h = v.h;
+            r.a1l = v.l;
+        }
         if (qmax >= 2) {
-            const ff v = ff_from_d(z.pa * (z.pb * (z.pc * (x.F2 + 2 * x.F1 * y.F1 + y.F2) - f) + 0.5));
+            const ff t = ff_add(ff_add(x.F2, ff_mul(ff{2.0f * x.F1.h, 2.0f * x.F1.l}, y.F1)), y.F2);
+            const ff v = ff_mul(z.pa, ff_add(ff_mul(z.pb, ff_add(ff_mul(z.pc, t), ff_neg(f))), ff{0.5f, 0.0f}));
             r.a2h = v.h;
             r.a2l = v.l;
         }
