@@ -422,30 +422,48 @@ __global__ void k_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, 
 //   K0=(p+2)(p+3)(p1+1)(p1+2), K1=(p+1)(p+3)(p1+2)(p2+2), K2=(p+2)(p+4)(p1+3)(p2+3), K3=(p+2)(p+3)(p2+3)(p2+4);
 // table 1 (l1 == l2, eq. (30)): {(p+2)(p1+1)/(4(p+1)^2-1), (p+1)(p2+2)/(4(p+2)^2-1), 0, 0};
 // p1 = p-2m, p2 = p+2m.
+// the q recurrence coefficients of degree index p for one m (they depend on m alone)
+CAPS_DEV void ptab_entry(int mt, int p, double4 *tm, double4 *tp, float4 *fm, float4 *fp)
+{
+    const double m = mt > 0 ? mt : 1;
+    const double pp = p, p1 = pp - 2 * m, p2 = pp + 2 * m;
+    auto invD = [](double x) { return 1.0 / (4 * x * x - 1); };
+    const double4 v0 = make_double4((pp + 2) * (pp + 3) * ((p1 + 1) * (p1 + 2)) * invD(pp + 1),
+                                    (pp + 1) * (pp + 3) * ((p1 + 2) * (p2 + 2)) * invD(pp + 2),
+                                    (pp + 2) * (pp + 4) * ((p1 + 3) * (p2 + 3)) * invD(pp + 3),
+                                    (pp + 2) * (pp + 3) * ((p2 + 3) * (p2 + 4)) * invD(pp + 4));
+    const double4 v1 = make_double4((pp + 2) * (p1 + 1) * invD(pp + 1), (pp + 1) * (p2 + 2) * invD(pp + 2), 0.0, 0.0);
+    if (tm) { *tm = v0; *tp = v1; }
+    if (fm) {
+        const double s = 0x1p-30;
+        for (int t = 0; t < 2; t++) {
+            const double4 v = t ? v1 : v0;
+            const ff x = ff_from_d(v.x * s), y = ff_from_d(v.y * s), z = ff_from_d(v.z * s), w = ff_from_d(v.w * s);
+            float4 *f = t ? fp : fm;
+            f[0] = make_float4(x.h, y.h, z.h, w.h);
+            f[1] = make_float4(x.l, y.l, z.l, w.l);
+        }
+    }
+}
+
 __global__ void k_ptab(const Task *tasks, int ntask, double4 *ptab, float4 *ptabf, int pstride)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int task = blockIdx.y;
     if (p >= pstride || task >= ntask) return;
-    const double m = tasks[task].m > 0 ? tasks[task].m : 1;
-    const double pp = p, p1 = pp - 2 * m, p2 = pp + 2 * m;
-    auto invD = [](double x) { return 1.0 / (4 * x * x - 1); };
-    ptab[((size_t)task * 2 + 0) * pstride + p] =
-        make_double4((pp + 2) * (pp + 3) * ((p1 + 1) * (p1 + 2)) * invD(pp + 1),
-                     (pp + 1) * (pp + 3) * ((p1 + 2) * (p2 + 2)) * invD(pp + 2),
-                     (pp + 2) * (pp + 4) * ((p1 + 3) * (p2 + 3)) * invD(pp + 3),
-                     (pp + 2) * (pp + 3) * ((p2 + 3) * (p2 + 4)) * invD(pp + 4));
-    ptab[((size_t)task * 2 + 1) * pstride + p] =
-        make_double4((pp + 2) * (p1 + 1) * invD(pp + 1), (pp + 1) * (p2 + 2) * invD(pp + 2), 0.0, 0.0);
-    if (ptabf) {
-        for (int t = 0; t < 2; t++) {
-            const double4 v = ptab[((size_t)task * 2 + t) * pstride + p];
-            const double s = 0x1p-30;
-            const ff x = ff_from_d(v.x * s), y = ff_from_d(v.y * s), z = ff_from_d(v.z * s), w = ff_from_d(v.w * s);
-            ptabf[(((size_t)task * 2 + t) * pstride + p) * 2 + 0] = make_float4(x.h, y.h, z.h, w.h);
-            ptabf[(((size_t)task * 2 + t) * pstride + p) * 2 + 1] = make_float4(x.l, y.l, z.l, w.l);
-        }
-    }
+    ptab_entry(tasks[task].m, p, ptab + ((size_t)task * 2 + 0) * pstride + p, ptab + ((size_t)task * 2 + 1) * pstride + p,
+               ptabf ? ptabf + (((size_t)task * 2 + 0) * pstride + p) * 2 : nullptr,
+               ptabf ? ptabf + (((size_t)task * 2 + 1) * pstride + p) * 2 : nullptr);
+}
+
+// the float-float tables once per distinct m of a chunk (groups), indexed like the a_0..a_2 rows
+__global__ void k_ptab_groups(const int *group_m, int ngroup, float4 *ptabf, int pstride)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = blockIdx.y;
+    if (p >= pstride || g >= ngroup) return;
+    ptab_entry(group_m[g], p, nullptr, nullptr, ptabf + (((size_t)g * 2 + 0) * pstride + p) * 2,
+               ptabf + (((size_t)g * 2 + 1) * pstride + p) * 2);
 }
 
 // per distinct m of a chunk and per (l1>=l2) pair: a_0 (as a scaled double), a_1,
@@ -1025,6 +1043,14 @@ size_t a12_bytes(int ldim, int ngroup)
 {
     const size_t L = ldim + 2;
     return L * (L + 1) / 2 * ngroup * sizeof(A012);
+}
+
+void launch_ptab_groups(const int *group_m, int ngroup, float4 *ptabf, int pstride, cudaStream_t st)
+{
+    dim3 gp((pstride + 127) / 128, ngroup);
+    k_ptab_groups<<<gp, 128, 0, st>>>(group_m, ngroup, ptabf, pstride);
+    COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
 }
 
 void launch_ptab_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, double4 *ptab, float4 *ptabf, int pstride, ffe *KF,

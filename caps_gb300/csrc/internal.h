@@ -52,6 +52,8 @@ void launch_ptab(const Task *tasks, int ntask, double4 *ptab, int pstride, cudaS
 void launch_itab(const Task *tasks, const int *tlist, int nlist, int ldim, const sd *K, int nu_stride, const double *lft,
                  const double2 *xtab, const double4 *ptab, int pstride, sd *I, int *status, cudaStream_t st, const void *a12,
                  bool band);
+// float-float q recurrence tables once per distinct m (group_m), row g per group
+void launch_ptab_groups(const int *group_m, int ngroup, float4 *ptabf, int pstride, cudaStream_t st);
 void launch_ptab_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, double4 *ptab, float4 *ptabf, int pstride, ffe *KF,
                      cudaStream_t st);
 // mixed form: q-sums with one a_q recurrence per (pair, subgroup of same-m tasks) (itab_ff.cu);

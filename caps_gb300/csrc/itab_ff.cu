@@ -66,7 +66,7 @@ CAPS_DEV void iacc_add(IAcc &A, ff t, int et)
 }
 
 // grid (ceil(npair/128), ngroups) or, for the band, (ceil(2L/128), ngroups);
-// groups[g] = {first list position, count <= G, a_0..a_2 row}: the group's tasks are
+// groups[g] = {first list position, count <= G, a_0..a_2 and p-table row}: the group's tasks are
 // tlist[x], ..., tlist[x + count - 1] (tlist == nullptr: tasks x, ..., x + count - 1).
 // They share m (hence lmin, mu, the p table and the a_0..a_2 row) and the material.
 // BAND computes only the pairs that the diagonal of M reads, l1 - l2 in {0, 2} (the EE and
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(128, 7) k_itab_grp(const Task *tasks, const in
         const float m2f = 2.0f * mm, dlf = (float)(l1 - l2), pA = m2f * dlf;
         const ff ApF = ff_mul(ff{pA, fmaf(m2f, dlf, -pA)}, ff{(float)(l1 + l2 + 1), 0.0f});
         const ff Ap2 = diag ? ff{0.0f, 0.0f} : ff_shift(ff_mul(ApF, ApF), -30 - sig);
-        const float4 *pt = ptabf + ((size_t)t0 * 2 + (diag ? 1 : 0)) * pstride * 2;
+        const float4 *pt = ptabf + ((size_t)grp.z * 2 + (diag ? 1 : 0)) * pstride * 2; // the m's table
         // b_{q-2} = a_1, b_{q-1} = a_2, D_2 = 1, normalised by the exponent of a_2
         const int e_b = fexpo(A12.a2h);
         ff bm2 = ff_shift(a1f, -e_b), bm1 = ff_shift(a2f, -e_b);

@@ -612,7 +612,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         if (caps->precision == CAPS_PREC_MIXED) {
             // mixed form: the q-sums in float-float on the FP32 pipe
             float4 *d_ptabf = (float4 *)g_eng.ptabf.get((size_t)nt * 2 * pstride * 2 * sizeof(float4));
-            launch_ptab_kff(d_tasks, nt, d_K, nu_stride, d_ptab, d_ptabf, pstride, d_KF, st);
+            launch_ptab_groups(d_gm, ngroup, d_ptabf, pstride, st); // the recurrence tables depend on m alone
             if (diag_first) {
                 d_Saf = g_eng.Saf.get((size_t)nt * L * 16);
                 d_Sbf = g_eng.Sbf.get((size_t)nt * L * 16);
