@@ -66,9 +66,11 @@ __global__ void k_to_delta32(int ntask, int n, const double *A, size_t lda, size
 // (I + Lam_kk)^{-1} (lower triangular, row-major MB x MB per task) for the panel solve and
 // the block's share of ||Lam||_F^2.  Per column j every thread forms the pivot from
 // T[j][j]; threads 0..63 scale row tid of column j into colj; the rank-1 update of the
-// trailing triangle is spread over rows (tid mod 64) and every fourth column from
-// j + 1 + tid / 64 (a warp covers 32 rows of one column: T rows 65 floats apart, distinct
-// banks).  W follows column-parallel, one column per thread, by forward substitution.
+// trailing triangle takes the entries (i, c), j < c <= i, from a list of the whole triangle
+// ordered by column (last column first), so that step j's entries are a prefix of it and
+// the 256 threads share them evenly (consecutive threads: consecutive rows of one column,
+// T rows 65 floats apart, distinct banks).  W follows column-parallel, one column per
+// thread, by forward substitution.
 __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float *S, size_t sstride, int *status, float *Winv,
                                                  double *fro)
 {
@@ -78,8 +80,15 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
     __shared__ float W[MB][MB + 1];
     __shared__ float colj[MB];
     __shared__ double red8[8];
+    // the entries (i, c), 1 <= c <= i <= 63, as i | c << 8, columns 63, 62, ..., 1, rows
+    // ascending within a column; column c starts at (63 - c)(64 - c) / 2
+    __shared__ unsigned short tri[(MB - 1) * MB / 2];
     const int tid = threadIdx.x;
     const int nb = min(MB, n - k0);
+    if (tid >= 1 && tid < MB) {
+        const int c = tid, first = (MB - 1 - c) * (MB - c) / 2;
+        for (int i = c; i < MB; i++) tri[first + i - c] = (unsigned short)(i | c << 8);
+    }
     float *Sm = S + (size_t)task * sstride + (size_t)k0 * n + k0;
     {
         // the block's lower triangle, 16 loads in flight per thread
@@ -97,7 +106,6 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
     }
     __syncthreads();
     bool bad = false;
-    const int i = tid & (MB - 1), cs = tid / MB;
     for (int j = 0; j < nb; j++) {
         // phase 1: every thread forms the pivot from T[j][j], threads j+1..nb-1 scale their
         // entry of column j (T[j][j] itself is rewritten only in phase 2, which reads
@@ -113,11 +121,12 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
             colj[tid] = cj;
         }
         __syncthreads();
-        // phase 2: rank-1 update of the trailing triangle from colj
+        // phase 2: rank-1 update of the trailing triangle (c > j: a prefix of the list) from colj
         if (tid == 0) T[j][j] = lam;
-        if (i > j && i < nb) {
-            const float ci = colj[i];
-            for (int c = j + 1 + cs; c <= i; c += 4) T[i][c] -= ci * colj[c];
+        const int cnt = (MB - 1 - j) * (MB - j) / 2;
+        for (int e = tid; e < cnt; e += 256) {
+            const int v = tri[e], ri = v & 0xff, c = v >> 8;
+            if (ri < nb) T[ri][c] -= colj[ri] * colj[c];
         }
         __syncthreads();
     }
