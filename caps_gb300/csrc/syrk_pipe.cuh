@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
         }
         for (int i = 0; i < 2; i++) {
             umma::mbar_init(&tfull[i], 1);
-            umma::mbar_init(&tempty[i], PIPE_EPI_WARPS * 32);
+            umma::mbar_init(&tempty[i], (img ? 2 : 1) * PIPE_EPI_WARPS * 32);
         }
     }
     umma::fence_before();
@@ -190,7 +190,51 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
     umma::fence_after();
     const uint32_t tmem = tslot;
 
-    if (warp < PIPE_PRODUCER_WARPS && img) {
+    // epilogue warps: 17-24, and with images (one producer thread) also the otherwise idle
+    // producer warps 1-8; warp w reads TMEM lane quadrant w mod 4, and the warps of one
+    // quadrant split the tile's columns (halves, or quarters with images)
+    const int eidx = warp > PIPE_PRODUCER_WARPS ? warp - PIPE_PRODUCER_WARPS - 1 + (img ? PIPE_EPI_WARPS : 0)
+                     : (img && warp >= 1 && warp <= PIPE_EPI_WARPS) ? warp - 1 : -1;
+    if (eidx >= 0) {
+        // ---- epilogue ----
+        const int per_quad = (img ? 2 : 1) * PIPE_EPI_WARPS / 4;
+        const int HW = TN / per_quad; // columns per warp
+        const int quad = warp & 3, half = eidx >> 2;
+        int tt = 0;
+        for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+            const PipeTile T = pipe_tile<TN>(t, tpt, ncb, n, t0, cend, status);
+            if (!T.valid) continue;
+            float *Sm = S + (size_t)T.task * sstride;
+            const int b = tt & 1, ub = tt >> 1;
+            const int R = T.row0 + quad * 32 + lane;
+            bool ok = true;
+            for (int part = 0; part < HW / 16; part++) {
+                const int cb = T.col0 + half * HW + part * 16;
+                float c[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int C = cb + j;
+                    c[j] = (R < n && C < cend && R >= C) ? Sm[(size_t)C * n + R] : 0.0f;
+                }
+                if (part == 0) {
+                    ok = umma::mbar_wait(&tfull[b], ub & 1, PIPE_WAIT_ITERS);
+                    umma::fence_after();
+                    if (!ok) break;
+                }
+                float v[16];
+                umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * TN + half * HW + part * 16, v);
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int C = cb + j;
+                    if (R < n && C < cend && R >= C) Sm[(size_t)C * n + R] = c[j] - v[j];
+                }
+            }
+            if (!ok) { atomicOr(status + T.task, ST_ERR_WAIT); break; }
+            umma::fence_before();
+            mbar_arrive(&tempty[b]);
+            tt++;
+        }
+    } else if (warp < PIPE_PRODUCER_WARPS && img) {
         // ---- producer: bulk copies of the panel images (one thread) ----
         constexpr bool WIDE = TN == UM_M && TK == PIPE_IMG_TK; // whole trailing matrix
         constexpr bool REST = TN == 64 && TK == 64;            // rest of a 256-column panel
@@ -295,44 +339,6 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
                 umma::commit(&tfull[b]);
                 tt++;
             }
-        }
-    } else {
-        // ---- epilogue: warp w reads lane quadrant w mod 4 and column half (w - 17) / 4 ----
-        constexpr int HW = TN / 2; // columns per warp
-        const int quad = warp & 3, half = (warp - PIPE_PRODUCER_WARPS - 1) >> 2;
-        int tt = 0;
-        for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
-            const PipeTile T = pipe_tile<TN>(t, tpt, ncb, n, t0, cend, status);
-            if (!T.valid) continue;
-            float *Sm = S + (size_t)T.task * sstride;
-            const int b = tt & 1, ub = tt >> 1;
-            const int R = T.row0 + quad * 32 + lane;
-            bool ok = true;
-            for (int part = 0; part < HW / 16; part++) {
-                const int cb = T.col0 + half * HW + part * 16;
-                float c[16];
-#pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    const int C = cb + j;
-                    c[j] = (R < n && C < cend && R >= C) ? Sm[(size_t)C * n + R] : 0.0f;
-                }
-                if (part == 0) {
-                    ok = umma::mbar_wait(&tfull[b], ub & 1, PIPE_WAIT_ITERS);
-                    umma::fence_after();
-                    if (!ok) break;
-                }
-                float v[16];
-                umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * TN + half * HW + part * 16, v);
-#pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    const int C = cb + j;
-                    if (R < n && C < cend && R >= C) Sm[(size_t)C * n + R] = c[j] - v[j];
-                }
-            }
-            if (!ok) { atomicOr(status + T.task, ST_ERR_WAIT); break; }
-            umma::fence_before();
-            mbar_arrive(&tempty[b]);
-            tt++;
         }
     }
     umma::fence_before();
