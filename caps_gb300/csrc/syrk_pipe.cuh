@@ -1,24 +1,28 @@
 // syrk_pipe.cuh -- persistent, warp-specialised form of the tcgen05 trailing update
-// (same arithmetic as k_syrk_umma: S_tile -= P_rows P_cols^T over a panel of kw = 64 or 128
-// columns, split TF32 hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory).
+// (same arithmetic as k_syrk_umma: S_tile -= P_rows P_cols^T over panel columns k0 .. k0+kw,
+// split TF32 hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory).
 //
-// One CTA per SM walks a static list of 128 x 64 tiles over all matrices of the batch
+// One CTA per SM walks a static list of 128 x TN tiles over all matrices of the batch
 // (tile t = blockIdx.x, blockIdx.x + gridDim.x, ...), with three roles that overlap
 // across tiles instead of running one after another:
-//   * producer warps 0-15 stage each 64-column chunk of the two panel slices, split into
-//     TF32 hi/lo in the canonical K-major layout, into one of two shared-memory stages
-//     (96 KB each) and arrive on that stage's "full" mbarrier;
-//   * warp 16 (one thread) waits for a full stage, issues the 8 k-steps x 3 MMAs into one
-//     of two 64-column tensor-memory accumulators, and commits to the stage's "empty"
+//   * producers fill NS shared-memory stages with the hi/lo slices of a TK-column chunk of
+//     the two panel slices in the canonical K-major layout: either one thread of warp 0
+//     with four cp.async.bulk copies of images that the panel solves prepared (completion
+//     counted on the stage's "full" mbarrier by transaction bytes), or, without images, 16
+//     warps that load, split and store through registers and arrive on "full";
+//   * warp 16 (one thread) waits for a full stage, issues TK/8 k-steps x 3 MMAs into one
+//     of two TN-column tensor-memory accumulators, and commits to the stage's "empty"
 //     mbarrier (the slices may be overwritten once the MMAs have read them) and, after a
 //     tile's last chunk, to the accumulator's "full" mbarrier;
-//   * epilogue warps 17-24 load the tile of S, wait for the accumulator, read it back with
-//     tcgen05.ld (warp w reads lanes 32 (w mod 4) .. +31, columns 32 ((w - 17) / 4) .. +31),
-//     store S - acc and arrive on the accumulator's "empty" mbarrier.
+//   * epilogue warps 17-24 (with images also warps 1-8) load the tile of S, wait for the
+//     accumulator, read it back with tcgen05.ld (warp w reads lanes 32 (w mod 4) .. +31 and
+//     its share of the columns), store S - acc and arrive on the accumulator's "empty"
+//     mbarrier.
 // Every wait is bounded (PIPE_WAIT_ITERS polls of mbarrier.try_wait); a role that gives up
 // marks the tile's matrix with ST_ERR_WAIT and leaves its loop, the others then give up at
-// their next wait, and the CTA frees its tensor memory and returns.  All roles walk the
-// same tile list and skip the same tiles (matrices whose factorisation already failed).
+// their next wait, the bulk-copy thread waits (bounded) for its last copies, and the CTA
+// frees its tensor memory and returns.  All roles walk the same tile list and skip the same
+// tiles (matrices whose factorisation already failed).
 #pragma once
 #include "common.cuh"
 #include "umma.cuh"
