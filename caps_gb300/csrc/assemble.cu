@@ -399,23 +399,6 @@ CAPS_DEV void qacc_add(QAcc &A, double mant, int ex)
 }
 
 
-// ---- float-float arithmetic on the FP32 pipe (about 48 significant bits) ----
-// value = h + l with |l| <= ulp(h)/2; error-free transformations of Dekker/Knuth.
-// float-float copy of the K table (mantissa split into two floats, same exponent)
-__global__ void k_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, ffe *KF)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int task = blockIdx.y;
-    if (task >= ntask) return;
-    const Task &T = tasks[task];
-    if (i >= T.nu_max - T.mu + 1) return;
-    for (int p = 0; p < 2; p++) {
-        const sd k = K[(size_t)(task * 2 + p) * nu_stride + i];
-        const ff f = ff_from_d(k.m);
-        KF[(size_t)(task * 2 + p) * nu_stride + i] = ffe{f.h, f.l, k.e, 0};
-    }
-}
-
 // per task, for p in [0, pstride): the p-dependent factors of the recurrence with the
 // alpha denominators 1/(4x^2-1) folded in.  Table 0 (l1 != l2, eqs. (26)-(27)):
 //   {K0/(4(p+1)^2-1), K1/(4(p+2)^2-1), K2/(4(p+3)^2-1), K3/(4(p+4)^2-1)},
@@ -1050,20 +1033,6 @@ void launch_ptab_groups(const int *group_m, int ngroup, float4 *ptabf, int pstri
     dim3 gp((pstride + 127) / 128, ngroup);
     k_ptab_groups<<<gp, 128, 0, st>>>(group_m, ngroup, ptabf, pstride);
     COUNT_LAUNCH(1);
-    CK(cudaGetLastError());
-}
-
-void launch_ptab_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, double4 *ptab, float4 *ptabf, int pstride, ffe *KF,
-                     cudaStream_t st)
-{
-    dim3 gp((pstride + 127) / 128, ntask);
-    k_ptab<<<gp, 128, 0, st>>>(tasks, ntask, ptab, ptabf, pstride);
-    COUNT_LAUNCH(1);
-    if (K) { // K == nullptr: KF already holds the float-float table (k_kred_ff)
-        dim3 gk((nu_stride + 127) / 128, ntask);
-        k_kff<<<gk, 128, 0, st>>>(tasks, ntask, K, nu_stride, KF);
-        COUNT_LAUNCH(1);
-    }
     CK(cudaGetLastError());
 }
 

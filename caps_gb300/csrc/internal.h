@@ -54,11 +54,9 @@ void launch_itab(const Task *tasks, const int *tlist, int nlist, int ldim, const
                  bool band);
 // float-float q recurrence tables once per distinct m (group_m), row g per group
 void launch_ptab_groups(const int *group_m, int ngroup, float4 *ptabf, int pstride, cudaStream_t st);
-void launch_ptab_kff(const Task *tasks, int ntask, const sd *K, int nu_stride, double4 *ptab, float4 *ptabf, int pstride, ffe *KF,
-                     cudaStream_t st);
 // mixed form: q-sums with one a_q recurrence per (pair, subgroup of same-m tasks) (itab_ff.cu);
 // groups index tlist (nullptr: the tasks themselves); band: only the pairs the diagonal reads.
-// The p tables and the float-float K table come first (launch_ptab_kff).
+// The p tables come first (launch_ptab_groups).
 int itab_group_size();
 void launch_itab_grp(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim, const ffe *KF, int nu_stride,
                      const float4 *ptabf, int pstride, const void *a12, void *Iout, bool ffe_out, bool band, int *status,
