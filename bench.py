@@ -3,8 +3,10 @@ plane-sphere free energy at R/L=150 (Drude gold, T=300 K, ldim=1050, matrices
 of dimension 2100), on the GPU through the library's C-ABI.
 
 One step = one complete free-energy evaluation (Matsubara sum with the
-reference's m cutoff 1e-9 and xi truncation 1e-6, ~980 matrices), i.e. the
-call caps_free_energy() a user of the library makes.
+reference's m cutoff 1e-9 and xi truncation 1e-6, 978 matrices), i.e. the
+call caps_free_energy() a user of the library makes.  Matrices are counted over
+the reference's own (xi, m) set in both arms; the CPU arm times a systematic
+sample of that set.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
   python bench.py --impl reference ...   # CPU restatement of the reference on host cores
@@ -34,7 +36,6 @@ OMEGAP_EV, GAMMA_EV = 9.0, 0.035
 CUTOFF, EPSREL = 1e-9, 1e-6
 WORKLOAD = ("Drude gold (wp=9 eV, gamma=0.035 eV), R/L=150, L=1e-6 m, T=300 K, ldim=1050 (matrix dim 2100), "
             "full Matsubara sum (cutoff 1e-9, epsrel 1e-6)")
-E_REFERENCE = None  # filled from tests/golden when present
 
 
 def rank_env():
@@ -122,54 +123,89 @@ def load_reference_energy():
     return None
 
 
-def cpu_sample_tasks(n, seed=0):
-    """a fixed sample of (xi, m) of the workload: Matsubara n in 1..9, m in 0..109"""
-    import numpy as np
-    rng = np.random.default_rng(seed)
-    Ts = 2 * math.pi * 1.38064852e-23 * (R + L) * T / (1.0545718e-34 * 299792458.0)
-    ns = rng.integers(1, 10, n)
-    ms = rng.integers(0, 110, n)
-    return [k * Ts for k in ns], [int(m) for m in ms]
+def matsubara_spacing():
+    return 2 * math.pi * 1.38064852e-23 * (R + L) * T / (1.0545718e-34 * 299792458.0)
 
 
-def cpu_baseline(nmat, threads):
-    """the CPU restatement of the reference (oracle port) on host threads: det/s on a bounded sample"""
+def workload_pairs(ref):
+    """the (xi, m) matrices of one free energy of the workload, in (n, m) order: those the
+    reference's truncation visits (m cutoff 1e-9 per frequency, frequency cutoff 1e-6),
+    read from the reference library's own run of the workload; with their values"""
+    Ts = matsubara_spacing()
+    xi, ms, vals = [], [], []
+    for k, terms in enumerate(ref["terms"]):
+        for m, v in enumerate(terms):
+            xi.append((k + 1) * Ts)
+            ms.append(m)
+            vals.append(v)
+    return xi, ms, vals
+
+
+def cpu_sample(ref, nmat, step=0):
+    """a systematic sample of nmat matrices of the workload's own (xi, m) set: every
+    (N / nmat)-th matrix in (n, m) order, the offset moving with the step, so trace-rule
+    matrices (the high-m end of every frequency) and full factorisations enter at their
+    true shares"""
+    xi, ms, _ = workload_pairs(ref)
+    N = len(xi)
+    nmat = min(nmat, N)
+    off = (0.5 + 0.618034 * step) % 1.0
+    idx = sorted(set(min(N - 1, int((i + off) * N / nmat)) for i in range(nmat)))
+    return [xi[i] for i in idx], [ms[i] for i in idx], N
+
+
+def cpu_baseline(ref, nmat, threads, step=0):
+    """the CPU restatement of the reference (oracle port) on host threads over a sample of
+    the workload: (matrices/s, seconds, matrices sampled, matrices in one free energy)"""
     from oracle import binding as ob
-    xi, m = cpu_sample_tasks(nmat)
+    xi, m, N = cpu_sample(ref, nmat, step)
     t = time.time()
     ob.logdetD_batch(R, L, LDIM, xi, m, (OMEGAP_EV, GAMMA_EV), threads=threads)
     dt = time.time() - t
-    return nmat / dt, dt
+    return len(xi) / dt, dt, len(xi), N
+
+
+def workload_config():
+    """the workload, identical in both arms"""
+    return {"workload": WORKLOAD,
+            "matrices": "the (xi, m) matrices of one free energy under the reference's truncation "
+                        "(978 of dimension 2100, 446 of them ending at the trace rule)",
+            "counted": "logdetD/s over that set: matrices a method computes beyond it are not counted",
+            "l2": "no flush needed: every matrix (35 MB) and the per-chunk working set (>10 GB) exceed L2"}
 
 
 def run_reference(args, dist, rank, world):
     threads = os.cpu_count() or 1
-    per_step = args.cpu_sample or threads  # default: one matrix per host thread per step
+    per_step = args.cpu_sample or 2 * threads
     if rank != 0:
         return
-    for _ in range(args.warmup):
-        cpu_baseline(per_step, threads)
+    ref = load_reference_energy()
+    for k in range(args.warmup):
+        cpu_baseline(ref, per_step, threads, step=k)
     t0 = time.time()
-    total = 0
+    total, N = 0, 0
     for k in range(args.steps):
-        cpu_baseline(per_step, threads)
-        total += per_step
+        _, _, n, N = cpu_baseline(ref, per_step, threads, step=args.warmup + k)
+        total += n
     dt = time.time() - t0
     value = total / dt
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (inputs fully set by the geometry/material scalars)", "impl": "reference",
-        "config": {"workload": WORKLOAD, "sample_per_step": "%d (xi,m) matrices of the workload, fixed seed" % per_step},
+        "config": workload_config(),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "%d matrices per step (dim 2100), oracle restatement of the reference (C, dense LU) on %d host threads" % (per_step, threads)},
+                         "sample": "%d matrices per step, a systematic sample of the workload's %d, by the oracle "
+                                   "port of the reference (C: adaptive Gauss-Legendre K integrals, dense LU) on %d host "
+                                   "threads" % (per_step, N, threads)},
+        "projected_time_to_E_s": N / value,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
 # DRAM bytes per algorithmic byte of the trailing update (k_syrk_pipe, all four launch kinds
-# of a 256-column panel), from the ncu capture summarised in profiles/k_syrk_pipe_c3.md
+# of a 256-column panel), from one ncu capture of 48 factored matrices of this workload
 SYRK_DRAM_PER_ALGORITHMIC = 1.14
 
 
@@ -184,6 +220,45 @@ def measured_hbm_peak():
         return 6800.0, "of fallback (6.8 TB/s, one earlier GB300 measurement)"
 
 
+def time_energy(cg, precision, net, calls):
+    """(time-to-E s, info, E, device ms per phase) of `calls` free energies after one warm-up"""
+    c = cg.Caps(R, L, ldim=LDIM)
+    c.set_drude(OMEGAP_EV, GAMMA_EV)
+    c.set_precision(precision)
+    c.free_energy(T, CUTOFF, EPSREL, mlp=net)
+    cg.reset_timings()
+    t = time.time()
+    for _ in range(calls):
+        E, info = c.free_energy(T, CUTOFF, EPSREL, mlp=net)
+    t = (time.time() - t) / calls
+    ph = [x / calls for x in cg.timings(cumulative=True)]
+    return t, info, E, ph
+
+
+def per_matrix_errors(cg, ref):
+    """every matrix of the workload's set in both forms (one batch each) against the
+    reference library's values: max and 99th percentile of |d logdetD| / max(1, |x|)"""
+    import numpy as np
+    xi, ms, want = workload_pairs(ref)
+    want = np.array(want)
+    got = {}
+    for name, prec in (("mixed", cg.PREC_MIXED), ("fp64", cg.PREC_FP64)):
+        c = cg.Caps(R, L, ldim=LDIM)
+        c.set_drude(OMEGAP_EV, GAMMA_EV)
+        c.set_precision(prec)
+        got[name] = np.array(c.logdetD_batch(xi, ms)[0])
+    scale = np.maximum(1.0, np.abs(want))
+
+    def stats(a, b):
+        e = np.abs(a - b) / scale
+        return {"max": float(e.max()), "p99": float(np.percentile(e, 99)), "median": float(np.median(e))}
+    return {"matrices": len(xi),
+            "mixed_vs_reference": stats(got["mixed"], want),
+            "fp64_vs_reference": stats(got["fp64"], want),
+            "mixed_vs_fp64": stats(got["mixed"], got["fp64"]),
+            "bar": "1e-10 max(1,|x|) for the FP64 form; the mixed form is judged on E (|dE/E| <= 1e-6)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -195,8 +270,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain", action="store_true",
                     help="plain truncation schedule instead of the learned proposal")
-    ap.add_argument("--no-fp64-reference", action="store_true",
-                    help="skip the side measurement of the plain FP64 form")
+    ap.add_argument("--no-side", action="store_true",
+                    help="skip the side measurements (plain forms, per-matrix errors)")
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: one batch of 8 matrices of the workload (n in {1,5}, m in {0,20,40,60})")
     ap.add_argument("--ncu-matrices", type=int, default=8,
@@ -205,7 +280,7 @@ def main():
     args = ap.parse_args()
     if args.ncu_case:
         import caps_gb300 as cg
-        Ts = 2 * math.pi * 1.38064852e-23 * (R + L) * T / (1.0545718e-34 * 299792458.0)
+        Ts = matsubara_spacing()
         caps = cg.Caps(R, L, ldim=LDIM)
         caps.set_drude(OMEGAP_EV, GAMMA_EV)
         caps.set_precision(cg.PREC_MIXED if args.precision == "mixed" else cg.PREC_FP64)
@@ -237,18 +312,18 @@ def main():
     import caps_gb300 as cg
 
     fp64_peak = cg.fp64_peak()
-    fp32_peak = cg.fp32_peak()
+    prec = cg.PREC_MIXED if args.precision == "mixed" else cg.PREC_FP64
     caps = cg.Caps(R, L, ldim=LDIM)
     caps.set_drude(OMEGAP_EV, GAMMA_EV)
-    caps.set_precision(cg.PREC_MIXED if args.precision == "mixed" else cg.PREC_FP64)
+    caps.set_precision(prec)
 
     net, train_info = None, None
     args.learned = not args.plain
     if args.learned:
+        # trained on small geometries (R/L <= 50) and other Drude metals: the workload's
+        # geometry and material are held out of the training data
         from caps_gb300 import learned
-        t_tr = time.time()
         net, train_info = learned.train(seed=0)
-        train_info["seconds"] = time.time() - t_tr
 
     E = None
     for _ in range(args.warmup):
@@ -275,59 +350,76 @@ def main():
     cg.kernel_timing(False)
 
     ndet = sum(i["ndet"] for i in infos)
+    nset = sum(i["ndet"] - i["nwasted"] for i in infos)   # matrices of the reference's set
     dev_s = ph[5] * 1e-3
 
-    # the plain FP64 GPU form on the same workload (1 warm-up + 2 timed calls), for the
-    # mixed+learned vs FP64 ratio of the metric
-    fp64 = None
-    if not args.no_fp64_reference and (args.learned or args.precision != "fp64"):
-        c64 = cg.Caps(R, L, ldim=LDIM)
-        c64.set_drude(OMEGAP_EV, GAMMA_EV)
-        c64.free_energy(T, CUTOFF, EPSREL)
-        cg.reset_timings()
-        t64 = time.time()
-        E64 = None
-        for _ in range(2):
-            E64, i64 = c64.free_energy(T, CUTOFF, EPSREL)
-        t64 = (time.time() - t64) / 2
-        d64 = cg.timings(cumulative=True)[5] * 1e-3 / 2
-        fp64 = {"time_to_E_s": t64, "value": i64["ndet"] / d64, "matrices": i64["ndet"], "E": E64,
-                "phases_ms": dict(zip(["setup_mie", "K", "I", "elements", "factor", "total"], [x / 2 for x in cg.timings(cumulative=True)]))}
+    ref = load_reference_energy()
+    side = {}
+    if not args.no_side:
+        # the same workload in the other forms (one warm-up, then timed calls), outside the
+        # timed region: the plain FP64 GPU form (the metric's denominator) and, for the
+        # mixed form, its plain-truncation run, which isolates what the network gains
+        names = {"fp64_plain_form": (cg.PREC_FP64, None, 2)}
+        if args.learned and args.precision == "mixed":
+            names["mixed_plain_form"] = (cg.PREC_MIXED, None, 3)
+        for name, (p, n_, calls) in names.items():
+            t_, i_, E_, ph_ = time_energy(cg, p, n_, calls)
+            side[name] = {"time_to_E_s": t_, "value": (i_["ndet"] - i_["nwasted"]) / (ph_[5] * 1e-3),
+                          "matrices_computed": i_["ndet"], "matrices_beyond_cutoffs": i_["nwasted"], "E": E_,
+                          "E_rel_err": abs(E_ - ref["E"]) / abs(ref["E"]) if ref else None,
+                          "phases_ms": dict(zip(["setup_mie", "K", "I", "elements", "factor", "total"], ph_))}
+        if ref is not None and "terms" in ref:
+            side["per_matrix_error"] = per_matrix_errors(cg, ref)
+
     wall_max = allmax(dist, wall)
     dev_max = allmax(dist, dev_s)
-    ndet_all = allsum(dist, ndet)
+    nset_all = allsum(dist, nset)
     if rank != 0:
         return
 
-    value = ndet_all / dev_max          # device time (CUDA events on the launching stream)
-    e2e = ndet_all / wall_max           # wall time of the public API call, host work and copies included
+    value = nset_all / dev_max          # device time (CUDA events on the launching stream)
+    e2e = nset_all / wall_max           # wall time of the public API call, host work and copies included
+    tte = wall_max / args.steps
     fac_s = ph[4] * 1e-3
     achieved = wk["factor_flops"] / fac_s / 1e12 if fac_s > 0 else None
     hbm_peak, hbm_src = measured_hbm_peak()
     syrk_gbs = syrk_bytes / (syrk_ms * 1e-3) / 1e9 if syrk_ms > 0 else None
-    ref = load_reference_energy()
     err = abs(E - ref["E"]) / abs(ref["E"]) if ref else None
 
     cpu = None
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and ref is not None:
         threads = os.cpu_count() or 1
         nm = args.cpu_sample or 2 * threads
-        v, dt = cpu_baseline(nm, threads)
+        v, dt, n_, N = cpu_baseline(ref, nm, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "%d (xi,m) matrices of the workload (dim 2100, fixed seed), %.1f s on %d host threads" % (nm, dt, threads)}
+               "sample": "%d matrices, a systematic sample of the workload's %d (dim 2100), %.1f s on %d host threads, "
+                         "oracle port of the reference (C: adaptive Gauss-Legendre K integrals, dense LU)" % (n_, N, dt, threads),
+               "projected_time_to_E_s": N / v}
 
+    learned_gain = None
+    if train_info is not None and "mixed_plain_form" in side:
+        saved = side["mixed_plain_form"]["time_to_E_s"] - tte
+        cost = train_info["data_seconds"] + train_info["train_seconds"]
+        learned_gain = {"time_to_E_plain_s": side["mixed_plain_form"]["time_to_E_s"], "time_to_E_learned_s": tte,
+                        "saved_per_E_s": saved, "speedup": side["mixed_plain_form"]["time_to_E_s"] / tte,
+                        "training_cost_s": cost,
+                        "break_even_free_energies": (cost / saved) if saved > 0 else None,
+                        "held_out": "the workload's geometry (R/L=150) and material (gold) are not in the training data"}
+
+    fp64 = side.get("fp64_plain_form")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": wall_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else
                  "f64 (Mie, K, log-factorials, exponents, pivot logs, correction) + float-float q-sums + f32 delta-Cholesky",
         "data": "synthetic (inputs fully set by the geometry/material scalars)",
-        "config": {"workload": WORKLOAD, "matrices_per_step": ndet / args.steps, "precision": args.precision,
+        "config": workload_config(),
+        "method": {"precision": args.precision,
                    "truncation": "learned (MLP proposal, reference rules verify)" if args.learned else "plain (extrapolating schedule)",
-                   "wasted_matrices_per_step": sum(i["nwasted"] for i in infos) / args.steps,
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "no flush needed: every matrix (35 MB) and the per-chunk working set (>10 GB) exceed L2"},
-        "time_to_E_s": wall_max / args.steps,
+                   "matrices_computed_per_step": ndet / args.steps,
+                   "matrices_beyond_cutoffs_per_step": (ndet - nset) / args.steps,
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "time_to_E_s": tte,
         "E": E, "E_reference": ref["E"] if ref else None, "E_rel_err": err,
         "phases_ms_per_step": {k: v / args.steps for k, v in zip(["setup_mie", "K", "I", "elements", "factor", "total"], ph)},
         "roofline": ({"bound": "fp64", "kernel": "FP64 Cholesky (potf2+trsm+syrk), n^3/3 flops per factored matrix",
@@ -347,18 +439,21 @@ def main():
                       "peak_source": hbm_src,
                       "launches": syrk_n, "avg_launch_ms": syrk_ms / syrk_n if syrk_n else None,
                       "algorithmic_bytes_per_launch": syrk_bytes / syrk_n if syrk_n else None,
-                      "traffic_source": "DRAM bytes per algorithmic byte of the k_syrk_pipe launches from one ncu "
-                                        "capture (profiles/k_syrk_pipe_c3.md), times this run's algorithmic bytes per "
+                      "traffic_source": "DRAM bytes per algorithmic byte of the k_syrk_pipe launches in one ncu capture "
+                                        "of 48 factored matrices of this workload, times this run's algorithmic bytes per "
                                         "launch (the images are written by the panel solves, outside these launches)",
                       "fp32_accurate_tflops_factorisation": achieved}),
         "dominant_kernel": None if args.precision == "fp64" else {
-            "kernel": "k_itab_grp<3> (float-float q-sums)", "phase_share_of_step": ph[2] / ph[5] if ph[5] else None,
+            "kernel": "k_itab_grp (float-float q-sums)", "phase_share_of_step": ph[2] / ph[5] if ph[5] else None,
             "bound": "FP32/ALU instruction issue; no HBM or tensor roofline applies (DRAM idle)",
-            "evidence": "profiles/k_itab_grp_c3_small.md"},
+            "evidence": "ncu issue-slot and pipe figures of the q-sum kernel on a small case of this workload"},
         "cpu_baseline": cpu,
         "learned_training": train_info,
+        "learned_gain": learned_gain,
         "fp64_plain_form": fp64,
-        "time_to_E_speedup_vs_fp64_plain": (fp64["time_to_E_s"] / (wall_max / args.steps)) if fp64 else None,
+        "mixed_plain_form": side.get("mixed_plain_form"),
+        "per_matrix_error": side.get("per_matrix_error"),
+        "time_to_E_speedup_vs_fp64_plain": (fp64["time_to_E_s"] / tte) if fp64 else None,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": ctr["h2d"] / args.steps, "d2h_bytes_per_step": ctr["d2h"] / args.steps},
         "gpu_launches": ctr["launches"],
         "clocks": clk,

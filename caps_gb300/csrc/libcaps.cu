@@ -1274,25 +1274,13 @@ extern "C" int caps_mlp_proposal(caps_t *self, double T, double cutoff, double e
     const double v0 = fabs(caps_ht_drude(self));
     const double lc = log(cutoff);
     // frequencies in blocks of NB, stopping at the first block that reaches the Matsubara
-    // cutoff; features as caps_mlp_features forms them, the frequency-independent ones
-    // once (a prediction depends on its own features only)
-    float xm[5];
-    caps_mlp_features(1.0 / self->LbyR, Ts, 0, wp, ga, xm);
+    // cutoff; features as caps_mlp_features forms them
     std::vector<float> X((size_t)NB * MCAP * 5), Y((size_t)NB * MCAP);
     for (int n0 = 1; n0 <= NPROBE; n0 += NB) {
         const int nb = std::min(NB, NPROBE - n0 + 1);
-        for (int k = 0; k < nb; k++) {
-            float xn[5];
-            caps_mlp_features(1.0 / self->LbyR, (n0 + k) * Ts, 0, wp, ga, xn);
-            for (int m = 0; m < MCAP; m++) {
-                float *x = &X[((size_t)k * MCAP + m) * 5];
-                x[0] = xm[0];
-                x[1] = xn[1];
-                x[2] = (float)(m / 200.0);
-                x[3] = xm[3];
-                x[4] = xm[4];
-            }
-        }
+        for (int k = 0; k < nb; k++)
+            for (int m = 0; m < MCAP; m++)
+                caps_mlp_features(1.0 / self->LbyR, (n0 + k) * Ts, m, wp, ga, &X[((size_t)k * MCAP + m) * 5]);
         caps_mlp_predict(mlp, X.data(), nb * MCAP, Y.data());
         for (int k = 0; k < nb; k++) {
             const int n = n0 + k;

@@ -1,7 +1,7 @@
 // mlp.cu -- a small MLP trained on the GPU that predicts log|logdetD(xi, m)|.
 //
 // Network: 5 inputs -> 64 -> 64 -> 64 -> 1, SiLU activations, FP32.  Inputs are
-// the normalised features (log R/L, log xi_, m, omega_p, gamma) built by the
+// the normalised features (log R/L, 2 xi L/c, m/sqrt(R/L), omega_p, gamma) built by the
 // caller.  Hand-written kernels:
 //   k_mlp_fwdbwd  one CTA of 64 threads (one per neuron) walks a slice of the
 //                 batch: forward pass, MSE loss, backward pass; per-CTA gradient
@@ -275,12 +275,17 @@ extern "C" void caps_mlp_predict(caps_mlp_t *m, const float *X, int n, float *y)
     CK(cudaMemcpy(y, m->out, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost));
 }
 
-// features of one (geometry, material, xi_, m): the normalisation the network is trained with
+// features of one (geometry, material, xi_, m): the normalisation the network is trained with.
+// The frequency enters as 2 xi L / c = 2 xi_ / (1 + R/L), the exponent of the round trip's
+// decay e^{-2 xi L / c}, and m as m / sqrt(R/L), the scale on which the m sum of a
+// plane-sphere geometry ends; log(R/L) carries what is left.  With these, geometries of
+// different R/L put their values on nearly the same surface, so a network trained on small
+// R/L serves larger ones.
 extern "C" void caps_mlp_features(double RbyL, double xi_, int m, double omegap_eV, double gamma_eV, float *x)
 {
     x[0] = (float)(log(RbyL) / 5.0);
-    x[1] = (float)(log(xi_) / 7.0);
-    x[2] = (float)(m / 200.0);
+    x[1] = (float)(2.0 * xi_ / (1.0 + RbyL) / 8.0);
+    x[2] = (float)(m / sqrt(RbyL) / 10.0);
     x[3] = (float)(omegap_eV / 10.0);
     x[4] = (float)(gamma_eV / 0.05);
 }

@@ -2,12 +2,12 @@
 //
 // Who needs it: callers that must not allocate device memory while they run --
 // code executing inside a framework that owns every byte of the device through
-// its own pool, code that runs between a stream-capture begin and end (where
-// cudaMalloc is not permitted), or a host that may not grow its heap at that
-// point.  caps_logdetD() grows a workspace with cudaMalloc on first use; this
-// entry point instead takes all of its scratch from one file-scope device array
-// of fixed size, NOALLOC_SCRATCH_BYTES (32 MiB), which exists on every GPU that
-// loads the library until the process exits.
+// its own pool allocator (a cudaMalloc behind its back can fail or fragment the
+// pool), or a host that may not grow its heap at that point.  caps_logdetD()
+// grows a workspace with cudaMalloc on first use; this entry point instead takes
+// all of its scratch from one file-scope device array of fixed size,
+// NOALLOC_SCRATCH_BYTES (32 MiB), which exists on every GPU that loads the
+// library until the process exits.
 //
 // Limits (rejected with an error code and a message, never truncated):
 //   ldim <= 512 (matrix dimension <= 1024), lmin + ldim <= 2048, and at most
@@ -24,8 +24,11 @@
 // first call before any stream capture begins.
 //
 // It runs the same kernels as caps_logdetD, with the same HODLR/LU semantics
-// of caps_t::detalg, on the legacy default stream, and copies the result to
-// the caller's host double.
+// of caps_t::detalg, on the legacy default stream.  The call synchronises the
+// host with that stream twice (once to read the quadrature panel count, once for
+// the result) and copies the result to the caller's host double.  Rejected input
+// and failed CUDA API calls return a negative code with a message; a kernel
+// launch that fails aborts the process, as every launch of the library does.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -46,7 +49,7 @@ static __device__ double g_noalloc_lfac[1024];
 
 static void *g_scratch_ptr[NOALLOC_MAX_DEVICES];
 static double *g_lfac_ptr[NOALLOC_MAX_DEVICES];
-static char g_noalloc_err[256];
+static thread_local char g_noalloc_err[256];   // per host thread, like caps_gpu_last_error
 
 extern "C" const char *caps_noalloc_last_error(void) { return g_noalloc_err; }
 

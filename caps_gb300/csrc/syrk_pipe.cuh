@@ -20,8 +20,8 @@
 //     mbarrier.
 // Every wait is bounded (PIPE_WAIT_ITERS polls of mbarrier.try_wait); a role that gives up
 // marks the tile's matrix with ST_ERR_WAIT and leaves its loop, the others then give up at
-// their next wait, the bulk-copy thread waits (bounded) for its last copies, and the CTA
-// frees its tensor memory and returns.  All roles walk the same tile list and skip the same
+// their next wait, the bulk-copy thread waits (bounded) for its last copies, the MMA thread
+// waits (bounded) for the MMAs it issued, and the CTA frees its tensor memory and returns.  All roles walk the same tile list and skip the same
 // tiles (matrices whose factorisation already failed).
 #pragma once
 #include "common.cuh"
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
     using Shape = PipeShape<TN, TK, NS>;
     constexpr int PA = UM_M * TK, PB = TN * TK;
     extern __shared__ __align__(1024) float pipe_sm[];
-    __shared__ uint64_t full[NS], empty[NS], tfull[2], tempty[2];
+    __shared__ uint64_t full[NS], empty[NS], tfull[2], tempty[2], drain;
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int cend = min(n, cmax);
@@ -188,6 +188,7 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
             umma::mbar_init(&tfull[i], 1);
             umma::mbar_init(&tempty[i], (img ? 2 : 1) * PIPE_EPI_WARPS * 32);
         }
+        umma::mbar_init(&drain, 1);
     }
     umma::fence_before();
     __syncthreads();
@@ -343,6 +344,10 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
                 umma::commit(&tfull[b]);
                 tt++;
             }
+            // every MMA this thread issued completes before the CTA frees tensor memory,
+            // also when a wait gave up with MMAs still in flight (bounded like every wait)
+            umma::commit(&drain);
+            umma::mbar_wait(&drain, 0, PIPE_WAIT_ITERS);
         }
     }
     umma::fence_before();

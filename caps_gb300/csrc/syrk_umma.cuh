@@ -94,13 +94,16 @@ __global__ void __launch_bounds__(UM_THREADS, 2) k_syrk_umma(int ntask, int n, i
 
     extern __shared__ __align__(128) float um_sm[];
     float *Ahi = um_sm, *Alo = Ahi + UM_M * UM_K, *Bhi = Alo + UM_M * UM_K, *Blo = Bhi + UM_N * UM_K;
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t mbar, drain;
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     float *Sm = S + (size_t)task * sstride;
 
     if (warp == 0) umma::alloc(&tslot, UM_N);
-    if (tid == 0) umma::mbar_init(&mbar, 1);
+    if (tid == 0) {
+        umma::mbar_init(&mbar, 1);
+        umma::mbar_init(&drain, 1);
+    }
     const int nchunk = (kw + UM_K - 1) / UM_K;
     bool ok = true;
     for (int ch = 0; ch < nchunk; ch++) {
@@ -158,6 +161,11 @@ __global__ void __launch_bounds__(UM_THREADS, 2) k_syrk_umma(int ntask, int n, i
         }
     } else
         atomicOr(status + task, ST_ERR_WAIT);
+    if (!ok && tid == 0) {
+        // a wait gave up: the MMAs issued so far complete before tensor memory is freed
+        umma::commit(&drain);
+        umma::mbar_wait(&drain, 0, UM_WAIT_ITERS);
+    }
     umma::fence_before();
     __syncthreads();
     if (warp == 0) {

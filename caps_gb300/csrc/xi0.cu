@@ -124,13 +124,33 @@ static double *lfac_table_device()
     return d_lfac;
 }
 
+// grow-only device buffers of the xi = 0 path, reused by every call; g_xi0_mu serialises
+// the calls that use them (the free energy calls the batch once per chunk of m)
+struct Xi0Buf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    template <class T> T *get(size_t count)
+    {
+        const size_t need = count * sizeof(T);
+        if (need > bytes) {
+            if (p) CK(cudaFree(p));
+            bytes = std::max(need, bytes + bytes / 4);
+            CK(cudaMalloc(&p, bytes));
+        }
+        return (T *)p;
+    }
+};
+static struct { Xi0Buf I, ratio, f, m, lmin, status, A, ld, md, tr, res; } g_x0;
+static std::mutex g_xi0_mu;
+
 // I_nu for nu = 0 .. numax and ratio_l, f_l for l = 0 .. lmax of the plasma xi=0 block,
-// as device arrays (caller frees); omegap_ = omegap (L+R)/c, alpha = omegap_/(1+L/R)
+// in the path's workspace (valid until the next call); omegap_ = omegap (L+R)/c,
+// alpha = omegap_/(1+L/R)
 static void plasma_tables_device(double omegap_, double alpha, int numax, int lmax, double **dI, double **dratio, double **df)
 {
-    CK(cudaMalloc(dI, (size_t)(numax + 1) * sizeof(double)));
-    CK(cudaMalloc(dratio, (size_t)(lmax + 1) * sizeof(double)));
-    CK(cudaMalloc(df, (size_t)(lmax + 1) * sizeof(double)));
+    *dI = g_x0.I.get<double>((size_t)numax + 1);
+    *dratio = g_x0.ratio.get<double>((size_t)lmax + 1);
+    *df = g_x0.f.get<double>((size_t)lmax + 1);
     const int nnu = numax + 1;
     k_plasma_I<<<(nnu + 3) / 4, 128>>>(0, nnu, omegap_, lfac_table_device(), gl16(), *dI);
     COUNT_LAUNCH(1);
@@ -150,8 +170,7 @@ struct Engine;
 // omegap (rad/s)
 int logdetD0_batch(caps_t *self, const int *ms, int n, int which, double *out, double omegap)
 {
-    static std::mutex mu;
-    std::lock_guard<std::mutex> lk(mu);
+    std::lock_guard<std::mutex> lk(g_xi0_mu);
     double *d_lfac = lfac_table_device();
     const int ldim = self->ldim;
     std::vector<int> lmins(n);
@@ -167,17 +186,11 @@ int logdetD0_batch(caps_t *self, const int *ms, int n, int which, double *out, d
         const double omegap_ = omegap * self->calL / CAPS_c;
         plasma_tables_device(omegap_, omegap_ / (1 + self->LbyR), 2 * lmax, lmax, &d_I, &d_ratio, &d_f);
     }
-    int *d_m, *d_lmin, *d_status;
-    double *d_A, *d_ld, *d_md, *d_tr, *d_res;
     const size_t mstride = (size_t)ldim * ldim;
-    CK(cudaMalloc(&d_m, n * sizeof(int)));
-    CK(cudaMalloc(&d_lmin, n * sizeof(int)));
-    CK(cudaMalloc(&d_status, n * sizeof(int)));
-    CK(cudaMalloc(&d_A, n * mstride * sizeof(double)));
-    CK(cudaMalloc(&d_ld, (size_t)n * ldim * sizeof(double)));
-    CK(cudaMalloc(&d_md, (size_t)n * ldim * sizeof(double)));
-    CK(cudaMalloc(&d_tr, n * sizeof(double)));
-    CK(cudaMalloc(&d_res, n * sizeof(double)));
+    int *d_m = g_x0.m.get<int>(n), *d_lmin = g_x0.lmin.get<int>(n), *d_status = g_x0.status.get<int>(n);
+    double *d_A = g_x0.A.get<double>(n * mstride);
+    double *d_ld = g_x0.ld.get<double>((size_t)n * ldim), *d_md = g_x0.md.get<double>((size_t)n * ldim);
+    double *d_tr = g_x0.tr.get<double>(n), *d_res = g_x0.res.get<double>(n);
     cudaStream_t st = 0;
     CK(cudaMemcpy(d_m, ms, n * sizeof(int), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(d_lmin, lmins.data(), n * sizeof(int), cudaMemcpyHostToDevice));
@@ -193,9 +206,6 @@ int logdetD0_batch(caps_t *self, const int *ms, int n, int which, double *out, d
     std::vector<int> hs(n);
     CK(cudaMemcpy(out, d_res, n * sizeof(double), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(hs.data(), d_status, n * sizeof(int), cudaMemcpyDeviceToHost));
-    CK(cudaFree(d_m)); CK(cudaFree(d_lmin)); CK(cudaFree(d_status)); CK(cudaFree(d_A));
-    CK(cudaFree(d_ld)); CK(cudaFree(d_md)); CK(cudaFree(d_tr)); CK(cudaFree(d_res));
-    if (d_I) { CK(cudaFree(d_I)); CK(cudaFree(d_ratio)); CK(cudaFree(d_f)); }
     int nerr = 0;
     for (int k = 0; k < n; k++) nerr += (hs[k] & ~0xF) != 0;
     return nerr;
@@ -205,13 +215,11 @@ int logdetD0_batch(caps_t *self, const int *ms, int n, int which, double *out, d
 // (caps_integrate_plasma, caps_kernel_M0_MM_plasma)
 void plasma_tables_host(double omegap_, double alpha, int numax, int lmax, std::vector<double> &I, std::vector<double> &ratio)
 {
-    static std::mutex mu;
-    std::lock_guard<std::mutex> lk(mu);
+    std::lock_guard<std::mutex> lk(g_xi0_mu);
     double *d_I, *d_ratio, *d_f;
     plasma_tables_device(omegap_, alpha, numax, lmax, &d_I, &d_ratio, &d_f);
     I.resize(numax + 1);
     ratio.resize(lmax + 1);
     CK(cudaMemcpy(I.data(), d_I, I.size() * sizeof(double), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(ratio.data(), d_ratio, ratio.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaFree(d_I)); CK(cudaFree(d_ratio)); CK(cudaFree(d_f));
 }

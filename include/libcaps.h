@@ -290,17 +290,20 @@ double caps_gpu_fp32_peak(void);
 
 /* log det(1-M) of one (xi_, m), like caps_logdetD, for callers that cannot
  * allocate device memory at call time (a framework that owns the whole device
- * through its own pool, or code running while a stream is being captured).
- * No counterpart in the reference.  All scratch lives in one fixed 32 MiB
- * file-scope device array (held on every GPU that loads the library until
- * exit); no cudaMalloc/cudaFree or allocating library call is made.
+ * through its own pool allocator, where an outside cudaMalloc can fail or
+ * fragment the pool).  No counterpart in the reference.  All scratch lives in
+ * one fixed 32 MiB file-scope device array (held on every GPU that loads the
+ * library until exit); no cudaMalloc/cudaFree or allocating library call is made.
  * Limits: ldim <= 512, lmin+ldim <= 2048, <= 256 K-quadrature panels; larger
- * cases return a negative code with a message (caps_noalloc_last_error()).
- * The first call on a device resolves the array's address (cudaGetSymbolAddress)
- * and uploads constant tables: make it before any stream capture.  Calls share
- * the array: calls that overlap on the GPU race.  Runs on the legacy default
- * stream.  Returns 0, a negative code for rejected input, or the status bits
- * of a numerical failure (CAPS_ST_ERR_*); *logdet receives the result. */
+ * cases return a negative code with a message (caps_noalloc_last_error(), per
+ * host thread).  The first call on a device resolves the array's address
+ * (cudaGetSymbolAddress) and uploads constant tables: make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race.  Runs on
+ * the legacy default stream and synchronises the host with it before returning.
+ * A failed kernel launch aborts, as in every entry point of the library.
+ * Returns 0, a negative code for rejected input or a failed CUDA API call, or
+ * the status bits of a numerical failure (CAPS_ST_ERR_*); *logdet receives the
+ * result. */
 int caps_logdetD_noalloc(caps_t *self, double xi_, int m, double *logdet);
 const char *caps_noalloc_last_error(void);
 

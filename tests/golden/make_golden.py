@@ -3,7 +3,7 @@
 Run here, where the reference source tree and its build (oracle/_ref, made by
 oracle/Makefile.ref) exist:
 
-    python tests/golden/make_golden.py [--ref /root/reference] [--heavy]
+    CAPS_REFERENCE_SRC=<CaPS source tree> python tests/golden/make_golden.py [--heavy]
 
 Two sources:
  1. known-answer vectors of the reference's own unit tests, read as text from
@@ -63,6 +63,19 @@ def parse_tests(ref):
     out["test_logdetD0"] = dict(source="src/tests/test_logdetD.c:108-142", tolerance=1e-10, detalg="HODLR",
                                 note="omegap in units of c/(L+R)", ht_plasma=cases,
                                 m0_RbyL1000=dict(R=1.0, L=0.001, ldim=12000, m=0, EE=float(an.group(1)), MM=float(an.group(2))))
+
+    t = _read_c(os.path.join(ref, "src/tests/test_fresnel.c"))
+    R, L = (float(x) for x in re.search(r"caps_init\(([\d.e+-]+),([\d.e+-]+)\)", t).groups())
+    cases = []
+    for blk in re.split(r"userdata\[0\] = ", t)[1:]:
+        wp = float(re.match(r"([\d.e+-]+)/CAPS_hbar_eV", blk).group(1))
+        ga = float(re.search(r"userdata\[1\] = ([\d.e+-]+)/CAPS_hbar_eV", blk).group(1))
+        for xi, k, te, tm in re.findall(r"caps_fresnel\(caps, ([\d.e+-]+), ([\d.e+-]+), &rTE, &rTM\);\s*"
+                                        r"AssertAlmostEqual\(&test, rTE, (-?[\d.e+-]+)\);\s*"
+                                        r"AssertAlmostEqual\(&test, rTM, (-?[\d.e+-]+)\);", blk):
+            cases.append(dict(omegap_eV=wp, gamma_eV=ga, xi=float(xi), k=float(k), rTE=float(te), rTM=float(tm)))
+    out["test_fresnel"] = dict(source="src/tests/test_fresnel.c:10-7025", tolerance=2e-15, R=R, L=L,
+                               note="Drude epsilon-1 with omega_p, gamma in eV (userdata = value/hbar_eV)", cases=cases)
 
     t = _read_c(os.path.join(ref, "src/tests/test_mie.c"))
     cases = []
@@ -208,12 +221,19 @@ def reference_values(ref_lib, heavy):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("CAPS_REFERENCE_SRC", "/root/reference"))
+    ap.add_argument("--ref", default=os.environ.get("CAPS_REFERENCE_SRC"),
+                    help="CaPS source tree (default: $CAPS_REFERENCE_SRC)")
     ap.add_argument("--heavy", action="store_true")
+    ap.add_argument("--unit-tests-only", action="store_true", help="re-parse the unit-test vectors only")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("set CAPS_REFERENCE_SRC (or --ref) to the CaPS source tree")
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
     g = parse_tests(a.ref)
     json.dump(g, open(os.path.join(HERE, "reference_unit_tests.json"), "w"), indent=1)
+    if a.unit_tests_only:
+        print({k: len(x.get("cases", [])) for k, x in g.items()})
+        return
     lib = os.path.join(ROOT, "oracle", "_ref", "libcaps_ref.so")
     v = reference_values(lib, a.heavy)
     json.dump(v, open(os.path.join(HERE, "reference_values.json"), "w"), indent=1)

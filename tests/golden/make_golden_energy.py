@@ -97,7 +97,7 @@ def F_xi(pool, R, L, ldim, drude, xi, cutoff, detalg, chunk):
             if v == 0 or v / terms[0] < cutoff:
                 t = terms[:]
                 t[0] /= 2
-                return kahan(t), len(terms), len(terms) + (len(vals) - 1 - vals.index(v)) * 0
+                return kahan(t), len(terms), terms
         m0 += chunk
 
 
@@ -115,20 +115,22 @@ def energy(R, L, ldim, T, drude, cutoff=1e-9, epsrel=1e-6, detalg=1, procs=8):
             drude_ht = _lib.caps_ht_drude(c)
             s, _, _ = F_xi(pool, R, L, ldim, drude, 0.0, cutoff, detalg, procs)
             v0 = drude_ht + s
-        v, xis, ndet = [v0], [0.0], 0
+        v, xis, ndet, per_m = [v0], [0.0], 0, []
         n = 1
         while True:
-            s, nm, _ = F_xi(pool, R, L, ldim, drude, n * Ts, cutoff, detalg, procs)
+            s, nm, terms = F_xi(pool, R, L, ldim, drude, n * Ts, cutoff, detalg, procs)
             ndet += nm
             v.append(s)
             xis.append(n * Ts)
+            per_m.append(terms)
             print("n=%d xi=%.16g v=%.16g m=%d" % (n, n * Ts, s, nm), file=sys.stderr, flush=True)
             if abs(s / v[0]) < epsrel:
                 break
             n += 1
     w = v[:]
     w[0] /= 2
-    return Ts / math.pi * kahan(w), dict(xi=xis, logdetD=v, ndet=ndet)
+    # terms[k][m]: the reference's logdetD(xi_{k+1}, m) for every m its cutoff visits
+    return Ts / math.pi * kahan(w), dict(xi=xis, logdetD=v, ndet=ndet, terms=per_m)
 
 
 def energy_t0(R, L, ldim, drude, cutoff=1e-9, epsrel=1e-6, detalg=1, procs=8):

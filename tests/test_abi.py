@@ -44,3 +44,21 @@ def test_host_helpers_match_oracle():
     assert d.ldim == 101  # ceil(max(20, 5/(L/R))) in floating point, as the reference computes it
     assert cg.lib.caps_init(-1.0, 1.0) is None
     assert cg.lib.caps_set_ldim(d._h, 0) == 0
+
+
+def test_fresnel_reference_vectors(unit_vectors):
+    """the host helper caps_fresnel against all 3430 asserts of the reference's
+    src/tests/test_fresnel.c (Drude metals, relative tolerance 2e-15)"""
+    import caps_gb300 as cg
+    from conftest import relx
+    t = unit_vectors["test_fresnel"]
+    c = cg.Caps(t["R"], t["L"])
+    mat, bad = None, []
+    for v in t["cases"]:
+        if (v["omegap_eV"], v["gamma_eV"]) != mat:
+            mat = (v["omegap_eV"], v["gamma_eV"])
+            c.set_drude(*mat)
+        te, tm = c.fresnel(v["xi"], v["k"])
+        if not (relx(te, v["rTE"]) < t["tolerance"] and relx(tm, v["rTM"]) < t["tolerance"]):
+            bad.append((v, te, tm))
+    assert len(t["cases"]) == 1715 and not bad, (len(bad), bad[:3])
