@@ -301,11 +301,12 @@ k_ktab_ff(const Task *tasks, const double *edges, int max_panels, const float4 *
     }
 }
 
-// Mixed form of k_kred: the warps' float-float partials aligned to the largest exponent
-// and summed in float-float, written as the float-float K table (h in [1, 2)) that the
-// q-sums read
+// Mixed form of k_kred: the warps' float-float partials aligned to the largest exponent and
+// summed in float-float, written as the paired table the q-sums read: TM and TE of one
+// (task, nu) as one float4 (TM h, l, TE h, l; the larger of the two h in [1, 2)) under their
+// common exponent (KPe), so that one alignment serves both polarisations
 __global__ void k_kred_ff(const Task *tasks, int ntask, const float2 *partF, const int *partE, int max_warps, int nu_stride,
-                          ffe *KF, int *status)
+                          float4 *KP, int *KPe, int *status)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int task = blockIdx.y;
@@ -314,11 +315,10 @@ __global__ void k_kred_ff(const Task *tasks, int ntask, const float2 *partF, con
     const int nnu = T.nu_max - T.mu + 1;
     if (i >= nnu) return;
     const int nwarp = (T.npanel + 1) / 2;
+    ffe kp[2];
     for (int p = 1; p >= 0; p--) {
-        ffe *out = KF + (size_t)(task * 2 + p) * nu_stride + i;
         if (p == 0 && T.is_pr) { // K_TE = -K_TM for perfect reflectors (integration.c:638)
-            const ffe k = KF[(size_t)(task * 2 + 1) * nu_stride + i];
-            *out = ffe{-k.h, -k.l, k.e, 0};
+            kp[0] = ffe{-kp[1].h, -kp[1].l, kp[1].e, 0};
             continue;
         }
         const size_t base = (size_t)(task * 2 + p) * max_warps * nu_stride + i;
@@ -336,10 +336,14 @@ __global__ void k_kred_ff(const Task *tasks, int ntask, const float2 *partF, con
         const int k = fexpo(s.h);
         if (s.h == 0.0f || k == 128) {
             atomicOr(status + task, ST_ERR_NONFINITE);
-            *out = ffe{s.h, 0.0f, 0, 0};
+            kp[p] = ffe{s.h, 0.0f, 0, 0};
         } else
-            *out = ffe{fshift(s.h, -k), fshift(s.l, -k), emax + k, 0};
+            kp[p] = ffe{fshift(s.h, -k), fshift(s.l, -k), emax + k, 0};
     }
+    const int e = max(kp[1].e, kp[0].e);
+    const ff tm = ff_shift(ff{kp[1].h, kp[1].l}, kp[1].e - e), te = ff_shift(ff{kp[0].h, kp[0].l}, kp[0].e - e);
+    KP[(size_t)task * nu_stride + i] = make_float4(tm.h, tm.l, te.h, te.l);
+    KPe[(size_t)task * nu_stride + i] = e;
 }
 
 __global__ void k_kred(const Task *tasks, int ntask, const double *partM, const int *partE, int max_warps, int nu_stride,
@@ -1056,10 +1060,10 @@ void launch_ktab_ff(bool pr, const Task *tasks, int ntask, int max_warps, const 
 }
 
 void launch_kred_ff(const Task *tasks, int ntask, int max_nnu, const float2 *partF, const int *partE, int max_warps, int nu_stride,
-                    ffe *KF, int *status, cudaStream_t st)
+                    float4 *KP, int *KPe, int *status, cudaStream_t st)
 {
     dim3 g((max_nnu + 127) / 128, ntask);
-    k_kred_ff<<<g, 128, 0, st>>>(tasks, ntask, partF, partE, max_warps, nu_stride, KF, status);
+    k_kred_ff<<<g, 128, 0, st>>>(tasks, ntask, partF, partE, max_warps, nu_stride, KP, KPe, status);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

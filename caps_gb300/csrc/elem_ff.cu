@@ -5,7 +5,7 @@
 // survive on the way is the cancellation inside the B, C, D combinations (up to ~1e5
 // for m = 0).  The combinations are therefore formed in float-float with a separate
 // power-of-two exponent ("fe" below, ~48-bit mantissa) from the float-float I table
-// that k_itab_grp writes, and the result goes straight into the FP32 delta matrix:
+// that k_itab_pk writes, and the result goes straight into the FP32 delta matrix:
 // no FP64 matrix is formed, and the FP64 pipe is used only for the diagonal, which
 // the logdet correction needs in FP64.  Per element block the kernel also leaves a
 // per-warp sum of squares, from which k_stats_ff takes the Frobenius norm for the
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, const int *tl
 
 // the diagonal of M alone (kernel_logdet computes it first, matrix.c:62-66): grid
 // (ceil(ldim/EB), ntask), thread a writes M_ii of the diagonal block (a, a) in FP64, from
-// the band of I values that k_itab_grp's band mode leaves
+// the band of I values that k_itab_pk's band mode leaves
 __global__ void __launch_bounds__(EB) k_diag_ff(const Task *tasks, int ntask, int ldim, const ffe *__restrict__ I,
                                                 const ffe *__restrict__ Saf, const ffe *__restrict__ Sbf,
                                                 const float4 *__restrict__ uvf, double *diag, int *status)

@@ -38,12 +38,13 @@ void launch_ktab(bool pr, const Task *tasks, int ntask, int max_warps, const dou
                  int nu_stride, const double *lfac_tab, double *partM, int *partE, cudaStream_t st);
 void launch_kred(const Task *tasks, int ntask, int max_nnu, const double *partM, const int *partE, int max_warps, int nu_stride,
                  sd *K, int *status, cudaStream_t st);
-// mixed form: the K integrals in float-float straight into the float-float K table
+// mixed form: the K integrals in float-float
 struct ffe;
 void launch_ktab_ff(bool pr, const Task *tasks, int ntask, int max_warps, const double *edges, int max_panels, const double2 *coefAB,
                     float4 *coefF, int nu_stride, const double *lfac_tab, float2 *partF, int *partE, cudaStream_t st);
+// KP, KPe: TM and TE of one (task, nu) under one exponent, the table the q-sums read
 void launch_kred_ff(const Task *tasks, int ntask, int max_nnu, const float2 *partF, const int *partE, int max_warps, int nu_stride,
-                    ffe *KF, int *status, cudaStream_t st);
+                    float4 *KP, int *KPe, int *status, cudaStream_t st);
 void launch_tables(const double *lfac_tab, double *lft, int nlf, double2 *xtab, int nx, cudaStream_t st);
 struct ffe;
 // FP64 q-sums of the listed tasks (tlist, nlist; tlist == nullptr: tasks 0..nlist-1); band:
@@ -58,9 +59,9 @@ void launch_ptab_groups(const int *group_m, int ngroup, float4 *ptabf, int pstri
 // groups index tlist (nullptr: the tasks themselves); band: only the pairs the diagonal reads.
 // The p tables come first (launch_ptab_groups).
 int itab_group_size();
-void launch_itab_grp(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim, const ffe *KF, int nu_stride,
-                     const float4 *ptabf, int pstride, const void *a12, void *Iout, bool ffe_out, bool band, int *status,
-                     cudaStream_t st);
+void launch_itab_grp(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim, const float4 *KP,
+                     const int *KPe, int nu_stride, const float4 *ptabf, int pstride, const void *a12, void *Iout, bool ffe_out,
+                     bool band, int *status, cudaStream_t st);
 // sphere-sphere: B = 1 - M^2 and (M^2)_ii from A = 1 - M and M_ii (square.cu)
 void launch_square(int ntask, int n, const double *A, size_t lda, size_t mstride, const double *mdiag, double *B,
                    const int *status, double *mdiag2, cudaStream_t st);

@@ -88,7 +88,7 @@ struct Engine {
     cudaStream_t side = nullptr;          // Mie coefficients and scale factors, beside setup and K
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, KF, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF, tlist, groups2, glist2;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF, tlist, groups2, glist2, KP, KPe;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -550,14 +550,16 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         int *d_pE = (int *)g_eng.partE.get((size_t)nt * 2 * max_warps * nu_stride * sizeof(int));
         const bool mixed = caps->precision == CAPS_PREC_MIXED;
         sd *d_K = nullptr;
-        ffe *d_KF = nullptr;
+        float4 *d_KP = nullptr;
+        int *d_KPe = nullptr;
         if (mixed) {
-            // mixed form: float-float K straight into the table the q-sums read
-            d_KF = (ffe *)g_eng.KF.get((size_t)nt * 2 * nu_stride * 16);
+            // mixed form: float-float K, TM and TE paired, the table the q-sums read
+            d_KP = (float4 *)g_eng.KP.get((size_t)nt * nu_stride * sizeof(float4));
+            d_KPe = (int *)g_eng.KPe.get((size_t)nt * nu_stride * sizeof(int));
             float4 *d_coefF = (float4 *)g_eng.coefF.get((size_t)nt * nu_stride * sizeof(float4));
             launch_ktab_ff(is_pr, d_tasks, nt, max_warps, d_edges, MAX_PANELS, d_coef, d_coefF, nu_stride, g_eng.d_lfac,
                            (float2 *)d_pM, d_pE, st);
-            launch_kred_ff(d_tasks, nt, nnu_max, (const float2 *)d_pM, d_pE, max_warps, nu_stride, d_KF, d_status, st);
+            launch_kred_ff(d_tasks, nt, nnu_max, (const float2 *)d_pM, d_pE, max_warps, nu_stride, d_KP, d_KPe, d_status, st);
         } else {
             d_K = (sd *)g_eng.K.get((size_t)nt * 2 * nu_stride * sizeof(sd));
             launch_ktab(is_pr, d_tasks, nt, max_warps, d_edges, MAX_PANELS, d_coef, nu_stride, g_eng.d_lfac, d_pM, d_pE, st);
@@ -618,7 +620,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
                 d_Sbf = g_eng.Sbf.get((size_t)nt * L * 16);
                 d_uvf = (float4 *)g_eng.uvf.get((size_t)nt * L * sizeof(float4));
                 launch_scale_ff(nt, ldim, d_Sa, d_Sb, d_uv, d_Saf, d_Sbf, d_uvf, st);
-                launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KF, nu_stride, d_ptabf, pstride, d_a12, d_I, true, true,
+                launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KP, d_KPe, nu_stride, d_ptabf, pstride, d_a12, d_I, true, true,
                                 d_status, st);
                 CK(cudaEventRecord(g_eng.ev[3], st));
                 launch_diag_ff(d_tasks, nt, ldim, d_I, d_Saf, d_Sbf, d_uvf, d_dg, d_status, st);
@@ -638,11 +640,11 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
                     launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, d_a12t, st, false, dgl, (int)gl.size(), false);
                 }
                 CK(cudaEventRecord(g_eng.ev[5], st));
-                launch_itab_grp(d_tasks, d_list, dg2, nlist > 0 ? (int)sub2.size() : 0, ldim, d_KF, nu_stride, d_ptabf, pstride, d_a12,
+                launch_itab_grp(d_tasks, d_list, dg2, nlist > 0 ? (int)sub2.size() : 0, ldim, d_KP, d_KPe, nu_stride, d_ptabf, pstride, d_a12,
                                 d_I, true, false, d_status, st);
             } else {
                 for (int k = 3; k <= 5; k++) CK(cudaEventRecord(g_eng.ev[k], st));
-                launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KF, nu_stride, d_ptabf, pstride, d_a12, d_I, ff_elem, false,
+                launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KP, d_KPe, nu_stride, d_ptabf, pstride, d_a12, d_I, ff_elem, false,
                                 d_status, st);
             }
         } else {

@@ -162,3 +162,32 @@ def test_mixed_update_variants(variant):
     assert all(s == 3 for s in d["st"]), d["st"]  # all factored
     for a, b in zip(d["out"], d["ref"]):
         assert abs(a - b) <= TOL_MIXED * max(1.0, abs(b)), (variant, a, b)
+
+
+def test_mixed_correction_error_by_dimension(cg, unit_vectors):
+    """the per-matrix error of the mixed form's first-order correction (log det A ~
+    2 sum log1p(Lam_jj) + tr Delta) against the FP64 form as the dimension grows: the
+    hardest matrices (lowest frequency, m = 0 ..) at dimension 2100 (Drude gold, R/L=150),
+    12000 (plasma, R/L=1000, L=100 nm) and 20000 (perfect reflectors, R/L=1000, the
+    reference's own unit-test geometry); each within 5e-8 max(1, |logdetD|)"""
+    cases = {
+        2100: (150e-6, 1e-6, 1050, (9.0, 0.035), [124.298] * 4, [0, 5, 20, 60]),
+        12000: (1e-4, 1e-7, 6000, (9.0, 0.0), [50.05, 500.5, 2502.5, 500.5], [0, 0, 0, 60]),
+        20000: (1.0, 0.001, 10000, None, [1.0, 1.0, 10.0], [0, 40, 0]),
+    }
+    worst = {}
+    for dim, (R, L, ldim, drude, xi, ms) in cases.items():
+        out = {}
+        for prec in (cg.PREC_FP64, cg.PREC_MIXED):
+            c = cg.Caps(R, L, ldim=ldim, detalg=cg.DETALG_LU)
+            if drude:
+                c.set_drude(*drude)
+            c.set_precision(prec)
+            v, st = c.logdetD_batch(xi, ms)
+            assert max(st) < 16, (dim, prec, list(st))
+            out[prec] = v
+        err = [abs(a - b) / max(1.0, abs(b)) for a, b in zip(out[cg.PREC_MIXED], out[cg.PREC_FP64])]
+        worst[dim] = max(err)
+        print("dimension %d: logdetD %s, mixed-form error %s" % (dim, ["%.6g" % x for x in out[cg.PREC_FP64]],
+                                                                  ["%.1e" % e for e in err]))
+    assert all(e <= TOL_MIXED for e in worst.values()), worst
