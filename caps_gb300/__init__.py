@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(_HERE, "_build", "libcaps_gb300.so")
 
 DETALG_HODLR, DETALG_LU, DETALG_QR, DETALG_CHOLESKY = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
+PATH_AUTO, PATH_HODLR, PATH_DENSE = 0, 1, 2
 HBAR_EV = 6.582119514e-16
 C_LIGHT = 299792458.0
 
@@ -57,6 +58,7 @@ def _load():
         "caps_sphere_sphere_T0": (d, [vp, d, d, C.POINTER(_EnergyInfo)]),
         "caps_free_energy_psd": (d, [vp, d, d, d, i, C.POINTER(_EnergyInfo)]),
         "caps_gpu_set_precision": (i, [vp, i]),
+        "caps_gpu_set_path": (i, [vp, i]),
         "caps_gpu_last_error": (C.c_char_p, []),
         "caps_gpu_set_stream": (None, [vp]),
         "caps_gpu_timings": (i, [dp, i]),
@@ -195,6 +197,10 @@ class Caps:
 
     def set_precision(self, prec):
         return lib.caps_gpu_set_precision(self._h, prec)
+
+    def set_path(self, path):
+        """determinant path under DETALG_HODLR: PATH_AUTO, PATH_HODLR or PATH_DENSE"""
+        return lib.caps_gpu_set_path(self._h, path)
 
     def set_drude(self, omegap_eV, gamma_eV):
         """Drude metal (gamma=0: plasma) for plate and sphere, via caps_epsilonm1_drude."""

@@ -130,6 +130,7 @@ enum : int {
     ST_ERR_NONFINITE = 32, // non-finite matrix element or integral
     ST_ERR_GRID = 64,      // quadrature grid did not fit the node budget
     ST_ERR_WAIT = 128,     // a bounded wait for the tensor cores ran out
+    ST_ERR_HODLR = 256,    // HODLR: an off-diagonal block needed more than the largest rank
 };
 
 } // namespace capsgpu

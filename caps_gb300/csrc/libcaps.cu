@@ -88,7 +88,7 @@ struct Engine {
     cudaStream_t side = nullptr;          // Mie coefficients and scale factors, beside setup and K
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF, tlist, groups2, glist2, KP, KPe;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF, tlist, groups2, glist2, KP, KPe, hwork;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -304,6 +304,7 @@ extern "C" caps_t *caps_init(double R, double L)
     s->epsrel = CAPS_EPSREL;
     s->detalg = DETALG_HODLR;
     s->precision = CAPS_PREC_FP64;
+    s->path = CAPS_PATH_AUTO;
     return s;
 }
 
@@ -352,6 +353,13 @@ extern "C" int caps_gpu_set_precision(caps_t *self, int p)
     return 1;
 }
 
+extern "C" int caps_gpu_set_path(caps_t *self, int path)
+{
+    if (path != CAPS_PATH_AUTO && path != CAPS_PATH_HODLR && path != CAPS_PATH_DENSE) return 0;
+    self->path = path;
+    return 1;
+}
+
 extern "C" double caps_epsilonm1_plate(caps_t *self, double xi_) { return self->epsilonm1_plate(xi_ * CAPS_c / self->calL, self->userdata_plate); }
 extern "C" double caps_epsilonm1_sphere(caps_t *self, double xi_) { return self->epsilonm1_sphere(xi_ * CAPS_c / self->calL, self->userdata_sphere); }
 
@@ -376,6 +384,7 @@ struct BatchOpts {
     double *M_out = nullptr; // host buffer for the dense M of a single task (row-major)
     double *mie_out_a = nullptr, *mie_out_b = nullptr; // Mie of task 0's window
     bool square = false;     // sphere-sphere: log det(1 - M^2) (FP64, dense rules)
+    bool force_dense = false; // factor densely even where the HODLR path applies
 };
 
 static void h2d(void *dst, const void *src, size_t bytes, cudaStream_t st)
@@ -458,14 +467,19 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     // mixed precision without a dense-M request: elements go straight into the FP32 delta
     // matrix (no FP64 matrix)
     const bool ff_elem = caps->precision == CAPS_PREC_MIXED && O.factor && !O.M_out && !O.square;
+    // HODLR semantics in FP64: the HODLR path (elements on demand) where it applies
+    const bool hodlr = O.factor && !O.square && !O.M_out && !O.force_dense && caps->detalg == DETALG_HODLR &&
+                       caps->precision == CAPS_PREC_FP64 &&
+                       (caps->path == CAPS_PATH_HODLR || (caps->path == CAPS_PATH_AUTO && dim >= CAPS_HODLR_AUTO_DIM));
     const size_t mat_bytes = O.square ? 16 : ff_elem ? 4 + 1 : (caps->precision == CAPS_PREC_MIXED ? 12 : 8);
-    const size_t per_task = (size_t)dim * dim * mat_bytes + (size_t)2 * L * L * sizeof(sd) + (size_t)2 * nu_stride * sizeof(sd)
+    const size_t dense_bytes = hodlr ? hodlr_work_bytes(ldim, 1) : (size_t)dim * dim * mat_bytes + (size_t)2 * L * L * sizeof(sd)
+                                                                    + (size_t)L * (L + 1) / 2 * 32; // a_0..a_2 table (one row per task)
+    const size_t per_task = dense_bytes + (size_t)2 * nu_stride * sizeof(sd)
                           + (size_t)nu_stride * sizeof(double2) + (size_t)3 * L * sizeof(sd) + (size_t)dim * 8
                           + (size_t)2 * 256 * nu_stride * 12  // partial sums, up to 256 warps
-                          + (size_t)(4 * (caps->ldim + 4096)) * sizeof(double4)  // p tables
-                          + (size_t)L * (L + 1) / 2 * 32;                         // a_0..a_2 table (at most one row per task)
+                          + (size_t)(4 * (caps->ldim + 4096)) * sizeof(double4); // p tables
     size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes + g_eng.S32.bytes
-                                             + g_eng.a12.bytes + g_eng.part.bytes + g_eng.B.bytes));
+                                             + g_eng.a12.bytes + g_eng.part.bytes + g_eng.B.bytes + g_eng.hwork.bytes));
     int chunk = (int)std::max<size_t>(1, std::min<size_t>(budget / per_task, 65535));
     chunk = std::min(chunk, n);
 
@@ -568,15 +582,15 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         CK(cudaEventRecord(g_eng.ev[2], st));
         CK(cudaStreamWaitEvent(st, g_eng.ev_join, 0)); // Mie and scale factors from here on
 
-        sd *d_I = (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
+        sd *d_I = hodlr ? nullptr : (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
         double4 *d_ptab = (double4 *)g_eng.ptab.get((size_t)nt * 2 * pstride * sizeof(double4));
-        void *d_a12 = g_eng.a12.get(a12_bytes(ldim, ngroup));
+        void *d_a12 = hodlr ? nullptr : g_eng.a12.get(a12_bytes(ldim, ngroup));
         // a_0..a_2 per m; the mixed form's trace rule first needs only the band of each m
         void *d_a12t = nullptr;
         if (caps->precision == CAPS_PREC_MIXED) {
             d_a12t = g_eng.a12t.get(a12_tab_bytes(ldim, ngroup));
             launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, d_a12t, st, true, nullptr, -1, ff_elem);
-        } else
+        } else if (!hodlr)
             launch_a12(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, st);
         const size_t lda = dim, mstride = (size_t)dim * dim;
         double *d_trace = (double *)g_eng.trace.get(nt * sizeof(double));
@@ -647,6 +661,16 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
                 launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KP, d_KPe, nu_stride, d_ptabf, pstride, d_a12, d_I, ff_elem, false,
                                 d_status, st);
             }
+        } else if (hodlr) {
+            // HODLR: M_ii for the trace rule, then the undecided matrices by HODLR with their
+            // elements formed on demand (no I table, no dense matrix)
+            launch_ptab(d_tasks, nt, d_ptab, pstride, st);
+            hodlr_diag(d_tasks, nt, ldim, d_K, nu_stride, d_ptab, pstride, d_lft, d_Sa, d_Sb, d_uv, d_dg, d_status, st);
+            CK(cudaEventRecord(g_eng.ev[3], st));
+            launch_stats(nullptr, nt, dim, nullptr, lda, mstride, d_dg, O.mode, d_trace, d_res, d_status, st);
+            CK(cudaEventRecord(g_eng.ev[4], st));
+            undecided();
+            CK(cudaEventRecord(g_eng.ev[5], st));
         } else {
             launch_ptab(d_tasks, nt, d_ptab, pstride, st);
             if (diag_first) {
@@ -665,7 +689,9 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
 
         double *d_A = nullptr;
         float *d_S = nullptr;
-        if (ff_elem) {
+        if (hodlr) {
+            // (no element phase)
+        } else if (ff_elem) {
             d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
             float *d_part = (float *)g_eng.part.get((size_t)nt * elem_ff_part_floats(ldim) * sizeof(float));
             launch_elem_ff(d_tasks, d_list, nlist, ldim, d_Saf, d_Sbf, d_uvf, d_I, d_S, mstride, d_dg, d_part, d_status, st);
@@ -694,6 +720,10 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
             void *d_work = g_eng.mwork.get(mixed_work_bytes(nt, dim));
             launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, true, d_work);
+        } else if (hodlr) {
+            if (nlist > 0)
+                hodlr_logdet_batch(d_tasks, d_list, nlist, ldim, d_K, nu_stride, d_ptab, pstride, d_lft, d_Sa, d_Sb, d_uv, d_trace,
+                                   d_status, d_res, g_eng.hwork.get(hodlr_work_bytes(ldim, nlist)), st);
         } else if (O.factor) {
             double *d_ld = (double *)g_eng.logdiag.get((size_t)nt * dim * sizeof(double));
             launch_cholesky(nt, dim, d_A, lda, mstride, d_status, d_ld, st);
@@ -739,7 +769,10 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         for (int i = 0; i < nt; i++) {
             const int dst = order[c0 + i];
             if (O.factor) out[dst] = hres[i];
-            if (hst[i] == ST_FACTOR) { g_counters.nfactor++; g_counters.factor_flops += (double)dim * dim * dim / 3.0; }
+            if (hst[i] == ST_FACTOR) {
+                g_counters.nfactor++;
+                if (!hodlr) g_counters.factor_flops += (double)dim * dim * dim / 3.0;
+            }
             if (status_out) status_out[dst] = hst[i];
             if (hst[i] & ~0xF) {
                 nerr++;
@@ -758,7 +791,24 @@ extern "C" int caps_logdetD_batch(caps_t *self, const double *xi_, const int *m,
     if (n <= 0) return 0;
     BatchOpts O;
     O.mode = detalg_mode(self);
-    return run_batch(self, xi_, m, n, out, status, O);
+    std::vector<int> st_local;
+    if (!status) { st_local.resize(n); status = st_local.data(); }
+    int nerr = run_batch(self, xi_, m, n, out, status, O);
+    // matrices whose HODLR compression ran over its rank limit: factored densely instead
+    std::vector<double> rx;
+    std::vector<int> rm, ri;
+    for (int i = 0; i < n; i++)
+        if (status[i] & ST_ERR_HODLR) { rx.push_back(xi_[i]); rm.push_back(m[i]); ri.push_back(i); }
+    if (!ri.empty()) {
+        O.force_dense = true;
+        std::vector<double> ro(ri.size());
+        std::vector<int> rs(ri.size());
+        run_batch(self, rx.data(), rm.data(), (int)ri.size(), ro.data(), rs.data(), O);
+        nerr = 0;
+        for (size_t k = 0; k < ri.size(); k++) { out[ri[k]] = ro[k]; status[ri[k]] = rs[k]; }
+        for (int i = 0; i < n; i++) nerr += (status[i] & ~0xF) != 0;
+    }
+    return nerr;
 }
 
 // sphere-sphere (cass.c:23-64): log det(1 - M^2) of the plane-sphere round trip M at

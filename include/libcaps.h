@@ -61,6 +61,8 @@ typedef struct caps
     detalg_t detalg;
     /* private: arithmetic of the factorisation, see caps_gpu_set_precision */
     int precision;
+    /* private: determinant path under DETALG_HODLR, see caps_gpu_set_path */
+    int path;
 } caps_t;
 
 /* Matrix object of one (xi, m) (src/include/libcaps.h:101-109).  The GPU
@@ -174,6 +176,8 @@ void caps_integrate_plasma_free(integration_plasma_t *self);                    
 #define CAPS_ST_ERR_PIVOT 16  /* non-positive pivot: result NaN */
 #define CAPS_ST_ERR_NONFINITE 32 /* non-finite integral or element: result NaN */
 #define CAPS_ST_ERR_GRID  64  /* quadrature grid exceeded its node budget: result NaN */
+#define CAPS_ST_ERR_WAIT  128 /* a bounded wait for the tensor cores ran out: result NaN */
+#define CAPS_ST_ERR_HODLR 256 /* HODLR block rank over its limit (the batch call then factors it densely) */
 
 /* log det(1-M) for n (xi_[i], m[i]) pairs of one geometry, all matrices
  * assembled and factored as one GPU batch (replaces n calls of caps_logdetD,
@@ -185,6 +189,18 @@ int caps_logdetD_batch(caps_t *self, const double *xi_, const int *m, int n, dou
 #define CAPS_PREC_FP64  0  /* plain FP64 Cholesky */
 #define CAPS_PREC_MIXED 1  /* tensor-core factorisation + FP64 log-det correction */
 int caps_gpu_set_precision(caps_t *self, int precision);
+
+/* determinant path of an FP64 caps object with DETALG_HODLR (the default): a HODLR
+ * factorisation with the elements evaluated on demand (src/libhodlr, matrix.c:125-147) or the
+ * dense batched Cholesky with the same result rules.  Automatic: HODLR from dimension
+ * CAPS_HODLR_AUTO_DIM on (where sampling the off-diagonal blocks needs fewer q-sums than the
+ * dense I table).  The mixed precision form always factors densely.  Returns 1, or 0 for an
+ * unknown path. */
+#define CAPS_PATH_AUTO  0
+#define CAPS_PATH_HODLR 1
+#define CAPS_PATH_DENSE 2
+#define CAPS_HODLR_AUTO_DIM 4000
+int caps_gpu_set_path(caps_t *self, int path);
 
 /* Free energy E (L+R)/(hbar c) at temperature T via the Matsubara sum with the
  * reference's m cutoff and xi truncation (src/caps.c:307-396, 749-852).
