@@ -20,6 +20,14 @@ HBAR_EV = 6.582119514e-16
 C_LIGHT = 299792458.0
 
 
+def gauss_laguerre(n):
+    """nodes x and weights w e^x of the n-point Gauss-Laguerre rule"""
+    x, w = np.empty(n), np.empty(n)
+    if not lib.caps_gauss_laguerre(int(n), x.ctypes.data_as(C.POINTER(C.c_double)), w.ctypes.data_as(C.POINTER(C.c_double))):
+        raise ValueError("unsupported number of points")
+    return x, w
+
+
 class _EnergyInfo(C.Structure):
     _fields_ = [("nxi", C.c_int), ("ndet", C.c_int), ("nwasted", C.c_int), ("seconds", C.c_double),
                 ("xi", C.POINTER(C.c_double)), ("logdetD", C.POINTER(C.c_double))]
@@ -54,6 +62,8 @@ def _load():
         "caps_integrate_plasma": (d, [vp, i, i, i, dp, dp]),
         "caps_free_energy": (d, [vp, d, d, d, C.POINTER(_EnergyInfo)]),
         "caps_free_energy_T0": (d, [vp, d, d, i, C.POINTER(_EnergyInfo)]),
+        "caps_free_energy_T0_gl": (d, [vp, d, i, C.POINTER(_EnergyInfo)]),
+        "caps_gauss_laguerre": (i, [i, dp, dp]),
         "caps_logdetD2_batch": (i, [vp, dp, ip, i, dp, ip]),
         "caps_sphere_sphere_T0": (d, [vp, d, d, C.POINTER(_EnergyInfo)]),
         "caps_free_energy_psd": (d, [vp, d, d, d, i, C.POINTER(_EnergyInfo)]),
@@ -312,6 +322,10 @@ class Caps:
         """free energy at T = 0, E (L+R)/(hbar c); method "qagi" (the reference's default) or "fcqs"."""
         m = {"qagi": 0, "fcqs": 1}[method]
         return self._energy(lambda info: lib.caps_free_energy_T0(self._h, float(cutoff), float(epsrel), m, info))
+
+    def free_energy_T0_gl(self, n=60, cutoff=1e-9):
+        """free energy at T = 0 by an n-point Gauss-Laguerre rule in x = 2 xi L/c"""
+        return self._energy(lambda info: lib.caps_free_energy_T0_gl(self._h, float(cutoff), int(n), info))
 
     def logdetD2_batch(self, xi_, m):
         """sphere-sphere: log det(1 - M^2) per (xi, m); make the object with L = d/2"""

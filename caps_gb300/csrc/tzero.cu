@@ -550,6 +550,93 @@ extern "C" double caps_free_energy_T0(caps_t *self, double cutoff, double epsrel
     return integral / alpha / M_PI;
 }
 
+// ---- Gauss-Laguerre rule: int_0^inf e^{-x} f(x) dx ~ sum_i w_i f(x_i) ----
+// Nodes: eigenvalues of the n x n Jacobi matrix of the Laguerre polynomials (diagonal 2k + 1,
+// off-diagonal k; Golub and Welsch 1969), found by bisection on Sturm counts and polished by
+// Newton's method on L_n; weights w_i = x_i / ((n + 1) L_{n+1}(x_i))^2.  The caller receives
+// w_i e^{x_i} (the integrand without its e^{-x}), formed from logarithms.
+static void laguerre(int n, double x, double *Ln, double *dLn, double *Ln1)
+{
+    double p0 = 1.0, p1 = 1.0 - x; // L_0, L_1
+    if (n == 0) p1 = 1.0;
+    for (int k = 1; k < n; k++) { const double p2 = ((2 * k + 1 - x) * p1 - k * p0) / (k + 1); p0 = p1; p1 = p2; }
+    // p1 = L_n, p0 = L_{n-1}; L_n' = n (L_n - L_{n-1}) / x; L_{n+1} = ((2n + 1 - x) L_n - n L_{n-1}) / (n + 1)
+    *Ln = p1;
+    *dLn = n * (p1 - p0) / x;
+    *Ln1 = ((2 * n + 1 - x) * p1 - n * p0) / (n + 1);
+}
+
+extern "C" int caps_gauss_laguerre(int n, double *x, double *w_ex)
+{
+    if (n < 1 || n > 200) return 0;
+    // Sturm count of the symmetric tridiagonal matrix below lam: the number of negative
+    // pivots of T - lam I
+    auto below = [&](double lam) {
+        int cnt = 0;
+        double d = 1.0 - lam; // k = 0
+        if (d < 0) cnt++;
+        for (int k = 1; k < n; k++) {
+            const double e2 = (double)k * k;
+            d = (2 * k + 1 - lam) - e2 / (d == 0.0 ? 1e-300 : d);
+            if (d < 0) cnt++;
+        }
+        return cnt;
+    };
+    const double hi0 = 4.0 * n + 2.0; // Gershgorin bound: 2n - 1 + 2(n - 1) < 4n
+    for (int i = 0; i < n; i++) {
+        double lo = 0.0, hi = hi0;
+        for (int it = 0; it < 200 && hi - lo > 1e-15 * hi; it++) {
+            const double mid = 0.5 * (lo + hi);
+            if (below(mid) > i) hi = mid; else lo = mid;
+        }
+        double z = 0.5 * (lo + hi), Ln, dLn, Ln1;
+        for (int it = 0; it < 3; it++) {
+            laguerre(n, z, &Ln, &dLn, &Ln1);
+            if (dLn == 0.0) break;
+            const double dz = Ln / dLn;
+            if (!(std::fabs(dz) < 1e-3 * (hi - lo + 1e-12) + 1e-12 * z)) break; // stay inside the bracket
+            z -= dz;
+        }
+        laguerre(n, z, &Ln, &dLn, &Ln1);
+        x[i] = z;
+        w_ex[i] = std::exp(std::log(z) - 2 * std::log(std::fabs((n + 1) * Ln1)) + z);
+    }
+    return 1;
+}
+
+// ---- free energy at T = 0 by an n-point Gauss-Laguerre rule in x = 2 xi L / c ----
+extern "C" double caps_free_energy_T0_gl(caps_t *self, double cutoff, int n, caps_energy_info_t *info)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    const double L = self->L, R = self->R, LbyR = L / R;
+    const double alpha = 2 * L / (L + R);
+    const double xi_cutoff = -(1 + 1 / LbyR) * std::log(2 * LbyR * 1e-100) / 2; // PFA cut (caps.c:252-262)
+    std::vector<double> x(n), w(n), xs, F(n, 0.0);
+    TERMINATE(!caps_gauss_laguerre(n, x.data(), w.data()), "Gauss-Laguerre rule of %d points not supported", n);
+    std::vector<int> where;
+    for (int i = 0; i < n; i++) {
+        const double xi_ = x[i] / alpha;
+        if (!(LbyR < 0.1 && xi_ > xi_cutoff)) { xs.push_back(xi_); where.push_back(i); }
+    }
+    int ndet = 0, nwasted = 0;
+    std::vector<double> v(xs.size());
+    if (!xs.empty()) fxi_batch(self, xs.data(), (int)xs.size(), cutoff, v.data(), &ndet, &nwasted, 0);
+    for (size_t k = 0; k < xs.size(); k++) F[where[k]] = v[k];
+    double s = 0, c = 0;
+    for (int i = 0; i < n; i++) { const double y = w[i] * F[i] - c, u = s + y; c = (u - s) - y; s = u; }
+    if (info) {
+        info->nxi = n;
+        info->ndet = ndet;
+        info->nwasted = nwasted;
+        info->seconds = seconds_since(t0);
+        for (int i = 0; i < n && i < 4096; i++) {
+            if (info->xi) info->xi[i] = x[i] / alpha;
+            if (info->logdetD) info->logdetD[i] = F[i];
+        }
+    }
+    return s / alpha / M_PI;
+}
+
 // ---- free energy at T > 0 by Pade spectrum decomposition ----
 extern "C" double caps_free_energy_psd(caps_t *self, double T, double cutoff, double epsrel, int order, caps_energy_info_t *info)
 {

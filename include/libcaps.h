@@ -223,6 +223,12 @@ double caps_free_energy(caps_t *self, double T, double cutoff, double epsrel, ca
  * function values are evaluated as one GPU batch.  info (optional): nxi = integrand
  * evaluations; xi/logdetD record the first 4096 of them. */
 double caps_free_energy_T0(caps_t *self, double cutoff, double epsrel, int method, caps_energy_info_t *info);
+/* Free energy at T = 0 by an n-point Gauss-Laguerre rule in x = 2 xi L/c (no reference
+ * counterpart; the reference integrates the same E = 1/(alpha pi) int_0^inf dx F(x/alpha)
+ * adaptively): all n frequencies and their m sums in one batch, the PFA cut as above. */
+double caps_free_energy_T0_gl(caps_t *self, double cutoff, int n, caps_energy_info_t *info);
+/* the n-point Gauss-Laguerre rule (n <= 200): nodes x and weights times e^x; returns 1 */
+int caps_gauss_laguerre(int n, double *x, double *w_ex);
 /* Free energy at T > 0 by Pade spectrum decomposition (src/caps.c:811-831) of the given
  * order (<= 0: the reference's automatic order, caps.c:635-639); all poles in one batch. */
 double caps_free_energy_psd(caps_t *self, double T, double cutoff, double epsrel, int order, caps_energy_info_t *info);

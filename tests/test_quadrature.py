@@ -85,3 +85,21 @@ def test_psd_low_poles_are_matsubara(lib):
     for k in range(5):
         assert abs(xi[k] / (2 * math.pi * (k + 1)) - 1) < 4e-16, (k, xi[k])
         assert abs(eta[k] - 1) < 1e-14, (k, eta[k])
+
+
+def test_gauss_laguerre_rule():
+    """caps_gauss_laguerre (the T = 0 Gauss-Laguerre driver's rule): numpy's nodes and weights,
+    and the moments int_0^inf e^-x x^k dx = k! exact for k <= 2n - 1"""
+    import math
+
+    import numpy as np
+
+    import caps_gb300 as cg
+    for n in (5, 20, 60):
+        x, wex = cg.gauss_laguerre(n)
+        xr, wr = np.polynomial.laguerre.laggauss(n)
+        assert np.max(np.abs(x - xr) / xr) < 1e-12
+        assert np.max(np.abs(wex * np.exp(-x) - wr) / wr) < 1e-10
+        for k in (0, 1, n, 2 * n - 1):
+            s = sum(math.exp(math.log(wi) - xi + k * math.log(xi)) for xi, wi in zip(x, wex))
+            assert abs(s / math.factorial(k) - 1) < 1e-11, (n, k, s)
