@@ -317,6 +317,15 @@ def main():
     caps.set_drude(OMEGAP_EV, GAMMA_EV)
     caps.set_precision(prec)
 
+    # autotuner (untimed set-up): the trailing-update schedule of the mixed form, or the FP64
+    # determinant path, timed on eight matrices of the workload
+    Ts = matsubara_spacing()
+    t_at = time.time()
+    chosen, at_ms = caps.autotune(Ts, nprobe=8)
+    autotune = {"candidates_ms_per_matrix": at_ms, "chosen": chosen, "seconds": time.time() - t_at,
+                "candidates": (["panel images by bulk copies", "panel staged through registers", "one CTA per tile"]
+                               if args.precision == "mixed" else ["dense Cholesky", "HODLR"])}
+
     net, train_info = None, None
     args.learned = not args.plain
     if args.learned:
@@ -448,6 +457,7 @@ def main():
             "bound": "FP32/ALU instruction issue; no HBM or tensor roofline applies (DRAM idle)",
             "evidence": "ncu issue-slot and pipe figures of the q-sum kernel on a small case of this workload"},
         "cpu_baseline": cpu,
+        "autotune": autotune,
         "learned_training": train_info,
         "learned_gain": learned_gain,
         "fp64_plain_form": fp64,

@@ -28,6 +28,10 @@ def gauss_laguerre(n):
     return x, w
 
 
+class _AutotuneInfo(C.Structure):
+    _fields_ = [("ncand", C.c_int), ("chosen", C.c_int), ("ms_per_matrix", C.c_double * 4)]
+
+
 class _EnergyInfo(C.Structure):
     _fields_ = [("nxi", C.c_int), ("ndet", C.c_int), ("nwasted", C.c_int), ("seconds", C.c_double),
                 ("xi", C.POINTER(C.c_double)), ("logdetD", C.POINTER(C.c_double))]
@@ -69,6 +73,7 @@ def _load():
         "caps_free_energy_psd": (d, [vp, d, d, d, i, C.POINTER(_EnergyInfo)]),
         "caps_gpu_set_precision": (i, [vp, i]),
         "caps_gpu_set_path": (i, [vp, i]),
+        "caps_gpu_autotune": (i, [vp, d, i, vp]),
         "caps_gpu_last_error": (C.c_char_p, []),
         "caps_gpu_set_stream": (None, [vp]),
         "caps_gpu_timings": (i, [dp, i]),
@@ -207,6 +212,13 @@ class Caps:
 
     def set_precision(self, prec):
         return lib.caps_gpu_set_precision(self._h, prec)
+
+    def autotune(self, xi_, nprobe=8):
+        """time the candidate schedules on nprobe matrices of this workload, keep the fastest;
+        returns (chosen index, device ms per matrix of each candidate)"""
+        info = _AutotuneInfo()
+        lib.caps_gpu_autotune(self._h, float(xi_), int(nprobe), C.byref(info))
+        return info.chosen, list(info.ms_per_matrix[:info.ncand])
 
     def set_path(self, path):
         """determinant path under DETALG_HODLR: PATH_AUTO, PATH_HODLR or PATH_DENSE"""

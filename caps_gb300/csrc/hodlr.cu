@@ -732,6 +732,14 @@ static HTree hodlr_tree(int n)
     return T;
 }
 
+// largest rank a node of level l can hold: its shorter side (its sizes differ by at most one
+// from the level's first node), at most HL_RMAX
+static int hl_level_rank(const HTree &T, int l)
+{
+    const HNode &N = T.nodes[(1 << l) - 1];
+    return std::min(HL_RMAX, N.size - N.c0 + 1);
+}
+
 size_t hodlr_work_bytes(int ldim, int nbatch)
 {
     const HTree T = hodlr_tree(2 * ldim);
@@ -743,7 +751,7 @@ size_t hodlr_work_bytes(int ldim, int nbatch)
     }
     const size_t leaf = (size_t)(1 << T.NL) * hl_leaf_scratch();
     size_t node = 0;
-    for (int l = 0; l < T.NL; l++) node = std::max(node, (size_t)(1 << l) * hl_node_scratch(HL_RMAX));
+    for (int l = 0; l < T.NL; l++) node = std::max(node, (size_t)(1 << l) * hl_node_scratch(hl_level_rank(T, l)));
     const size_t scratch = std::max(aca, std::max(leaf, node));
     return (size_t)nbatch * ((size_t)T.qstride * 8 + (size_t)nn * (sizeof(int) + sizeof(double)) + scratch) + nn * sizeof(HNode) + 4096;
 }
@@ -822,7 +830,7 @@ void hodlr_logdet_batch(const Task *tasks, const int *tlist, int nbatch, int ldi
     COUNT_LAUNCH(1);
     // nodes, bottom-up
     for (int l = T.NL - 1; l >= 0; l--) {
-        k_hodlr_node<<<dim3(1 << l, nbatch), HL_T, 0, st>>>(C, l, scratch, hl_node_scratch(HL_RMAX));
+        k_hodlr_node<<<dim3(1 << l, nbatch), HL_T, 0, st>>>(C, l, scratch, hl_node_scratch(hl_level_rank(T, l)));
         COUNT_LAUNCH(1);
     }
     k_hodlr_final<<<(nbatch + 127) / 128, 128, 0, st>>>(C, nbatch, result);

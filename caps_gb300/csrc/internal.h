@@ -100,9 +100,11 @@ size_t mixed_work_bytes(int ntask, int n);
 void kernel_timer_enable(bool on);
 void kernel_timer_collect(long long nfactored);
 void kernel_timer_stats(double *ms, double *bytes, long long *launches);
+// schedules of the mixed form's trailing update
+enum { MIXED_SCHED_IMAGES = 0, MIXED_SCHED_REGSTAGE = 1, MIXED_SCHED_PER_TILE = 2, MIXED_SCHED_COUNT = 3 };
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
                            const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc,
-                           bool convert, void *work);
+                           bool convert, void *work, int sched);
 void launch_final(int ntask, int n, const double *logdiag, const double *trace, int *status, double *result, int mode, cudaStream_t st);
 
 // HODLR log-determinants of the listed tasks (hodlr.cu), FP64, elements on demand; the

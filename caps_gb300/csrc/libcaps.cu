@@ -99,6 +99,17 @@ struct Engine {
 };
 static Engine g_eng;
 
+// schedules chosen by caps_gpu_autotune, per (precision, matrix dimension): for the mixed form
+// the trailing-update schedule (MIXED_SCHED_*); absent entries use MIXED_SCHED_IMAGES
+static std::map<std::pair<int, int>, int> g_sched;
+static std::mutex g_sched_mu;
+static int schedule_for(int precision, int dim)
+{
+    std::lock_guard<std::mutex> lk(g_sched_mu);
+    auto it = g_sched.find({precision, dim});
+    return it == g_sched.end() ? MIXED_SCHED_IMAGES : it->second;
+}
+
 static void engine_init()
 {
     if (g_eng.ready) return;
@@ -715,11 +726,13 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         static const bool tc = getenv("CAPS_MIXED_SIMT") == nullptr;
         if (ff_elem) {
             void *d_work = g_eng.mwork.get(mixed_work_bytes(nt, dim));
-            launch_cholesky_mixed(nt, dim, nullptr, 0, 0, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, false, d_work);
+            launch_cholesky_mixed(nt, dim, nullptr, 0, 0, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, false, d_work,
+                                  schedule_for(caps->precision, dim));
         } else if (O.factor && caps->precision == CAPS_PREC_MIXED && !O.square) {
             d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
             void *d_work = g_eng.mwork.get(mixed_work_bytes(nt, dim));
-            launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, true, d_work);
+            launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, true, d_work,
+                                  schedule_for(caps->precision, dim));
         } else if (hodlr) {
             if (nlist > 0)
                 hodlr_logdet_batch(d_tasks, d_list, nlist, ldim, d_K, nu_stride, d_ptab, pstride, d_lft, d_Sa, d_Sb, d_uv, d_trace,
@@ -809,6 +822,52 @@ extern "C" int caps_logdetD_batch(caps_t *self, const double *xi_, const int *m,
         for (int i = 0; i < n; i++) nerr += (status[i] & ~0xF) != 0;
     }
     return nerr;
+}
+
+// Autotuner: for this object's dimension and precision, time each candidate schedule on a
+// probe batch of the object's own workload (nprobe matrices at xi_, m = 0, 1, ... -- the
+// low m of a frequency are the matrices that reach the factorisation) and keep the fastest:
+// the trailing-update schedule of the mixed form (process-wide, per dimension), or the
+// determinant path of the FP64 form under DETALG_HODLR (dense Cholesky or HODLR, stored in
+// the object).  Each candidate runs twice; the second run's device time of the batch counts.
+// The schedules give the same result to the rounding of the FP32 update (mixed) or to the
+// compression tolerance (HODLR); within a process a dimension keeps its choice.
+extern "C" int caps_gpu_autotune(caps_t *self, double xi_, int nprobe, caps_autotune_info_t *info)
+{
+    if (nprobe <= 0 || !(xi_ > 0)) return 0;
+    const int dim = 2 * self->ldim;
+    std::vector<double> xs(nprobe, xi_), out(nprobe);
+    std::vector<int> ms(nprobe), st(nprobe);
+    for (int k = 0; k < nprobe; k++) ms[k] = k;
+    const bool mixed = self->precision == CAPS_PREC_MIXED;
+    const int ncand = mixed ? MIXED_SCHED_COUNT : (self->detalg == DETALG_HODLR ? 2 : 1);
+    std::vector<double> ms_per(ncand, 0.0);
+    const int saved_path = self->path;
+    for (int c = 0; c < ncand; c++) {
+        if (mixed) {
+            std::lock_guard<std::mutex> lk(g_sched_mu);
+            g_sched[{CAPS_PREC_MIXED, dim}] = c;
+        } else
+            self->path = c == 0 ? CAPS_PATH_DENSE : CAPS_PATH_HODLR;
+        caps_logdetD_batch(self, xs.data(), ms.data(), nprobe, out.data(), st.data());
+        caps_logdetD_batch(self, xs.data(), ms.data(), nprobe, out.data(), st.data());
+        ms_per[c] = g_eng.timings[5] / nprobe;
+    }
+    int best = 0;
+    for (int c = 1; c < ncand; c++)
+        if (ms_per[c] < ms_per[best]) best = c;
+    if (mixed) {
+        std::lock_guard<std::mutex> lk(g_sched_mu);
+        g_sched[{CAPS_PREC_MIXED, dim}] = best;
+        self->path = saved_path;
+    } else
+        self->path = ncand == 1 ? saved_path : (best == 0 ? CAPS_PATH_DENSE : CAPS_PATH_HODLR);
+    if (info) {
+        info->ncand = ncand;
+        info->chosen = best;
+        for (int c = 0; c < ncand && c < 4; c++) info->ms_per_matrix[c] = ms_per[c];
+    }
+    return 1;
 }
 
 // sphere-sphere (cass.c:23-64): log det(1 - M^2) of the plane-sphere round trip M at

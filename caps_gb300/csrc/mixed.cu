@@ -527,7 +527,7 @@ size_t mixed_work_bytes(int ntask, int n)
 
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
                            const double *mdiag, const double *trace, double *result, int mode, cudaStream_t st, bool tc, bool convert,
-                           void *work)
+                           void *work, int sched)
 {
     // work: mixed_work_bytes(ntask, n) of scratch (diagonal-block inverses, Frobenius partials,
     // panel images)
@@ -540,11 +540,16 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     // already holds it.  mdiag: M_ii in FP64, n per task (tr(A - I) = -tr M).
     // Trailing update: tcgen05 (k_syrk_umma); CAPS_MIXED_MMASYNC=1 selects the mma.sync
     // kernel, tc = false (CAPS_MIXED_SIMT=1) the FFMA one.
+    // The schedule of the trailing update (sched, chosen by the caller's autotuner):
+    // MIXED_SCHED_IMAGES the persistent kernel fed by bulk copies of the panel images,
+    // MIXED_SCHED_REGSTAGE the persistent kernel staging the panel through registers (16
+    // producer warps), MIXED_SCHED_PER_TILE one CTA per tile.  The environment overrides it:
+    // CAPS_MIXED_REGSTAGE=1, CAPS_MIXED_NOPIPE=1, CAPS_MIXED_MMASYNC=1 (mma.sync).
     static const bool legacy_mma = getenv("CAPS_MIXED_MMASYNC") != nullptr;
-    static const bool no_pipe = getenv("CAPS_MIXED_NOPIPE") != nullptr;
-    // CAPS_MIXED_REGSTAGE=1: the whole-trailing-matrix update stages the panel through
-    // registers (16 producer warps) instead of copying prepared images
-    static const bool reg_stage = getenv("CAPS_MIXED_REGSTAGE") != nullptr;
+    static const bool env_no_pipe = getenv("CAPS_MIXED_NOPIPE") != nullptr;
+    static const bool env_reg_stage = getenv("CAPS_MIXED_REGSTAGE") != nullptr;
+    const bool no_pipe = env_no_pipe || (!env_reg_stage && sched == MIXED_SCHED_PER_TILE);
+    const bool reg_stage = env_reg_stage || (!env_no_pipe && sched == MIXED_SCHED_REGSTAGE);
     // the persistent updates read the panel from images that the panel solves write (and X
     // then stays out of S); the register-staged and one-CTA-per-tile updates read S
     const bool use_img = !reg_stage && !no_pipe;

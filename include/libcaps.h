@@ -202,6 +202,20 @@ int caps_gpu_set_precision(caps_t *self, int precision);
 #define CAPS_HODLR_AUTO_DIM 4000
 int caps_gpu_set_path(caps_t *self, int path);
 
+/* Autotuner (no reference counterpart): times the candidate schedules for this object's
+ * dimension and precision on nprobe matrices of its own workload (xi_, m = 0 .. nprobe-1)
+ * and keeps the fastest.  Mixed form: the tensor-core trailing update's schedule (0 panel
+ * images by bulk copies, 1 panel staged through registers, 2 one CTA per tile), kept for the
+ * dimension for the rest of the process.  FP64 under DETALG_HODLR: the determinant path
+ * (0 dense, 1 HODLR), stored in the object as by caps_gpu_set_path.  info (optional) receives
+ * the device milliseconds per matrix of each candidate.  Returns 1, or 0 for bad arguments. */
+typedef struct {
+    int ncand;               /* candidates timed */
+    int chosen;              /* index of the fastest */
+    double ms_per_matrix[4]; /* device time per matrix of each candidate */
+} caps_autotune_info_t;
+int caps_gpu_autotune(caps_t *self, double xi_, int nprobe, caps_autotune_info_t *info);
+
 /* Free energy E (L+R)/(hbar c) at temperature T via the Matsubara sum with the
  * reference's m cutoff and xi truncation (src/caps.c:307-396, 749-852).
  * The xi = 0 term follows the reference's material rules.  info arrays may be

@@ -79,3 +79,35 @@ def test_hodlr_unit_vectors_RbyL1000(cg, unit_vectors):
         assert s < 16, (v, s)
         assert relx(got, v["logdetD"]) < t["tolerance"], (v, got)
     print("R/L=1000, dimension 20000: %d matrices by HODLR in %.2f s" % (len(cases), th))
+
+
+def test_large_aspect_workload_vs_reference(cg):
+    """plasma, R/L = 1000, L = 100 nm, ldim 6000 (dimension 12000) at three nodes of the
+    60-point Gauss-Laguerre rule (tests/golden/reference_c4.json, the reference library's LU
+    and HODLR values): the FP64 form (automatic path: HODLR) at 1e-10, the mixed form at 5e-8"""
+    import json
+    import os
+
+    from conftest import GOLDEN
+    d = json.load(open(os.path.join(GOLDEN, "reference_c4.json")))
+    cases = d["cases"]
+    v0 = cases[0]
+    for prec, tol in ((cg.PREC_FP64, TOL), (cg.PREC_MIXED, 5e-8)):
+        c = caps(cg, v0["R"], v0["L"], v0["ldim"], (v0["omegap_eV"], v0["gamma_eV"]))
+        c.set_precision(prec)
+        out, st = c.logdetD_batch([v["xi"] for v in cases], [v["m"] for v in cases])
+        for v, got, s in zip(cases, out, st):
+            assert s < 16, (v, s)
+            assert rel(got, v["LU"]) < tol, (prec, v["xi"], v["m"], got, v["LU"])
+            assert rel(got, v["HODLR"]) < tol, (prec, v["xi"], v["m"], got, v["HODLR"])
+
+
+def test_hodlr_free_energy_T0_gauss_laguerre(cg):
+    """a T = 0 free energy (20-point Gauss-Laguerre rule, plasma, R/L = 100, L = 100 nm,
+    dimension 1400) through the HODLR path equals the dense FP64 path's to 1e-10"""
+    E = {}
+    for path in (cg.PATH_HODLR, cg.PATH_DENSE):
+        c = caps(cg, 1e-5, 1e-7, 700, (9.0, 0.0), path)
+        E[path], info = c.free_energy_T0_gl(20)
+        assert info["ndet"] > 0
+    assert abs(E[cg.PATH_HODLR] - E[cg.PATH_DENSE]) <= 1e-10 * abs(E[cg.PATH_DENSE]), E
