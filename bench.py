@@ -277,7 +277,26 @@ def main():
     ap.add_argument("--ncu-matrices", type=int, default=8,
                     help="matrices in the profiling case; other than 8: n = 1..4, m = 0, 4, 8, ... (all factored), "
                          "e.g. 48 for a trailing-matrix working set above L2")
+    ap.add_argument("--hodlr-case", choices=["r150", "r1000"], default=None,
+                    help="profiling case: --ncu-matrices matrices through the FP64 HODLR path, of this workload (r150) "
+                         "or of the large-aspect one (r1000: plasma, R/L=1000, L=100 nm, ldim 6000, dimension 12000)")
     args = ap.parse_args()
+    if args.hodlr_case:
+        import caps_gb300 as cg
+        n = args.ncu_matrices
+        if args.hodlr_case == "r150":
+            caps = cg.Caps(R, L, ldim=LDIM)
+            caps.set_drude(OMEGAP_EV, GAMMA_EV)
+            xi, ms = [matsubara_spacing()] * n, [(10 * k) % 100 for k in range(n)]
+        else:
+            caps = cg.Caps(1e-4, 1e-7, ldim=6000)
+            caps.set_drude(9.0, 0.0)
+            xi, ms = [(250.0, 500.5, 1000.0, 2000.0)[k % 4] for k in range(n)], [(7 * k) % 200 for k in range(n)]
+        caps.set_path(cg.PATH_HODLR)
+        t = time.time()
+        out, st = caps.logdetD_batch(xi, ms)
+        print(json.dumps({"logdetD": list(out), "status": [int(s) for s in st], "seconds": time.time() - t}))
+        return
     if args.ncu_case:
         import caps_gb300 as cg
         Ts = matsubara_spacing()
