@@ -280,7 +280,29 @@ def main():
     ap.add_argument("--hodlr-case", choices=["r150", "r1000"], default=None,
                     help="profiling case: --ncu-matrices matrices through the FP64 HODLR path, of this workload (r150) "
                          "or of the large-aspect one (r1000: plasma, R/L=1000, L=100 nm, ldim 6000, dimension 12000)")
+    ap.add_argument("--c4", action="store_true",
+                    help="the large-aspect T = 0 free energy once (plasma, R/L=1000, L=100 nm, ldim 6000, 60-point "
+                         "Gauss-Laguerre rule) in the chosen precision; --path picks the FP64 determinant path")
+    ap.add_argument("--path", default="auto", choices=["auto", "hodlr", "dense"])
     args = ap.parse_args()
+    if args.c4:
+        import caps_gb300 as cg
+        caps = cg.Caps(1e-4, 1e-7, ldim=6000)
+        caps.set_drude(9.0, 0.0)
+        caps.set_precision(cg.PREC_MIXED if args.precision == "mixed" else cg.PREC_FP64)
+        caps.set_path({"auto": cg.PATH_AUTO, "hodlr": cg.PATH_HODLR, "dense": cg.PATH_DENSE}[args.path])
+        cg.counters(reset=True)
+        w0 = cg.work()
+        t = time.time()
+        E, info = caps.free_energy_T0_gl(60)
+        dt = time.time() - t
+        w1 = cg.work()
+        print(json.dumps({"workload": "plasma (wp=9 eV), R/L=1000, L=1e-7 m, T=0, ldim=6000 (dimension 12000), "
+                                      "60-point Gauss-Laguerre rule in 2 xi L/c",
+                          "precision": args.precision, "path": args.path, "E": E, "time_to_E_s": dt,
+                          "matrices": info["ndet"], "matrices_beyond_cutoffs": info["nwasted"],
+                          "matrices_factored": w1["nfactor"] - w0["nfactor"], "gpu_launches": cg.counters()["launches"]}))
+        return
     if args.hodlr_case:
         import caps_gb300 as cg
         n = args.ncu_matrices
