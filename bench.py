@@ -364,7 +364,8 @@ def main():
     t_at = time.time()
     chosen, at_ms = caps.autotune(Ts, nprobe=8)
     autotune = {"candidates_ms_per_matrix": at_ms, "chosen": chosen, "seconds": time.time() - t_at,
-                "candidates": (["panel images by bulk copies", "panel staged through registers", "one CTA per tile"]
+                "candidates": (["dense: panel images by bulk copies", "dense: panel staged through registers",
+                                "dense: one CTA per tile", "HODLR (float-float sampled elements, FP64 factorisation)"]
                                if args.precision == "mixed" else ["dense Cholesky", "HODLR"])}
 
     net, train_info = None, None

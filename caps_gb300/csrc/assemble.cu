@@ -15,6 +15,7 @@
 #include "special.cuh"
 #include "kgrid.cuh"
 #include "qsum64.cuh"
+#include "qsum_ff.cuh"
 #include "internal.h"
 
 namespace capsgpu {
@@ -474,8 +475,6 @@ __global__ void k_a12(const int *group_m, const int *group_lmin, int ngroup, int
 // FP64 form keeps k_a12.  The mixed table is written as float-float (A012F), so the
 // q-sum kernel needs no FP64 instruction.
 // per-m tables of the mixed form, formed in FP64 and stored as float-float
-struct A12L { ff F1, F2; ffe eG; };         // per l, index l - (lmin - 1)
-struct A12J { ff h1, pa, pb, pc; ffe eH; }; // per l1 + l2, index l1 + l2 - 2(lmin - 1)
 CAPS_DEV ffe ffe_from_sd(sd v)
 {
     if (v.m == 0.0) return ffe{0.0f, 0.0f, FFE_ZERO_E, 0};
@@ -537,34 +536,7 @@ __global__ void k_a12_mix(const int *group_m, const int *group_lmin, const int *
         while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
         a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
     }
-    const int mt = group_m[g], mm = mt > 0 ? mt : 1;
-    const int l1 = group_lmin[g] - 1 + a1, l2 = group_lmin[g] - 1 + a2;
-    A012F r{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0, 0};
-    if (!(l2 < mm || l2 < mt || l1 < 1)) {
-        const int qmax = min(min(l1, l2), (l1 + l2 - 2 * mm) / 2);
-        // the closed forms of a_0, a_1, a_2 in float-float (FP32 pipe) from the per-m tables
-        const A12L x = tl[(size_t)g * L + a1], y = tl[(size_t)g * L + a2];
-        const A12J z = tj[(size_t)g * NJ + a1 + a2];
-        ff p = ff_mul(ff_mul(ff{x.eG.h, x.eG.l}, ff{y.eG.h, y.eG.l}), ff{z.eH.h, z.eH.l});
-        int e = x.eG.e + y.eG.e + z.eH.e;
-        const int k = fexpo(p.h);
-        if (k > -127) { p = ff_shift(p, -k); e += k; }
-        r.a0h = p.h;
-        r.a0l = p.l;
-        r.a0e = e;
-        const ff f = ff_add(x.F1, y.F1);
-        if (qmax >= 1) {
-            const ff v = ff_mul(ff{(float)(l1 + l2) - 1.5f, 0.0f}, ff_add(ff{1.0f, 0.0f}, ff_neg(ff_mul(z.h1, f))));
-            r.a1h = v.h;
-            r.a1l = v.l;
-        }
-        if (qmax >= 2) {
-            const ff t = ff_add(ff_add(x.F2, ff_mul(ff{2.0f * x.F1.h, 2.0f * x.F1.l}, y.F1)), y.F2);
-            const ff v = ff_mul(z.pa, ff_add(ff_mul(z.pb, ff_add(ff_mul(z.pc, t), ff_neg(f))), ff{0.5f, 0.0f}));
-            r.a2h = v.h;
-            r.a2l = v.l;
-        }
-    }
+    const A012F r = a012f_pair(group_m[g], group_lmin[g], a1, a2, tl + (size_t)g * L, tj + (size_t)g * NJ);
     tab[(size_t)g * npair + pid] = r;
 }
 

@@ -34,6 +34,7 @@
 #include "common.cuh"
 #include "internal.h"
 #include "qsum64.cuh"
+#include "qsum_ff.cuh"
 
 namespace capsgpu {
 
@@ -66,6 +67,14 @@ struct HCtx {
     const double *trace;
     int *status;
     double *part;       // per matrix: one log-det partial per node (leaves included), level-major
+    // mixed form: the I values by the float-float q-sums (paired K table, float-float p
+    // tables and a_0..a_2 tables per m group); the rest of the path stays FP64
+    int mixed;
+    const float4 *KP;
+    const int *KPe;
+    const float4 *ptabf;
+    const A12L *tl;
+    const A12J *tj;
 };
 
 __device__ __forceinline__ int node_id(int level, int k) { return (1 << level) - 1 + k; }
@@ -136,6 +145,17 @@ __device__ void hl_ipair(const HCtx &C, int task, int x, int y, sd &tm, sd &te)
     const int mm = T.m > 0 ? T.m : 1;
     if (l2 < mm || l2 < T.m || l1 < 1) { // I = 0 for l < m (integration.c:631)
         tm = te = sd{0, 0};
+        return;
+    }
+    if (C.mixed) {
+        const int g = T.mgroup, L = C.ldim + 2;
+        const A012F A = a012f_pair(T.m, T.lmin, a1, a2, C.tl + (size_t)g * L, C.tj + (size_t)g * (2 * L - 1));
+        ffe res[1][2];
+        if (qsum_ff_pair<1>(T, &task, 1, l1, l2, A, C.KP, C.KPe, C.nu_stride, C.ptabf + (size_t)g * 2 * C.pstride * 2, C.pstride,
+                            QSUM_FF_STOP_BITS, res))
+            atomicOr(C.status + task, ST_ERR_NONFINITE);
+        tm = sd_norm((double)res[0][1].h + (double)res[0][1].l, res[0][1].e);
+        te = sd_norm((double)res[0][0].h + (double)res[0][0].l, res[0][0].e);
         return;
     }
     const A012 A = a012_pair(T.m, T.lmin, a1, a2, C.lft);
@@ -759,9 +779,18 @@ size_t hodlr_work_bytes(int ldim, int nbatch)
 int hodlr_levels(int ldim) { return hodlr_tree(2 * ldim).NL; }
 
 static HCtx hodlr_ctx(const Task *tasks, const int *tlist, int ldim, const sd *K, int nu_stride, const double4 *ptab, int pstride,
-                      const double *lft, const sd *Sa, const sd *Sb, const double2 *uv, const double *trace, int *status)
+                      const double *lft, const sd *Sa, const sd *Sb, const double2 *uv, const double *trace, int *status,
+                      const HodlrMixed *mx)
 {
     HCtx C{};
+    if (mx) {
+        C.mixed = 1;
+        C.KP = mx->KP;
+        C.KPe = mx->KPe;
+        C.ptabf = mx->ptabf;
+        C.tl = (const A12L *)mx->a12t;
+        C.tj = (const A12J *)((const char *)mx->a12t + (size_t)(ldim + 2) * mx->ngroup * sizeof(A12L));
+    }
     C.tasks = tasks;
     C.tlist = tlist;
     C.ldim = ldim;
@@ -779,9 +808,9 @@ static HCtx hodlr_ctx(const Task *tasks, const int *tlist, int ldim, const sd *K
 }
 
 void hodlr_diag(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double4 *ptab, int pstride, const double *lft,
-                const sd *Sa, const sd *Sb, const double2 *uv, double *mdiag, int *status, cudaStream_t st)
+                const sd *Sa, const sd *Sb, const double2 *uv, double *mdiag, int *status, cudaStream_t st, const HodlrMixed *mx)
 {
-    const HCtx C = hodlr_ctx(tasks, nullptr, ldim, K, nu_stride, ptab, pstride, lft, Sa, Sb, uv, nullptr, status);
+    const HCtx C = hodlr_ctx(tasks, nullptr, ldim, K, nu_stride, ptab, pstride, lft, Sa, Sb, uv, nullptr, status, mx);
     k_hodlr_diag<<<dim3((ldim + 127) / 128, ntask), 128, 0, st>>>(C, ntask, mdiag);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
@@ -791,7 +820,7 @@ void hodlr_diag(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stri
 // ST_ERR_HODLR marks a matrix whose compression exceeded HL_RMAX
 void hodlr_logdet_batch(const Task *tasks, const int *tlist, int nbatch, int ldim, const sd *K, int nu_stride, const double4 *ptab,
                         int pstride, const double *lft, const sd *Sa, const sd *Sb, const double2 *uv, const double *trace,
-                        int *status, double *result, void *work, cudaStream_t st)
+                        int *status, double *result, void *work, cudaStream_t st, const HodlrMixed *mx)
 {
     if (nbatch <= 0) return;
     static bool attr = false;
@@ -805,7 +834,7 @@ void hodlr_logdet_batch(const Task *tasks, const int *tlist, int nbatch, int ldi
     HNode *d_nodes = (HNode *)w;
     w += (nn * sizeof(HNode) + 255) & ~(size_t)255;
     CK(cudaMemcpyAsync(d_nodes, T.nodes.data(), nn * sizeof(HNode), cudaMemcpyHostToDevice, st));
-    HCtx C = hodlr_ctx(tasks, tlist, ldim, K, nu_stride, ptab, pstride, lft, Sa, Sb, uv, trace, status);
+    HCtx C = hodlr_ctx(tasks, tlist, ldim, K, nu_stride, ptab, pstride, lft, Sa, Sb, uv, trace, status, mx);
     C.nodes = d_nodes;
     C.NL = T.NL;
     C.qstride = T.qstride;

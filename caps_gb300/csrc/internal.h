@@ -107,15 +107,23 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
                            bool convert, void *work, int sched);
 void launch_final(int ntask, int n, const double *logdiag, const double *trace, int *status, double *result, int mode, cudaStream_t st);
 
-// HODLR log-determinants of the listed tasks (hodlr.cu), FP64, elements on demand; the
-// diagonal of M alone for the trace rule; workspace bytes for nbatch matrices
+// HODLR log-determinants of the listed tasks (hodlr.cu), elements on demand; the diagonal of
+// M alone for the trace rule; workspace bytes for nbatch matrices.  mx == nullptr: the I
+// values by the FP64 q-sums (K, ptab); otherwise by the float-float q-sums from these tables
+struct HodlrMixed {
+    const float4 *KP;    // paired K table (k_kred_ff)
+    const int *KPe;
+    const float4 *ptabf; // float-float p tables per m group (launch_ptab_groups)
+    const void *a12t;    // a_0..a_2 tables per m group (launch_a12_mixed with tabs)
+    int ngroup;
+};
 size_t hodlr_work_bytes(int ldim, int nbatch);
 int hodlr_levels(int ldim);
 void hodlr_diag(const Task *tasks, int ntask, int ldim, const sd *K, int nu_stride, const double4 *ptab, int pstride, const double *lft,
-                const sd *Sa, const sd *Sb, const double2 *uv, double *mdiag, int *status, cudaStream_t st);
+                const sd *Sa, const sd *Sb, const double2 *uv, double *mdiag, int *status, cudaStream_t st, const HodlrMixed *mx);
 void hodlr_logdet_batch(const Task *tasks, const int *tlist, int nbatch, int ldim, const sd *K, int nu_stride, const double4 *ptab,
                         int pstride, const double *lft, const sd *Sa, const sd *Sb, const double2 *uv, const double *trace,
-                        int *status, double *result, void *work, cudaStream_t st);
+                        int *status, double *result, void *work, cudaStream_t st, const HodlrMixed *mx);
 
 // F for n abscissae at once; QUADPACK qagi with every node of a step in one call (tzero.cu)
 using BatchFn = std::function<void(const double *x, int n, double *y)>;

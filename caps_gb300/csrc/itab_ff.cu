@@ -22,23 +22,11 @@
 #include "common.cuh"
 #include "ff.cuh"
 #include "internal.h"
+#include "qsum_ff.cuh"
 
 namespace capsgpu {
 
-// float-float quotient x / y (Dekker 1971: one correction of the leading quotient).  The
-// reciprocal is the hardware approximation (relative error ~2^-23): the correction
-// q2 = (x - q1 y) r then leaves a relative error ~2^-45, below the 2^-44 the q-sums keep.
-CAPS_DEV ff ff_div(ff x, ff y)
-{
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y.h));
-    const float q1 = x.h * r;
-    const ff p = ff_mul(ff{q1, 0.0f}, y);
-    const ff rem = ff_add(x, ff_neg(p));
-    return ff_fast2(q1, rem.h * r);
-}
-
-// The q-sums with both polarisations of a task under one exponent frame: the paired K
+// The q-sums (qsum_ff.cuh) with both polarisations of a task under one exponent frame: the paired K
 // table (KP: TM h, l, TE h, l; KPe: their common exponent) lets one alignment serve both, and
 // a_q is scaled into the task's frame once (an exact power of two) before the two float-float
 // products.  Per task the state is the two float-float sums, the frame exponent, the two stop
@@ -57,13 +45,6 @@ CAPS_DEV ff ff_div(ff x, ff y)
 // the full kernel forms.  Output: I tables as float-float (ffe) or, with ffe_out false, as
 // scaled doubles.  The kernel is bound by FP32/ALU issue and the latency of float-float
 // dependency chains, so occupancy pays (MINB blocks of 128 per SM).
-struct PAcc {
-    float th, tl, eh, el; // TM and TE sums, (h + l) 2^e
-    int e;
-    int thr_t, thr_e;     // exponent (frame units) below which a term is insignificant
-    int last;             // last q with a significant term (2 before the loop: q = 3, 4, 5 may stop it)
-};
-
 template <int G, bool BAND, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_itab_pk(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim,
                                                  const float4 *__restrict__ KP, const int *__restrict__ KPe, int nu_stride,
@@ -117,129 +98,15 @@ __global__ void __launch_bounds__(128, MINB) k_itab_pk(const Task *tasks, const 
         for (int g = 0; g < ng; g++) { store(g, 1, 0.0f, 0.0f, FFE_ZERO_E); store(g, 0, 0.0f, 0.0f, FFE_ZERO_E); }
         return;
     }
-    const bool both = !T.is_pr;
-    const int l12 = l1 + l2;
-    const int qmax = min(min(l1, l2), (l12 - 2 * mm) / 2);
-    const A012F A12 = a12[(size_t)grp.z * npair + pid];
-    const ff a1f{A12.a1h, A12.a1l}, a2f{A12.a2h, A12.a2l};
-    const int koff = -T.mu;
-
-    // add c K(nu) (c in frame units of exponent ec) to task g's sums; true if significant
-    auto add = [&](PAcc &A, int g, ff c, int ec, int nu) {
-        const size_t k = (size_t)tk[g] * nu_stride + (nu + koff);
-        const float4 kv = KP[k];
-        int d = ec + KPe[k] - A.e;
-        if (d > 30) { // a term far above the frame: move the frame up (exact shifts)
-            A.th = fshift(A.th, -d); A.tl = fshift(A.tl, -d); A.eh = fshift(A.eh, -d); A.el = fshift(A.el, -d);
-            A.thr_t -= d; A.thr_e -= d; A.e += d; d = 0;
-        }
-        const float p2 = __uint_as_float((unsigned)max(127 + d, 0) << 23);
-        const ff cs{c.h * p2, c.l * p2};
-        const ff tT = ff_mul(cs, ff{kv.x, kv.y});
-        const ff sT = ff_add(ff{A.th, A.tl}, tT);
-        A.th = sT.h; A.tl = sT.l;
-        bool sig = fexpo(tT.h) >= A.thr_t;
-        if (both) {
-            const ff tE = ff_mul(cs, ff{kv.z, kv.w});
-            const ff sE = ff_add(ff{A.eh, A.el}, tE);
-            A.eh = sE.h; A.el = sE.l;
-            sig |= fexpo(tE.h) >= A.thr_e;
-        }
-        return sig;
-    };
-
-    PAcc acc[G];
-#pragma unroll
-    for (int g = 0; g < G; g++) {
-        PAcc &A = acc[g];
-        A = PAcc{0.0f, 0.0f, 0.0f, 0.0f, 0, 0, 0, -(1 << 30)};
-        if (g >= ng) continue;
-        const size_t k = (size_t)tk[g] * nu_stride + (l12 + koff);
-        const float4 k0 = KP[k];
-        A.th = k0.x; A.tl = k0.y; A.eh = k0.z; A.el = k0.w; A.e = KPe[k];
-        A.thr_t = fexpo(k0.x) - stop_bits;
-        A.thr_e = fexpo(k0.z) - stop_bits;
-        A.last = 2;
-        if (qmax >= 1) add(A, g, a1f, 0, l12 - 2);
-        if (qmax >= 2) add(A, g, a2f, 0, l12 - 4);
-    }
-
-    if (qmax >= 3) {
-        const long long Si = l1 + l2 + 1, Di = l1 - l2;
-        int ip = l12 - 6; // p of q = 3
-        const long long n1st = ((long long)(ip + 1 - Si) * (ip + 1 + Si)) * ((long long)(ip + 1 - Di) * (ip + 1 + Di));
-        const int sig = (n1st == 0 ? 0 : (63 - __clzll(n1st < 0 ? -n1st : n1st))) - 20;
-        const int sa = sig / 2, sc = sig - sa;
-        const float fS = (float)Si, fD = (float)Di;
-        const float sA = __uint_as_float((unsigned)(127 - sa) << 23), sC = __uint_as_float((unsigned)(127 - sc) << 23);
-        auto Nf = [&](float x) {
-            const float p1 = x - fS, p2 = x + fS, q1 = x - fD, q2 = x + fD;
-            const float ah = p1 * p2, ch = q1 * q2;
-            const ff av{ah * sA, fmaf(p1, p2, -ah) * sA}, cv{ch * sC, fmaf(q1, q2, -ch) * sC};
-            return ff_mul(av, cv);
-        };
-        const bool diag = (l1 == l2);
-        const float m2f = 2.0f * mm, dlf = (float)(l1 - l2), pA = m2f * dlf;
-        const ff ApF = ff_mul(ff{pA, fmaf(m2f, dlf, -pA)}, ff{(float)(l1 + l2 + 1), 0.0f});
-        const ff Ap2 = diag ? ff{0.0f, 0.0f} : ff_shift(ff_mul(ApF, ApF), -30 - sig);
-        const float4 *pt = ptabf + ((size_t)grp.z * 2 + (diag ? 1 : 0)) * pstride * 2;
-        const int e_b = fexpo(A12.a2h);
-        ff bm2 = ff_shift(a1f, -e_b), bm1 = ff_shift(a2f, -e_b);
-        int eb = e_b, eD = 0;
-        ff Dq{1.0f, 0.0f}, Zprev{1.0f, 0.0f};
-        float fx = (float)(ip + 1);
-        ff N3 = Nf(fx + 2.0f), N4 = Nf(fx + 3.0f);
-        bool any = true;
-        for (int q = 3; q <= qmax && any; q++, ip -= 2, fx -= 2.0f) {
-            const ff N1 = Nf(fx), N2 = Nf(fx + 1.0f);
-            const float4 kh = pt[2 * ip], kl = pt[2 * ip + 1];
-            const ff X = ff_add(Ap2, ff_add(ff_mul(ff{kh.y, kl.y}, N2), ff_mul(ff{kh.z, kl.z}, N3)));
-            const ff Y = ff_mul(ff{kh.w, kl.w}, N4);
-            const ff Z = ff_mul(ff{kh.x, kl.x}, N1);
-            const ff b = ff_add(ff_mul(X, bm1), ff_neg(ff_mul(ff_mul(Y, Zprev), bm2)));
-            Dq = ff_mul(Dq, Z);
-            N3 = N1; N4 = N2; Zprev = Z;
-            bm2 = bm1; bm1 = b;
-            {
-                const int kb = fexpo(bm1.h);
-                if (kb > 40 || (kb < -40 && kb > -127)) { bm1 = ff_shift(bm1, -kb); bm2 = ff_shift(bm2, -kb); eb += kb; }
-                const int kd = fexpo(Dq.h);
-                if (kd > 40 || kd < -40) { Dq = ff_shift(Dq, -kd); eD += kd; }
-            }
-            const ff aq = ff_div(bm1, Dq);
-            const int ea = eb - eD;
-            any = false;
-#pragma unroll
-            for (int g = 0; g < G; g++) {
-                PAcc &A = acc[g];
-                if (q - A.last > 3) continue; // stopped (never true for g >= ng: last = -2^30)
-                if (add(A, g, aq, ea, ip)) A.last = q;
-                any |= q + 1 - A.last <= 3;
-            }
-        }
-    }
-
-    // I = a_0 sum; TE of a perfect reflector is -TM
-    const ff a0f{A12.a0h, A12.a0l};
+    ffe res[G][2];
+    const unsigned bad = qsum_ff_pair<G>(T, tk, ng, l1, l2, a12[(size_t)grp.z * npair + pid], KP, KPe, nu_stride,
+                                          ptabf + (size_t)grp.z * 2 * pstride * 2, pstride, stop_bits, res);
 #pragma unroll
     for (int g = 0; g < G; g++) {
         if (g >= ng) break;
-        const PAcc &A = acc[g];
-        ff r = ff_mul(a0f, ff{A.th, A.tl});
-        int k = fexpo(r.h);
-        if (k == -127 || k == 128) atomicOr(status + tk[g], ST_ERR_NONFINITE);
-        if (k == 128 || k == -127) k = 0;
-        r = ff_shift(r, -k);
-        const int eT = r.h == 0.0f ? FFE_ZERO_E : A.e + A12.a0e + k;
-        store(g, 1, r.h, r.l, eT);
-        if (both) {
-            ff s = ff_mul(a0f, ff{A.eh, A.el});
-            int ke = fexpo(s.h);
-            if (ke == 128 || ke == -127) ke = 0;
-            s = ff_shift(s, -ke);
-            store(g, 0, s.h, s.l, s.h == 0.0f ? FFE_ZERO_E : A.e + A12.a0e + ke);
-        } else
-            store(g, 0, -r.h, -r.l, eT);
+        if (bad & (1u << g)) atomicOr(status + tk[g], ST_ERR_NONFINITE);
+        store(g, 1, res[g][1].h, res[g][1].l, res[g][1].e);
+        store(g, 0, res[g][0].h, res[g][0].l, res[g][0].e);
     }
 }
 
@@ -253,7 +120,7 @@ __global__ void __launch_bounds__(128, MINB) k_itab_pk(const Task *tasks, const 
 // G = 3 at seven blocks 40.6, G = 4 at six 43.0, G = 5 at five 42.9, G = 6 at five 44.8,
 // against 55.4 for the per-polarisation kernel in the same run; E identical in all five.
 constexpr int IGRP = 3;
-constexpr int ITAB_STOP_BITS = 44; // early stop below 2^-44 of the q = 0 term
+constexpr int ITAB_STOP_BITS = QSUM_FF_STOP_BITS;
 int itab_group_size() { return IGRP; }
 
 void launch_itab_grp(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim, const float4 *KP, const int *KPe,

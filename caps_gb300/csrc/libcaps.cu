@@ -475,13 +475,15 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     // chunk size from free memory
     size_t freeb = 0, totb = 0;
     CK(cudaMemGetInfo(&freeb, &totb));
+    // HODLR semantics: the HODLR path (elements on demand) where it applies; the FP64 form
+    // takes it from CAPS_HODLR_AUTO_DIM on, the mixed form from CAPS_HODLR_AUTO_DIM_MIXED on
+    const bool mixed = caps->precision == CAPS_PREC_MIXED;
+    const bool hodlr = O.factor && !O.square && !O.M_out && !O.force_dense && caps->detalg == DETALG_HODLR &&
+                       (caps->path == CAPS_PATH_HODLR ||
+                        (caps->path == CAPS_PATH_AUTO && dim >= (mixed ? CAPS_HODLR_AUTO_DIM_MIXED : CAPS_HODLR_AUTO_DIM)));
     // mixed precision without a dense-M request: elements go straight into the FP32 delta
     // matrix (no FP64 matrix)
-    const bool ff_elem = caps->precision == CAPS_PREC_MIXED && O.factor && !O.M_out && !O.square;
-    // HODLR semantics in FP64: the HODLR path (elements on demand) where it applies
-    const bool hodlr = O.factor && !O.square && !O.M_out && !O.force_dense && caps->detalg == DETALG_HODLR &&
-                       caps->precision == CAPS_PREC_FP64 &&
-                       (caps->path == CAPS_PATH_HODLR || (caps->path == CAPS_PATH_AUTO && dim >= CAPS_HODLR_AUTO_DIM));
+    const bool ff_elem = mixed && O.factor && !O.M_out && !O.square && !hodlr;
     const size_t mat_bytes = O.square ? 16 : ff_elem ? 4 + 1 : (caps->precision == CAPS_PREC_MIXED ? 12 : 8);
     const size_t dense_bytes = hodlr ? hodlr_work_bytes(ldim, 1) : (size_t)dim * dim * mat_bytes + (size_t)2 * L * L * sizeof(sd)
                                                                     + (size_t)L * (L + 1) / 2 * 32; // a_0..a_2 table (one row per task)
@@ -599,8 +601,9 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         // a_0..a_2 per m; the mixed form's trace rule first needs only the band of each m
         void *d_a12t = nullptr;
         if (caps->precision == CAPS_PREC_MIXED) {
+            // (the HODLR path needs the per-m tables alone: its pairs combine them on demand)
             d_a12t = g_eng.a12t.get(a12_tab_bytes(ldim, ngroup));
-            launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, d_a12t, st, true, nullptr, -1, ff_elem);
+            launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, d_a12t, st, true, nullptr, hodlr ? 0 : -1, ff_elem);
         } else if (!hodlr)
             launch_a12(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, st);
         const size_t lda = dim, mstride = (size_t)dim * dim;
@@ -636,7 +639,20 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
                 d_list = dl;
             }
         };
-        if (caps->precision == CAPS_PREC_MIXED) {
+        HodlrMixed hmx{};
+        if (caps->precision == CAPS_PREC_MIXED && hodlr) {
+            // mixed HODLR: M_ii for the trace rule and, for the undecided matrices, every sampled
+            // element from float-float q-sums; compression and factorisation in FP64
+            float4 *d_ptabf = (float4 *)g_eng.ptabf.get((size_t)nt * 2 * pstride * 2 * sizeof(float4));
+            launch_ptab_groups(d_gm, ngroup, d_ptabf, pstride, st);
+            hmx = HodlrMixed{d_KP, d_KPe, d_ptabf, d_a12t, ngroup};
+            hodlr_diag(d_tasks, nt, ldim, nullptr, nu_stride, nullptr, pstride, d_lft, d_Sa, d_Sb, d_uv, d_dg, d_status, st, &hmx);
+            CK(cudaEventRecord(g_eng.ev[3], st));
+            launch_stats(nullptr, nt, dim, nullptr, lda, mstride, d_dg, O.mode, d_trace, d_res, d_status, st);
+            CK(cudaEventRecord(g_eng.ev[4], st));
+            undecided();
+            CK(cudaEventRecord(g_eng.ev[5], st));
+        } else if (caps->precision == CAPS_PREC_MIXED) {
             // mixed form: the q-sums in float-float on the FP32 pipe
             float4 *d_ptabf = (float4 *)g_eng.ptabf.get((size_t)nt * 2 * pstride * 2 * sizeof(float4));
             launch_ptab_groups(d_gm, ngroup, d_ptabf, pstride, st); // the recurrence tables depend on m alone
@@ -676,7 +692,7 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             // HODLR: M_ii for the trace rule, then the undecided matrices by HODLR with their
             // elements formed on demand (no I table, no dense matrix)
             launch_ptab(d_tasks, nt, d_ptab, pstride, st);
-            hodlr_diag(d_tasks, nt, ldim, d_K, nu_stride, d_ptab, pstride, d_lft, d_Sa, d_Sb, d_uv, d_dg, d_status, st);
+            hodlr_diag(d_tasks, nt, ldim, d_K, nu_stride, d_ptab, pstride, d_lft, d_Sa, d_Sb, d_uv, d_dg, d_status, st, nullptr);
             CK(cudaEventRecord(g_eng.ev[3], st));
             launch_stats(nullptr, nt, dim, nullptr, lda, mstride, d_dg, O.mode, d_trace, d_res, d_status, st);
             CK(cudaEventRecord(g_eng.ev[4], st));
@@ -724,7 +740,11 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
 
         // CAPS_MIXED_SIMT=1 selects the FP32 FFMA trailing update instead of split-TF32 tensor cores
         static const bool tc = getenv("CAPS_MIXED_SIMT") == nullptr;
-        if (ff_elem) {
+        if (hodlr) {
+            if (nlist > 0)
+                hodlr_logdet_batch(d_tasks, d_list, nlist, ldim, d_K, nu_stride, d_ptab, pstride, d_lft, d_Sa, d_Sb, d_uv, d_trace,
+                                   d_status, d_res, g_eng.hwork.get(hodlr_work_bytes(ldim, nlist)), st, mixed ? &hmx : nullptr);
+        } else if (ff_elem) {
             void *d_work = g_eng.mwork.get(mixed_work_bytes(nt, dim));
             launch_cholesky_mixed(nt, dim, nullptr, 0, 0, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, false, d_work,
                                   schedule_for(caps->precision, dim));
@@ -733,10 +753,6 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
             void *d_work = g_eng.mwork.get(mixed_work_bytes(nt, dim));
             launch_cholesky_mixed(nt, dim, d_A, lda, mstride, d_status, d_S, mstride, d_dg, d_trace, d_res, O.mode, st, tc, true, d_work,
                                   schedule_for(caps->precision, dim));
-        } else if (hodlr) {
-            if (nlist > 0)
-                hodlr_logdet_batch(d_tasks, d_list, nlist, ldim, d_K, nu_stride, d_ptab, pstride, d_lft, d_Sa, d_Sb, d_uv, d_trace,
-                                   d_status, d_res, g_eng.hwork.get(hodlr_work_bytes(ldim, nlist)), st);
         } else if (O.factor) {
             double *d_ld = (double *)g_eng.logdiag.get((size_t)nt * dim * sizeof(double));
             launch_cholesky(nt, dim, d_A, lda, mstride, d_status, d_ld, st);
@@ -829,7 +845,8 @@ extern "C" int caps_logdetD_batch(caps_t *self, const double *xi_, const int *m,
 // low m of a frequency are the matrices that reach the factorisation) and keep the fastest:
 // the trailing-update schedule of the mixed form (process-wide, per dimension), or the
 // determinant path of the FP64 form under DETALG_HODLR (dense Cholesky or HODLR, stored in
-// the object).  Each candidate runs twice; the second run's device time of the batch counts.
+// the object; under DETALG_HODLR the mixed form's candidates include its HODLR path too).
+// Each candidate runs twice; the second run's device time of the batch counts.
 // The schedules give the same result to the rounding of the FP32 update (mixed) or to the
 // compression tolerance (HODLR); within a process a dimension keeps its choice.
 extern "C" int caps_gpu_autotune(caps_t *self, double xi_, int nprobe, caps_autotune_info_t *info)
@@ -840,13 +857,18 @@ extern "C" int caps_gpu_autotune(caps_t *self, double xi_, int nprobe, caps_auto
     std::vector<int> ms(nprobe), st(nprobe);
     for (int k = 0; k < nprobe; k++) ms[k] = k;
     const bool mixed = self->precision == CAPS_PREC_MIXED;
-    const int ncand = mixed ? MIXED_SCHED_COUNT : (self->detalg == DETALG_HODLR ? 2 : 1);
+    const bool can_hodlr = self->detalg == DETALG_HODLR;
+    // mixed: the dense schedules, then (under DETALG_HODLR) the HODLR path; FP64: dense, HODLR
+    const int ncand = mixed ? MIXED_SCHED_COUNT + (can_hodlr ? 1 : 0) : (can_hodlr ? 2 : 1);
     std::vector<double> ms_per(ncand, 0.0);
     const int saved_path = self->path;
     for (int c = 0; c < ncand; c++) {
         if (mixed) {
-            std::lock_guard<std::mutex> lk(g_sched_mu);
-            g_sched[{CAPS_PREC_MIXED, dim}] = c;
+            self->path = c < MIXED_SCHED_COUNT ? CAPS_PATH_DENSE : CAPS_PATH_HODLR;
+            if (c < MIXED_SCHED_COUNT) {
+                std::lock_guard<std::mutex> lk(g_sched_mu);
+                g_sched[{CAPS_PREC_MIXED, dim}] = c;
+            }
         } else
             self->path = c == 0 ? CAPS_PATH_DENSE : CAPS_PATH_HODLR;
         caps_logdetD_batch(self, xs.data(), ms.data(), nprobe, out.data(), st.data());
@@ -856,12 +878,18 @@ extern "C" int caps_gpu_autotune(caps_t *self, double xi_, int nprobe, caps_auto
     int best = 0;
     for (int c = 1; c < ncand; c++)
         if (ms_per[c] < ms_per[best]) best = c;
-    if (mixed) {
-        std::lock_guard<std::mutex> lk(g_sched_mu);
-        g_sched[{CAPS_PREC_MIXED, dim}] = best;
+    if (ncand == 1)
         self->path = saved_path;
+    else if (mixed) {
+        // the fastest dense schedule is kept for the dimension in any case
+        int bs = 0;
+        for (int c = 1; c < MIXED_SCHED_COUNT; c++)
+            if (ms_per[c] < ms_per[bs]) bs = c;
+        std::lock_guard<std::mutex> lk(g_sched_mu);
+        g_sched[{CAPS_PREC_MIXED, dim}] = bs;
+        self->path = best == MIXED_SCHED_COUNT ? CAPS_PATH_HODLR : CAPS_PATH_DENSE;
     } else
-        self->path = ncand == 1 ? saved_path : (best == 0 ? CAPS_PATH_DENSE : CAPS_PATH_HODLR);
+        self->path = best == 0 ? CAPS_PATH_DENSE : CAPS_PATH_HODLR;
     if (info) {
         info->ncand = ncand;
         info->chosen = best;

@@ -194,20 +194,23 @@ int caps_gpu_set_precision(caps_t *self, int precision);
  * factorisation with the elements evaluated on demand (src/libhodlr, matrix.c:125-147) or the
  * dense batched Cholesky with the same result rules.  Automatic: HODLR from dimension
  * CAPS_HODLR_AUTO_DIM on (where sampling the off-diagonal blocks needs fewer q-sums than the
- * dense I table).  The mixed precision form always factors densely.  Returns 1, or 0 for an
- * unknown path. */
+ * dense I table).  The mixed form takes HODLR only when asked (CAPS_PATH_HODLR or the
+ * autotuner); its sampled elements then come from the float-float q-sums, its compression and
+ * factorisation stay FP64.  Returns 1, or 0 for an unknown path. */
 #define CAPS_PATH_AUTO  0
 #define CAPS_PATH_HODLR 1
 #define CAPS_PATH_DENSE 2
 #define CAPS_HODLR_AUTO_DIM 4000
+#define CAPS_HODLR_AUTO_DIM_MIXED 1000000000 /* the mixed form factors densely unless asked */
 int caps_gpu_set_path(caps_t *self, int path);
 
 /* Autotuner (no reference counterpart): times the candidate schedules for this object's
  * dimension and precision on nprobe matrices of its own workload (xi_, m = 0 .. nprobe-1)
  * and keeps the fastest.  Mixed form: the tensor-core trailing update's schedule (0 panel
  * images by bulk copies, 1 panel staged through registers, 2 one CTA per tile), kept for the
- * dimension for the rest of the process.  FP64 under DETALG_HODLR: the determinant path
- * (0 dense, 1 HODLR), stored in the object as by caps_gpu_set_path.  info (optional) receives
+ * dimension for the rest of the process, and under DETALG_HODLR candidate 3, the HODLR path;
+ * FP64 under DETALG_HODLR: the determinant path (0 dense, 1 HODLR).  The chosen path is
+ * stored in the object as by caps_gpu_set_path.  info (optional) receives
  * the device milliseconds per matrix of each candidate.  Returns 1, or 0 for bad arguments. */
 typedef struct {
     int ncand;               /* candidates timed */

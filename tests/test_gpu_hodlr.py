@@ -111,3 +111,38 @@ def test_hodlr_free_energy_T0_gauss_laguerre(cg):
         E[path], info = c.free_energy_T0_gl(20)
         assert info["ndet"] > 0
     assert abs(E[cg.PATH_HODLR] - E[cg.PATH_DENSE]) <= 1e-10 * abs(E[cg.PATH_DENSE]), E
+
+
+@pytest.mark.parametrize("name", ["pr_RbyL50_ldim350", "drude_RbyL150_ldim1050"])
+def test_mixed_hodlr_vs_reference_fixtures(cg, ref_values, name):
+    """the mixed form's HODLR path (float-float sampled elements, FP64 compression and
+    factorisation) against the reference library's HODLR and LU values at the mixed bar"""
+    cases = ref_values[name]
+    c0 = cases[0]
+    c = caps(cg, c0["R"], c0["L"], c0["ldim"], c0["drude"], cg.PATH_HODLR)
+    c.set_precision(cg.PREC_MIXED)
+    out, st = c.logdetD_batch([v["xi"] for v in cases], [v["m"] for v in cases])
+    for v, got, s in zip(cases, out, st):
+        assert s < 16, (v, s)
+        assert rel(got, v["HODLR"]) < 5e-8, (name, v["xi"], v["m"], got, v["HODLR"])
+        assert rel(got, v["LU"]) < 5e-8, (name, v["xi"], v["m"], got, v["LU"])
+
+
+def test_mixed_hodlr_large_aspect_vs_reference(cg):
+    """dimension 12000 (plasma, R/L = 1000, L = 100 nm): the mixed HODLR path against the
+    reference library's values at the mixed bar"""
+    import json
+    import os
+
+    from conftest import GOLDEN
+    cases = json.load(open(os.path.join(GOLDEN, "reference_c4.json")))["cases"]
+    v0 = cases[0]
+    c = caps(cg, v0["R"], v0["L"], v0["ldim"], (v0["omegap_eV"], v0["gamma_eV"]), cg.PATH_HODLR)
+    c.set_precision(cg.PREC_MIXED)
+    out, st = c.logdetD_batch([v["xi"] for v in cases], [v["m"] for v in cases])
+    worst = 0.0
+    for v, got, s in zip(cases, out, st):
+        assert s < 16, (v, s)
+        worst = max(worst, rel(got, v["LU"]))
+        assert rel(got, v["LU"]) < 5e-8, (v["xi"], v["m"], got, v["LU"])
+    print("mixed HODLR, dimension 12000: largest error against the reference's LU %.1e" % worst)
