@@ -397,7 +397,14 @@ def main():
     ctr = cg.counters()
     wk = cg.work()
     ph = cg.timings(cumulative=True)   # device ms per phase, summed over the timed steps
-    syrk_ms, syrk_bytes, syrk_n = cg.kernel_stats()
+    syrk_ms, syrk_bytes, syrk_n = cg.kernel_stats(0)
+    panel_kernels = {}
+    for kind, name in ((1, "k_trsm_inv (panel solve; writes the split-TF32 panel images)"),
+                       (2, "k_potf2_w (64 x 64 diagonal block and its inverse, one CTA per matrix)")):
+        ms_, by_, n_ = cg.kernel_stats(kind)
+        if n_:
+            panel_kernels[name] = {"launches": n_, "ms_per_step": ms_ / args.steps, "algorithmic_GBps": by_ / (ms_ * 1e-3) / 1e9,
+                                   "avg_launch_us": ms_ / n_ * 1e3}
     cg.kernel_timing(False)
 
     ndet = sum(i["ndet"] for i in infos)
@@ -493,7 +500,10 @@ def main():
                       "traffic_source": "DRAM bytes per algorithmic byte of the k_syrk_pipe launches in one ncu capture "
                                         "of 48 factored matrices of this workload, times this run's algorithmic bytes per "
                                         "launch (the images are written by the panel solves, outside these launches)",
-                      "fp32_accurate_tflops_factorisation": achieved}),
+                      "fp32_accurate_tflops_factorisation": achieved,
+                      "panel_kernels": panel_kernels or None,
+                      "panel_kernels_note": "the panel solve is bytes-bound like the update (its rate against the same peak); "
+                                            "the diagonal block is latency-bound: 64 dependent column steps per matrix"}),
         "dominant_kernel": None if args.precision == "fp64" else {
             "kernel": "k_itab_grp (float-float q-sums)", "phase_share_of_step": ph[2] / ph[5] if ph[5] else None,
             "bound": "FP32/ALU instruction issue; no HBM or tensor roofline applies (DRAM idle)",

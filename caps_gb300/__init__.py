@@ -82,6 +82,7 @@ def _load():
         "caps_gpu_fp64_peak": (d, []),
         "caps_gpu_kernel_timing": (None, [i]),
         "caps_gpu_kernel_stats": (None, [dp, dp, C.POINTER(C.c_longlong)]),
+        "caps_gpu_kernel_stats_kind": (None, [i, dp, dp, C.POINTER(C.c_longlong)]),
         "caps_gpu_fp32_peak": (d, []),
         "caps_gpu_work": (None, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
         "caps_logdetD_noalloc": (i, [vp, d, i, dp]),
@@ -121,14 +122,15 @@ def set_stream(handle):
 
 
 def kernel_timing(enable):
-    """live CUDA-event timing of the tcgen05 trailing update on/off (resets the totals)"""
+    """live CUDA-event timing of the factorisation's kernels on/off (resets the totals)"""
     lib.caps_gpu_kernel_timing(1 if enable else 0)
 
 
-def kernel_stats():
-    """(device ms, algorithmic bytes, launches) of the tcgen05 trailing update since kernel_timing(True)"""
+def kernel_stats(kind=0):
+    """(device ms, algorithmic bytes, launches) since kernel_timing(True) of the tcgen05 trailing
+    update (kind 0), the panel solve (1) or the diagonal block (2)"""
     ms, by, n = C.c_double(0), C.c_double(0), C.c_longlong(0)
-    lib.caps_gpu_kernel_stats(C.byref(ms), C.byref(by), C.byref(n))
+    lib.caps_gpu_kernel_stats_kind(int(kind), C.byref(ms), C.byref(by), C.byref(n))
     return ms.value, by.value, n.value
 
 

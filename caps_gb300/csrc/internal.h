@@ -99,7 +99,8 @@ size_t mixed_work_bytes(int ntask, int n);
 // live CUDA-event timing of the tcgen05 trailing update (mixed.cu)
 void kernel_timer_enable(bool on);
 void kernel_timer_collect(long long nfactored);
-void kernel_timer_stats(double *ms, double *bytes, long long *launches);
+enum { KT_SYRK = 0, KT_TRSM = 1, KT_POTF2 = 2, KT_KINDS = 3 };
+void kernel_timer_stats(int kind, double *ms, double *bytes, long long *launches);
 // schedules of the mixed form's trailing update
 enum { MIXED_SCHED_IMAGES = 0, MIXED_SCHED_REGSTAGE = 1, MIXED_SCHED_PER_TILE = 2, MIXED_SCHED_COUNT = 3 };
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,

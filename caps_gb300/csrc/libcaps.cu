@@ -169,9 +169,14 @@ extern "C" void caps_gpu_kernel_timing(int enable)
     kernel_timer_enable(enable != 0);
 }
 
+extern "C" void caps_gpu_kernel_stats_kind(int kind, double *ms, double *bytes, long long *launches)
+{
+    kernel_timer_stats(kind, ms, bytes, launches);
+}
+
 extern "C" void caps_gpu_kernel_stats(double *ms, double *bytes, long long *launches)
 {
-    kernel_timer_stats(ms, bytes, launches);
+    kernel_timer_stats(KT_SYRK, ms, bytes, launches);
 }
 
 extern "C" void caps_gpu_work(long long *nmat, long long *nfactor, double *factor_flops)

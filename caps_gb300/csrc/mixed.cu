@@ -458,11 +458,11 @@ __global__ void __launch_bounds__(256) k_final_mixed(int ntask, int n, const flo
     result[task] = ld;
 }
 
-// live timing of the tcgen05 trailing update (off unless caps_gpu_kernel_timing(1)):
-// CUDA events on the launching stream around every k_syrk_umma launch, and the
-// launch's algorithmic bytes per factored matrix (the trailing triangle read and
-// written once, the panel rows read once); kernel_timer_collect() resolves the events of
-// a finished batch and scales the bytes by the number of matrices it factored
+// live timing of the factorisation's kernels (off unless caps_gpu_kernel_timing(1)): CUDA
+// events on the launching stream around every launch of kind KT_SYRK (the tcgen05 trailing
+// update), KT_TRSM (the panel solve k_trsm_inv) and KT_POTF2 (the diagonal block k_potf2_w),
+// with each launch's algorithmic bytes per factored matrix; kernel_timer_collect() resolves
+// the events of a finished batch and scales the bytes by the number of matrices it factored
 namespace {
 struct KernelTimer {
     bool on = false;
@@ -481,37 +481,43 @@ struct KernelTimer {
         return pool[used++];
     }
 };
-KernelTimer g_kt;
+KernelTimer g_kts[KT_KINDS];
+KernelTimer &g_kt = g_kts[KT_SYRK];
 } // namespace
 
 void kernel_timer_enable(bool on)
 {
-    g_kt.on = on;
-    g_kt.used = 0;
-    g_kt.per_matrix_bytes.clear();
-    g_kt.ms = g_kt.bytes = 0;
-    g_kt.launches = 0;
+    for (KernelTimer &k : g_kts) {
+        k.on = on;
+        k.used = 0;
+        k.per_matrix_bytes.clear();
+        k.ms = k.bytes = 0;
+        k.launches = 0;
+    }
 }
 
 void kernel_timer_collect(long long nfactored)
 {
-    if (!g_kt.on) return;
-    for (size_t i = 0; i < g_kt.per_matrix_bytes.size(); i++) {
-        float f;
-        CK(cudaEventElapsedTime(&f, g_kt.pool[2 * i], g_kt.pool[2 * i + 1]));
-        g_kt.ms += f;
-        g_kt.bytes += g_kt.per_matrix_bytes[i] * (double)nfactored;
-        g_kt.launches++;
+    for (KernelTimer &k : g_kts) {
+        if (!k.on) continue;
+        for (size_t i = 0; i < k.per_matrix_bytes.size(); i++) {
+            float f;
+            CK(cudaEventElapsedTime(&f, k.pool[2 * i], k.pool[2 * i + 1]));
+            k.ms += f;
+            k.bytes += k.per_matrix_bytes[i] * (double)nfactored;
+            k.launches++;
+        }
+        k.used = 0;
+        k.per_matrix_bytes.clear();
     }
-    g_kt.used = 0;
-    g_kt.per_matrix_bytes.clear();
 }
 
-void kernel_timer_stats(double *ms, double *bytes, long long *launches)
+void kernel_timer_stats(int kind, double *ms, double *bytes, long long *launches)
 {
-    if (ms) *ms = g_kt.ms;
-    if (bytes) *bytes = g_kt.bytes;
-    if (launches) *launches = g_kt.launches;
+    const KernelTimer &k = g_kts[kind >= 0 && kind < KT_KINDS ? kind : 0];
+    if (ms) *ms = k.ms;
+    if (bytes) *bytes = k.bytes;
+    if (launches) *launches = k.launches;
 }
 
 // scratch: diagonal-block inverses, Frobenius partials, then (256-byte aligned) the panel
@@ -604,8 +610,14 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     // panel for its whole-trailing-matrix update.
     constexpr int PANEL = PIPE_IMG_CH * PIPE_IMG_TK; // outer panel width, 256
     auto factor_panel = [&](int k0, bool images) {
+        KernelTimer &tp = g_kts[KT_POTF2], &tt = g_kts[KT_TRSM];
+        if (tp.on) CK(cudaEventRecord(tp.next(), st));
         k_potf2_w<<<ntask, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part);
         COUNT_LAUNCH(1);
+        if (tp.on) { // the diagonal block read and written, its inverse written
+            CK(cudaEventRecord(tp.next(), st));
+            tp.per_matrix_bytes.push_back(3.0 * MB * MB * 4);
+        }
         const int rest = n - k0 - MB;
         if (rest <= 0) return false;
         const int t2 = k0 / PANEL * PANEL + PANEL;
@@ -614,9 +626,18 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         const int blk = (k0 % PANEL) / MB;
         const bool im64 = images && blk < PIPE_IMG64_BLOCKS && k0 + MB < std::min(t2, n);
         dim3 gt((rest + MT - 1) / MT, ntask);
+        if (tt.on) CK(cudaEventRecord(tt.next(), st));
         k_trsm_inv<<<gt, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part, im ? img : nullptr, t2,
                                       im ? (n - t2 + UM_M - 1) / UM_M : 0, im64 ? img64 : nullptr, blk, !images);
         COUNT_LAUNCH(1);
+        if (tt.on) { // the panel's rows below read; written: X (without images) or the split images
+            CK(cudaEventRecord(tt.next(), st));
+            double w = 0;
+            if (!images) w = 4.0 * rest * MB;
+            if (im) w += 8.0 * (n - t2) * MB;
+            if (im64) w += 8.0 * rest * MB;
+            tt.per_matrix_bytes.push_back(4.0 * rest * MB + w);
+        }
         return true;
     };
     if (tc && !legacy_mma) {

@@ -314,13 +314,17 @@ void caps_gpu_counters(long long *launches, long long *h2d_bytes, long long *d2h
  * factorisations (n^3/3 each) since the last counter reset */
 void caps_gpu_work(long long *nmat, long long *nfactor, double *factor_flops);
 
-/* live timing of the mixed form's tcgen05 trailing update (k_syrk_umma): with
- * caps_gpu_kernel_timing(1), CUDA events on the library's stream bracket every launch;
- * caps_gpu_kernel_stats returns the summed device milliseconds, the algorithmic bytes
- * (trailing triangle read and written once plus the panel rows, per factored matrix)
- * and the launch count since the last enable.  caps_gpu_kernel_timing(0) stops it. */
+/* live timing of the mixed form's factorisation kernels: with caps_gpu_kernel_timing(1),
+ * CUDA events on the library's stream bracket every launch; caps_gpu_kernel_stats returns
+ * for the tcgen05 trailing update the summed device milliseconds, the algorithmic bytes
+ * (trailing triangle read and written once plus the panel rows, per factored matrix) and
+ * the launch count since the last enable; caps_gpu_kernel_stats_kind the same for kind 0
+ * (trailing update), 1 (panel solve: the panel rows read, X or its split-TF32 images
+ * written) or 2 (diagonal block: read, written, its inverse written).
+ * caps_gpu_kernel_timing(0) stops it. */
 void caps_gpu_kernel_timing(int enable);
 void caps_gpu_kernel_stats(double *ms, double *bytes, long long *launches);
+void caps_gpu_kernel_stats_kind(int kind, double *ms, double *bytes, long long *launches);
 
 /* measured FP64 FMA throughput of the current device, TFLOP/s (a short probe kernel) */
 double caps_gpu_fp64_peak(void);
