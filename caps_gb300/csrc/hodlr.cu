@@ -150,12 +150,10 @@ __device__ void hl_ipair(const HCtx &C, int task, int x, int y, sd &tm, sd &te)
     if (C.mixed) {
         const int g = T.mgroup, L = C.ldim + 2;
         const A012F A = a012f_pair(T.m, T.lmin, a1, a2, C.tl + (size_t)g * L, C.tj + (size_t)g * (2 * L - 1));
-        ffe res[1][2];
+        auto put = [&](int, int pol, float h, float l, int e) { (pol ? tm : te) = sd_norm((double)h + (double)l, e); };
         if (qsum_ff_pair<1>(T, &task, 1, l1, l2, A, C.KP, C.KPe, C.nu_stride, C.ptabf + (size_t)g * 2 * C.pstride * 2, C.pstride,
-                            QSUM_FF_STOP_BITS, res))
+                            QSUM_FF_STOP_BITS, put))
             atomicOr(C.status + task, ST_ERR_NONFINITE);
-        tm = sd_norm((double)res[0][1].h + (double)res[0][1].l, res[0][1].e);
-        te = sd_norm((double)res[0][0].h + (double)res[0][0].l, res[0][0].e);
         return;
     }
     const A012 A = a012_pair(T.m, T.lmin, a1, a2, C.lft);

@@ -98,16 +98,11 @@ __global__ void __launch_bounds__(128, MINB) k_itab_pk(const Task *tasks, const 
         for (int g = 0; g < ng; g++) { store(g, 1, 0.0f, 0.0f, FFE_ZERO_E); store(g, 0, 0.0f, 0.0f, FFE_ZERO_E); }
         return;
     }
-    ffe res[G][2];
     const unsigned bad = qsum_ff_pair<G>(T, tk, ng, l1, l2, a12[(size_t)grp.z * npair + pid], KP, KPe, nu_stride,
-                                          ptabf + (size_t)grp.z * 2 * pstride * 2, pstride, stop_bits, res);
+                                          ptabf + (size_t)grp.z * 2 * pstride * 2, pstride, stop_bits, store);
 #pragma unroll
-    for (int g = 0; g < G; g++) {
-        if (g >= ng) break;
-        if (bad & (1u << g)) atomicOr(status + tk[g], ST_ERR_NONFINITE);
-        store(g, 1, res[g][1].h, res[g][1].l, res[g][1].e);
-        store(g, 0, res[g][0].h, res[g][0].l, res[g][0].e);
-    }
+    for (int g = 0; g < G; g++)
+        if (g < ng && (bad & (1u << g))) atomicOr(status + tk[g], ST_ERR_NONFINITE);
 }
 
 // tasks per subgroup.  q-sums of the R/L=150 free energy (ms), first float-float version:

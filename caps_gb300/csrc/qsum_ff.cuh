@@ -83,13 +83,13 @@ CAPS_DEV A012F a012f_pair(int mt, int lmin, int a1, int a2, const A12L *__restri
 }
 
 // I = a_0 sum_q a_q K_q of the pair (l1 >= l2 >= m', l1 >= 1) for the ng <= G tasks tk[] that
-// share T's m: res[g][1] TM, res[g][0] TE as (h + l) 2^e.  ptm: the m's float-float p table
-// (two rows of 2 pstride float4: l1 != l2, l1 == l2).  Returns a bit per task whose TM sum is
-// zero or not finite.
-template <int G>
+// share T's m, handed to out(g, pol, h, l, e) (pol 1 TM, 0 TE; value (h + l) 2^e) as each is
+// done.  ptm: the m's float-float p table (two rows of 2 pstride float4: l1 != l2, l1 == l2).
+// Returns a bit per task whose TM sum is zero or not finite.
+template <int G, class OUT>
 CAPS_DEV unsigned qsum_ff_pair(const Task &T, const int *tk, int ng, int l1, int l2, const A012F &A12, const float4 *__restrict__ KP,
                                const int *__restrict__ KPe, int nu_stride, const float4 *__restrict__ ptm, int pstride, int stop_bits,
-                               ffe (&res)[G][2])
+                               OUT out)
 {
     const int mm = T.m > 0 ? T.m : 1;
     const bool both = !T.is_pr;
@@ -206,15 +206,15 @@ CAPS_DEV unsigned qsum_ff_pair(const Task &T, const int *tk, int ng, int l1, int
         if (k == 128 || k == -127) k = 0;
         r = ff_shift(r, -k);
         const int eT = r.h == 0.0f ? FFE_ZERO_E : A.e + A12.a0e + k;
-        res[g][1] = ffe{r.h, r.l, eT, 0};
+        out(g, 1, r.h, r.l, eT);
         if (both) {
             ff s = ff_mul(a0f, ff{A.eh, A.el});
             int ke = fexpo(s.h);
             if (ke == 128 || ke == -127) ke = 0;
             s = ff_shift(s, -ke);
-            res[g][0] = ffe{s.h, s.l, s.h == 0.0f ? FFE_ZERO_E : A.e + A12.a0e + ke, 0};
+            out(g, 0, s.h, s.l, s.h == 0.0f ? FFE_ZERO_E : A.e + A12.a0e + ke);
         } else
-            res[g][0] = ffe{-r.h, -r.l, eT, 0};
+            out(g, 0, -r.h, -r.l, eT);
     }
     return bad;
 }
