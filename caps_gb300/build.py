@@ -19,7 +19,7 @@ LIB = os.path.join(BUILD, "libcaps_gb300.so")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
 
-SOURCES = ["libcaps.cu", "assemble.cu", "cholesky.cu", "xi0.cu", "noalloc.cu", "mixed.cu", "mlp.cu", "elem_ff.cu", "itab_ff.cu", "tzero.cu", "material.cu", "square.cu", "capc.cu", "hodlr.cu"]
+SOURCES = ["libcaps.cu", "assemble.cu", "cholesky.cu", "xi0.cu", "noalloc.cu", "mixed.cu", "mlp.cu", "elem_ff.cu", "itab_ff.cu", "tzero.cu", "material.cu", "square.cu", "capc.cu", "hodlr.cu", "sweep.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

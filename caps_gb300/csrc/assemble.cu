@@ -509,33 +509,20 @@ __global__ void k_a12_tabs(const int *group_m, const int *group_lmin, int ngroup
     tj[(size_t)g * NJ + i] = A12J{ff_from_d(h1), ff_from_d((s - 1) * (s - 7) / 4), ff_from_d(pb), ff_from_d(pc), ffe_from_sd(eH)};
 }
 
-// grid (ceil(npair/128), nlist) or, for the band (l1 - l2 in {0, 2}, the pairs the diagonal
-// of M reads), (ceil(2L/128), nlist); block row y fills group glist[y] (glist == nullptr: y)
-template <bool BAND>
+// grid (ceil(npair/128), nlist); block row y fills group glist[y] (glist == nullptr: y)
 __global__ void k_a12_mix(const int *group_m, const int *group_lmin, const int *glist, int nlist, int ldim, const A12L *__restrict__ tl,
                           const A12J *__restrict__ tj, A012F *tab)
 {
     const int L = ldim + 2, NJ = 2 * L - 1;
     const long long npair = (long long)L * (L + 1) / 2;
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if ((int)blockIdx.y >= nlist) return;
+    if ((int)blockIdx.y >= nlist || tid >= npair) return;
     const int g = glist ? glist[blockIdx.y] : (int)blockIdx.y;
-    long long pid;
-    int a1, a2;
-    if (BAND) {
-        if (tid >= 2LL * L) return;
-        a2 = (int)(tid >> 1);
-        a1 = a2 + 2 * (int)(tid & 1);
-        if (a1 >= L) return;
-        pid = (long long)a1 * (a1 + 1) / 2 + a2;
-    } else {
-        if (tid >= npair) return;
-        pid = tid;
-        a1 = (int)((sqrtf(8.0f * (float)pid + 1.0f) - 1.0f) * 0.5f);
-        while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
-        while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
-        a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
-    }
+    const long long pid = tid;
+    int a1 = (int)((sqrtf(8.0f * (float)pid + 1.0f) - 1.0f) * 0.5f);
+    while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
+    while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
+    const int a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
     const A012F r = a012f_pair(group_m[g], group_lmin[g], a1, a2, tl + (size_t)g * L, tj + (size_t)g * NJ);
     tab[(size_t)g * npair + pid] = r;
 }
@@ -788,7 +775,7 @@ size_t a12_tab_bytes(int ldim, int ngroup)
 }
 
 void launch_a12_mixed(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, void *work,
-                      cudaStream_t st, bool tabs, const int *glist, int nlist, bool band)
+                      cudaStream_t st, bool tabs, const int *glist, int nlist)
 {
     const long long L = ldim + 2, npair = L * (L + 1) / 2;
     A12L *tl = (A12L *)work;
@@ -800,11 +787,8 @@ void launch_a12_mixed(const int *group_m, const int *group_lmin, int ngroup, int
     }
     if (nlist < 0) nlist = ngroup;
     if (nlist > 0) {
-        dim3 g((unsigned)(((band ? 2 * L : npair) + 127) / 128), nlist);
-        if (band)
-            k_a12_mix<true><<<g, 128, 0, st>>>(group_m, group_lmin, glist, nlist, ldim, tl, tj, (A012F *)tab);
-        else
-            k_a12_mix<false><<<g, 128, 0, st>>>(group_m, group_lmin, glist, nlist, ldim, tl, tj, (A012F *)tab);
+        dim3 g((unsigned)((npair + 127) / 128), nlist);
+        k_a12_mix<<<g, 128, 0, st>>>(group_m, group_lmin, glist, nlist, ldim, tl, tj, (A012F *)tab);
         COUNT_LAUNCH(1);
     }
     CK(cudaGetLastError());

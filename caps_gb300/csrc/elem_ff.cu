@@ -92,15 +92,14 @@ __global__ void k_scale_ff(int ntask, int L, const sd *Sa, const sd *Sb, const d
 // columns lmin + i2 - 1 (i1, i2 index [lmin-1, lmin+ldim]); each is one linear combination
 // of I values times the scale factors.  One routine for the full assembly and for the
 // diagonal that the trace shortcut reads, so that both give the same numbers.
-template <bool OFFD>
-CAPS_DEV void elem_block(const Task &T, int L, const ffe *ITM, const ffe *ITE, int i1, int i2, size_t so, const ffe *__restrict__ Saf,
-                         const ffe *__restrict__ Sbf, const float4 *__restrict__ uvf, fe &EE, fe &MM, fe &EM, fe &ME)
+// Iv(pol, x, y) returns I of polarisation pol (1 = TM, 0 = TE) at window indices (x, y).
+template <bool OFFD, class IV>
+CAPS_DEV void elem_block(const Task &T, int i1, int i2, size_t so, const ffe *__restrict__ Saf, const ffe *__restrict__ Sbf,
+                         const float4 *__restrict__ uvf, IV Iv, fe &EE, fe &MM, fe &EM, fe &ME)
 {
     const fe sa1 = fe_ld(Saf[so + i1]), sa2 = fe_ld(Saf[so + i2]);
     const fe sb1 = fe_ld(Sbf[so + i1]), sb2 = fe_ld(Sbf[so + i2]);
-    // the table is symmetric; I(x, y) is read at t[y L + x] so that consecutive
-    // threads (consecutive x) read consecutive entries
-    auto Iv = [&](const ffe *t, int x, int y) { return fe_ld(t[(size_t)y * L + x]); };
+    const int ITM = 1, ITE = 0;
     EM = fe{0.0f, 0.0f, 0};
     ME = fe{0.0f, 0.0f, 0};
     if (T.m == 0) {
@@ -163,10 +162,12 @@ __global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, const int *tl
     float wsum = 0.0f;
     if (valid) {
         const Task &T = tasks[task];
-        const ffe *ITM = I + (size_t)(task * 2 + 1) * L * L;
-        const ffe *ITE = I + (size_t)(task * 2 + 0) * L * L;
+        // the table is symmetric; I(x, y) is read at t[y L + x] so that consecutive
+        // threads (consecutive x) read consecutive entries
+        const ffe *It = I + (size_t)task * 2 * L * L;
+        auto Iv = [&](int p, int x, int y) { return fe_ld(It[(size_t)p * L * L + (size_t)y * L + x]); };
         fe EE, MM, EM, ME;
-        elem_block<true>(T, L, ITM, ITE, a + 1, b + 1, (size_t)task * L, Saf, Sbf, uvf, EE, MM, EM, ME);
+        elem_block<true>(T, a + 1, b + 1, (size_t)task * L, Saf, Sbf, uvf, Iv, EE, MM, EM, ME);
         bool bad = false;
         const float ee = fe_to_float(EE, bad), mm = fe_to_float(MM, bad);
         const float em = fe_to_float(EM, bad), me = fe_to_float(ME, bad);
@@ -192,8 +193,8 @@ __global__ void __launch_bounds__(EB) k_elem_ff(const Task *tasks, const int *tl
 
 // the diagonal of M alone (kernel_logdet computes it first, matrix.c:62-66): grid
 // (ceil(ldim/EB), ntask), thread a writes M_ii of the diagonal block (a, a) in FP64, from
-// the band of I values that k_itab_pk's band mode leaves
-__global__ void __launch_bounds__(EB) k_diag_ff(const Task *tasks, int ntask, int ldim, const ffe *__restrict__ I,
+// the band seeds (pairs l1 - l2 in {0, 2}, sweep.cu's k_seed_ff)
+__global__ void __launch_bounds__(EB) k_diag_ff(const Task *tasks, int ntask, int ldim, const ffe *__restrict__ seed,
                                                 const ffe *__restrict__ Saf, const ffe *__restrict__ Sbf,
                                                 const float4 *__restrict__ uvf, double *diag, int *status)
 {
@@ -202,10 +203,13 @@ __global__ void __launch_bounds__(EB) k_diag_ff(const Task *tasks, int ntask, in
     const int a = blockIdx.x * EB + threadIdx.x;
     if (task >= ntask || a >= ldim) return;
     const Task &T = tasks[task];
-    const ffe *ITM = I + (size_t)(task * 2 + 1) * L * L;
-    const ffe *ITE = I + (size_t)(task * 2 + 0) * L * L;
+    // the diagonal block reads I at |x - y| in {0, 2} only
+    auto Iv = [&](int p, int x, int y) {
+        const int kind = x == y ? SEED_D0 : SEED_D2;
+        return fe_ld(seed[((size_t)(task * 2 + p) * SEED_KINDS + kind) * L + min(x, y)]);
+    };
     fe EE, MM, EM, ME;
-    elem_block<false>(T, L, ITM, ITE, a + 1, a + 1, (size_t)task * L, Saf, Sbf, uvf, EE, MM, EM, ME);
+    elem_block<false>(T, a + 1, a + 1, (size_t)task * L, Saf, Sbf, uvf, Iv, EE, MM, EM, ME);
     bool bad = false;
     fe_to_float(EE, bad);
     fe_to_float(MM, bad);
@@ -227,7 +231,10 @@ __global__ void k_stats_ff(const int *tlist, int nlist, int ldim, const double *
     const int task = tlist ? tlist[blockIdx.x] : (int)blockIdx.x;
     const int n = 2 * ldim, per_b = nbx * (EB / 32);
     __shared__ double red[256];
-    if (part) {
+    if (part && nbx == 0) { // one sum per task (k_sweep_ff)
+        if (threadIdx.x == 0) red[0] = (double)part[task];
+        __syncthreads();
+    } else if (part) {
         const float *p = part + (size_t)task * ldim * per_b;
         double s = 0.0;
         for (int i = threadIdx.x; i < ldim * per_b; i += blockDim.x) {
@@ -288,11 +295,11 @@ void launch_scale_ff(int ntask, int ldim, const sd *Sa, const sd *Sb, const doub
     CK(cudaGetLastError());
 }
 
-void launch_diag_ff(const Task *tasks, int ntask, int ldim, const void *I, const void *Saf, const void *Sbf, const float4 *uvf,
+void launch_diag_ff(const Task *tasks, int ntask, int ldim, const void *seed, const void *Saf, const void *Sbf, const float4 *uvf,
                     double *diag, int *status, cudaStream_t st)
 {
     dim3 g((ldim + EB - 1) / EB, ntask);
-    k_diag_ff<<<g, EB, 0, st>>>(tasks, ntask, ldim, (const ffe *)I, (const ffe *)Saf, (const ffe *)Sbf, uvf, diag, status);
+    k_diag_ff<<<g, EB, 0, st>>>(tasks, ntask, ldim, (const ffe *)seed, (const ffe *)Saf, (const ffe *)Sbf, uvf, diag, status);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }
@@ -309,10 +316,11 @@ void launch_elem_ff(const Task *tasks, const int *tlist, int nlist, int ldim, co
 }
 
 void launch_stats_ff(const int *tlist, int nlist, int ldim, const double *diag, const float *part, int mode, double *trace,
-                     double *result, int *status, cudaStream_t st)
+                     double *result, int *status, cudaStream_t st, bool part_per_task)
 {
     if (nlist <= 0) return;
-    k_stats_ff<<<nlist, 256, 0, st>>>(tlist, nlist, ldim, diag, part, (ldim + EB - 1) / EB, mode, trace, result, status);
+    k_stats_ff<<<nlist, 256, 0, st>>>(tlist, nlist, ldim, diag, part, part_per_task ? 0 : (ldim + EB - 1) / EB, mode, trace, result,
+                                      status);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

@@ -55,13 +55,13 @@ void launch_itab(const Task *tasks, const int *tlist, int nlist, int ldim, const
                  bool band);
 // float-float q recurrence tables once per distinct m (group_m), row g per group
 void launch_ptab_groups(const int *group_m, int ngroup, float4 *ptabf, int pstride, cudaStream_t st);
-// mixed form: q-sums with one a_q recurrence per (pair, subgroup of same-m tasks) (itab_ff.cu);
-// groups index tlist (nullptr: the tasks themselves); band: only the pairs the diagonal reads.
-// The p tables come first (launch_ptab_groups).
+// mixed form: q-sums of every pair with one a_q recurrence per (pair, subgroup of same-m tasks)
+// (itab_ff.cu); groups index tlist (nullptr: the tasks themselves).  The p tables come first
+// (launch_ptab_groups).
 int itab_group_size();
 void launch_itab_grp(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim, const float4 *KP,
                      const int *KPe, int nu_stride, const float4 *ptabf, int pstride, const void *a12, void *Iout, bool ffe_out,
-                     bool band, int *status, cudaStream_t st);
+                     int *status, cudaStream_t st);
 // sphere-sphere: B = 1 - M^2 and (M^2)_ii from A = 1 - M and M_ii (square.cu)
 void launch_square(int ntask, int n, const double *A, size_t lda, size_t mstride, const double *mdiag, double *B,
                    const int *status, double *mdiag2, cudaStream_t st);
@@ -70,10 +70,10 @@ void launch_a12(const int *group_m, const int *group_lmin, int ngroup, int ldim,
 size_t a12_bytes(int ldim, int ngroup);
 // mixed form: the same from per-m tables (work: a12_tab_bytes of scratch)
 size_t a12_tab_bytes(int ldim, int ngroup);
-// tabs: the per-m tables first; then the pairs of the listed groups (glist == nullptr: groups
-// 0..nlist-1, nlist < 0: all), band: only the pairs the diagonal reads
+// tabs: the per-m tables first; then every pair of the listed groups (glist == nullptr: groups
+// 0..nlist-1, nlist < 0: all)
 void launch_a12_mixed(const int *group_m, const int *group_lmin, int ngroup, int ldim, const double *lft, void *tab, void *work,
-                      cudaStream_t st, bool tabs = true, const int *glist = nullptr, int nlist = -1, bool band = false);
+                      cudaStream_t st, bool tabs = true, const int *glist = nullptr, int nlist = -1);
 // elements of the listed tasks into A = 1 - M and M_ii; diag_only: M_ii alone (from the band)
 void launch_elem(const Task *tasks, const int *tlist, int nlist, int ldim, const sd *I, const sd *Sa, const sd *Sb, const double2 *uv,
                  double *A, size_t lda, size_t mat_stride, double *mdiag, int *status, cudaStream_t st, bool diag_only);
@@ -85,15 +85,32 @@ size_t elem_ff_part_floats(int ldim);
 // float-float copies of the scale factors (Saf, Sbf: L ffe per task; uvf: L float4 per task)
 void launch_scale_ff(int ntask, int ldim, const sd *Sa, const sd *Sb, const double2 *uv, void *Saf, void *Sbf, float4 *uvf,
                      cudaStream_t st);
-// the diagonal of M alone, from the band of the I table
-void launch_diag_ff(const Task *tasks, int ntask, int ldim, const void *I, const void *Saf, const void *Sbf, const float4 *uvf,
+// q-sums of seed pairs at every window index w (sweep.cu), one array of L float-float values per
+// (task, polarisation, kind): seed[((task * 2 + pol) * SEED_KINDS + kind) * L + w] holds the pair
+// (w, w), (w+1, w), (w+2, w) or (w, c), c the window index of the first l with I != 0
+enum { SEED_D0 = 0, SEED_D1 = 1, SEED_D2 = 2, SEED_COL = 3, SEED_KINDS = 4 };
+size_t seed_bytes(int ldim, int ntask);
+// band: kinds D0 and D2 (what the diagonal of M reads); otherwise D1 and COL (the rest of the
+// recurrence's seeds).  a12t: the per-m tables of launch_a12_mixed (ngroup_all groups)
+void launch_seed_ff(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim, const float4 *KP, const int *KPe,
+                    int nu_stride, const float4 *ptabf, int pstride, const void *a12t, int ngroup_all, void *seed, bool band,
+                    int *status, cudaStream_t st);
+// M of the listed tasks by the I recurrence from all four seed kinds, straight into the FP32
+// delta matrix, with one sum of squares per task in part[task]; sweep_fits: the window fits the
+// kernel's shared-memory ring
+bool sweep_fits(int ldim);
+void launch_sweep_ff(const Task *tasks, const int *tlist, int nlist, int ldim, const void *seed, const void *Saf, const void *Sbf,
+                     float *S, size_t sstride, float *part, int *status, cudaStream_t st);
+// the diagonal of M alone, from the band seeds
+void launch_diag_ff(const Task *tasks, int ntask, int ldim, const void *seed, const void *Saf, const void *Sbf, const float4 *uvf,
                     double *diag, int *status, cudaStream_t st);
 // the listed tasks (tlist, nlist; tlist == nullptr: tasks 0..nlist-1)
 void launch_elem_ff(const Task *tasks, const int *tlist, int nlist, int ldim, const void *Saf, const void *Sbf, const float4 *uvf,
                     const void *I, float *S, size_t sstride, double *diag, float *part, int *status, cudaStream_t st);
-// part == nullptr: the trace rule alone, undecided tasks keep status 0
+// part == nullptr: the trace rule alone, undecided tasks keep status 0; part_per_task: part holds
+// one sum of squares per task (launch_sweep_ff), otherwise k_elem_ff's per-warp partials
 void launch_stats_ff(const int *tlist, int nlist, int ldim, const double *diag, const float *part, int mode, double *trace,
-                     double *result, int *status, cudaStream_t st);
+                     double *result, int *status, cudaStream_t st, bool part_per_task = false);
 void launch_cholesky(int ntask, int n, double *A, size_t lda, size_t mstride, int *status, double *logdiag, cudaStream_t st);
 size_t mixed_work_bytes(int ntask, int n);
 // live CUDA-event timing of the tcgen05 trailing update (mixed.cu)

@@ -36,16 +36,13 @@ namespace capsgpu {
 // polarisation has had a significant term for three steps.  Each sum is a function of its own
 // (pair, task) alone, so results do not depend on how tasks are grouped.
 //
-// grid (ceil(npair/128), ngroups) or, for the band, (ceil(2L/128), ngroups);
-// groups[g] = {first list position, count <= G, a_0..a_2 and p-table row}: the group's tasks are
-// tlist[x], ..., tlist[x + count - 1] (tlist == nullptr: tasks x, ..., x + count - 1).
-// They share m (hence lmin, mu, the p table and the a_0..a_2 row) and the material.
-// BAND computes only the pairs that the diagonal of M reads, l1 - l2 in {0, 2} (the EE and
-// MM entries of a diagonal 2x2 block, integration.c:762-888); each pair's sum is the one
-// the full kernel forms.  Output: I tables as float-float (ffe) or, with ffe_out false, as
-// scaled doubles.  The kernel is bound by FP32/ALU issue and the latency of float-float
-// dependency chains, so occupancy pays (MINB blocks of 128 per SM).
-template <int G, bool BAND, int MINB>
+// grid (ceil(npair/128), ngroups); groups[g] = {first list position, count <= G, a_0..a_2 and
+// p-table row}: the group's tasks are tlist[x], ..., tlist[x + count - 1] (tlist == nullptr:
+// tasks x, ..., x + count - 1).  They share m (hence lmin, mu, the p table and the a_0..a_2 row)
+// and the material.  Output: I tables as float-float (ffe) or, with ffe_out false, as scaled
+// doubles.  The kernel is bound by FP32/ALU issue and the latency of float-float dependency
+// chains, so occupancy pays (MINB blocks of 128 per SM).
+template <int G, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_itab_pk(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim,
                                                  const float4 *__restrict__ KP, const int *__restrict__ KPe, int nu_stride,
                                                  const float4 *__restrict__ ptabf, int pstride, const A012F *__restrict__ a12,
@@ -55,23 +52,12 @@ __global__ void __launch_bounds__(128, MINB) k_itab_pk(const Task *tasks, const 
     const long long npair = (long long)L * (L + 1) / 2;
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int gi = blockIdx.y;
-    if (gi >= ngroups) return;
-    long long pid;
-    int a1, a2;
-    if (BAND) {
-        if (tid >= 2LL * L) return;
-        a2 = (int)(tid >> 1);
-        a1 = a2 + 2 * (int)(tid & 1);
-        if (a1 >= L) return;
-        pid = (long long)a1 * (a1 + 1) / 2 + a2;
-    } else {
-        if (tid >= npair) return;
-        pid = tid;
-        a1 = (int)((sqrtf(8.0f * (float)pid + 1.0f) - 1.0f) * 0.5f);
-        while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
-        while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
-        a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
-    }
+    if (gi >= ngroups || tid >= npair) return;
+    const long long pid = tid;
+    int a1 = (int)((sqrtf(8.0f * (float)pid + 1.0f) - 1.0f) * 0.5f);
+    while ((long long)(a1 + 1) * (a1 + 2) / 2 <= pid) a1++;
+    while ((long long)a1 * (a1 + 1) / 2 > pid) a1--;
+    const int a2 = (int)(pid - (long long)a1 * (a1 + 1) / 2);
     const int4 grp = groups[gi];
     const int ng = grp.y;
     int tk[G];
@@ -119,19 +105,14 @@ constexpr int ITAB_STOP_BITS = QSUM_FF_STOP_BITS;
 int itab_group_size() { return IGRP; }
 
 void launch_itab_grp(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim, const float4 *KP, const int *KPe,
-                     int nu_stride, const float4 *ptabf, int pstride, const void *a12, void *Iout, bool ffe_out, bool band,
-                     int *status, cudaStream_t st)
+                     int nu_stride, const float4 *ptabf, int pstride, const void *a12, void *Iout, bool ffe_out, int *status,
+                     cudaStream_t st)
 {
     if (ngroups <= 0) return;
     const long long L = ldim + 2, npair = L * (L + 1) / 2;
-    dim3 g((unsigned)(((band ? 2 * L : npair) + 127) / 128), ngroups);
-    const A012F *A = (const A012F *)a12;
-    if (band)
-        k_itab_pk<IGRP, true, 7><<<g, 128, 0, st>>>(tasks, tlist, groups, ngroups, (int)ldim, KP, KPe, nu_stride, ptabf, pstride, A,
-                                                    Iout, ffe_out, status, ITAB_STOP_BITS);
-    else
-        k_itab_pk<IGRP, false, 7><<<g, 128, 0, st>>>(tasks, tlist, groups, ngroups, (int)ldim, KP, KPe, nu_stride, ptabf, pstride, A,
-                                                     Iout, ffe_out, status, ITAB_STOP_BITS);
+    dim3 g((unsigned)((npair + 127) / 128), ngroups);
+    k_itab_pk<IGRP, 7><<<g, 128, 0, st>>>(tasks, tlist, groups, ngroups, (int)ldim, KP, KPe, nu_stride, ptabf, pstride,
+                                          (const A012F *)a12, Iout, ffe_out, status, ITAB_STOP_BITS);
     COUNT_LAUNCH(1);
     CK(cudaGetLastError());
 }

@@ -88,7 +88,7 @@ struct Engine {
     cudaStream_t side = nullptr;          // Mie coefficients and scale factors, beside setup and K
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double *d_lfac = nullptr;
-    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF, tlist, groups2, glist2, KP, KPe, hwork;
+    DevBuf tasks, edges, coef, partM, partE, K, I, Sa, Sb, uv, A, logdiag, trace, result, status, mie_a, mie_b, xi, eps, lft, xtab, ptab, S32, ptabf, a12, gm, glmin, Saf, Sbf, uvf, part, diag, groups, B, diag2, mwork, a12t, coefF, tlist, groups2, glist2, KP, KPe, hwork, seed;
     std::vector<double> host_pinned_dummy;
     double timings[6] = {0, 0, 0, 0, 0, 0};
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
@@ -489,15 +489,21 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     // mixed precision without a dense-M request: elements go straight into the FP32 delta
     // matrix (no FP64 matrix)
     const bool ff_elem = mixed && O.factor && !O.M_out && !O.square && !hodlr;
+    // ... and, where the window fits its shared-memory ring, M comes from the I recurrence seeded
+    // by 4 L q-sums per matrix (sweep.cu) instead of the q-sums of every pair
+    const bool sweep = ff_elem && sweep_fits(ldim);
     const size_t mat_bytes = O.square ? 16 : ff_elem ? 4 + 1 : (caps->precision == CAPS_PREC_MIXED ? 12 : 8);
-    const size_t dense_bytes = hodlr ? hodlr_work_bytes(ldim, 1) : (size_t)dim * dim * mat_bytes + (size_t)2 * L * L * sizeof(sd)
-                                                                    + (size_t)L * (L + 1) / 2 * 32; // a_0..a_2 table (one row per task)
+    const size_t dense_bytes = hodlr ? hodlr_work_bytes(ldim, 1)
+                             : sweep ? (size_t)dim * dim * 4 + seed_bytes(ldim, 1)
+                                     : (size_t)dim * dim * mat_bytes + (size_t)2 * L * L * sizeof(sd)
+                                           + (size_t)L * (L + 1) / 2 * 32; // a_0..a_2 table (one row per task)
     const size_t per_task = dense_bytes + (size_t)2 * nu_stride * sizeof(sd)
                           + (size_t)nu_stride * sizeof(double2) + (size_t)3 * L * sizeof(sd) + (size_t)dim * 8
                           + (size_t)2 * 256 * nu_stride * 12  // partial sums, up to 256 warps
                           + (size_t)(4 * (caps->ldim + 4096)) * sizeof(double4); // p tables
     size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes + g_eng.S32.bytes
-                                             + g_eng.a12.bytes + g_eng.part.bytes + g_eng.B.bytes + g_eng.hwork.bytes));
+                                             + g_eng.a12.bytes + g_eng.part.bytes + g_eng.B.bytes + g_eng.hwork.bytes
+                                             + g_eng.seed.bytes));
     int chunk = (int)std::max<size_t>(1, std::min<size_t>(budget / per_task, 65535));
     chunk = std::min(chunk, n);
 
@@ -600,22 +606,23 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         CK(cudaEventRecord(g_eng.ev[2], st));
         CK(cudaStreamWaitEvent(st, g_eng.ev_join, 0)); // Mie and scale factors from here on
 
-        sd *d_I = hodlr ? nullptr : (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
+        sd *d_I = (hodlr || sweep) ? nullptr : (sd *)g_eng.I.get((size_t)nt * 2 * L * L * sizeof(sd));
         double4 *d_ptab = (double4 *)g_eng.ptab.get((size_t)nt * 2 * pstride * sizeof(double4));
-        void *d_a12 = hodlr ? nullptr : g_eng.a12.get(a12_bytes(ldim, ngroup));
+        void *d_a12 = (hodlr || sweep) ? nullptr : g_eng.a12.get(a12_bytes(ldim, ngroup));
         // a_0..a_2 per m; the mixed form's trace rule first needs only the band of each m
         void *d_a12t = nullptr;
         if (caps->precision == CAPS_PREC_MIXED) {
-            // (the HODLR path needs the per-m tables alone: its pairs combine them on demand)
+            // (the HODLR path and the seeds need the per-m tables alone: their pairs combine them
+            // on demand)
             d_a12t = g_eng.a12t.get(a12_tab_bytes(ldim, ngroup));
-            launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, d_a12t, st, true, nullptr, hodlr ? 0 : -1, ff_elem);
+            launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, d_a12t, st, true, nullptr, (hodlr || ff_elem) ? 0 : -1);
         } else if (!hodlr)
             launch_a12(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, st);
         const size_t lda = dim, mstride = (size_t)dim * dim;
         double *d_trace = (double *)g_eng.trace.get(nt * sizeof(double));
         double *d_res = (double *)g_eng.result.get(nt * sizeof(double));
         double *d_dg = (double *)g_eng.diag.get((size_t)nt * dim * sizeof(double));
-        void *d_Saf = nullptr, *d_Sbf = nullptr;
+        void *d_Saf = nullptr, *d_Sbf = nullptr, *d_seed = nullptr;
         float4 *d_uvf = nullptr;
         int nlist = nt;            // matrices assembled in full
         const int *d_list = nullptr; // their chunk indices (nullptr: all of them)
@@ -666,10 +673,12 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
                 d_Sbf = g_eng.Sbf.get((size_t)nt * L * 16);
                 d_uvf = (float4 *)g_eng.uvf.get((size_t)nt * L * sizeof(float4));
                 launch_scale_ff(nt, ldim, d_Sa, d_Sb, d_uv, d_Saf, d_Sbf, d_uvf, st);
-                launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KP, d_KPe, nu_stride, d_ptabf, pstride, d_a12, d_I, true, true,
-                                d_status, st);
+                // the band of q-sums that M_ii reads (l1 - l2 in {0, 2})
+                d_seed = g_eng.seed.get(seed_bytes(ldim, nt));
+                launch_seed_ff(d_tasks, nullptr, d_sub, nsub, ldim, d_KP, d_KPe, nu_stride, d_ptabf, pstride, d_a12t, ngroup, d_seed,
+                               true, d_status, st);
                 CK(cudaEventRecord(g_eng.ev[3], st));
-                launch_diag_ff(d_tasks, nt, ldim, d_I, d_Saf, d_Sbf, d_uvf, d_dg, d_status, st);
+                launch_diag_ff(d_tasks, nt, ldim, d_seed, d_Saf, d_Sbf, d_uvf, d_dg, d_status, st);
                 launch_stats_ff(nullptr, nt, ldim, d_dg, nullptr, O.mode, d_trace, d_res, d_status, st);
                 CK(cudaEventRecord(g_eng.ev[4], st));
                 undecided();
@@ -677,20 +686,26 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
                 if (nlist > 0) {
                     dg2 = (int4 *)g_eng.groups2.get(sub2.size() * sizeof(int4));
                     h2d(dg2, sub2.data(), sub2.size() * sizeof(int4), st);
+                }
+                if (nlist > 0 && !sweep) {
                     // all pairs of the a_0..a_2 rows of the m that still need them
                     std::vector<int> gl;
                     for (const int4 &g : sub2)
                         if (gl.empty() || gl.back() != g.z) gl.push_back(g.z);
                     int *dgl = (int *)g_eng.glist2.get(gl.size() * sizeof(int));
                     h2d(dgl, gl.data(), gl.size() * sizeof(int), st);
-                    launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, d_a12t, st, false, dgl, (int)gl.size(), false);
+                    launch_a12_mixed(d_gm, d_glm, ngroup, ldim, d_lft, d_a12, d_a12t, st, false, dgl, (int)gl.size());
                 }
                 CK(cudaEventRecord(g_eng.ev[5], st));
-                launch_itab_grp(d_tasks, d_list, dg2, nlist > 0 ? (int)sub2.size() : 0, ldim, d_KP, d_KPe, nu_stride, d_ptabf, pstride, d_a12,
-                                d_I, true, false, d_status, st);
+                if (sweep) // the rest of the recurrence's seeds: l1 - l2 = 1 and the first column
+                    launch_seed_ff(d_tasks, d_list, dg2, nlist > 0 ? (int)sub2.size() : 0, ldim, d_KP, d_KPe, nu_stride, d_ptabf, pstride,
+                                   d_a12t, ngroup, d_seed, false, d_status, st);
+                else
+                    launch_itab_grp(d_tasks, d_list, dg2, nlist > 0 ? (int)sub2.size() : 0, ldim, d_KP, d_KPe, nu_stride, d_ptabf, pstride,
+                                    d_a12, d_I, true, d_status, st);
             } else {
                 for (int k = 3; k <= 5; k++) CK(cudaEventRecord(g_eng.ev[k], st));
-                launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KP, d_KPe, nu_stride, d_ptabf, pstride, d_a12, d_I, ff_elem, false,
+                launch_itab_grp(d_tasks, nullptr, d_sub, nsub, ldim, d_KP, d_KPe, nu_stride, d_ptabf, pstride, d_a12, d_I, ff_elem,
                                 d_status, st);
             }
         } else if (hodlr) {
@@ -723,6 +738,11 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
         float *d_S = nullptr;
         if (hodlr) {
             // (no element phase)
+        } else if (ff_elem && sweep) {
+            d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
+            float *d_part = (float *)g_eng.part.get((size_t)nt * sizeof(float));
+            launch_sweep_ff(d_tasks, d_list, nlist, ldim, d_seed, d_Saf, d_Sbf, d_S, mstride, d_part, d_status, st);
+            launch_stats_ff(d_list, nlist, ldim, d_dg, d_part, O.mode, d_trace, d_res, d_status, st, true);
         } else if (ff_elem) {
             d_S = (float *)g_eng.S32.get((size_t)nt * mstride * sizeof(float));
             float *d_part = (float *)g_eng.part.get((size_t)nt * elem_ff_part_floats(ldim) * sizeof(float));

@@ -1,0 +1,375 @@
+// sweep.cu -- the mixed form's round-trip matrix from a band of q-sums and a three-term
+// recurrence of the I integrals, with the elements formed as the rows of the table appear.
+//
+// The q-sum of every (l1, l2) pair (integration.c:491-609) costs O(l) terms, O(ldim^3) per
+// matrix.  The I integrals also obey the three-term recurrence of the associated Legendre
+// functions in either degree, (2l+1) x P_l^m = (l-m+1) P_{l+1}^m + (l+m) P_{l-1}^m, which,
+// applied once in each degree of I_{l1 l2} = int w(x) P_{l1}^{m'} P_{l2}^{m'} (m' = max(m,1)),
+// links four neighbours:
+//   (l1-m'+1) I(l1+1, l2) = (2l1+1)/(2l2+1) [(l2-m'+1) I(l1, l2+1) + (l2+m') I(l1, l2-1)]
+//                           - (l1+m') I(l1-1, l2).
+// Seeded with q-sums on the diagonal (l1 = l2), the first subdiagonal (l1 = l2 + 1) and the
+// first column of the window, it fills the lower triangle row by row, moving away from the
+// diagonal.  Against the q-sums of the reference's algorithm the filled values agree to ~1e-11
+// relative (also 1000 rows from the seeds, from xi = 0.1 to 1119, m = 0 to 400), and
+// log det(1 - M) built from them moves by <= 5e-14 relative in float-float arithmetic -- far
+// below the FP32 storage of M, which dominates the mixed form's error.  The recurrence costs
+// O(1) per pair: the q-sums shrink to 4 L pairs per matrix (two of which the trace rule's
+// diagonal reads anyway).
+//
+// Scaling.  The table is held as T(w1, w2) = I(w1, w2) 2^{k(w1) + k(w2)} (w: index into the
+// window [lmin-1, lmin+ldim]) with k(w) = -floor(log2 I_TM(w, w) / 2), so that T_TM(w, w) lies in
+// [1, 4).  For a plate of real dielectric function the weight w(x) of the integral has one sign
+// per polarisation, so I_p is a signed Gram matrix and |T(w1, w2)| <= sqrt(T(w1,w1) T(w2,w2)) < 4:
+// every value sits in one fixed float-float frame (no per-entry exponent); far entries that
+// fall below 2^-121 of that frame flush to zero, as they do in the FP32 matrix.  The powers of
+// two enter the recurrence coefficients exactly.
+//
+// Elements (libcaps.c:761-831, integration.c:762-888) in this frame.  With
+// Um(w) = u(w) 2^{k(w) - k(w-1)}, Vp(w) = v(w) 2^{k(w) - k(w+1)} (u, v the coefficients of the
+// B, C, D combinations), dA(w) = Sa(w) 2^{-k(w)}, dB(w) = Sb(w) 2^{-k(w)} (Sa, Sb the symmetric
+// Mie and normalisation factors), and per polarisation
+//   J(x, y) = Um(x) T(x-1, y) - Vp(x) T(x+1, y)      (B, C, D differentiate in l1 ...)
+//   H(x, y) = Um(y) T(x, y-1) - Vp(y) T(x, y+1)      (... and in l2)
+//   B(x, y) = Um(y) J(x, y-1) - Vp(y) J(x, y+1),
+// the 2x2 block at window row x, column y is
+//   EE = dA(x) dA(y) [B_TM - m^2 T_TE],          MM = dB(x) dB(y) [m^2 T_TM - B_TE],
+//   EM = m dA(x) dB(y) [H_TE - J_TM],            ME = m dB(x) dA(y) [J_TE - H_TM]
+// (m = 0: EE = dA dA T_TM, MM = -dB dB T_TE).  Um = (l+1) Cm and Vp = l Cp for m >= 1, Cp and Cm
+// the column coefficients of the recurrence, so one pair of tables serves both.
+//
+// k_sweep_ff: one CTA per matrix.  Rows of T live in a ring of four shared-memory rows (both
+// polarisations), so one barrier per row orders the recurrence of row r against the elements
+// of row r-1.  A warp takes 30 consecutive columns per pass with 32 lanes: J of the two
+// outer lanes reaches the inner ones by shuffles.  The elements go straight into the FP32 delta
+// matrix (-M, lower triangle, column-major), with a per-matrix sum of squares for the
+// reference's Mercator bound; the FP64 diagonal comes from the band (k_diag_ff).
+#include "common.cuh"
+#include "ff.cuh"
+#include "internal.h"
+#include "qsum_ff.cuh"
+
+namespace capsgpu {
+
+// window index of the first l with I != 0: l = max(lmin - 1, m')
+CAPS_DEV int seed_col(const Task &T)
+{
+    const int mm = T.m > 0 ? T.m : 1;
+    return T.lmin - 1 >= mm ? 0 : 1;
+}
+
+// ---------------------------------------------------------------------------
+// seeds: q-sums of the pairs of two kinds per window index w
+// ---------------------------------------------------------------------------
+// grid (2 ceil(L/128), ngroups): the first half of the blocks computes kind0, the second kind1
+// (so that a warp runs sums of one kind and similar length).  groups as in launch_itab_grp; a_0,
+// a_1, a_2 come from the per-m tables (a012f_pair), so no pair table is formed.  seed[((task *
+// 2 + pol) * SEED_KINDS + kind) * L + w] receives the pair's value as float-float with exponent;
+// pairs outside the window are not written (nothing reads them).
+template <int G>
+__global__ void __launch_bounds__(128, 7) k_seed_ff(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim,
+                                                    const float4 *__restrict__ KP, const int *__restrict__ KPe, int nu_stride,
+                                                    const float4 *__restrict__ ptabf, int pstride, const A12L *__restrict__ tl,
+                                                    const A12J *__restrict__ tj, int kind0, int kind1, ffe *seed, int *status,
+                                                    int stop_bits)
+{
+    const int L = ldim + 2, NJ = 2 * L - 1, nbw = (L + 127) / 128;
+    const int gi = blockIdx.y;
+    if (gi >= ngroups) return;
+    const int kind = (int)blockIdx.x < nbw ? kind0 : kind1;
+    const int w = ((int)blockIdx.x % nbw) * 128 + threadIdx.x;
+    if (w >= L) return;
+    const int4 grp = groups[gi];
+    const int ng = grp.y;
+    int tk[G];
+#pragma unroll
+    for (int g = 0; g < G; g++) tk[g] = g < ng ? (tlist ? tlist[grp.x + g] : grp.x + g) : 0;
+    const Task &T = tasks[tk[0]];
+    int a1 = w, a2 = w;
+    if (kind == SEED_D1) a1 = w + 1;
+    else if (kind == SEED_D2) a1 = w + 2;
+    else if (kind == SEED_COL) a2 = seed_col(T);
+    if (a1 >= L) return;
+    auto store = [&](int g, int pol, float h, float l, int e) {
+        seed[((size_t)(tk[g] * 2 + pol) * SEED_KINDS + kind) * L + w] = ffe{h, l, e, 0};
+    };
+    const int mm = T.m > 0 ? T.m : 1, l1 = T.lmin - 1 + a1, l2 = T.lmin - 1 + a2;
+    if (a1 < a2 || l2 < mm || l2 < T.m || l1 < 1) { // I = 0 for l < m (integration.c:631)
+        for (int g = 0; g < ng; g++) { store(g, 1, 0.0f, 0.0f, FFE_ZERO_E); store(g, 0, 0.0f, 0.0f, FFE_ZERO_E); }
+        return;
+    }
+    const A012F A12 = a012f_pair(T.m, T.lmin, a1, a2, tl + (size_t)grp.z * L, tj + (size_t)grp.z * NJ);
+    const unsigned bad = qsum_ff_pair<G>(T, tk, ng, l1, l2, A12, KP, KPe, nu_stride, ptabf + (size_t)grp.z * 2 * pstride * 2,
+                                          pstride, stop_bits, store);
+#pragma unroll
+    for (int g = 0; g < G; g++)
+        if (g < ng && (bad & (1u << g))) atomicOr(status + tk[g], ST_ERR_NONFINITE);
+}
+
+// ---------------------------------------------------------------------------
+// the sweep
+// ---------------------------------------------------------------------------
+constexpr int SW_NT = 256, SW_NW = SW_NT / 32; // threads, warps per CTA
+constexpr int SW_CH = 30;                       // output columns of a warp pass (32 lanes)
+constexpr int SW_RING = 4;                      // rows of T held in shared memory
+constexpr size_t SW_BYTES_PER_L = SW_RING * 2 * sizeof(float2) + 2 * sizeof(float4) + sizeof(int);
+
+CAPS_DEV ff ff_sub(ff x, ff y) { return ff_add(x, ff_neg(y)); }
+// x c for c exactly representable in FP32 (small integers)
+CAPS_DEV ff ff_mulf(ff x, float c)
+{
+    const float p = x.h * c;
+    float e = fmaf(x.h, c, -p);
+    e = fmaf(x.l, c, e);
+    return ff_fast2(p, e);
+}
+
+// 1 / y in float-float: the hardware reciprocal and two corrections (relative error ~2^-48)
+CAPS_DEV ff ff_rcp(ff y)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y.h));
+    ff q{r, 0.0f};
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const ff e = ff_sub(ff{1.0f, 0.0f}, ff_mul(q, y));
+        q = ff_add(q, ff_mul(q, e));
+    }
+    return q;
+}
+
+// k(w) of the scaling: I_TM(w, w) 2^{2 k(w)} in [1, 4).  Window indices below the first
+// column (zero rows) take the first column's k.
+CAPS_DEV int sw_k(const ffe *__restrict__ d0tm, int w, int c)
+{
+    const ffe v = d0tm[w < c ? c : w];
+    return v.h == 0.0f ? 0 : -(v.e >> 1);
+}
+
+// a seed (h + l) 2^e in the frame: times 2^{k1 + k2}
+CAPS_DEV ff sw_seed(const ffe &v, int k12) { return v.h == 0.0f ? ff{0.0f, 0.0f} : ff_shift(ff{v.h, v.l}, v.e + k12); }
+
+// FP32 of (d1 2^e1) (d2 2^e2) v: the products in float-float, one rounding; below 2^-120 -> 0
+CAPS_DEV float sw_out(ff d1, int e1, ff d2, int e2, ff v, bool &bad)
+{
+    const ff p = ff_mul(ff_mul(d1, d2), v);
+    const float h = p.h + p.l;
+    const int k = fexpo(h);
+    if (k == -127) return 0.0f;
+    if (k == 128 || k + e1 + e2 > 125) { bad = true; return h; }
+    return fshift(h, e1 + e2);
+}
+
+CAPS_DEV float2 ld2(const float2 *p) { return *p; }
+
+// grid nlist (task tlist[b], or b), SW_NT threads, SW_BYTES_PER_L * L bytes of dynamic shared memory.
+// S receives -M (lower triangle, column-major, leading dimension 2 ldim); part[task] the sum of
+// squares of M (both triangles).  Tasks with an error status are skipped.
+__global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const int *tlist, int nlist, int ldim,
+                                                       const ffe *__restrict__ seed, const ffe *__restrict__ Saf,
+                                                       const ffe *__restrict__ Sbf, float *S, size_t sstride, float *part,
+                                                       int *status)
+{
+    extern __shared__ __align__(16) unsigned char sw_smem[];
+    __shared__ float red[SW_NW];
+    const int L = ldim + 2, n = 2 * ldim;
+    if ((int)blockIdx.x >= nlist) return;
+    const int task = tlist ? tlist[blockIdx.x] : (int)blockIdx.x;
+    if (status[task] & ~0xF) return; // uniform per block
+    const Task &T = tasks[task];
+    const int mt = T.m, mm = mt > 0 ? mt : 1, lm1 = T.lmin - 1, c = seed_col(T);
+    float2 *ring = reinterpret_cast<float2 *>(sw_smem);   // [SW_RING][pol][L], pol 1 = TM, 0 = TE
+    float4 *cpm = reinterpret_cast<float4 *>(ring + (size_t)SW_RING * 2 * L); // Cp h, l, Cm h, l
+    float4 *dab = cpm + L;                                                   // dA h, l, dB h, l
+    int *eab = reinterpret_cast<int *>(dab + L);                             // exponents of dA (low 16 bits), dB
+    auto sp = [&](int pol, int kind) { return seed + ((size_t)(task * 2 + pol) * SEED_KINDS + kind) * L; };
+    const ffe *d0tm = sp(1, SEED_D0);
+
+    // per window index: the recurrence's column coefficients and the element factors
+    for (int w = threadIdx.x; w < L; w += SW_NT) {
+        const int l = lm1 + w, kw = sw_k(d0tm, w, c);
+        ff cp{0.0f, 0.0f}, cmv{0.0f, 0.0f};
+        if (w >= c && w + 1 < L) cp = ff_shift(ff_from_d((double)(l - mm + 1) / (2.0 * l + 1)), kw - sw_k(d0tm, w + 1, c));
+        if (w >= c + 1) cmv = ff_shift(ff_from_d((double)(l + mm) / (2.0 * l + 1)), kw - sw_k(d0tm, w - 1, c));
+        cpm[w] = make_float4(cp.h, cp.l, cmv.h, cmv.l);
+        const ffe a = Saf[(size_t)task * L + w], b = Sbf[(size_t)task * L + w];
+        dab[w] = make_float4(a.h, a.l, b.h, b.l);
+        const int ea = a.h == 0.0f ? 0 : min(max(a.e - kw, -30000), 30000);
+        const int eb = b.h == 0.0f ? 0 : min(max(b.e - kw, -30000), 30000);
+        eab[w] = (int)(((unsigned)ea & 0xffffu) | ((unsigned)eb << 16));
+    }
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float m2 = (float)mt * (float)mt; // exact for m < 4096
+    float fro = 0.0f;
+    bool bad = false;
+    float *Sm = S + (size_t)task * sstride;
+    for (int r = 0; r < L; r++) {
+        // ---- row r of T
+        {
+            float2 *W = ring + (size_t)((r & 3) * 2) * L;
+            const float2 *P1 = ring + (size_t)(((r - 1) & 3) * 2) * L, *P2 = ring + (size_t)(((r - 2) & 3) * 2) * L;
+            // the recurrence divided by its row coefficient: R1 = 1 / Cp(r-1), R2 = R1 Cm(r-1)
+            ff R1{0.0f, 0.0f}, R2{0.0f, 0.0f};
+            if (r >= c + 3 && warp * SW_CH <= r) {
+                const float4 q = cpm[r - 1];
+                R1 = ff_rcp(ff{q.x, q.y});
+                R2 = ff_mul(R1, ff{q.z, q.w});
+            }
+            for (int k = warp; k * SW_CH <= r; k += SW_NW) {
+                const int y = k * SW_CH - 1 + lane;
+                if (lane == 0 || lane == 31 || y > r) continue;
+                ff vT{0.0f, 0.0f}, vE{0.0f, 0.0f};
+                if (y < c) {
+                } else if (y == r || y == r - 1 || y == c) {
+                    const int kind = y == r ? SEED_D0 : (y == r - 1 ? SEED_D1 : SEED_COL);
+                    const int wi = kind == SEED_COL ? r : y; // the pair (r, y) is stored at index wi
+                    const int k12 = sw_k(d0tm, r, c) + sw_k(d0tm, y, c);
+                    vT = sw_seed(sp(1, kind)[wi], k12);
+                    vE = sw_seed(sp(0, kind)[wi], k12);
+                } else {
+                    const float4 q = cpm[y];
+                    const ff Cp{q.x, q.y}, Cm{q.z, q.w};
+                    {
+                        const float2 a = ld2(P1 + L + y + 1), b = ld2(P1 + L + y - 1), d = ld2(P2 + L + y);
+                        const ff s = ff_add(ff_mul(Cp, ff{a.x, a.y}), ff_mul(Cm, ff{b.x, b.y}));
+                        vT = ff_sub(ff_mul(R1, s), ff_mul(R2, ff{d.x, d.y}));
+                    }
+                    {
+                        const float2 a = ld2(P1 + y + 1), b = ld2(P1 + y - 1), d = ld2(P2 + y);
+                        const ff s = ff_add(ff_mul(Cp, ff{a.x, a.y}), ff_mul(Cm, ff{b.x, b.y}));
+                        vE = ff_sub(ff_mul(R1, s), ff_mul(R2, ff{d.x, d.y}));
+                    }
+                }
+                W[L + y] = make_float2(vT.h, vT.l);
+                W[y] = make_float2(vE.h, vE.l);
+            }
+        }
+        __syncthreads();
+        // ---- elements of window row x = r - 1 (matrix block row x - 1), rows x-1, x, x+1 of T
+        const int x = r - 1;
+        if (x < 1) continue;
+        const float2 *Rm = ring + (size_t)(((x - 1) & 3) * 2) * L, *R0 = ring + (size_t)((x & 3) * 2) * L,
+                     *Rp = ring + (size_t)(((x + 1) & 3) * 2) * L;
+        // T(pol, i, j) for i, j in {x-1, x, x+1}, by symmetry from the lower triangle
+        auto Tv = [&](int p, int i, int j) {
+            const int hi = max(i, j), lo = min(i, j);
+            const float2 *Rr = hi == x + 1 ? Rp : (hi == x ? R0 : Rm);
+            const float2 v = ld2(Rr + (size_t)p * L + lo);
+            return ff{v.x, v.y};
+        };
+        const int lx = lm1 + x;
+        const float4 qx = cpm[x], dx = dab[x];
+        const int ex = eab[x];
+        const ff Umx = ff_mulf(ff{qx.z, qx.w}, (float)(lx + 1)), Vpx = ff_mulf(ff{qx.x, qx.y}, (float)lx);
+        const ff dAx{dx.x, dx.y}, dBx{dx.z, dx.w};
+        const ff mdAx = ff_mulf(dAx, (float)mt), mdBx = ff_mulf(dBx, (float)mt);
+        const int eAx = (int)(short)(ex & 0xffff), eBx = ex >> 16;
+        const int r0 = 2 * (x - 1);
+        for (int k = warp; k * SW_CH <= x; k += SW_NW) {
+            const int y = k * SW_CH - 1 + lane;
+            ff JT{0.0f, 0.0f}, JE{0.0f, 0.0f};
+            if (mt > 0 && y >= 0 && y <= x + 1) {
+                JT = ff_sub(ff_mul(Umx, Tv(1, x - 1, y)), ff_mul(Vpx, Tv(1, x + 1, y)));
+                JE = ff_sub(ff_mul(Umx, Tv(0, x - 1, y)), ff_mul(Vpx, Tv(0, x + 1, y)));
+            }
+            const ff JTm{__shfl_up_sync(0xffffffffu, JT.h, 1), __shfl_up_sync(0xffffffffu, JT.l, 1)};
+            const ff JTp{__shfl_down_sync(0xffffffffu, JT.h, 1), __shfl_down_sync(0xffffffffu, JT.l, 1)};
+            const ff JEm{__shfl_up_sync(0xffffffffu, JE.h, 1), __shfl_up_sync(0xffffffffu, JE.l, 1)};
+            const ff JEp{__shfl_down_sync(0xffffffffu, JE.h, 1), __shfl_down_sync(0xffffffffu, JE.l, 1)};
+            if (lane == 0 || lane == 31 || y < 1 || y > x) continue;
+            const float4 dy = dab[y];
+            const int ey = eab[y];
+            const ff dAy{dy.x, dy.y}, dBy{dy.z, dy.w};
+            const int eAy = (int)(short)(ey & 0xffff), eBy = ey >> 16;
+            const ff TTM = Tv(1, x, y), TTE = Tv(0, x, y);
+            float ee, mmv, em = 0.0f, me = 0.0f;
+            if (mt == 0) {
+                ee = sw_out(dAx, eAx, dAy, eAy, TTM, bad);
+                mmv = sw_out(dBx, eBx, dBy, eBy, ff_neg(TTE), bad);
+            } else {
+                const float4 qy = cpm[y];
+                const int ly = lm1 + y;
+                const ff Umy = ff_mulf(ff{qy.z, qy.w}, (float)(ly + 1)), Vpy = ff_mulf(ff{qy.x, qy.y}, (float)ly);
+                const ff BT = ff_sub(ff_mul(Umy, JTm), ff_mul(Vpy, JTp));
+                const ff BE = ff_sub(ff_mul(Umy, JEm), ff_mul(Vpy, JEp));
+                const ff HT = ff_sub(ff_mul(Umy, Tv(1, x, y - 1)), ff_mul(Vpy, Tv(1, x, y + 1)));
+                const ff HE = ff_sub(ff_mul(Umy, Tv(0, x, y - 1)), ff_mul(Vpy, Tv(0, x, y + 1)));
+                ee = sw_out(dAx, eAx, dAy, eAy, ff_sub(BT, ff_mulf(TTE, m2)), bad);
+                mmv = sw_out(dBx, eBx, dBy, eBy, ff_sub(ff_mulf(TTM, m2), BE), bad);
+                em = sw_out(mdAx, eAx, dBy, eBy, ff_sub(HE, JT), bad);
+                me = sw_out(mdBx, eBx, dAy, eAy, ff_sub(JE, HT), bad);
+            }
+            const int c0 = 2 * (y - 1);
+            *reinterpret_cast<float2 *>(Sm + (size_t)c0 * n + r0) = make_float2(-ee, -me);
+            if (y != x) {
+                *reinterpret_cast<float2 *>(Sm + (size_t)(c0 + 1) * n + r0) = make_float2(-em, -mmv);
+                fro += 2.0f * (ee * ee + me * me + mmv * mmv + em * em);
+            } else {
+                Sm[(size_t)(c0 + 1) * n + r0 + 1] = -mmv;
+                fro += ee * ee + mmv * mmv + 2.0f * me * me;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
+    if (lane == 0) red[warp] = fro;
+    const int anybad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+        float s = 0.0f;
+        for (int w = 0; w < SW_NW; w++) s += red[w];
+        part[task] = s;
+        if (anybad) atomicOr(status + task, ST_ERR_NONFINITE);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+size_t seed_bytes(int ldim, int ntask) { return (size_t)ntask * 2 * SEED_KINDS * (ldim + 2) * sizeof(ffe); }
+
+size_t sweep_smem_bytes(int ldim) { return SW_BYTES_PER_L * (size_t)(ldim + 2); }
+
+bool sweep_fits(int ldim)
+{
+    static int smax = -1;
+    if (smax < 0) {
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    }
+    return sweep_smem_bytes(ldim) + 256 <= (size_t)smax;
+}
+
+void launch_seed_ff(const Task *tasks, const int *tlist, const int4 *groups, int ngroups, int ldim, const float4 *KP, const int *KPe,
+                    int nu_stride, const float4 *ptabf, int pstride, const void *a12t, int ngroup_all, void *seed, bool band,
+                    int *status, cudaStream_t st)
+{
+    if (ngroups <= 0) return;
+    const int L = ldim + 2;
+    const A12L *tl = (const A12L *)a12t;
+    const A12J *tj = (const A12J *)((const char *)a12t + (size_t)L * ngroup_all * sizeof(A12L));
+    dim3 g(2 * ((L + 127) / 128), ngroups);
+    k_seed_ff<3><<<g, 128, 0, st>>>(tasks, tlist, groups, ngroups, ldim, KP, KPe, nu_stride, ptabf, pstride, tl, tj,
+                                    band ? SEED_D0 : SEED_D1, band ? SEED_D2 : SEED_COL, (ffe *)seed, status, QSUM_FF_STOP_BITS);
+    COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
+}
+
+void launch_sweep_ff(const Task *tasks, const int *tlist, int nlist, int ldim, const void *seed, const void *Saf, const void *Sbf,
+                     float *S, size_t sstride, float *part, int *status, cudaStream_t st)
+{
+    if (nlist <= 0) return;
+    static size_t attr = 0;
+    const size_t smem = sweep_smem_bytes(ldim);
+    if (smem > attr) {
+        CK(cudaFuncSetAttribute(k_sweep_ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = smem;
+    }
+    k_sweep_ff<<<nlist, SW_NT, smem, st>>>(tasks, tlist, nlist, ldim, (const ffe *)seed, (const ffe *)Saf, (const ffe *)Sbf, S, sstride,
+                                           part, status);
+    COUNT_LAUNCH(1);
+    CK(cudaGetLastError());
+}
+
+} // namespace capsgpu
