@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(128, 7) k_seed_ff(const Task *tasks, const int
 // ---------------------------------------------------------------------------
 constexpr int SW_NT = 256, SW_NW = SW_NT / 32; // threads, warps per CTA
 constexpr int SW_CH = 30;                       // output columns of a warp pass (32 lanes)
-constexpr int SW_RING = 4;                      // rows of T held in shared memory
+constexpr int SW_RING = 3;                      // rows of T held in shared memory
 constexpr size_t SW_BYTES_PER_L = SW_RING * 2 * sizeof(float2) + 2 * sizeof(float4) + sizeof(int);
 
 CAPS_DEV ff ff_sub(ff x, ff y) { return ff_add(x, ff_neg(y)); }
@@ -122,6 +122,37 @@ CAPS_DEV ff ff_mulf(ff x, float c)
     float e = fmaf(x.h, c, -p);
     e = fmaf(x.l, c, e);
     return ff_fast2(p, e);
+}
+// a x + b y: the two products with their rounding errors (fmaf), one exact sum of the leading
+// parts and one renormalisation (the float-float error of ff_add(ff_mul, ff_mul), fewer steps)
+CAPS_DEV ff ff_dot2(ff a, ff x, ff b, ff y)
+{
+    const float p = a.h * x.h, q = b.h * y.h;
+    float ep = fmaf(a.h, x.h, -p);
+    ep = fmaf(a.h, x.l, ep);
+    ep = fmaf(a.l, x.h, ep);
+    float eq = fmaf(b.h, y.h, -q);
+    eq = fmaf(b.h, y.l, eq);
+    eq = fmaf(b.l, y.h, eq);
+    const float s = p + q, bb = s - p;
+    const float t = (p - (s - bb)) + (q - bb);
+    return ff_fast2(s, t + (ep + eq));
+}
+// a x + b y + c z, c exactly representable in FP32
+CAPS_DEV ff ff_dot3f(ff a, ff x, ff b, ff y, float c, ff z)
+{
+    const float p = a.h * x.h, q = b.h * y.h, u = c * z.h;
+    float ep = fmaf(a.h, x.h, -p);
+    ep = fmaf(a.h, x.l, ep);
+    ep = fmaf(a.l, x.h, ep);
+    float eq = fmaf(b.h, y.h, -q);
+    eq = fmaf(b.h, y.l, eq);
+    eq = fmaf(b.l, y.h, eq);
+    float eu = fmaf(c, z.h, -u);
+    eu = fmaf(c, z.l, eu);
+    const float s1 = p + q, b1 = s1 - p, t1 = (p - (s1 - b1)) + (q - b1);
+    const float s2 = s1 + u, b2 = s2 - s1, t2 = (s1 - (s2 - b2)) + (u - b2);
+    return ff_fast2(s2, (t1 + t2) + (ep + (eq + eu)));
 }
 
 // 1 / y in float-float: the hardware reciprocal and two corrections (relative error ~2^-48)
@@ -149,22 +180,33 @@ CAPS_DEV int sw_k(const ffe *__restrict__ d0tm, int w, int c)
 // a seed (h + l) 2^e in the frame: times 2^{k1 + k2}
 CAPS_DEV ff sw_seed(const ffe &v, int k12) { return v.h == 0.0f ? ff{0.0f, 0.0f} : ff_shift(ff{v.h, v.l}, v.e + k12); }
 
-// FP32 of (d1 2^e1) (d2 2^e2) v: the products in float-float, one rounding; below 2^-120 -> 0
-CAPS_DEV float sw_out(ff d1, int e1, ff d2, int e2, ff v, bool &bad)
+// FP32 of (d1 d2 2^e) v: the float-float product d1 d2 unrounded, times v with one rounding
+// (error ~0.5 ulp); below 2^-120 -> 0, non-finite or above 2^125 sets bad
+CAPS_DEV float sw_out(ff d1, ff d2, int e, ff v, bool &bad)
 {
-    const ff p = ff_mul(ff_mul(d1, d2), v);
-    const float h = p.h + p.l;
+    const float a = d1.h * d2.h;
+    float ea = fmaf(d1.h, d2.h, -a);
+    ea = fmaf(d1.h, d2.l, ea);
+    ea = fmaf(d1.l, d2.h, ea);
+    const float h = fmaf(a, v.h, fmaf(ea, v.h, a * v.l));
     const int k = fexpo(h);
     if (k == -127) return 0.0f;
-    if (k == 128 || k + e1 + e2 > 125) { bad = true; return h; }
-    return fshift(h, e1 + e2);
+    if (k == 128 || k + e > 125) { bad = true; return h; }
+    return fshift(h, e);
 }
 
-CAPS_DEV float2 ld2(const float2 *p) { return *p; }
+CAPS_DEV ff ldff(const float2 *p) { const float2 v = *p; return ff{v.x, v.y}; }
 
 // grid nlist (task tlist[b], or b), SW_NT threads, SW_BYTES_PER_L * L bytes of dynamic shared memory.
 // S receives -M (lower triangle, column-major, leading dimension 2 ldim); part[task] the sum of
 // squares of M (both triangles).  Tasks with an error status are skipped.
+//
+// Per row r a warp pass takes columns y = 30 k - 1 + lane (lanes 1..30 own them, lanes 0 and 31
+// repeat the neighbours' edges): each lane forms T(r, y) (seed or recurrence from rows r-1 and
+// r-2 of the ring) and, with it, the elements of row x = r - 1 at its column.  Everything the
+// elements read is either in rows r-1, r-2 or the lane's own T(r, y), except T(r, r-2), which the
+// lane of column r forms a second time, and J at y +- 1 (shuffles).  Row r goes to the ring slot
+// that row r-3 held; one barrier per row.
 __global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const int *tlist, int nlist, int ldim,
                                                        const ffe *__restrict__ seed, const ffe *__restrict__ Saf,
                                                        const ffe *__restrict__ Sbf, float *S, size_t sstride, float *part,
@@ -202,77 +244,94 @@ __global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const 
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float m2 = (float)mt * (float)mt; // exact for m < 4096
+    const ff zero{0.0f, 0.0f};
     float fro = 0.0f;
     bool bad = false;
     float *Sm = S + (size_t)task * sstride;
     for (int r = 0; r < L; r++) {
-        // ---- row r of T
-        {
-            float2 *W = ring + (size_t)((r & 3) * 2) * L;
-            const float2 *P1 = ring + (size_t)(((r - 1) & 3) * 2) * L, *P2 = ring + (size_t)(((r - 2) & 3) * 2) * L;
-            // the recurrence divided by its row coefficient: R1 = 1 / Cp(r-1), R2 = R1 Cm(r-1)
-            ff R1{0.0f, 0.0f}, R2{0.0f, 0.0f};
-            if (r >= c + 3 && warp * SW_CH <= r) {
-                const float4 q = cpm[r - 1];
-                R1 = ff_rcp(ff{q.x, q.y});
-                R2 = ff_mul(R1, ff{q.z, q.w});
-            }
-            for (int k = warp; k * SW_CH <= r; k += SW_NW) {
-                const int y = k * SW_CH - 1 + lane;
-                if (lane == 0 || lane == 31 || y > r) continue;
-                ff vT{0.0f, 0.0f}, vE{0.0f, 0.0f};
-                if (y < c) {
-                } else if (y == r || y == r - 1 || y == c) {
-                    const int kind = y == r ? SEED_D0 : (y == r - 1 ? SEED_D1 : SEED_COL);
-                    const int wi = kind == SEED_COL ? r : y; // the pair (r, y) is stored at index wi
-                    const int k12 = sw_k(d0tm, r, c) + sw_k(d0tm, y, c);
-                    vT = sw_seed(sp(1, kind)[wi], k12);
-                    vE = sw_seed(sp(0, kind)[wi], k12);
-                } else {
-                    const float4 q = cpm[y];
-                    const ff Cp{q.x, q.y}, Cm{q.z, q.w};
-                    {
-                        const float2 a = ld2(P1 + L + y + 1), b = ld2(P1 + L + y - 1), d = ld2(P2 + L + y);
-                        const ff s = ff_add(ff_mul(Cp, ff{a.x, a.y}), ff_mul(Cm, ff{b.x, b.y}));
-                        vT = ff_sub(ff_mul(R1, s), ff_mul(R2, ff{d.x, d.y}));
-                    }
-                    {
-                        const float2 a = ld2(P1 + y + 1), b = ld2(P1 + y - 1), d = ld2(P2 + y);
-                        const ff s = ff_add(ff_mul(Cp, ff{a.x, a.y}), ff_mul(Cm, ff{b.x, b.y}));
-                        vE = ff_sub(ff_mul(R1, s), ff_mul(R2, ff{d.x, d.y}));
-                    }
-                }
-                W[L + y] = make_float2(vT.h, vT.l);
-                W[y] = make_float2(vE.h, vE.l);
-            }
+        float2 *W = ring + (size_t)((r % 3) * 2) * L;                 // row r
+        const float2 *P1 = ring + (size_t)(((r + 2) % 3) * 2) * L;    // row r-1
+        const float2 *P2 = ring + (size_t)(((r + 1) % 3) * 2) * L;    // row r-2
+        // the recurrence of row r divided by its row coefficient: R1 = 1 / Cp(r-1), R2 = R1 Cm(r-1)
+        ff R1 = zero, nR2 = zero;
+        if (r >= c + 3 && warp * SW_CH <= r) {
+            const float4 q = cpm[r - 1];
+            R1 = ff_rcp(ff{q.x, q.y});
+            nR2 = ff_neg(ff_mul(R1, ff{q.z, q.w}));
         }
-        __syncthreads();
-        // ---- elements of window row x = r - 1 (matrix block row x - 1), rows x-1, x, x+1 of T
-        const int x = r - 1;
-        if (x < 1) continue;
-        const float2 *Rm = ring + (size_t)(((x - 1) & 3) * 2) * L, *R0 = ring + (size_t)((x & 3) * 2) * L,
-                     *Rp = ring + (size_t)(((x + 1) & 3) * 2) * L;
-        // T(pol, i, j) for i, j in {x-1, x, x+1}, by symmetry from the lower triangle
-        auto Tv = [&](int p, int i, int j) {
-            const int hi = max(i, j), lo = min(i, j);
-            const float2 *Rr = hi == x + 1 ? Rp : (hi == x ? R0 : Rm);
-            const float2 v = ld2(Rr + (size_t)p * L + lo);
-            return ff{v.x, v.y};
+        const int kr = sw_k(d0tm, r, c);
+        // T(r, y), y in [0, r]: zero below the first column, seeds on the diagonal, the first
+        // subdiagonal and the first column, otherwise the recurrence from T(r-1, y+1), T(r-1, y-1)
+        // and T(r-2, y)
+        auto val = [&](int y, ff a1T, ff a1E, ff b1T, ff b1E, ff d2T, ff d2E, ff &vT, ff &vE) {
+            if (y < c) {
+                vT = vE = zero;
+            } else if (y == r || y == r - 1 || y == c) {
+                const int kind = y == r ? SEED_D0 : (y == r - 1 ? SEED_D1 : SEED_COL);
+                const int wi = kind == SEED_COL ? r : y; // the pair (r, y) is stored at index wi
+                const int k12 = kr + sw_k(d0tm, y, c);
+                vT = sw_seed(sp(1, kind)[wi], k12);
+                vE = sw_seed(sp(0, kind)[wi], k12);
+            } else {
+                const float4 q = cpm[y];
+                const ff Cp{q.x, q.y}, Cm{q.z, q.w};
+                vT = ff_dot2(R1, ff_dot2(Cp, a1T, Cm, b1T), nR2, d2T);
+                vE = ff_dot2(R1, ff_dot2(Cp, a1E, Cm, b1E), nR2, d2E);
+            }
         };
-        const int lx = lm1 + x;
-        const float4 qx = cpm[x], dx = dab[x];
-        const int ex = eab[x];
-        const ff Umx = ff_mulf(ff{qx.z, qx.w}, (float)(lx + 1)), Vpx = ff_mulf(ff{qx.x, qx.y}, (float)lx);
-        const ff dAx{dx.x, dx.y}, dBx{dx.z, dx.w};
-        const ff mdAx = ff_mulf(dAx, (float)mt), mdBx = ff_mulf(dBx, (float)mt);
-        const int eAx = (int)(short)(ex & 0xffff), eBx = ex >> 16;
+        // the element row x = r - 1 (matrix block row x - 1): row scalars
+        const int x = r - 1;
+        const bool elem = x >= 1;
+        ff Umx = zero, nVpx = zero, dAx = zero, dBx = zero, mdAx = zero, mdBx = zero;
+        int eAx = 0, eBx = 0;
+        if (elem) {
+            const float4 qx = cpm[x], dx = dab[x];
+            const int ex = eab[x];
+            Umx = ff_mulf(ff{qx.z, qx.w}, (float)(lm1 + x + 1));
+            nVpx = ff_neg(ff_mulf(ff{qx.x, qx.y}, (float)(lm1 + x)));
+            dAx = ff{dx.x, dx.y};
+            dBx = ff{dx.z, dx.w};
+            mdAx = ff_mulf(dAx, (float)mt);
+            mdBx = ff_mulf(dBx, (float)mt);
+            eAx = (int)(short)(ex & 0xffff);
+            eBx = ex >> 16;
+        }
         const int r0 = 2 * (x - 1);
-        for (int k = warp; k * SW_CH <= x; k += SW_NW) {
+        for (int k = warp; k * SW_CH <= r; k += SW_NW) {
             const int y = k * SW_CH - 1 + lane;
-            ff JT{0.0f, 0.0f}, JE{0.0f, 0.0f};
-            if (mt > 0 && y >= 0 && y <= x + 1) {
-                JT = ff_sub(ff_mul(Umx, Tv(1, x - 1, y)), ff_mul(Vpx, Tv(1, x + 1, y)));
-                JE = ff_sub(ff_mul(Umx, Tv(0, x - 1, y)), ff_mul(Vpx, Tv(0, x + 1, y)));
+            // rows r-1 and r-2 around the column (zero outside the filled triangle)
+            ff a1T = zero, a1E = zero, b1T = zero, b1E = zero, c1T = zero, c1E = zero, d2T = zero, d2E = zero;
+            if (y >= -1 && y <= r - 2) { a1T = ldff(P1 + L + y + 1); a1E = ldff(P1 + y + 1); }
+            if (y >= 1 && y <= r) { b1T = ldff(P1 + L + y - 1); b1E = ldff(P1 + y - 1); }
+            if (y >= 0 && y <= r - 1) { c1T = ldff(P1 + L + y); c1E = ldff(P1 + y); }
+            if (y >= 0 && y <= r - 2) { d2T = ldff(P2 + L + y); d2E = ldff(P2 + y); }
+            ff tT = zero, tE = zero;
+            if (y >= 0 && y <= r) {
+                val(y, a1T, a1E, b1T, b1E, d2T, d2E, tT, tE);
+                if (lane >= 1 && lane <= 30) {
+                    W[L + y] = make_float2(tT.h, tT.l);
+                    W[y] = make_float2(tE.h, tE.l);
+                }
+            }
+            if (!elem) continue; // uniform
+            // J(x, y) = Um(x) T(x-1, y) - Vp(x) T(x+1, y), y in [0, x+1]; T(x-1, y) is T(r-2, y),
+            // T(r-1, r-2) at y = x and T(r, r-2) at y = x + 1
+            ff JT = zero, JE = zero;
+            if (mt > 0 && y >= 0 && y <= r) {
+                ff mT = d2T, mE = d2E;
+                if (y == r - 1) { mT = b1T; mE = b1E; }
+                else if (y == r) {
+                    const int z = r - 2;
+                    ff zaT = zero, zaE = zero, zbT = zero, zbE = zero, zdT = zero, zdE = zero;
+                    if (z > c && z < r - 1) { // a recurrence column: T(r-1, r-1), T(r-1, r-3), T(r-2, r-2)
+                        zaT = ldff(P1 + L + z + 1); zaE = ldff(P1 + z + 1);
+                        zbT = ldff(P1 + L + z - 1); zbE = ldff(P1 + z - 1);
+                        zdT = ldff(P2 + L + z); zdE = ldff(P2 + z);
+                    }
+                    val(z, zaT, zaE, zbT, zbE, zdT, zdE, mT, mE);
+                }
+                JT = ff_dot2(Umx, mT, nVpx, tT);
+                JE = ff_dot2(Umx, mE, nVpx, tE);
             }
             const ff JTm{__shfl_up_sync(0xffffffffu, JT.h, 1), __shfl_up_sync(0xffffffffu, JT.l, 1)};
             const ff JTp{__shfl_down_sync(0xffffffffu, JT.h, 1), __shfl_down_sync(0xffffffffu, JT.l, 1)};
@@ -283,23 +342,24 @@ __global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const 
             const int ey = eab[y];
             const ff dAy{dy.x, dy.y}, dBy{dy.z, dy.w};
             const int eAy = (int)(short)(ey & 0xffff), eBy = ey >> 16;
-            const ff TTM = Tv(1, x, y), TTE = Tv(0, x, y);
             float ee, mmv, em = 0.0f, me = 0.0f;
             if (mt == 0) {
-                ee = sw_out(dAx, eAx, dAy, eAy, TTM, bad);
-                mmv = sw_out(dBx, eBx, dBy, eBy, ff_neg(TTE), bad);
+                ee = sw_out(dAx, dAy, eAx + eAy, c1T, bad);
+                mmv = sw_out(dBx, dBy, eBx + eBy, ff_neg(c1E), bad);
             } else {
                 const float4 qy = cpm[y];
                 const int ly = lm1 + y;
-                const ff Umy = ff_mulf(ff{qy.z, qy.w}, (float)(ly + 1)), Vpy = ff_mulf(ff{qy.x, qy.y}, (float)ly);
-                const ff BT = ff_sub(ff_mul(Umy, JTm), ff_mul(Vpy, JTp));
-                const ff BE = ff_sub(ff_mul(Umy, JEm), ff_mul(Vpy, JEp));
-                const ff HT = ff_sub(ff_mul(Umy, Tv(1, x, y - 1)), ff_mul(Vpy, Tv(1, x, y + 1)));
-                const ff HE = ff_sub(ff_mul(Umy, Tv(0, x, y - 1)), ff_mul(Vpy, Tv(0, x, y + 1)));
-                ee = sw_out(dAx, eAx, dAy, eAy, ff_sub(BT, ff_mulf(TTE, m2)), bad);
-                mmv = sw_out(dBx, eBx, dBy, eBy, ff_sub(ff_mulf(TTM, m2), BE), bad);
-                em = sw_out(mdAx, eAx, dBy, eBy, ff_sub(HE, JT), bad);
-                me = sw_out(mdBx, eBx, dAy, eAy, ff_sub(JE, HT), bad);
+                const ff Umy = ff_mulf(ff{qy.z, qy.w}, (float)(ly + 1)), nVpy = ff_neg(ff_mulf(ff{qy.x, qy.y}, (float)ly));
+                // T(x, y+1): row r-1 unless y = x, where it is T(r, x), the lane's own value
+                const ff pT = y == x ? tT : a1T, pE = y == x ? tE : a1E;
+                const ff HT = ff_dot2(Umy, b1T, nVpy, pT), HE = ff_dot2(Umy, b1E, nVpy, pE);
+                // EE = dA dA [B_TM - m^2 T_TE], MM = dB dB [m^2 T_TM - B_TE], B(x, y) = Um(y) J(x, y-1) - Vp(y) J(x, y+1)
+                const ff iEE = ff_dot3f(Umy, JTm, nVpy, JTp, -m2, c1E);
+                const ff iMM = ff_neg(ff_dot3f(Umy, JEm, nVpy, JEp, -m2, c1T));
+                ee = sw_out(dAx, dAy, eAx + eAy, iEE, bad);
+                mmv = sw_out(dBx, dBy, eBx + eBy, iMM, bad);
+                em = sw_out(mdAx, dBy, eAx + eBy, ff_sub(HE, JT), bad);
+                me = sw_out(mdBx, dAy, eBx + eAy, ff_sub(JE, HT), bad);
             }
             const int c0 = 2 * (y - 1);
             *reinterpret_cast<float2 *>(Sm + (size_t)c0 * n + r0) = make_float2(-ee, -me);
@@ -311,6 +371,7 @@ __global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const 
                 fro += ee * ee + mmv * mmv + 2.0f * me * me;
             }
         }
+        __syncthreads();
     }
     for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
     if (lane == 0) red[warp] = fro;
