@@ -505,9 +505,17 @@ def main():
                       "panel_kernels_note": "the panel solve is bytes-bound like the update (its rate against the same peak); "
                                             "the diagonal block is latency-bound: 64 dependent column steps per matrix"}),
         "dominant_kernel": None if args.precision == "fp64" else {
-            "kernel": "k_itab_grp (float-float q-sums)", "phase_share_of_step": ph[2] / ph[5] if ph[5] else None,
-            "bound": "FP32/ALU instruction issue; no HBM or tensor roofline applies (DRAM idle)",
-            "evidence": "ncu issue-slot and pipe figures of the q-sum kernel on a small case of this workload"},
+            "kernel": "the FP32 delta-form factorisation (k_syrk_pipe, the roofline kernel above, with the panel "
+                      "kernels k_trsm_inv and k_potf2_w)", "phase_share_of_step": ph[4] / ph[5] if ph[5] else None,
+            "bound": "HBM for the trailing update; the panel solve streams the panel, the diagonal block is latency-bound",
+            "evidence": "roofline and panel_kernels above; ncu captures of k_syrk_pipe on a 24- and 48-matrix case"},
+        "assembly_kernel": None if args.precision == "fp64" else {
+            "kernel": "k_sweep_ff (I table by the three-term Legendre recurrence from 4L seed q-sums, fused with "
+                      "the elements, straight into the FP32 delta matrix)",
+            "phase_share_of_step": (ph[2] + ph[3]) / ph[5] if ph[5] else None,
+            "bound": "latency: per-row barrier and float-float dependency chains at 16 warps per SM; "
+                     "FP32 work, DRAM idle",
+            "evidence": "ncu capture of k_sweep_ff on 48 matrices of this workload"},
         "cpu_baseline": cpu,
         "autotune": autotune,
         "learned_training": train_info,
