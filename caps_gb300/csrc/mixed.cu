@@ -63,14 +63,13 @@ __global__ void k_to_delta32(int ntask, int n, const double *A, size_t lda, size
 }
 
 // diagonal block in delta form, one CTA of 256 threads per matrix; also writes W =
-// (I + Lam_kk)^{-1} (lower triangular, row-major MB x MB per task) for the panel solve and
+// (I + Lam_kk)^{-1} (lower triangular, MB x MB per task, stored transposed) for the panel solve and
 // the block's share of ||Lam||_F^2.  Per column j every thread forms the pivot from
 // T[j][j]; threads 0..63 scale row tid of column j into colj; the rank-1 update of the
 // trailing triangle takes the entries (i, c), j < c <= i, from a list of the whole triangle
 // ordered by column (last column first), so that step j's entries are a prefix of it and
 // the 256 threads share them evenly (consecutive threads: consecutive rows of one column,
-// T rows 65 floats apart, distinct banks).  W follows column-parallel, one column per
-// thread, by forward substitution.
+// T rows 65 floats apart, distinct banks).  W follows blockwise (16 x 16 blocks).
 __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float *S, size_t sstride, int *status, float *Winv,
                                                  double *fro)
 {
@@ -79,6 +78,7 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
     __shared__ float T[MB][MB + 1];
     __shared__ float W[MB][MB + 1];
     __shared__ float colj[MB];
+    __shared__ float Yb[3][16][17]; // blocks of the blockwise inverse in progress
     __shared__ double red8[8];
     // the entries (i, c), 1 <= c <= i <= 63, as i | c << 8, columns 63, 62, ..., 1, rows
     // ascending within a column; column c starts at (63 - c)(64 - c) / 2
@@ -140,21 +140,56 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
     }
     sq = block_sum256(sq, red8);
     if (tid == 0) fro[(size_t)task * fro_slots(n) + (size_t)(k0 / MB) * (fro_nbr(n) + 1)] = sq;
-    // W = (I + Lam)^{-1} column by column (forward substitution, column tid)
-    if (tid < nb) {
-        const int jc = tid;
-        W[jc][jc] = 1.0f / (1.0f + T[jc][jc]);
-        for (int r = jc + 1; r < nb; r++) {
-            float acc = 0.0f;
-            for (int k = jc; k < r; k++) acc = fmaf(T[r][k], W[k][jc], acc);
-            W[r][jc] = -acc / (1.0f + T[r][r]);
+    // W = (I + Lam)^{-1} blockwise in 16 x 16 blocks: the four diagonal blocks by forward
+    // substitution, one thread per column with the column in registers; then the blocks below,
+    // by distance from the diagonal, X_ij = -X_ii sum_{k=j}^{i-1} L_ik X_kj (L = I + Lam).  Rows
+    // past nb read entries of T that were never loaded; they feed only rows past nb (the
+    // inverse of a lower triangular matrix is causal in the row index), which are not stored.
+    constexpr int QB = 16;
+    if (tid < MB) {
+        const int o = (tid / QB) * QB, c = tid % QB;
+        float x[QB];
+#pragma unroll
+        for (int r = 0; r < QB; r++) {
+            float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+            for (int k = 0; k < r; k++) {
+                if (k & 1) a1 = fmaf(T[o + r][o + k], x[k], a1);
+                else a0 = fmaf(T[o + r][o + k], x[k], a0);
+            }
+            const float d = 1.0f + T[o + r][o + r];
+            x[r] = r < c ? 0.0f : (r == c ? 1.0f / d : -(a0 + a1) / d);
+            W[o + r][o + c] = x[r];
         }
     }
     __syncthreads();
+    for (int dl = 1; dl < MB / QB; dl++) {
+        const int np = MB / QB - dl; // block pairs (i, j) = (p + dl, p) at this distance
+        for (int e = tid; e < np * QB * QB; e += 256) {
+            const int p = e / (QB * QB), r = (e / QB) % QB, c = e % QB, i = p + dl;
+            float acc = 0.0f;
+            for (int k = p; k < i; k++)
+#pragma unroll
+                for (int q = 0; q < QB; q++) acc = fmaf(T[i * QB + r][k * QB + q], W[k * QB + q][p * QB + c], acc);
+            Yb[p][r][c] = acc;
+        }
+        __syncthreads();
+        for (int e = tid; e < np * QB * QB; e += 256) {
+            const int p = e / (QB * QB), r = (e / QB) % QB, c = e % QB, i = p + dl;
+            float acc = 0.0f;
+#pragma unroll
+            for (int q = 0; q < QB; q++)
+                if (q <= r) acc = fmaf(W[i * QB + r][i * QB + q], Yb[p][q][c], acc);
+            W[i * QB + r][p * QB + c] = -acc;
+        }
+        __syncthreads();
+    }
+    // stored transposed, Wt[k MB + c] = W[c][k] (zero outside the lower triangle and past nb): the
+    // k-major layout in which the panel solve keeps it, so that its copy is a plain one
     float *Wt = Winv + (size_t)task * MB * MB;
     for (int e = tid; e < MB * MB; e += 256) {
-        const int r = e / MB, c = e % MB;
-        Wt[e] = (r < nb && c <= r) ? W[r][c] : 0.0f;
+        const int k = e / MB, c = e % MB;
+        Wt[e] = (c < nb && k <= c) ? W[c][k] : 0.0f;
     }
     if (__syncthreads_or(bad) && tid == 0) atomicOr(status + task, ST_ERR_PIVOT);
 }
@@ -200,8 +235,8 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
         }
 #pragma unroll
         for (int u = 0; u < MB * MB / 256; u++) {
-            const int e = threadIdx.x + 256 * u; // W row-major: e = c MB + k
-            Wk[e % MB][e / MB] = w[u];
+            const int e = threadIdx.x + 256 * u; // W stored transposed: e = k MB + c
+            Wk[e / MB][e % MB] = w[u];
         }
 #pragma unroll
         for (int u = 0; u < MT * MB / 256; u++) {
