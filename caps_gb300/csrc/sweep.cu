@@ -38,16 +38,19 @@
 // (m = 0: EE = dA dA T_TM, MM = -dB dB T_TE).  Um = (l+1) Cm and Vp = l Cp for m >= 1, Cp and Cm
 // the column coefficients of the recurrence, so one pair of tables serves both.
 //
-// k_sweep_ff: one CTA per matrix.  Rows of T live in a ring of four shared-memory rows (both
-// polarisations), so one barrier per row orders the recurrence of row r against the elements
-// of row r-1.  A warp takes 30 consecutive columns per pass with 32 lanes: J of the two
-// outer lanes reaches the inner ones by shuffles.  The elements go straight into the FP32 delta
-// matrix (-M, lower triangle, column-major), with a per-matrix sum of squares for the
-// reference's Mercator bound; the FP64 diagonal comes from the band (k_diag_ff).
+// k_sweep_ff: one CTA per matrix, warp-specialised.  Producer warps form the rows of T into a
+// ring of four shared-memory rows (both polarisations) and publish each on an mbarrier;
+// consumer warps form the elements of row x once row x + 1 is published, 30 columns per pass
+// of 32 lanes (J of the neighbours by shuffles), and release row x - 1 for reuse, so that
+// they wait only for a producer that falls behind, never for one another.  The elements go
+// straight into the FP32 delta matrix (-M, lower triangle, column-major), with a per-matrix
+// sum of squares for the reference's Mercator bound; the FP64 diagonal comes from the band
+// (k_diag_ff).
 #include "common.cuh"
 #include "ff.cuh"
 #include "internal.h"
 #include "qsum_ff.cuh"
+#include "umma.cuh"
 
 namespace capsgpu {
 
@@ -109,9 +112,11 @@ __global__ void __launch_bounds__(128, 7) k_seed_ff(const Task *tasks, const int
 // ---------------------------------------------------------------------------
 // the sweep
 // ---------------------------------------------------------------------------
-constexpr int SW_NT = 256, SW_NW = SW_NT / 32; // threads, warps per CTA
-constexpr int SW_CH = 30;                       // output columns of a warp pass (32 lanes)
-constexpr int SW_RING = 3;                      // rows of T held in shared memory
+constexpr int SW_NT = 320, SW_NW = SW_NT / 32; // threads, warps per CTA
+constexpr int SW_PW = 3, SW_CW = SW_NW - SW_PW;  // producer (recurrence) and consumer (element) warps
+constexpr int SW_CH = 30;                       // output columns of a consumer pass (32 lanes)
+constexpr int SW_RING = 4;                      // rows of T held in shared memory
+constexpr int SW_WAIT_ITERS = 1 << 22;          // polls of a bounded mbarrier wait
 constexpr size_t SW_BYTES_PER_L = SW_RING * 2 * sizeof(float2) + 2 * sizeof(float4) + sizeof(int);
 
 CAPS_DEV ff ff_sub(ff x, ff y) { return ff_add(x, ff_neg(y)); }
@@ -197,22 +202,52 @@ CAPS_DEV float sw_out(ff d1, ff d2, int e, ff v, bool &bad)
 
 CAPS_DEV ff ldff(const float2 *p) { const float2 v = *p; return ff{v.x, v.y}; }
 
+// bounded wait for phase `parity` of an mbarrier that also gives up once another role has
+// given up (*abort); a wait that runs out sets *abort
+CAPS_DEV bool sw_wait(uint64_t *mbar, uint32_t parity, volatile int *abort)
+{
+    const uint32_t a = umma::smem_u32(mbar);
+    for (int it = 0; it < SW_WAIT_ITERS; it++) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(a), "r"(parity)
+                     : "memory");
+        if (done) return true;
+        if ((it & 63) == 63 && *abort) return false;
+    }
+    *abort = 1;
+    return false;
+}
+CAPS_DEV void sw_arrive(uint64_t *mbar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma::smem_u32(mbar)) : "memory");
+}
+// barrier of the SW_PW producer warps alone (hardware barrier 1)
+CAPS_DEV void sw_producer_bar() { asm volatile("bar.sync 1, %0;" ::"n"(SW_PW * 32) : "memory"); }
+
 // grid nlist (task tlist[b], or b), SW_NT threads, SW_BYTES_PER_L * L bytes of dynamic shared memory.
 // S receives -M (lower triangle, column-major, leading dimension 2 ldim); part[task] the sum of
 // squares of M (both triangles).  Tasks with an error status are skipped.
 //
-// Per row r a warp pass takes columns y = 30 k - 1 + lane (lanes 1..30 own them, lanes 0 and 31
-// repeat the neighbours' edges): each lane forms T(r, y) (seed or recurrence from rows r-1 and
-// r-2 of the ring) and, with it, the elements of row x = r - 1 at its column.  Everything the
-// elements read is either in rows r-1, r-2 or the lane's own T(r, y), except T(r, r-2), which the
-// lane of column r forms a second time, and J at y +- 1 (shuffles).  Row r goes to the ring slot
-// that row r-3 held; one barrier per row.
+// Warp-specialised: SW_PW producer warps form the rows of T (lane y forms T(r, y) from rows r-1
+// and r-2) into a ring of SW_RING rows and publish each on its slot's "ready" mbarrier; SW_CW
+// consumer warps form the elements of row x once row x + 1 is ready, in passes of 30 columns
+// (32 lanes, the two outer ones repeating the neighbours' edges, J of the neighbours by
+// shuffles), and release row x - 1 on its slot's "free" mbarrier, which the producers wait
+// for before they reuse the slot.  Consumers therefore never wait for one another, only for a
+// producer that falls behind.  Row r also writes T(r, r-1) and T(r, r-2) past the diagonals
+// of rows r-1 and r-2 (index r), so that the consumers read rows x-1, x, x+1 up to column
+// x + 1 directly.  Every wait is bounded; a role that gives up flags the others, and the
+// matrix gets ST_ERR_WAIT.
 __global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const int *tlist, int nlist, int ldim,
                                                        const ffe *__restrict__ seed, const ffe *__restrict__ Saf,
                                                        const ffe *__restrict__ Sbf, float *S, size_t sstride, float *part,
                                                        int *status)
 {
     extern __shared__ __align__(16) unsigned char sw_smem[];
+    __shared__ uint64_t rready[SW_RING], rfree[SW_RING];
+    __shared__ int s_abort, s_ok;
     __shared__ float red[SW_NW];
     const int L = ldim + 2, n = 2 * ldim;
     if ((int)blockIdx.x >= nlist) return;
@@ -225,10 +260,12 @@ __global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const 
     float4 *dab = cpm + L;                                                   // dA h, l, dB h, l
     int *eab = reinterpret_cast<int *>(dab + L);                             // exponents of dA (low 16 bits), dB
     auto sp = [&](int pol, int kind) { return seed + ((size_t)(task * 2 + pol) * SEED_KINDS + kind) * L; };
+    auto rowp = [&](int r) { return ring + (size_t)((r % SW_RING) * 2) * L; }; // row r (r >= 0): TE at +0, TM at +L
     const ffe *d0tm = sp(1, SEED_D0);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     // per window index: the recurrence's column coefficients and the element factors
-    for (int w = threadIdx.x; w < L; w += SW_NT) {
+    for (int w = tid; w < L; w += SW_NT) {
         const int l = lm1 + w, kw = sw_k(d0tm, w, c);
         ff cp{0.0f, 0.0f}, cmv{0.0f, 0.0f};
         if (w >= c && w + 1 < L) cp = ff_shift(ff_from_d((double)(l - mm + 1) / (2.0 * l + 1)), kw - sw_k(d0tm, w + 1, c));
@@ -240,147 +277,140 @@ __global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const 
         const int eb = b.h == 0.0f ? 0 : min(max(b.e - kw, -30000), 30000);
         eab[w] = (int)(((unsigned)ea & 0xffffu) | ((unsigned)eb << 16));
     }
+    if (tid == 0) {
+        for (int i = 0; i < SW_RING; i++) {
+            umma::mbar_init(&rready[i], 1);
+            umma::mbar_init(&rfree[i], SW_CW);
+        }
+        s_abort = 0;
+    }
     __syncthreads();
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const float m2 = (float)mt * (float)mt; // exact for m < 4096
+    volatile int *abort = &s_abort;
     const ff zero{0.0f, 0.0f};
     float fro = 0.0f;
     bool bad = false;
-    float *Sm = S + (size_t)task * sstride;
-    for (int r = 0; r < L; r++) {
-        float2 *W = ring + (size_t)((r % 3) * 2) * L;                 // row r
-        const float2 *P1 = ring + (size_t)(((r + 2) % 3) * 2) * L;    // row r-1
-        const float2 *P2 = ring + (size_t)(((r + 1) % 3) * 2) * L;    // row r-2
-        // the recurrence of row r divided by its row coefficient: R1 = 1 / Cp(r-1), R2 = R1 Cm(r-1)
-        ff R1 = zero, nR2 = zero;
-        if (r >= c + 3 && warp * SW_CH <= r) {
-            const float4 q = cpm[r - 1];
-            R1 = ff_rcp(ff{q.x, q.y});
-            nR2 = ff_neg(ff_mul(R1, ff{q.z, q.w}));
-        }
-        const int kr = sw_k(d0tm, r, c);
-        // T(r, y), y in [0, r]: zero below the first column, seeds on the diagonal, the first
-        // subdiagonal and the first column, otherwise the recurrence from T(r-1, y+1), T(r-1, y-1)
-        // and T(r-2, y)
-        auto val = [&](int y, ff a1T, ff a1E, ff b1T, ff b1E, ff d2T, ff d2E, ff &vT, ff &vE) {
-            if (y < c) {
-                vT = vE = zero;
-            } else if (y == r || y == r - 1 || y == c) {
-                const int kind = y == r ? SEED_D0 : (y == r - 1 ? SEED_D1 : SEED_COL);
-                const int wi = kind == SEED_COL ? r : y; // the pair (r, y) is stored at index wi
-                const int k12 = kr + sw_k(d0tm, y, c);
-                vT = sw_seed(sp(1, kind)[wi], k12);
-                vE = sw_seed(sp(0, kind)[wi], k12);
-            } else {
-                const float4 q = cpm[y];
-                const ff Cp{q.x, q.y}, Cm{q.z, q.w};
-                vT = ff_dot2(R1, ff_dot2(Cp, a1T, Cm, b1T), nR2, d2T);
-                vE = ff_dot2(R1, ff_dot2(Cp, a1E, Cm, b1E), nR2, d2E);
+
+    if (warp < SW_PW) {
+        // ---- producers: rows of T ----
+        for (int r = 0; r < L; r++) {
+            const int s = r % SW_RING;
+            if (r >= SW_RING) { // slot s held row r - SW_RING: every consumer warp has released it
+                if (tid == 0) s_ok = sw_wait(&rfree[s], (r / SW_RING - 1) & 1, abort) ? 1 : 0;
+                sw_producer_bar();
+                if (!s_ok) break; // uniform over the producer warps
             }
-        };
-        // the element row x = r - 1 (matrix block row x - 1): row scalars
-        const int x = r - 1;
-        const bool elem = x >= 1;
-        ff Umx = zero, nVpx = zero, dAx = zero, dBx = zero, mdAx = zero, mdBx = zero;
-        int eAx = 0, eBx = 0;
-        if (elem) {
+            float2 *W = rowp(r);
+            const float2 *P1 = r >= 1 ? rowp(r - 1) : W, *P2 = r >= 2 ? rowp(r - 2) : W;
+            float2 *X1 = const_cast<float2 *>(P1), *X2 = const_cast<float2 *>(P2);
+            // the recurrence of row r divided by its row coefficient: R1 = 1 / Cp(r-1), R2 = R1 Cm(r-1)
+            ff R1 = zero, nR2 = zero;
+            if (r >= c + 3) {
+                const float4 q = cpm[r - 1];
+                R1 = ff_rcp(ff{q.x, q.y});
+                nR2 = ff_neg(ff_mul(R1, ff{q.z, q.w}));
+            }
+            const int kr = sw_k(d0tm, r, c);
+            for (int y = tid; y <= r; y += SW_PW * 32) {
+                ff vT = zero, vE = zero;
+                if (y < c) {
+                } else if (y == r || y == r - 1 || y == c) {
+                    const int kind = y == r ? SEED_D0 : (y == r - 1 ? SEED_D1 : SEED_COL);
+                    const int wi = kind == SEED_COL ? r : y; // the pair (r, y) is stored at index wi
+                    const int k12 = kr + sw_k(d0tm, y, c);
+                    vT = sw_seed(sp(1, kind)[wi], k12);
+                    vE = sw_seed(sp(0, kind)[wi], k12);
+                } else {
+                    const float4 q = cpm[y];
+                    const ff Cp{q.x, q.y}, Cm{q.z, q.w};
+                    vT = ff_dot2(R1, ff_dot2(Cp, ldff(P1 + L + y + 1), Cm, ldff(P1 + L + y - 1)), nR2, ldff(P2 + L + y));
+                    vE = ff_dot2(R1, ff_dot2(Cp, ldff(P1 + y + 1), Cm, ldff(P1 + y - 1)), nR2, ldff(P2 + y));
+                }
+                W[L + y] = make_float2(vT.h, vT.l);
+                W[y] = make_float2(vE.h, vE.l);
+                // T(r, r-1) and T(r, r-2) past the diagonals of rows r-1 and r-2
+                if (y == r - 1) { X1[L + r] = make_float2(vT.h, vT.l); X1[r] = make_float2(vE.h, vE.l); }
+                if (y == r - 2) { X2[L + r] = make_float2(vT.h, vT.l); X2[r] = make_float2(vE.h, vE.l); }
+            }
+            sw_producer_bar(); // row r complete before the next row reads it, and before it is published
+            if (tid == 0) sw_arrive(&rready[s]);
+        }
+    } else {
+        // ---- consumers: elements of rows x = 1 .. ldim ----
+        const int cw = warp - SW_PW;
+        const float m2 = (float)mt * (float)mt; // exact for m < 4096
+        float *Sm = S + (size_t)task * sstride;
+        bool ok = __all_sync(0xffffffffu, sw_wait(&rready[0], 0, abort) && sw_wait(&rready[1], 0, abort));
+        for (int x = 1; ok && x <= ldim; x++) {
+            ok = __all_sync(0xffffffffu, sw_wait(&rready[(x + 1) % SW_RING], ((x + 1) / SW_RING) & 1, abort));
+            if (!ok) break;
+            const float2 *Rm = rowp(x - 1), *R0 = rowp(x), *Rp = rowp(x + 1);
             const float4 qx = cpm[x], dx = dab[x];
             const int ex = eab[x];
-            Umx = ff_mulf(ff{qx.z, qx.w}, (float)(lm1 + x + 1));
-            nVpx = ff_neg(ff_mulf(ff{qx.x, qx.y}, (float)(lm1 + x)));
-            dAx = ff{dx.x, dx.y};
-            dBx = ff{dx.z, dx.w};
-            mdAx = ff_mulf(dAx, (float)mt);
-            mdBx = ff_mulf(dBx, (float)mt);
-            eAx = (int)(short)(ex & 0xffff);
-            eBx = ex >> 16;
-        }
-        const int r0 = 2 * (x - 1);
-        for (int k = warp; k * SW_CH <= r; k += SW_NW) {
-            const int y = k * SW_CH - 1 + lane;
-            // rows r-1 and r-2 around the column (zero outside the filled triangle)
-            ff a1T = zero, a1E = zero, b1T = zero, b1E = zero, c1T = zero, c1E = zero, d2T = zero, d2E = zero;
-            if (y >= -1 && y <= r - 2) { a1T = ldff(P1 + L + y + 1); a1E = ldff(P1 + y + 1); }
-            if (y >= 1 && y <= r) { b1T = ldff(P1 + L + y - 1); b1E = ldff(P1 + y - 1); }
-            if (y >= 0 && y <= r - 1) { c1T = ldff(P1 + L + y); c1E = ldff(P1 + y); }
-            if (y >= 0 && y <= r - 2) { d2T = ldff(P2 + L + y); d2E = ldff(P2 + y); }
-            ff tT = zero, tE = zero;
-            if (y >= 0 && y <= r) {
-                val(y, a1T, a1E, b1T, b1E, d2T, d2E, tT, tE);
-                if (lane >= 1 && lane <= 30) {
-                    W[L + y] = make_float2(tT.h, tT.l);
-                    W[y] = make_float2(tE.h, tE.l);
+            const ff Umx = ff_mulf(ff{qx.z, qx.w}, (float)(lm1 + x + 1)), nVpx = ff_neg(ff_mulf(ff{qx.x, qx.y}, (float)(lm1 + x)));
+            const ff dAx{dx.x, dx.y}, dBx{dx.z, dx.w};
+            const ff mdAx = ff_mulf(dAx, (float)mt), mdBx = ff_mulf(dBx, (float)mt);
+            const int eAx = (int)(short)(ex & 0xffff), eBx = ex >> 16;
+            const int r0 = 2 * (x - 1);
+            for (int k = cw; k * SW_CH <= x; k += SW_CW) {
+                const int y = k * SW_CH - 1 + lane;
+                // J(x, y) = Um(x) T(x-1, y) - Vp(x) T(x+1, y), y in [0, x+1]
+                ff JT = zero, JE = zero;
+                if (mt > 0 && y >= 0 && y <= x + 1) {
+                    JT = ff_dot2(Umx, ldff(Rm + L + y), nVpx, ldff(Rp + L + y));
+                    JE = ff_dot2(Umx, ldff(Rm + y), nVpx, ldff(Rp + y));
+                }
+                const ff JTm{__shfl_up_sync(0xffffffffu, JT.h, 1), __shfl_up_sync(0xffffffffu, JT.l, 1)};
+                const ff JTp{__shfl_down_sync(0xffffffffu, JT.h, 1), __shfl_down_sync(0xffffffffu, JT.l, 1)};
+                const ff JEm{__shfl_up_sync(0xffffffffu, JE.h, 1), __shfl_up_sync(0xffffffffu, JE.l, 1)};
+                const ff JEp{__shfl_down_sync(0xffffffffu, JE.h, 1), __shfl_down_sync(0xffffffffu, JE.l, 1)};
+                if (lane == 0 || lane == 31 || y < 1 || y > x) continue;
+                const float4 dy = dab[y];
+                const int ey = eab[y];
+                const ff dAy{dy.x, dy.y}, dBy{dy.z, dy.w};
+                const int eAy = (int)(short)(ey & 0xffff), eBy = ey >> 16;
+                const ff c1T = ldff(R0 + L + y), c1E = ldff(R0 + y);
+                float ee, mmv, em = 0.0f, me = 0.0f;
+                if (mt == 0) {
+                    ee = sw_out(dAx, dAy, eAx + eAy, c1T, bad);
+                    mmv = sw_out(dBx, dBy, eBx + eBy, ff_neg(c1E), bad);
+                } else {
+                    const float4 qy = cpm[y];
+                    const int ly = lm1 + y;
+                    const ff Umy = ff_mulf(ff{qy.z, qy.w}, (float)(ly + 1)), nVpy = ff_neg(ff_mulf(ff{qy.x, qy.y}, (float)ly));
+                    const ff HT = ff_dot2(Umy, ldff(R0 + L + y - 1), nVpy, ldff(R0 + L + y + 1));
+                    const ff HE = ff_dot2(Umy, ldff(R0 + y - 1), nVpy, ldff(R0 + y + 1));
+                    // EE = dA dA [B_TM - m^2 T_TE], MM = dB dB [m^2 T_TM - B_TE], B(x, y) = Um(y) J(x, y-1) - Vp(y) J(x, y+1)
+                    const ff iEE = ff_dot3f(Umy, JTm, nVpy, JTp, -m2, c1E);
+                    const ff iMM = ff_neg(ff_dot3f(Umy, JEm, nVpy, JEp, -m2, c1T));
+                    ee = sw_out(dAx, dAy, eAx + eAy, iEE, bad);
+                    mmv = sw_out(dBx, dBy, eBx + eBy, iMM, bad);
+                    em = sw_out(mdAx, dBy, eAx + eBy, ff_sub(HE, JT), bad);
+                    me = sw_out(mdBx, dAy, eBx + eAy, ff_sub(JE, HT), bad);
+                }
+                const int c0 = 2 * (y - 1);
+                *reinterpret_cast<float2 *>(Sm + (size_t)c0 * n + r0) = make_float2(-ee, -me);
+                if (y != x) {
+                    *reinterpret_cast<float2 *>(Sm + (size_t)(c0 + 1) * n + r0) = make_float2(-em, -mmv);
+                    fro += 2.0f * (ee * ee + me * me + mmv * mmv + em * em);
+                } else {
+                    Sm[(size_t)(c0 + 1) * n + r0 + 1] = -mmv;
+                    fro += ee * ee + mmv * mmv + 2.0f * me * me;
                 }
             }
-            if (!elem) continue; // uniform
-            // J(x, y) = Um(x) T(x-1, y) - Vp(x) T(x+1, y), y in [0, x+1]; T(x-1, y) is T(r-2, y),
-            // T(r-1, r-2) at y = x and T(r, r-2) at y = x + 1
-            ff JT = zero, JE = zero;
-            if (mt > 0 && y >= 0 && y <= r) {
-                ff mT = d2T, mE = d2E;
-                if (y == r - 1) { mT = b1T; mE = b1E; }
-                else if (y == r) {
-                    const int z = r - 2;
-                    ff zaT = zero, zaE = zero, zbT = zero, zbE = zero, zdT = zero, zdE = zero;
-                    if (z > c && z < r - 1) { // a recurrence column: T(r-1, r-1), T(r-1, r-3), T(r-2, r-2)
-                        zaT = ldff(P1 + L + z + 1); zaE = ldff(P1 + z + 1);
-                        zbT = ldff(P1 + L + z - 1); zbE = ldff(P1 + z - 1);
-                        zdT = ldff(P2 + L + z); zdE = ldff(P2 + z);
-                    }
-                    val(z, zaT, zaE, zbT, zbE, zdT, zdE, mT, mE);
-                }
-                JT = ff_dot2(Umx, mT, nVpx, tT);
-                JE = ff_dot2(Umx, mE, nVpx, tE);
-            }
-            const ff JTm{__shfl_up_sync(0xffffffffu, JT.h, 1), __shfl_up_sync(0xffffffffu, JT.l, 1)};
-            const ff JTp{__shfl_down_sync(0xffffffffu, JT.h, 1), __shfl_down_sync(0xffffffffu, JT.l, 1)};
-            const ff JEm{__shfl_up_sync(0xffffffffu, JE.h, 1), __shfl_up_sync(0xffffffffu, JE.l, 1)};
-            const ff JEp{__shfl_down_sync(0xffffffffu, JE.h, 1), __shfl_down_sync(0xffffffffu, JE.l, 1)};
-            if (lane == 0 || lane == 31 || y < 1 || y > x) continue;
-            const float4 dy = dab[y];
-            const int ey = eab[y];
-            const ff dAy{dy.x, dy.y}, dBy{dy.z, dy.w};
-            const int eAy = (int)(short)(ey & 0xffff), eBy = ey >> 16;
-            float ee, mmv, em = 0.0f, me = 0.0f;
-            if (mt == 0) {
-                ee = sw_out(dAx, dAy, eAx + eAy, c1T, bad);
-                mmv = sw_out(dBx, dBy, eBx + eBy, ff_neg(c1E), bad);
-            } else {
-                const float4 qy = cpm[y];
-                const int ly = lm1 + y;
-                const ff Umy = ff_mulf(ff{qy.z, qy.w}, (float)(ly + 1)), nVpy = ff_neg(ff_mulf(ff{qy.x, qy.y}, (float)ly));
-                // T(x, y+1): row r-1 unless y = x, where it is T(r, x), the lane's own value
-                const ff pT = y == x ? tT : a1T, pE = y == x ? tE : a1E;
-                const ff HT = ff_dot2(Umy, b1T, nVpy, pT), HE = ff_dot2(Umy, b1E, nVpy, pE);
-                // EE = dA dA [B_TM - m^2 T_TE], MM = dB dB [m^2 T_TM - B_TE], B(x, y) = Um(y) J(x, y-1) - Vp(y) J(x, y+1)
-                const ff iEE = ff_dot3f(Umy, JTm, nVpy, JTp, -m2, c1E);
-                const ff iMM = ff_neg(ff_dot3f(Umy, JEm, nVpy, JEp, -m2, c1T));
-                ee = sw_out(dAx, dAy, eAx + eAy, iEE, bad);
-                mmv = sw_out(dBx, dBy, eBx + eBy, iMM, bad);
-                em = sw_out(mdAx, dBy, eAx + eBy, ff_sub(HE, JT), bad);
-                me = sw_out(mdBx, dAy, eBx + eAy, ff_sub(JE, HT), bad);
-            }
-            const int c0 = 2 * (y - 1);
-            *reinterpret_cast<float2 *>(Sm + (size_t)c0 * n + r0) = make_float2(-ee, -me);
-            if (y != x) {
-                *reinterpret_cast<float2 *>(Sm + (size_t)(c0 + 1) * n + r0) = make_float2(-em, -mmv);
-                fro += 2.0f * (ee * ee + me * me + mmv * mmv + em * em);
-            } else {
-                Sm[(size_t)(c0 + 1) * n + r0 + 1] = -mmv;
-                fro += ee * ee + mmv * mmv + 2.0f * me * me;
-            }
+            __syncwarp();
+            if (lane == 0) sw_arrive(&rfree[(x - 1) % SW_RING]); // row x - 1 is done with
         }
-        __syncthreads();
     }
+    __syncthreads();
     for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
     if (lane == 0) red[warp] = fro;
     const int anybad = __syncthreads_or(bad);
-    if (threadIdx.x == 0) {
-        float s = 0.0f;
-        for (int w = 0; w < SW_NW; w++) s += red[w];
-        part[task] = s;
+    if (tid == 0) {
+        float sum = 0.0f;
+        for (int w = 0; w < SW_NW; w++) sum += red[w];
+        part[task] = sum;
         if (anybad) atomicOr(status + task, ST_ERR_NONFINITE);
+        if (s_abort) atomicOr(status + task, ST_ERR_WAIT);
     }
 }
 
