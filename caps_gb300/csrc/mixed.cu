@@ -600,7 +600,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         CK(cudaFuncSetAttribute(k_syrk_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
         CK(cudaFuncSetAttribute(k_syrk_pipe<64, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM));
         CK(cudaFuncSetAttribute(k_syrk_pipe<128, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM_WIDE));
-        CK(cudaFuncSetAttribute(k_syrk_pipe<128, 32, PIPE_IMG_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM_IMG));
+        CK(cudaFuncSetAttribute(k_syrk_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, PAIR_SMEM));
         int dev = 0;
         CK(cudaGetDevice(&dev));
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -620,9 +620,9 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
                                                                                              sstride, status, use_img ? img64 : nullptr);
         else { // the whole trailing matrix: 128 x 128 tiles (a third less staging per entry), 32-column chunks
             const int tw = ntask * pipe_tiles<128>(nr, 0);
-            if (use_img && kw == PIPE_IMG_CH * PIPE_IMG_TK) // the panel solves left the panel's images
-                k_syrk_pipe<128, 32, PIPE_IMG_STAGES><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_IMG, st>>>(
-                    ntask, n, k0, kw, t0, cmax, 0, S, sstride, status, img);
+            if (use_img && kw == PIPE_IMG_CH * PIPE_IMG_TK) // the panel solves left the panel's images: row-pair items
+                k_syrk_pair<<<std::min(ntask * pair_items(nr), nsm), PAIR_THREADS, PAIR_SMEM, st>>>(ntask, n, t0, S, sstride, status,
+                                                                                                  img);
             else
                 k_syrk_pipe<128, 32><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_WIDE, st>>>(ntask, n, k0, kw, t0, cmax, 0, S,
                                                                                               sstride, status, nullptr);

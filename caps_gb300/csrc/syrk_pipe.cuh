@@ -41,8 +41,6 @@ template <int TN, int TK, int NS = 2> struct PipeShape {
 };
 constexpr int PIPE_SMEM = PipeShape<64, 64>::SMEM;   // 192 KB
 constexpr int PIPE_SMEM_WIDE = PipeShape<128, 32>::SMEM; // 128 KB
-constexpr int PIPE_IMG_STAGES = 3;                       // stages of the image-fed update
-constexpr int PIPE_SMEM_IMG = PipeShape<128, 32, PIPE_IMG_STAGES>::SMEM; // 192 KB
 constexpr int PIPE_WAIT_ITERS = 1 << 22;
 constexpr int PIPE_PRODUCERS = PIPE_PRODUCER_WARPS * 32;
 
@@ -90,10 +88,10 @@ __device__ __forceinline__ void pipe_stage(const float *Sm, int n, int kc, int n
     }
 }
 
-// Panel images for the whole-trailing-matrix update (128 x 128 tiles, 32-column chunks):
+// Panel images for the whole-trailing-matrix update (k_syrk_pair below, 32-column chunks):
 // the panel P = S[t0 .., k0 .. k0 + 256) cut into 128-row blocks and 32-column chunks, each
 // chunk split into TF32 hi and lo and stored as the 16 KB image of a shared-memory slice
-// (the layout above), so that a stage is filled by four bulk copies:
+// (the layout above), hi and lo adjacent, so that one bulk copy brings both:
 // img[(((task nrb + rb) PIPE_IMG_CH + ch) 2 + part) PIPE_IMG_FLOATS + e], nrb = ceil((n - t0) / 128).
 // The panel solves that produce P write them (k_trsm_inv in mixed.cu).
 constexpr int PIPE_IMG_TK = 32, PIPE_IMG_CH = 8, PIPE_IMG_FLOATS = UM_M * PIPE_IMG_TK, PIPE_IMG_BYTES = PIPE_IMG_FLOATS * 4;
@@ -158,10 +156,11 @@ __device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, int ncb, int n, in
 }
 
 // S[t0.., t0..cmax) -= P P^T, P = columns k0 .. k0 + kw - 1, in 128 x TN tiles and TK-column
-// chunks; grid = min(tiles, SMs), 800 threads.  img != nullptr (128 x 128 tiles with 32-column
-// chunks, or 128 x 64 tiles with one 64-column chunk): the panel comes from its images
-// (written by the panel solves), one thread of warp 0 fills each stage with four bulk copies
-// and the other producer warps stay idle.
+// chunks; grid = min(tiles, SMs), 800 threads.  img != nullptr (128 x 64 tiles with one
+// 64-column chunk, the left-looking updates inside a 256-column panel): the panel comes from
+// its images (written by the panel solves), one thread of warp 0 fills each stage with four
+// bulk copies and the other producer warps stay idle.  (The image-fed whole-trailing-matrix
+// update is k_syrk_pair below.)
 template <int TN, int TK, int NS = 2>
 __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n, int k0, int kw, int t0, int cmax, int ncb,
                                                                float *S, size_t sstride, int *status, const float *img)
@@ -241,9 +240,8 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
         }
     } else if (warp < PIPE_PRODUCER_WARPS && img) {
         // ---- producer: bulk copies of the panel images (one thread) ----
-        constexpr bool WIDE = TN == UM_M && TK == PIPE_IMG_TK; // whole trailing matrix
-        constexpr bool REST = TN == 64 && TK == 64;            // rest of a 256-column panel
-        if constexpr (WIDE || REST) {
+        constexpr bool REST = TN == 64 && TK == 64; // rest of a 256-column panel
+        if constexpr (REST) {
             if (tid == 0) {
                 int it = 0, last[NS];
                 for (int s = 0; s < NS; s++) last[s] = -1;
@@ -252,23 +250,14 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
                     const PipeTile T = pipe_tile<TN>(t, tpt, ncb, n, t0, cend, status);
                     if (!T.valid) continue;
                     for (int ch = 0; ch < nchunk; ch++, it++) {
-                        const float *ahi, *alo, *bhi, *blo;
-                        if constexpr (WIDE) {
-                            const size_t o = (size_t)ch * 2 * PIPE_IMG_FLOATS;
-                            ahi = img + ((size_t)T.task * nr + (T.row0 - t0) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_FLOATS + o;
-                            bhi = img + ((size_t)T.task * nr + (T.col0 - t0) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_FLOATS + o;
-                            alo = ahi + PIPE_IMG_FLOATS;
-                            blo = bhi + PIPE_IMG_FLOATS;
-                        } else {
-                            // chunk ch is panel block ch, its image rows counted from k0 + 64 (ch + 1)
-                            const size_t nrb64 = pipe_img64_nrb(n);
-                            const int t1 = k0 + 64 * (ch + 1);
-                            const float *hi0 = img + ((size_t)ch * ntask + T.task) * 2 * nrb64 * PIPE_IMG64_FLOATS;
-                            ahi = hi0 + (size_t)((T.row0 - t1) / 64) * PIPE_IMG64_FLOATS;
-                            bhi = hi0 + (size_t)((T.col0 - t1) / 64) * PIPE_IMG64_FLOATS;
-                            alo = ahi + nrb64 * PIPE_IMG64_FLOATS;
-                            blo = bhi + nrb64 * PIPE_IMG64_FLOATS;
-                        }
+                        // chunk ch is panel block ch, its image rows counted from k0 + 64 (ch + 1)
+                        const size_t nrb64 = pipe_img64_nrb(n);
+                        const int t1 = k0 + 64 * (ch + 1);
+                        const float *hi0 = img + ((size_t)ch * ntask + T.task) * 2 * nrb64 * PIPE_IMG64_FLOATS;
+                        const float *ahi = hi0 + (size_t)((T.row0 - t1) / 64) * PIPE_IMG64_FLOATS;
+                        const float *bhi = hi0 + (size_t)((T.col0 - t1) / 64) * PIPE_IMG64_FLOATS;
+                        const float *alo = ahi + nrb64 * PIPE_IMG64_FLOATS;
+                        const float *blo = bhi + nrb64 * PIPE_IMG64_FLOATS;
                         const int s = it % NS, use = it / NS;
                         if (use > 0 && !umma::mbar_wait(&empty[s], (use - 1) & 1, PIPE_WAIT_ITERS)) {
                             ok = false;
@@ -355,6 +344,212 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
     if (warp == 0) {
         umma::fence_after();
         umma::dealloc(tmem, 2 * TN);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Row-pair items for the image-fed whole-trailing-matrix update
+// ---------------------------------------------------------------------------
+// A 128 x 128 tile needs two 128-row slices of the panel (its rows and its columns); copying
+// them from L2 into shared memory bounds the update.  Here a work item is row blocks 2q and
+// 2q + 1 against one column block j <= 2q, sharing the column block's slice: three slices per
+// chunk for two tiles.  The diagonal tile (2q + 1, 2q + 1) and, for an odd number of row
+// blocks, the last row block's tiles are items of one tile.  Row pair q has 2q + 2 items
+// (columns 0 .. 2q paired, then the diagonal single), starting at item q (q + 1).  Roles:
+// warp 0 lane 0 fills PAIR_STAGES stages of 32 panel columns with one bulk copy per slice (hi
+// and lo adjacent), warp 1 lane 0 issues the MMAs into one 128-column accumulator per tile of
+// the item (double-buffered: all 512 columns of tensor memory), warps 2..17 are the epilogue
+// (warp w reads tensor-memory lanes 32 (w mod 4); the four warps of a lane quadrant split the
+// columns).  Waits and failure handling as in k_syrk_pipe.
+constexpr int PAIR_STAGES = 2, PAIR_EPI_WARPS = 16;
+constexpr int PAIR_THREADS = (2 + PAIR_EPI_WARPS) * 32;                 // 576
+constexpr int PAIR_SLICE = UM_M * PIPE_IMG_TK;                          // floats of one hi or lo slice
+constexpr int PAIR_STAGE = 6 * PAIR_SLICE;                              // A0, A1, B (hi, lo each): 96 KB
+constexpr int PAIR_SMEM = PAIR_STAGES * PAIR_STAGE * 4;                 // 192 KB
+
+struct PairTile {
+    int task, ra, rb, col0; // rb < 0: one tile
+    bool valid;
+};
+__host__ __device__ inline int pair_items(int nr)
+{
+    const int np = nr / 2;
+    return np * (np + 1) + ((nr & 1) ? nr : 0);
+}
+__device__ __forceinline__ PairTile pair_tile(int t, int ipt, int nr, int t0, const int *status)
+{
+    PairTile T;
+    T.task = t / ipt;
+    const int p = t - T.task * ipt, np = nr / 2;
+    int ra, rb = -1, cj;
+    if (p < np * (np + 1)) {
+        int q = (int)((sqrtf(4.0f * p + 1.0f) - 1.0f) * 0.5f);
+        while ((q + 1) * (q + 2) <= p) q++;
+        while (q * (q + 1) > p) q--;
+        const int off = p - q * (q + 1);
+        if (off <= 2 * q) { ra = 2 * q; rb = 2 * q + 1; cj = off; }
+        else { ra = 2 * q + 1; cj = 2 * q + 1; }
+    } else {
+        ra = 2 * np;
+        cj = p - np * (np + 1);
+    }
+    T.ra = t0 + ra * UM_M;
+    T.rb = rb >= 0 ? t0 + rb * UM_M : -1;
+    T.col0 = t0 + cj * UM_M;
+    // skip matrices that are not being factored or failed before this launch
+    T.valid = (status[T.task] & ~ST_ERR_WAIT) == ST_FACTOR;
+    return T;
+}
+
+// S[t0.., t0..) -= P P^T over the PIPE_IMG_CH PIPE_IMG_TK = 256 panel columns of img (layout
+// above); grid = min(items, SMs), PAIR_THREADS threads, PAIR_SMEM bytes of dynamic shared memory
+__global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n, int t0, float *S, size_t sstride, int *status,
+                                                               const float *img)
+{
+    constexpr int PA = PAIR_SLICE, NCH = PIPE_IMG_CH;
+    extern __shared__ __align__(1024) float pipe_sm[];
+    __shared__ uint64_t full[PAIR_STAGES], empty[PAIR_STAGES], tfull[2], tempty[2], drain;
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nr = (n - t0 + UM_M - 1) / UM_M;
+    const int ipt = pair_items(nr);
+    const int nitem = ntask * ipt;
+
+    if (warp == 0) umma::alloc(&tslot, 512);
+    if (tid == 0) {
+        for (int i = 0; i < PAIR_STAGES; i++) {
+            umma::mbar_init(&full[i], 1);
+            umma::mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            umma::mbar_init(&tfull[i], 1);
+            umma::mbar_init(&tempty[i], PAIR_EPI_WARPS * 32);
+        }
+        umma::mbar_init(&drain, 1);
+    }
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = tslot;
+    auto slice = [&](int task, int rblock, int ch) { // hi slice of row block rblock, chunk ch; lo follows
+        return img + (((size_t)task * nr + rblock) * NCH + ch) * 2 * PA;
+    };
+
+    if (warp >= 2) {
+        // ---- epilogue ----
+        const int quad = warp & 3, part4 = (warp - 2) >> 2; // four warps per lane quadrant, 32 columns each
+        int tt = 0;
+        for (int t = blockIdx.x; t < nitem; t += gridDim.x) {
+            const PairTile T = pair_tile(t, ipt, nr, t0, status);
+            if (!T.valid) continue;
+            float *Sm = S + (size_t)T.task * sstride;
+            const int b = tt & 1, ub = tt >> 1;
+            bool ok = true, waited = false;
+            for (int h = 0; h < (T.rb >= 0 ? 2 : 1) && ok; h++) {
+                const int R = (h ? T.rb : T.ra) + quad * 32 + lane;
+                for (int part = 0; part < 2; part++) {
+                    const int cb = T.col0 + part4 * 32 + part * 16;
+                    float c[16];
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        const int C = cb + j;
+                        c[j] = (R < n && C < n && R >= C) ? Sm[(size_t)C * n + R] : 0.0f;
+                    }
+                    if (!waited) {
+                        ok = umma::mbar_wait(&tfull[b], ub & 1, PIPE_WAIT_ITERS);
+                        umma::fence_after();
+                        waited = true;
+                        if (!ok) break;
+                    }
+                    float v[16];
+                    umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * 256 + h * 128 + part4 * 32 + part * 16, v);
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        const int C = cb + j;
+                        if (R < n && C < n && R >= C) Sm[(size_t)C * n + R] = c[j] - v[j];
+                    }
+                }
+            }
+            if (!ok) { atomicOr(status + T.task, ST_ERR_WAIT); break; }
+            umma::fence_before();
+            mbar_arrive(&tempty[b]);
+            tt++;
+        }
+    } else if (warp == 0) {
+        // ---- producer: bulk copies of the images (one thread) ----
+        if (lane == 0) {
+            int it = 0, last[PAIR_STAGES];
+            for (int s = 0; s < PAIR_STAGES; s++) last[s] = -1;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < nitem; t += gridDim.x) {
+                const PairTile T = pair_tile(t, ipt, nr, t0, status);
+                if (!T.valid) continue;
+                const int ba = (T.ra - t0) / UM_M, bc = (T.col0 - t0) / UM_M, bb = T.rb >= 0 ? (T.rb - t0) / UM_M : -1;
+                for (int ch = 0; ch < NCH; ch++, it++) {
+                    const int s = it % PAIR_STAGES, use = it / PAIR_STAGES;
+                    if (use > 0 && !umma::mbar_wait(&empty[s], (use - 1) & 1, PIPE_WAIT_ITERS)) {
+                        ok = false;
+                        atomicOr(status + T.task, ST_ERR_WAIT);
+                        break;
+                    }
+                    float *st = pipe_sm + s * PAIR_STAGE;
+                    umma::mbar_arrive_tx(&full[s], (bb >= 0 ? 6 : 4) * PA * 4);
+                    umma::bulk_g2s(st, slice(T.task, ba, ch), 2 * PA * 4, &full[s]);                       // A0 hi, lo
+                    if (bb >= 0) umma::bulk_g2s(st + 2 * PA, slice(T.task, bb, ch), 2 * PA * 4, &full[s]); // A1 hi, lo
+                    umma::bulk_g2s(st + 4 * PA, slice(T.task, bc, ch), 2 * PA * 4, &full[s]);              // B hi, lo
+                    last[s] = use;
+                }
+            }
+            // the copies complete whatever the other roles do: wait (bounded) for the last fill of
+            // each stage, so that none is in flight when the CTA leaves
+            for (int s = 0; s < PAIR_STAGES; s++)
+                if (last[s] >= 0) umma::mbar_wait(&full[s], last[s] & 1, PIPE_WAIT_ITERS);
+        }
+    } else {
+        // ---- MMA issue (warp 1, one thread) ----
+        if (lane == 0) {
+            int it = 0, tt = 0;
+            constexpr uint32_t idesc = umma::idesc_tf32(UM_M, UM_M);
+            constexpr uint32_t LBO = 128, SBO = (PIPE_IMG_TK / 4) * 128;
+            for (int t = blockIdx.x; t < nitem; t += gridDim.x) {
+                const PairTile T = pair_tile(t, ipt, nr, t0, status);
+                if (!T.valid) continue;
+                const int b = tt & 1, ub = tt >> 1, nh = T.rb >= 0 ? 2 : 1;
+                bool ok = ub == 0 || umma::mbar_wait(&tempty[b], (ub - 1) & 1, PIPE_WAIT_ITERS);
+                umma::fence_after();
+                for (int ch = 0; ok && ch < NCH; ch++, it++) {
+                    const int s = it % PAIR_STAGES, use = it / PAIR_STAGES;
+                    if (!umma::mbar_wait(&full[s], use & 1, PIPE_WAIT_ITERS)) { ok = false; break; }
+                    umma::fence_after();
+                    const uint32_t base = umma::smem_u32(pipe_sm + s * PAIR_STAGE);
+                    const uint32_t bh = base + 4 * PA * 4, bl = bh + PA * 4;
+                    for (int h = 0; h < nh; h++) {
+                        const uint32_t ah = base + h * 2 * PA * 4, al = ah + PA * 4;
+                        const uint32_t acc = tmem + b * 256 + h * 128;
+                        for (int ks = 0; ks < PIPE_IMG_TK / 8; ks++) {
+                            const uint32_t o = ks * 256;
+                            umma::mma_tf32(acc, umma::desc_kmajor(al + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc,
+                                           ch > 0 || ks > 0);
+                            umma::mma_tf32(acc, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bl + o, LBO, SBO), idesc, 1);
+                            umma::mma_tf32(acc, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc, 1);
+                        }
+                    }
+                    umma::commit(&empty[s]);
+                }
+                if (!ok) { atomicOr(status + T.task, ST_ERR_WAIT); break; }
+                umma::commit(&tfull[b]);
+                tt++;
+            }
+            // every MMA this thread issued completes before the CTA frees tensor memory
+            umma::commit(&drain);
+            umma::mbar_wait(&drain, 0, PIPE_WAIT_ITERS);
+        }
+    }
+    umma::fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        umma::fence_after();
+        umma::dealloc(tmem, 512);
     }
 }
 
