@@ -64,12 +64,12 @@ __global__ void k_to_delta32(int ntask, int n, const double *A, size_t lda, size
 
 // diagonal block in delta form, one CTA of 256 threads per matrix; also writes W =
 // (I + Lam_kk)^{-1} (lower triangular, MB x MB per task, stored transposed) for the panel solve and
-// the block's share of ||Lam||_F^2.  Per column j every thread forms the pivot from
-// T[j][j]; threads 0..63 scale row tid of column j into colj; the rank-1 update of the
-// trailing triangle takes the entries (i, c), j < c <= i, from a list of the whole triangle
-// ordered by column (last column first), so that step j's entries are a prefix of it and
-// the 256 threads share them evenly (consecutive threads: consecutive rows of one column,
-// T rows 65 floats apart, distinct banks).  W follows blockwise (16 x 16 blocks).
+// the block's share of ||Lam||_F^2.  The factorisation runs in 16-column sub-panels (warp-level
+// diagonal block, substitution below it, rank-16 update of the rest); the updates take the
+// entries (i, c) of the trailing triangle from a list of the whole triangle ordered by column
+// (last column first), so that each sub-panel's entries are a prefix of it and the 256
+// threads share them evenly (consecutive threads: consecutive rows of one column, T rows 65
+// floats apart, distinct banks).  W follows blockwise (16 x 16 blocks).
 __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float *S, size_t sstride, int *status, float *Winv,
                                                  double *fro)
 {
@@ -106,27 +106,74 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
     }
     __syncthreads();
     bool bad = false;
-    for (int j = 0; j < nb; j++) {
-        // phase 1: every thread forms the pivot from T[j][j], threads j+1..nb-1 scale their
-        // entry of column j (T[j][j] itself is rewritten only in phase 2, which reads
-        // neither it nor column j of T)
-        const float d = T[j][j]; // pivot - 1
-        const float one_d = 1.0f + d;
-        bad |= !(one_d > 0.0f);
-        const float lam = d / (sqrtf(fmaxf(one_d, 1e-30f)) + 1.0f);
-        const float inv = 1.0f / (1.0f + lam);
-        if (tid > j && tid < nb) {
-            const float cj = T[tid][j] * inv;
-            T[tid][j] = cj;
-            colj[tid] = cj;
+    // blocked in 16-column sub-panels: (a) the sub-panel's diagonal block by warp 0 (lane i
+    // holds its row i in registers, column entries broadcast by shuffles), (b) the rows below it
+    // by forward substitution, one thread per row, (c) the rank-16 update of the rest of the
+    // triangle from the tail of the entry list; three barriers per sub-panel
+    constexpr int PB = 16;
+    for (int o = 0; o < nb; o += PB) {
+        const int w = min(PB, nb - o);
+        if (tid < 32) {
+            const int i = tid;
+            float t[PB];
+#pragma unroll
+            for (int k = 0; k < PB; k++) t[k] = (i < w && k <= i) ? T[o + i][o + k] : 0.0f;
+#pragma unroll
+            for (int j = 0; j < PB; j++) {
+                if (j < w) { // uniform
+                const float d = __shfl_sync(0xffffffffu, t[j], j); // pivot - 1
+                const float one_d = 1.0f + d;
+                bad |= !(one_d > 0.0f);
+                const float lam = d / (sqrtf(fmaxf(one_d, 1e-30f)) + 1.0f);
+                const float inv = 1.0f / (1.0f + lam);
+                if (i > j) t[j] *= inv;
+                else if (i == j) t[j] = lam;
+                if (i == 0) colj[o + j] = inv;
+                const float cj = t[j];
+#pragma unroll
+                for (int c = j + 1; c < PB; c++) {
+                    const float v = __shfl_sync(0xffffffffu, cj, c); // column j of row c
+                    if (i >= c && i < w) t[c] = fmaf(-cj, v, t[c]);
+                }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < PB; k++)
+                if (i < w && k <= i) T[o + i][o + k] = t[k];
         }
         __syncthreads();
-        // phase 2: rank-1 update of the trailing triangle (c > j: a prefix of the list) from colj
-        if (tid == 0) T[j][j] = lam;
-        const int cnt = (MB - 1 - j) * (MB - j) / 2;
-        for (int e = tid; e < cnt; e += 256) {
-            const int v = tri[e], ri = v & 0xff, c = v >> 8;
-            if (ri < nb) T[ri][c] -= colj[ri] * colj[c];
+        const int c0 = o + w;
+        if (tid < nb - c0) {
+            const int r = c0 + tid;
+            float x[PB];
+#pragma unroll
+            for (int k = 0; k < PB; k++) x[k] = k < w ? T[r][o + k] : 0.0f;
+#pragma unroll
+            for (int k = 0; k < PB; k++) {
+                if (k < w) {
+                    float a = x[k];
+#pragma unroll
+                    for (int j = 0; j < k; j++) a = fmaf(-x[j], T[o + k][o + j], a);
+                    x[k] = a * colj[o + k];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < PB; k++)
+                if (k < w) T[r][o + k] = x[k];
+        }
+        __syncthreads();
+        if (c0 < nb) {
+            // the entries (i, c), c0 <= c <= i, are the first (MB - c0)(MB - c0 + 1) / 2 of the list
+            const int cnt = (MB - c0) * (MB - c0 + 1) / 2;
+            for (int e = tid; e < cnt; e += 256) {
+                const int v = tri[e], ri = v & 0xff, c = v >> 8;
+                if (ri < nb) {
+                    float acc = 0.0f;
+#pragma unroll
+                    for (int k = 0; k < PB; k++) acc = fmaf(T[ri][o + k], T[c][o + k], acc);
+                    T[ri][c] -= acc;
+                }
+            }
         }
         __syncthreads();
     }
