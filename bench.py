@@ -486,24 +486,27 @@ def main():
                       "peak_source": "measured live: DFMA-chain probe kernel (caps_gpu_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
                       "traffic": None} if args.precision == "fp64" else
                      {"bound": "hbm",
-                      "kernel": "k_syrk_pipe: persistent warp-specialised tcgen05 trailing update of the FP32 delta-form "
-                                "Cholesky (256-column panels, split TF32, TMEM accumulators; the whole-trailing-matrix "
-                                "launches fed by bulk copies of split-TF32 panel images that the panel solves write); "
-                                "algorithmic bytes = target block read + written once and the panel rows read once, "
-                                "per factored matrix",
+                      "kernel": "tcgen05 trailing update of the FP32 delta-form Cholesky (256-column panels, split TF32, "
+                                "TMEM accumulators, persistent and warp-specialised): k_syrk_pair for the whole trailing "
+                                "matrix (row-pair items sharing the column slice, fed by bulk copies of split-TF32 panel "
+                                "images that the panel solves write) and k_syrk_pipe<64, 64> for the left-looking block "
+                                "updates; algorithmic bytes = target block read + written once and the panel rows read "
+                                "once, per factored matrix",
                       "achieved": syrk_gbs, "peak": hbm_peak, "unit": "GB/s",
                       "frac": syrk_gbs / hbm_peak if syrk_gbs else None,
                       "traffic": syrk_bytes / syrk_n * SYRK_DRAM_PER_ALGORITHMIC if syrk_n else None,
                       "peak_source": hbm_src,
                       "launches": syrk_n, "avg_launch_ms": syrk_ms / syrk_n if syrk_n else None,
                       "algorithmic_bytes_per_launch": syrk_bytes / syrk_n if syrk_n else None,
-                      "traffic_source": "DRAM bytes per algorithmic byte of the k_syrk_pipe launches in one ncu capture "
-                                        "of 48 factored matrices of this workload, times this run's algorithmic bytes per "
-                                        "launch (the images are written by the panel solves, outside these launches)",
+                      "traffic_source": "DRAM bytes per algorithmic byte of the update launches of one 256-column panel in "
+                                        "ncu captures of 24 and 48 factored matrices of this workload (whole-trailing-matrix "
+                                        "update 1.02, block updates 1.03 / 1.32 / 1.47), times this run's algorithmic bytes "
+                                        "per launch (the images are written by the panel solves, outside these launches)",
                       "fp32_accurate_tflops_factorisation": achieved,
                       "panel_kernels": panel_kernels or None,
                       "panel_kernels_note": "the panel solve is bytes-bound like the update (its rate against the same peak); "
-                                            "the diagonal block is latency-bound: 64 dependent column steps per matrix"}),
+                                            "the diagonal block is latency-bound: a dependent factorisation and inverse "
+                                            "per 64 x 64 block"}),
         "dominant_kernel": None if args.precision == "fp64" else {
             "kernel": "the FP32 delta-form factorisation (k_syrk_pipe, the roofline kernel above, with the panel "
                       "kernels k_trsm_inv and k_potf2_w)", "phase_share_of_step": ph[4] / ph[5] if ph[5] else None,
