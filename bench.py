@@ -272,6 +272,9 @@ def main():
                     help="plain truncation schedule instead of the learned proposal")
     ap.add_argument("--no-side", action="store_true",
                     help="skip the side measurements (plain forms, per-matrix errors)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the library's default schedule and path instead of timing the candidates (for runs under "
+                         "a profiler, whose serialised launches distort the candidates' times)")
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: one batch of 8 matrices of the workload (n in {1,5}, m in {0,20,40,60})")
     ap.add_argument("--ncu-matrices", type=int, default=8,
@@ -362,11 +365,14 @@ def main():
     # determinant path, timed on eight matrices of the workload
     Ts = matsubara_spacing()
     t_at = time.time()
-    chosen, at_ms = caps.autotune(Ts, nprobe=8)
-    autotune = {"candidates_ms_per_matrix": at_ms, "chosen": chosen, "seconds": time.time() - t_at,
-                "candidates": (["dense: panel images by bulk copies", "dense: panel staged through registers",
-                                "dense: one CTA per tile", "HODLR (float-float sampled elements, FP64 factorisation)"]
-                               if args.precision == "mixed" else ["dense Cholesky", "HODLR"])}
+    if args.no_autotune:
+        autotune = {"skipped": "library defaults: dense path at this dimension, panel images by bulk copies"}
+    else:
+        chosen, at_ms = caps.autotune(Ts, nprobe=8)
+        autotune = {"candidates_ms_per_matrix": at_ms, "chosen": chosen, "seconds": time.time() - t_at,
+                    "candidates": (["dense: panel images by bulk copies", "dense: panel staged through registers",
+                                    "dense: one CTA per tile", "HODLR (float-float sampled elements, FP64 factorisation)"]
+                                   if args.precision == "mixed" else ["dense Cholesky", "HODLR"])}
 
     net, train_info = None, None
     args.learned = not args.plain
