@@ -522,8 +522,8 @@ def main():
             "kernel": "k_sweep_ff (I table by the three-term Legendre recurrence from 4L seed q-sums, fused with "
                       "the elements, straight into the FP32 delta matrix)",
             "phase_share_of_step": (ph[2] + ph[3]) / ph[5] if ph[5] else None,
-            "bound": "latency: per-row barrier and float-float dependency chains at 16 warps per SM; "
-                     "FP32 work, DRAM idle",
+            "bound": "latency: float-float dependency chains (producer and consumer warps on mbarriers, 20 warps "
+                     "per SM); FP32 work, DRAM idle",
             "evidence": "ncu capture of k_sweep_ff on 48 matrices of this workload"},
         "cpu_baseline": cpu,
         "autotune": autotune,

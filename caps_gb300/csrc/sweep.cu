@@ -117,7 +117,7 @@ constexpr int SW_PW = 3, SW_CW = SW_NW - SW_PW;  // producer (recurrence) and co
 constexpr int SW_CH = 30;                       // output columns of a consumer pass (32 lanes)
 constexpr int SW_RING = 4;                      // rows of T held in shared memory
 constexpr int SW_WAIT_ITERS = 1 << 22;          // polls of a bounded mbarrier wait
-constexpr size_t SW_BYTES_PER_L = SW_RING * 2 * sizeof(float2) + 2 * sizeof(float4) + sizeof(int);
+constexpr size_t SW_BYTES_PER_L = SW_RING * 2 * sizeof(float2) + 2 * sizeof(float4) + 2 * sizeof(int);
 
 CAPS_DEV ff ff_sub(ff x, ff y) { return ff_add(x, ff_neg(y)); }
 // x c for c exactly representable in FP32 (small integers)
@@ -248,6 +248,7 @@ __global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const 
     extern __shared__ __align__(16) unsigned char sw_smem[];
     __shared__ uint64_t rready[SW_RING], rfree[SW_RING];
     __shared__ int s_abort, s_ok;
+    __shared__ float2 seedrow[2][3][2]; // scaled seeds of the producers' next row: [row parity][D0, D1, COL][TE, TM]
     __shared__ float red[SW_NW];
     const int L = ldim + 2, n = 2 * ldim;
     if ((int)blockIdx.x >= nlist) return;
@@ -259,17 +260,20 @@ __global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const 
     float4 *cpm = reinterpret_cast<float4 *>(ring + (size_t)SW_RING * 2 * L); // Cp h, l, Cm h, l
     float4 *dab = cpm + L;                                                   // dA h, l, dB h, l
     int *eab = reinterpret_cast<int *>(dab + L);                             // exponents of dA (low 16 bits), dB
+    int *ktab = eab + L;                                                     // k(w) of the scaling
     auto sp = [&](int pol, int kind) { return seed + ((size_t)(task * 2 + pol) * SEED_KINDS + kind) * L; };
     auto rowp = [&](int r) { return ring + (size_t)((r % SW_RING) * 2) * L; }; // row r (r >= 0): TE at +0, TM at +L
     const ffe *d0tm = sp(1, SEED_D0);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    // per window index: the recurrence's column coefficients and the element factors
+    // per window index: k(w), then the recurrence's column coefficients and the element factors
+    for (int w = tid; w < L; w += SW_NT) ktab[w] = sw_k(d0tm, w, c);
+    __syncthreads();
     for (int w = tid; w < L; w += SW_NT) {
-        const int l = lm1 + w, kw = sw_k(d0tm, w, c);
+        const int l = lm1 + w, kw = ktab[w];
         ff cp{0.0f, 0.0f}, cmv{0.0f, 0.0f};
-        if (w >= c && w + 1 < L) cp = ff_shift(ff_from_d((double)(l - mm + 1) / (2.0 * l + 1)), kw - sw_k(d0tm, w + 1, c));
-        if (w >= c + 1) cmv = ff_shift(ff_from_d((double)(l + mm) / (2.0 * l + 1)), kw - sw_k(d0tm, w - 1, c));
+        if (w >= c && w + 1 < L) cp = ff_shift(ff_from_d((double)(l - mm + 1) / (2.0 * l + 1)), kw - ktab[w + 1]);
+        if (w >= c + 1) cmv = ff_shift(ff_from_d((double)(l + mm) / (2.0 * l + 1)), kw - ktab[w - 1]);
         cpm[w] = make_float4(cp.h, cp.l, cmv.h, cmv.l);
         const ffe a = Saf[(size_t)task * L + w], b = Sbf[(size_t)task * L + w];
         dab[w] = make_float4(a.h, a.l, b.h, b.l);
@@ -292,6 +296,20 @@ __global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const 
 
     if (warp < SW_PW) {
         // ---- producers: rows of T ----
+        // the seeds of row r (pairs (r, r), (r, r-1), (r, c)), scaled into the frame, into
+        // seedrow[r & 1] by threads 0..5 one row ahead, so that their loads are off the row's path
+        auto fetch_seeds = [&](int r) {
+            if (tid < 6 && r < L) {
+                const int kind = tid >> 1, pol = tid & 1;
+                const int y = kind == 0 ? r : (kind == 1 ? r - 1 : c), wi = kind == 2 ? r : y;
+                const int skind = kind == 0 ? SEED_D0 : (kind == 1 ? SEED_D1 : SEED_COL);
+                ff v = zero;
+                if (y >= c && wi >= 0) v = sw_seed(sp(pol, skind)[wi], ktab[r] + ktab[y]);
+                seedrow[r & 1][kind][pol] = make_float2(v.h, v.l);
+            }
+        };
+        fetch_seeds(0);
+        sw_producer_bar();
         for (int r = 0; r < L; r++) {
             const int s = r % SW_RING;
             if (r >= SW_RING) { // slot s held row r - SW_RING: every consumer warp has released it
@@ -309,16 +327,15 @@ __global__ void __launch_bounds__(SW_NT, 2) k_sweep_ff(const Task *tasks, const 
                 R1 = ff_rcp(ff{q.x, q.y});
                 nR2 = ff_neg(ff_mul(R1, ff{q.z, q.w}));
             }
-            const int kr = sw_k(d0tm, r, c);
+            fetch_seeds(r + 1); // read at row r + 1, after the barriers below
             for (int y = tid; y <= r; y += SW_PW * 32) {
                 ff vT = zero, vE = zero;
                 if (y < c) {
                 } else if (y == r || y == r - 1 || y == c) {
-                    const int kind = y == r ? SEED_D0 : (y == r - 1 ? SEED_D1 : SEED_COL);
-                    const int wi = kind == SEED_COL ? r : y; // the pair (r, y) is stored at index wi
-                    const int k12 = kr + sw_k(d0tm, y, c);
-                    vT = sw_seed(sp(1, kind)[wi], k12);
-                    vE = sw_seed(sp(0, kind)[wi], k12);
+                    const int kind = y == r ? 0 : (y == r - 1 ? 1 : 2);
+                    const float2 t1 = seedrow[r & 1][kind][1], t0 = seedrow[r & 1][kind][0];
+                    vT = ff{t1.x, t1.y};
+                    vE = ff{t0.x, t0.y};
                 } else {
                     const float4 q = cpm[y];
                     const ff Cp{q.x, q.y}, Cm{q.z, q.w};

@@ -65,10 +65,10 @@ def test_sweep_smallest_windows(cg, ldim):
         assert rel(v, u) <= TOL, (x, m, u, v)
 
 
-@pytest.mark.parametrize("ldim", [2300, 2400])
+@pytest.mark.parametrize("ldim", [2200, 2400])
 def test_sweep_ring_limit(cg, ldim):
-    """ldim 2300 (the recurrence sweep: 100 bytes of shared memory per l) and 2400 (beyond the
-    ring: the full q-sum table), Drude, R/L = 400, dimensions 4600 and 4800"""
+    """ldim 2200 (the recurrence sweep: 104 bytes of shared memory per l) and 2400 (beyond the
+    ring: the full q-sum table), Drude, R/L = 400, dimensions 4400 and 4800"""
     xi = [2.0, 2.0, 20.0]
     ms = [0, 4, 1]
     a, b = both(cg, 400e-6, 1e-6, ldim, xi, ms, (9.0, 0.035), min_factored=2)
