@@ -204,9 +204,11 @@ def run_reference(args, dist, rank, world):
     print(json.dumps(line), flush=True)
 
 
-# DRAM bytes per algorithmic byte of the trailing update (k_syrk_pipe, all four launch kinds
-# of a 256-column panel), from one ncu capture of 48 factored matrices of this workload
-SYRK_DRAM_PER_ALGORITHMIC = 1.14
+# DRAM bytes per algorithmic byte of the trailing update (k_syrk_pair and k_syrk_blk, all 32
+# update launches of the factorisation), from one ncu capture of 24 factored matrices of this
+# workload: below 1 because the FP16 panel images that the panel solves have just written are
+# partly still in L2 when the update reads them; nothing is read twice
+SYRK_DRAM_PER_ALGORITHMIC = 0.79
 
 
 def measured_hbm_peak():
@@ -405,7 +407,7 @@ def main():
     ph = cg.timings(cumulative=True)   # device ms per phase, summed over the timed steps
     syrk_ms, syrk_bytes, syrk_n = cg.kernel_stats(0)
     panel_kernels = {}
-    for kind, name in ((1, "k_trsm_inv (panel solve; writes the split-TF32 panel images)"),
+    for kind, name in ((1, "k_trsm_inv (panel solve; writes the FP16 panel images)"),
                        (2, "k_potf2_w (64 x 64 diagonal block and its inverse, one CTA per matrix)")):
         ms_, by_, n_ = cg.kernel_stats(kind)
         if n_:
@@ -492,32 +494,33 @@ def main():
                       "peak_source": "measured live: DFMA-chain probe kernel (caps_gpu_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
                       "traffic": None} if args.precision == "fp64" else
                      {"bound": "hbm",
-                      "kernel": "tcgen05 trailing update of the FP32 delta-form Cholesky (256-column panels, split TF32, "
-                                "TMEM accumulators, persistent and warp-specialised): k_syrk_pair for the whole trailing "
-                                "matrix (row-pair items sharing the column slice, fed by bulk copies of split-TF32 panel "
-                                "images that the panel solves write) and k_syrk_pipe<64, 64> for the left-looking block "
-                                "updates; algorithmic bytes = target block read + written once and the panel rows read "
-                                "once, per factored matrix",
+                      "kernel": "tcgen05 trailing update of the FP32 delta-form Cholesky (256-column panels; panel as "
+                                "FP16 pairs hi + lo of 2^14 x, products hi hi + hi lo + lo hi accumulated in FP32 in "
+                                "TMEM; persistent and warp-specialised): k_syrk_pair for the whole trailing matrix "
+                                "(row-pair items sharing the column slice) and k_syrk_blk for the left-looking block "
+                                "updates, both fed by bulk copies of the panel images that the panel solves write; "
+                                "algorithmic bytes = target block read + written once (FP32) and the panel rows read "
+                                "once (4 bytes per entry), per factored matrix",
                       "achieved": syrk_gbs, "peak": hbm_peak, "unit": "GB/s",
                       "frac": syrk_gbs / hbm_peak if syrk_gbs else None,
                       "traffic": syrk_bytes / syrk_n * SYRK_DRAM_PER_ALGORITHMIC if syrk_n else None,
                       "peak_source": hbm_src,
                       "launches": syrk_n, "avg_launch_ms": syrk_ms / syrk_n if syrk_n else None,
                       "algorithmic_bytes_per_launch": syrk_bytes / syrk_n if syrk_n else None,
-                      "traffic_source": "DRAM bytes per algorithmic byte of the update launches of one 256-column panel in "
-                                        "ncu captures of 24 and 48 factored matrices of this workload (whole-trailing-matrix "
-                                        "update 1.02, block updates 1.03 / 1.32 / 1.47), times this run's algorithmic bytes "
-                                        "per launch (the images are written by the panel solves, outside these launches)",
+                      "traffic_source": "DRAM bytes per algorithmic byte over all 32 update launches of the factorisation "
+                                        "of 24 matrices of this workload in one ncu capture (whole-trailing-matrix updates "
+                                        "0.80, block updates 0.78: the images just written by the panel solves are partly "
+                                        "read from L2), times this run's algorithmic bytes per launch",
                       "fp32_accurate_tflops_factorisation": achieved,
                       "panel_kernels": panel_kernels or None,
                       "panel_kernels_note": "the panel solve is bytes-bound like the update (its rate against the same peak); "
                                             "the diagonal block is latency-bound: a dependent factorisation and inverse "
                                             "per 64 x 64 block"}),
         "dominant_kernel": None if args.precision == "fp64" else {
-            "kernel": "the FP32 delta-form factorisation (k_syrk_pipe, the roofline kernel above, with the panel "
+            "kernel": "the FP32 delta-form factorisation (k_syrk_pair and k_syrk_blk, the roofline kernels above, with the panel "
                       "kernels k_trsm_inv and k_potf2_w)", "phase_share_of_step": ph[4] / ph[5] if ph[5] else None,
             "bound": "HBM for the trailing update; the panel solve streams the panel, the diagonal block is latency-bound",
-            "evidence": "roofline and panel_kernels above; ncu captures of k_syrk_pipe on a 24- and 48-matrix case"},
+            "evidence": "roofline and panel_kernels above; ncu captures of k_syrk_pair and k_syrk_blk on a 24-matrix case"},
         "assembly_kernel": None if args.precision == "fp64" else {
             "kernel": "k_sweep_ff (I table by the three-term Legendre recurrence from 4L seed q-sums, fused with "
                       "the elements, straight into the FP32 delta matrix)",

@@ -131,6 +131,7 @@ enum : int {
     ST_ERR_GRID = 64,      // quadrature grid did not fit the node budget
     ST_ERR_WAIT = 128,     // a bounded wait for the tensor cores ran out
     ST_ERR_HODLR = 256,    // HODLR: an off-diagonal block needed more than the largest rank
+    ST_ERR_RANGE = 512,    // mixed form: a factor entry |x| >= 4, outside the range of the FP16 panel images
 };
 
 } // namespace capsgpu

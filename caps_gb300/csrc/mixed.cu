@@ -249,16 +249,17 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
 // per k a thread reads its four rows and its four columns as one float4 each for 16 FMAs.
 constexpr int MT = 64;
 // img != nullptr: rows at or below t2 (the first row of the trailing matrix of this 256-column
-// panel) also go to the panel's split-TF32 images for the whole-trailing-matrix update
-// (layout of syrk_pipe.cuh, nrb 128-row blocks per matrix); img64 != nullptr: every row goes
-// to the image of 64-column block blk64 of the panel for the left-looking updates of the
-// later blocks (layout of syrk_pipe.cuh).
+// panel) also go to the panel's FP16 images for the whole-trailing-matrix update (layout of
+// syrk_pipe.cuh, nrb 128-row blocks per matrix); img64 != nullptr: every row goes to the FP16
+// image of 64-column block blk64 of the panel for the left-looking updates of the later
+// blocks (layout of syrk_pipe.cuh).  An entry |x| >= 4, outside the images' range, marks the
+// matrix ST_ERR_RANGE.
 // Rows past n are left unwritten there; they only reach accumulator rows and columns that
 // are never stored.  store_x false: X is not written back to S (with both images, nothing
 // reads it there again: later steps read S only in their own columns, the final sums only
 // its diagonal).
-__global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, const int *status,
-                                                  const float *Winv, double *fro, float *img, int t2, int nrb, float *img64,
+__global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, int *status,
+                                                  const float *Winv, double *fro, __half *img, int t2, int nrb, __half *img64,
                                                   int blk64, bool store_x)
 {
     const int task = blockIdx.y;
@@ -322,40 +323,52 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
         }
     }
     if (img) {
-        // columns 4 cg .. 4 cg + 3 of this block are one 16-byte row of a core matrix
+        // columns 4 cg .. 4 cg + 3 of this block are half of one 16-byte row of a core matrix
+        // (the two column groups of a warp fill it, its 16 rows two whole core matrices)
         const int kk = k0 % (PIPE_IMG_CH * PIPE_IMG_TK) + 4 * cg; // column within the panel
-        const int ch = kk / PIPE_IMG_TK, kq = (kk % PIPE_IMG_TK) / 4;
+        const int ch = kk / PIPE_IMG_TK, kc = kk % PIPE_IMG_TK;
+        bool big = false;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const int r = rg + 16 * i, R = r0 + r;
             if (r < rows && R >= t2) {
                 const int rr = R - t2, rb = rr / UM_M, q = rr % UM_M;
-                float *hi = img + (((size_t)task * nrb + rb) * PIPE_IMG_CH + ch) * 2 * PIPE_IMG_FLOATS;
-                const int e = ((q / 8) * (PIPE_IMG_TK / 4) + kq) * 32 + (q % 8) * 4;
-                float h[4], l[4];
+                __half *hi = img + (((size_t)task * nrb + rb) * PIPE_IMG_CH + ch) * 2 * PIPE_IMG_HALVES;
+                const int e = ((q / 8) * (PIPE_IMG_TK / 8) + kc / 8) * 64 + (q % 8) * 8 + kc % 8;
+                uint32_t h[4], l[4];
 #pragma unroll
-                for (int j = 0; j < 4; j++) um_split(acc[i][j], h[j], l[j]);
-                *reinterpret_cast<float4 *>(hi + e) = make_float4(h[0], h[1], h[2], h[3]);
-                *reinterpret_cast<float4 *>(hi + PIPE_IMG_FLOATS + e) = make_float4(l[0], l[1], l[2], l[3]);
+                for (int j = 0; j < 4; j++) {
+                    img_split16(acc[i][j], h[j], l[j]);
+                    big |= !(fabsf(acc[i][j]) < PIPE_IMG_XMAX);
+                }
+                *reinterpret_cast<uint2 *>(hi + e) = make_uint2(h[0] | h[1] << 16, h[2] | h[3] << 16);
+                *reinterpret_cast<uint2 *>(hi + PIPE_IMG_HALVES + e) = make_uint2(l[0] | l[1] << 16, l[2] | l[3] << 16);
             }
         }
+        if (big) atomicOr(status + task, ST_ERR_RANGE);
     }
     if (img64) {
-        // this block's 64 rows are 64-row block blockIdx.x of the image (rows from k0 + 64)
+        // this block's 64 rows are 64-row block blockIdx.x of the image (rows from k0 + 64);
+        // columns 4 cg .. 4 cg + 3 are half of one 16-byte row of a core matrix
         const int nrb64 = pipe_img64_nrb(n);
-        float *hi = img64 + (((size_t)blk64 * ntask + task) * 2 * nrb64 + blockIdx.x) * PIPE_IMG64_FLOATS;
+        __half *hi = img64 + (((size_t)blk64 * ntask + task) * 2 * nrb64 + blockIdx.x) * PIPE_IMG64_HALVES;
+        bool big = false;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             const int r = rg + 16 * i;
             if (r < rows) {
-                const int e = ((r / 8) * 16 + cg) * 32 + (r % 8) * 4;
-                float h[4], l[4];
+                const int e = ((r / 8) * 8 + cg / 2) * 64 + (r % 8) * 8 + 4 * (cg % 2);
+                uint32_t h[4], l[4];
 #pragma unroll
-                for (int j = 0; j < 4; j++) um_split(acc[i][j], h[j], l[j]);
-                *reinterpret_cast<float4 *>(hi + e) = make_float4(h[0], h[1], h[2], h[3]);
-                *reinterpret_cast<float4 *>(hi + (size_t)nrb64 * PIPE_IMG64_FLOATS + e) = make_float4(l[0], l[1], l[2], l[3]);
+                for (int j = 0; j < 4; j++) {
+                    img_split16(acc[i][j], h[j], l[j]);
+                    big |= !(fabsf(acc[i][j]) < PIPE_IMG_XMAX);
+                }
+                *reinterpret_cast<uint2 *>(hi + e) = make_uint2(h[0] | h[1] << 16, h[2] | h[3] << 16);
+                *reinterpret_cast<uint2 *>(hi + (size_t)nrb64 * PIPE_IMG64_HALVES + e) = make_uint2(l[0] | l[1] << 16, l[2] | l[3] << 16);
             }
         }
+        if (big) atomicOr(status + task, ST_ERR_RANGE);
     }
     __shared__ double red8[8];
     sq = block_sum256(sq, red8);
@@ -621,8 +634,8 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     // panel images)
     float *Winv = (float *)work;
     double *part = (double *)((char *)work + (size_t)ntask * MB * MB * sizeof(float));
-    float *img = (float *)((char *)work + mixed_img_offset(ntask, n));
-    float *img64 = img + (size_t)ntask * pipe_img_bytes(n) / 4;
+    __half *img = (__half *)((char *)work + mixed_img_offset(ntask, n));
+    __half *img64 = (__half *)((char *)img + (size_t)ntask * pipe_img_bytes(n));
     CK(cudaMemsetAsync(part, 0, (size_t)ntask * fro_slots(n) * sizeof(double), st));
     // convert: A is the FP64 matrix 1 - M and S receives its delta form here; otherwise S
     // already holds it.  mdiag: M_ii in FP64, n per task (tr(A - I) = -tr M).
@@ -648,6 +661,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         CK(cudaFuncSetAttribute(k_syrk_pipe<64, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM));
         CK(cudaFuncSetAttribute(k_syrk_pipe<128, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, PIPE_SMEM_WIDE));
         CK(cudaFuncSetAttribute(k_syrk_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, PAIR_SMEM));
+        CK(cudaFuncSetAttribute(k_syrk_blk, cudaFuncAttributeMaxDynamicSharedMemorySize, BLK_SMEM));
         int dev = 0;
         CK(cudaGetDevice(&dev));
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -662,9 +676,11 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         if (no_pipe)
             k_syrk_umma<<<dim3(ncb == 1 ? nr : nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb == 1,
                                                                                                  S, sstride, status);
-        else if (ncb > 0) // one 64-column block from the panel's earlier blocks: 128 x 64 tiles, 64-column chunks
+        else if (ncb > 0 && use_img) // one 64-column block from the FP16 images of the panel's earlier blocks
+            k_syrk_blk<<<std::min(ntask * nr, nsm), BLK_THREADS, BLK_SMEM, st>>>(ntask, n, k0, t0, S, sstride, status, img64);
+        else if (ncb > 0) // the same from S: 128 x 64 tiles, 64-column chunks
             k_syrk_pipe<64, 64><<<std::min(ntask * tpt, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb, S,
-                                                                                             sstride, status, use_img ? img64 : nullptr);
+                                                                                             sstride, status);
         else { // the whole trailing matrix: 128 x 128 tiles (a third less staging per entry), 32-column chunks
             const int tw = ntask * pipe_tiles<128>(nr, 0);
             if (use_img && kw == PIPE_IMG_CH * PIPE_IMG_TK) // the panel solves left the panel's images: row-pair items
@@ -672,7 +688,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
                                                                                                   img);
             else
                 k_syrk_pipe<128, 32><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_WIDE, st>>>(ntask, n, k0, kw, t0, cmax, 0, S,
-                                                                                              sstride, status, nullptr);
+                                                                                              sstride, status);
         }
         COUNT_LAUNCH(1);
         if (g_kt.on) {
@@ -688,8 +704,8 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         COUNT_LAUNCH(1);
     }
     // diagonal block k0 and the panel solve below it; false when nothing lies below.  With
-    // images, the solve also writes the split-TF32 images of the rows below the 256-column
-    // panel for its whole-trailing-matrix update.
+    // images, the solve also writes the FP16 images of the rows below the 256-column panel for
+    // its whole-trailing-matrix update, and of its own rows for the panel's later blocks.
     constexpr int PANEL = PIPE_IMG_CH * PIPE_IMG_TK; // outer panel width, 256
     auto factor_panel = [&](int k0, bool images) {
         KernelTimer &tp = g_kts[KT_POTF2], &tt = g_kts[KT_TRSM];
@@ -716,8 +732,8 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
             CK(cudaEventRecord(tt.next(), st));
             double w = 0;
             if (!images) w = 4.0 * rest * MB;
-            if (im) w += 8.0 * (n - t2) * MB;
-            if (im64) w += 8.0 * rest * MB;
+            if (im) w += 4.0 * (n - t2) * MB;
+            if (im64) w += 4.0 * rest * MB;
             tt.per_matrix_bytes.push_back(4.0 * rest * MB + w);
         }
         return true;

@@ -24,6 +24,8 @@
 // waits (bounded) for the MMAs it issued, and the CTA frees its tensor memory and returns.  All roles walk the same tile list and skip the same
 // tiles (matrices whose factorisation already failed).
 #pragma once
+#include <cuda_fp16.h>
+
 #include "common.cuh"
 #include "umma.cuh"
 #include "syrk_umma.cuh"
@@ -88,26 +90,43 @@ __device__ __forceinline__ void pipe_stage(const float *Sm, int n, int kc, int n
     }
 }
 
-// Panel images for the whole-trailing-matrix update (k_syrk_pair below, 32-column chunks):
-// the panel P = S[t0 .., k0 .. k0 + 256) cut into 128-row blocks and 32-column chunks, each
-// chunk split into TF32 hi and lo and stored as the 16 KB image of a shared-memory slice
-// (the layout above), hi and lo adjacent, so that one bulk copy brings both:
-// img[(((task nrb + rb) PIPE_IMG_CH + ch) 2 + part) PIPE_IMG_FLOATS + e], nrb = ceil((n - t0) / 128).
+// Panel images for the whole-trailing-matrix update (k_syrk_pair below, 64-column chunks):
+// the panel P = S[t0 .., k0 .. k0 + 256) scaled by 2^14, cut into 128-row blocks and
+// 64-column chunks, each chunk split into FP16 hi = fp16(2^14 x) and lo = fp16(2^14 x - hi)
+// and stored as the 16 KB image of a shared-memory slice (K-major core matrices of 8 rows x
+// 8 halves, 8-row groups 1024 B apart), hi and lo adjacent, so that one bulk copy brings both:
+// img[(((task nrb + rb) PIPE_IMG_CH + ch) 2 + part) PIPE_IMG_HALVES + e], nrb = ceil((n - t0) / 128),
+// e = ((q / 8) 8 + k / 8) 64 + (q mod 8) 8 + k mod 8 for row q and column k of the chunk.
 // The panel solves that produce P write them (k_trsm_inv in mixed.cu).
-constexpr int PIPE_IMG_TK = 32, PIPE_IMG_CH = 8, PIPE_IMG_FLOATS = UM_M * PIPE_IMG_TK, PIPE_IMG_BYTES = PIPE_IMG_FLOATS * 4;
+// Range: P holds entries of a Cholesky factor of A = 1 - M, |x| <= sqrt(A_ii) < sqrt(2) for
+// |M_ii| < 1, so 2^14 x stays below the FP16 maximum 65504 (the writer flags |x| >= 4).
+// Entries from 2^-17 up have both halves normal: 22 significant bits, as many as the
+// split-TF32 pair; smaller ones keep an absolute resolution of 2^-38.  The products of two
+// scaled entries are exact in the FP32 accumulator, which the update scales back by 2^-28.
+constexpr int PIPE_IMG_TK = 64, PIPE_IMG_CH = 4, PIPE_IMG_HALVES = UM_M * PIPE_IMG_TK, PIPE_IMG_BYTES = PIPE_IMG_HALVES * 2;
+constexpr float PIPE_IMG_SCALE = 16384.0f, PIPE_IMG_UNSCALE2 = 1.0f / (16384.0f * 16384.0f), PIPE_IMG_XMAX = 4.0f;
 // bytes of image space per matrix of dimension n
 __host__ __device__ inline size_t pipe_img_bytes(int n) { return (size_t)((n + UM_M - 1) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_BYTES; }
-// Images for the left-looking updates inside a 256-column panel (128 x 64 tiles, 64-column
-// chunks): 64-column block b = 0, 1, 2 of the panel (columns k0 + 64 b ..), rows from
-// t1 = k0 + 64 (b + 1), cut into 64-row blocks of 16 KB, all hi blocks of a matrix and then
-// all lo blocks, so that a 128-row slice is two consecutive blocks:
-// img[(((b ntask + task) 2 + part) PIPE_IMG64_NRB(n) + rb) PIPE_IMG64_FLOATS + e].  The update of
-// block j reads chunk b < j from block b's image.
-constexpr int PIPE_IMG64_FLOATS = 64 * 64, PIPE_IMG64_BLOCKS = 3;
+// the FP16 pair of 2^14 x (bits of hi, lo)
+__device__ __forceinline__ void img_split16(float x, uint32_t &hi, uint32_t &lo)
+{
+    const float s = x * PIPE_IMG_SCALE;
+    const __half h = __float2half_rn(s);
+    hi = __half_as_ushort(h);
+    lo = __half_as_ushort(__float2half_rn(s - __half2float(h)));
+}
+// Images for the left-looking updates inside a 256-column panel (k_syrk_blk below, 128 x 64
+// tiles, 64-column chunks), FP16 pairs of 2^14 x as above: 64-column block b = 0, 1, 2 of the
+// panel (columns k0 + 64 b ..), rows from t1 = k0 + 64 (b + 1), cut into 64-row blocks of 8 KB
+// (the core-matrix layout above), all hi blocks of a matrix and then all lo blocks, so that a
+// 128-row slice is two consecutive blocks:
+// img[(((b ntask + task) 2 + part) pipe_img64_nrb(n) + rb) PIPE_IMG64_HALVES + e].  The update
+// of block j reads chunk b < j from block b's image.
+constexpr int PIPE_IMG64_HALVES = 64 * 64, PIPE_IMG64_BLOCKS = 3;
 __host__ __device__ inline int pipe_img64_nrb(int n) { return 2 * ((n + UM_M - 1) / UM_M) + 2; }
 __host__ __device__ inline size_t pipe_img64_bytes(int n)
 {
-    return (size_t)PIPE_IMG64_BLOCKS * 2 * pipe_img64_nrb(n) * PIPE_IMG64_FLOATS * 4;
+    return (size_t)PIPE_IMG64_BLOCKS * 2 * pipe_img64_nrb(n) * PIPE_IMG64_HALVES * 2;
 }
 
 struct PipeTile {
@@ -156,14 +175,11 @@ __device__ __forceinline__ PipeTile pipe_tile(int t, int tpt, int ncb, int n, in
 }
 
 // S[t0.., t0..cmax) -= P P^T, P = columns k0 .. k0 + kw - 1, in 128 x TN tiles and TK-column
-// chunks; grid = min(tiles, SMs), 800 threads.  img != nullptr (128 x 64 tiles with one
-// 64-column chunk, the left-looking updates inside a 256-column panel): the panel comes from
-// its images (written by the panel solves), one thread of warp 0 fills each stage with four
-// bulk copies and the other producer warps stay idle.  (The image-fed whole-trailing-matrix
-// update is k_syrk_pair below.)
+// chunks staged through registers from S; grid = min(tiles, SMs), 800 threads.  (The
+// image-fed updates are k_syrk_pair and k_syrk_blk below.)
 template <int TN, int TK, int NS = 2>
 __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n, int k0, int kw, int t0, int cmax, int ncb,
-                                                               float *S, size_t sstride, int *status, const float *img)
+                                                               float *S, size_t sstride, int *status)
 {
     using Shape = PipeShape<TN, TK, NS>;
     constexpr int PA = UM_M * TK, PB = TN * TK;
@@ -180,12 +196,12 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
     if (warp == 0) umma::alloc(&tslot, 2 * TN);
     if (tid == 0) {
         for (int i = 0; i < NS; i++) {
-            umma::mbar_init(&full[i], img ? 1 : PIPE_PRODUCERS);
+            umma::mbar_init(&full[i], PIPE_PRODUCERS);
             umma::mbar_init(&empty[i], 1);
         }
         for (int i = 0; i < 2; i++) {
             umma::mbar_init(&tfull[i], 1);
-            umma::mbar_init(&tempty[i], (img ? 2 : 1) * PIPE_EPI_WARPS * 32);
+            umma::mbar_init(&tempty[i], PIPE_EPI_WARPS * 32);
         }
         umma::mbar_init(&drain, 1);
     }
@@ -194,15 +210,12 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
     umma::fence_after();
     const uint32_t tmem = tslot;
 
-    // epilogue warps: 17-24, and with images (one producer thread) also the otherwise idle
-    // producer warps 1-8; warp w reads TMEM lane quadrant w mod 4, and the warps of one
-    // quadrant split the tile's columns (halves, or quarters with images)
-    const int eidx = warp > PIPE_PRODUCER_WARPS ? warp - PIPE_PRODUCER_WARPS - 1 + (img ? PIPE_EPI_WARPS : 0)
-                     : (img && warp >= 1 && warp <= PIPE_EPI_WARPS) ? warp - 1 : -1;
+    // epilogue warps: 17-24; warp w reads TMEM lane quadrant w mod 4, and the two warps of
+    // one quadrant take half of the tile's columns each
+    const int eidx = warp > PIPE_PRODUCER_WARPS ? warp - PIPE_PRODUCER_WARPS - 1 : -1;
     if (eidx >= 0) {
         // ---- epilogue ----
-        const int per_quad = (img ? 2 : 1) * PIPE_EPI_WARPS / 4;
-        const int HW = TN / per_quad; // columns per warp
+        const int HW = TN / (PIPE_EPI_WARPS / 4); // columns per warp
         const int quad = warp & 3, half = eidx >> 2;
         int tt = 0;
         for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
@@ -237,47 +250,6 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
             umma::fence_before();
             mbar_arrive(&tempty[b]);
             tt++;
-        }
-    } else if (warp < PIPE_PRODUCER_WARPS && img) {
-        // ---- producer: bulk copies of the panel images (one thread) ----
-        constexpr bool REST = TN == 64 && TK == 64; // rest of a 256-column panel
-        if constexpr (REST) {
-            if (tid == 0) {
-                int it = 0, last[NS];
-                for (int s = 0; s < NS; s++) last[s] = -1;
-                bool ok = true;
-                for (int t = blockIdx.x; ok && t < ntile; t += gridDim.x) {
-                    const PipeTile T = pipe_tile<TN>(t, tpt, ncb, n, t0, cend, status);
-                    if (!T.valid) continue;
-                    for (int ch = 0; ch < nchunk; ch++, it++) {
-                        // chunk ch is panel block ch, its image rows counted from k0 + 64 (ch + 1)
-                        const size_t nrb64 = pipe_img64_nrb(n);
-                        const int t1 = k0 + 64 * (ch + 1);
-                        const float *hi0 = img + ((size_t)ch * ntask + T.task) * 2 * nrb64 * PIPE_IMG64_FLOATS;
-                        const float *ahi = hi0 + (size_t)((T.row0 - t1) / 64) * PIPE_IMG64_FLOATS;
-                        const float *bhi = hi0 + (size_t)((T.col0 - t1) / 64) * PIPE_IMG64_FLOATS;
-                        const float *alo = ahi + nrb64 * PIPE_IMG64_FLOATS;
-                        const float *blo = bhi + nrb64 * PIPE_IMG64_FLOATS;
-                        const int s = it % NS, use = it / NS;
-                        if (use > 0 && !umma::mbar_wait(&empty[s], (use - 1) & 1, PIPE_WAIT_ITERS)) {
-                            ok = false;
-                            atomicOr(status + T.task, ST_ERR_WAIT);
-                            break;
-                        }
-                        float *st = pipe_sm + s * Shape::STAGE;
-                        umma::mbar_arrive_tx(&full[s], 2 * (PA + PB) * 4);
-                        umma::bulk_g2s(st, ahi, PA * 4, &full[s]);
-                        umma::bulk_g2s(st + PA, alo, PA * 4, &full[s]);
-                        umma::bulk_g2s(st + 2 * PA, bhi, PB * 4, &full[s]);
-                        umma::bulk_g2s(st + 2 * PA + PB, blo, PB * 4, &full[s]);
-                        last[s] = use;
-                    }
-                }
-                // the copies complete whatever the other roles do: wait (bounded) for the
-                // last fill of each stage, so that none is in flight when the CTA leaves
-                for (int s = 0; s < NS; s++)
-                    if (last[s] >= 0) umma::mbar_wait(&full[s], last[s] & 1, PIPE_WAIT_ITERS);
-            }
         }
     } else if (warp < PIPE_PRODUCER_WARPS) {
         // ---- producers ----
@@ -356,16 +328,17 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
 // chunk for two tiles.  The diagonal tile (2q + 1, 2q + 1) and, for an odd number of row
 // blocks, the last row block's tiles are items of one tile.  Row pair q has 2q + 2 items
 // (columns 0 .. 2q paired, then the diagonal single), starting at item q (q + 1).  Roles:
-// warp 0 lane 0 fills PAIR_STAGES stages of 32 panel columns with one bulk copy per slice (hi
-// and lo adjacent), warp 1 lane 0 issues the MMAs into one 128-column accumulator per tile of
+// warp 0 lane 0 fills PAIR_STAGES stages of 64 panel columns with one bulk copy per slice (hi
+// and lo adjacent, FP16 images of 2^14 P), warp 1 lane 0 issues the FP16 MMAs (hi hi + hi lo
+// + lo hi, FP32 accumulation) into one 128-column accumulator per tile of
 // the item (double-buffered: all 512 columns of tensor memory), warps 2..17 are the epilogue
 // (warp w reads tensor-memory lanes 32 (w mod 4); the four warps of a lane quadrant split the
 // columns).  Waits and failure handling as in k_syrk_pipe.
 constexpr int PAIR_STAGES = 2, PAIR_EPI_WARPS = 16;
 constexpr int PAIR_THREADS = (2 + PAIR_EPI_WARPS) * 32;                 // 576
-constexpr int PAIR_SLICE = UM_M * PIPE_IMG_TK;                          // floats of one hi or lo slice
+constexpr int PAIR_SLICE = PIPE_IMG_BYTES;                              // bytes of one hi or lo slice: 16 KB
 constexpr int PAIR_STAGE = 6 * PAIR_SLICE;                              // A0, A1, B (hi, lo each): 96 KB
-constexpr int PAIR_SMEM = PAIR_STAGES * PAIR_STAGE * 4;                 // 192 KB
+constexpr int PAIR_SMEM = PAIR_STAGES * PAIR_STAGE;                     // 192 KB
 
 struct PairTile {
     int task, ra, rb, col0; // rb < 0: one tile
@@ -404,10 +377,10 @@ __device__ __forceinline__ PairTile pair_tile(int t, int ipt, int nr, int t0, co
 // S[t0.., t0..) -= P P^T over the PIPE_IMG_CH PIPE_IMG_TK = 256 panel columns of img (layout
 // above); grid = min(items, SMs), PAIR_THREADS threads, PAIR_SMEM bytes of dynamic shared memory
 __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n, int t0, float *S, size_t sstride, int *status,
-                                                               const float *img)
+                                                               const __half *img)
 {
     constexpr int PA = PAIR_SLICE, NCH = PIPE_IMG_CH;
-    extern __shared__ __align__(1024) float pipe_sm[];
+    extern __shared__ __align__(1024) unsigned char pair_sm[];
     __shared__ uint64_t full[PAIR_STAGES], empty[PAIR_STAGES], tfull[2], tempty[2], drain;
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -432,7 +405,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
     umma::fence_after();
     const uint32_t tmem = tslot;
     auto slice = [&](int task, int rblock, int ch) { // hi slice of row block rblock, chunk ch; lo follows
-        return img + (((size_t)task * nr + rblock) * NCH + ch) * 2 * PA;
+        return img + (((size_t)task * nr + rblock) * NCH + ch) * 2 * PIPE_IMG_HALVES;
     };
 
     if (warp >= 2) {
@@ -466,7 +439,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
 #pragma unroll
                     for (int j = 0; j < 16; j++) {
                         const int C = cb + j;
-                        if (R < n && C < n && R >= C) Sm[(size_t)C * n + R] = c[j] - v[j];
+                        if (R < n && C < n && R >= C) Sm[(size_t)C * n + R] = fmaf(v[j], -PIPE_IMG_UNSCALE2, c[j]);
                     }
                 }
             }
@@ -492,11 +465,11 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
                         atomicOr(status + T.task, ST_ERR_WAIT);
                         break;
                     }
-                    float *st = pipe_sm + s * PAIR_STAGE;
-                    umma::mbar_arrive_tx(&full[s], (bb >= 0 ? 6 : 4) * PA * 4);
-                    umma::bulk_g2s(st, slice(T.task, ba, ch), 2 * PA * 4, &full[s]);                       // A0 hi, lo
-                    if (bb >= 0) umma::bulk_g2s(st + 2 * PA, slice(T.task, bb, ch), 2 * PA * 4, &full[s]); // A1 hi, lo
-                    umma::bulk_g2s(st + 4 * PA, slice(T.task, bc, ch), 2 * PA * 4, &full[s]);              // B hi, lo
+                    unsigned char *st = pair_sm + s * PAIR_STAGE;
+                    umma::mbar_arrive_tx(&full[s], (bb >= 0 ? 6 : 4) * PA);
+                    umma::bulk_g2s(st, slice(T.task, ba, ch), 2 * PA, &full[s]);                       // A0 hi, lo
+                    if (bb >= 0) umma::bulk_g2s(st + 2 * PA, slice(T.task, bb, ch), 2 * PA, &full[s]); // A1 hi, lo
+                    umma::bulk_g2s(st + 4 * PA, slice(T.task, bc, ch), 2 * PA, &full[s]);              // B hi, lo
                     last[s] = use;
                 }
             }
@@ -509,8 +482,8 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
         // ---- MMA issue (warp 1, one thread) ----
         if (lane == 0) {
             int it = 0, tt = 0;
-            constexpr uint32_t idesc = umma::idesc_tf32(UM_M, UM_M);
-            constexpr uint32_t LBO = 128, SBO = (PIPE_IMG_TK / 4) * 128;
+            constexpr uint32_t idesc = umma::idesc_f16(UM_M, UM_M);
+            constexpr uint32_t LBO = 128, SBO = (PIPE_IMG_TK / 8) * 128;
             for (int t = blockIdx.x; t < nitem; t += gridDim.x) {
                 const PairTile T = pair_tile(t, ipt, nr, t0, status);
                 if (!T.valid) continue;
@@ -521,17 +494,17 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
                     const int s = it % PAIR_STAGES, use = it / PAIR_STAGES;
                     if (!umma::mbar_wait(&full[s], use & 1, PIPE_WAIT_ITERS)) { ok = false; break; }
                     umma::fence_after();
-                    const uint32_t base = umma::smem_u32(pipe_sm + s * PAIR_STAGE);
-                    const uint32_t bh = base + 4 * PA * 4, bl = bh + PA * 4;
+                    const uint32_t base = umma::smem_u32(pair_sm + s * PAIR_STAGE);
+                    const uint32_t bh = base + 4 * PA, bl = bh + PA;
                     for (int h = 0; h < nh; h++) {
-                        const uint32_t ah = base + h * 2 * PA * 4, al = ah + PA * 4;
+                        const uint32_t ah = base + h * 2 * PA, al = ah + PA;
                         const uint32_t acc = tmem + b * 256 + h * 128;
-                        for (int ks = 0; ks < PIPE_IMG_TK / 8; ks++) {
+                        for (int ks = 0; ks < PIPE_IMG_TK / 16; ks++) { // K = 16 halves: two core matrices
                             const uint32_t o = ks * 256;
-                            umma::mma_tf32(acc, umma::desc_kmajor(al + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc,
-                                           ch > 0 || ks > 0);
-                            umma::mma_tf32(acc, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bl + o, LBO, SBO), idesc, 1);
-                            umma::mma_tf32(acc, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc, 1);
+                            umma::mma_f16(acc, umma::desc_kmajor(al + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc,
+                                          ch > 0 || ks > 0);
+                            umma::mma_f16(acc, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bl + o, LBO, SBO), idesc, 1);
+                            umma::mma_f16(acc, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc, 1);
                         }
                     }
                     umma::commit(&empty[s]);
@@ -550,6 +523,164 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
     if (warp == 0) {
         umma::fence_after();
         umma::dealloc(tmem, 512);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Left-looking block update from the FP16 images
+// ---------------------------------------------------------------------------
+// S[t0.., t0 .. t0 + 64) -= P P^T with P = columns k0 .. t0 of the current 256-column panel
+// (t0 - k0 = 64, 128 or 192: one 64-column chunk per earlier block of the panel, read from
+// that block's images), one 128 x 64 tile per row block.  Roles as in k_syrk_pair: warp 0 lane
+// 0 fills BLK_STAGES stages of 48 KB with four bulk copies (A hi, A lo: two consecutive 64-row
+// image blocks of 8 KB each; B hi, B lo: one block each), warp 1 lane 0 issues the FP16 MMAs
+// into one of BLK_ACC 64-column accumulators, warps 2..17 are the epilogue (warp w reads lane
+// quadrant w mod 4, 16 of the 64 columns).  Waits and failure handling as in k_syrk_pipe.
+constexpr int BLK_STAGES = 4, BLK_ACC = 4, BLK_EPI_WARPS = 16;
+constexpr int BLK_THREADS = (2 + BLK_EPI_WARPS) * 32;                     // 576
+constexpr int BLK_A = UM_M * 64 * 2, BLK_B = 64 * 64 * 2;                 // bytes of one hi or lo slice
+constexpr int BLK_STAGE = 2 * (BLK_A + BLK_B);                            // 48 KB
+constexpr int BLK_SMEM = BLK_STAGES * BLK_STAGE;                          // 192 KB
+__global__ void __launch_bounds__(BLK_THREADS, 1) k_syrk_blk(int ntask, int n, int k0, int t0, float *S, size_t sstride, int *status,
+                                                             const __half *img)
+{
+    extern __shared__ __align__(1024) unsigned char blk_sm[];
+    __shared__ uint64_t full[BLK_STAGES], empty[BLK_STAGES], tfull[BLK_ACC], tempty[BLK_ACC], drain;
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int cend = min(n, t0 + 64);
+    const int nr = (n - t0 + UM_M - 1) / UM_M; // row blocks: tile t -> (task t / nr, row block t mod nr)
+    const int ntile = ntask * nr;
+    const int nchunk = (t0 - k0) / 64;
+    const int nrb64 = pipe_img64_nrb(n);
+
+    if (warp == 0) umma::alloc(&tslot, BLK_ACC * 64);
+    if (tid == 0) {
+        for (int i = 0; i < BLK_STAGES; i++) {
+            umma::mbar_init(&full[i], 1);
+            umma::mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < BLK_ACC; i++) {
+            umma::mbar_init(&tfull[i], 1);
+            umma::mbar_init(&tempty[i], BLK_EPI_WARPS * 32);
+        }
+        umma::mbar_init(&drain, 1);
+    }
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = tslot;
+    // skip matrices that are not being factored or failed before this launch
+    auto valid = [&](int task) { return (status[task] & ~ST_ERR_WAIT) == ST_FACTOR; };
+
+    if (warp >= 2) {
+        // ---- epilogue ----
+        const int quad = warp & 3, part = (warp - 2) >> 2;
+        int tt = 0;
+        for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+            const int task = t / nr, row0 = t0 + (t - task * nr) * UM_M;
+            if (!valid(task)) continue;
+            float *Sm = S + (size_t)task * sstride;
+            const int b = tt % BLK_ACC, ub = tt / BLK_ACC;
+            const int R = row0 + quad * 32 + lane, cb = t0 + part * 16;
+            float c[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int C = cb + j;
+                c[j] = (R < n && C < cend && R >= C) ? Sm[(size_t)C * n + R] : 0.0f;
+            }
+            if (!umma::mbar_wait(&tfull[b], ub & 1, PIPE_WAIT_ITERS)) {
+                atomicOr(status + task, ST_ERR_WAIT);
+                break;
+            }
+            umma::fence_after();
+            float v[16];
+            umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * 64 + part * 16, v);
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int C = cb + j;
+                if (R < n && C < cend && R >= C) Sm[(size_t)C * n + R] = fmaf(v[j], -PIPE_IMG_UNSCALE2, c[j]);
+            }
+            umma::fence_before();
+            mbar_arrive(&tempty[b]);
+            tt++;
+        }
+    } else if (warp == 0) {
+        // ---- producer: bulk copies of the images (one thread) ----
+        if (lane == 0) {
+            int it = 0, last[BLK_STAGES];
+            for (int s = 0; s < BLK_STAGES; s++) last[s] = -1;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < ntile; t += gridDim.x) {
+                const int task = t / nr, row0 = t0 + (t - task * nr) * UM_M;
+                if (!valid(task)) continue;
+                for (int ch = 0; ch < nchunk; ch++, it++) {
+                    // chunk ch is panel block ch, its image rows counted from k0 + 64 (ch + 1)
+                    const int t1 = k0 + 64 * (ch + 1);
+                    const __half *hi0 = img + ((size_t)ch * ntask + task) * 2 * nrb64 * PIPE_IMG64_HALVES;
+                    const __half *ahi = hi0 + (size_t)((row0 - t1) / 64) * PIPE_IMG64_HALVES;
+                    const __half *bhi = hi0 + (size_t)((t0 - t1) / 64) * PIPE_IMG64_HALVES;
+                    const int s = it % BLK_STAGES, use = it / BLK_STAGES;
+                    if (use > 0 && !umma::mbar_wait(&empty[s], (use - 1) & 1, PIPE_WAIT_ITERS)) {
+                        ok = false;
+                        atomicOr(status + task, ST_ERR_WAIT);
+                        break;
+                    }
+                    unsigned char *st = blk_sm + s * BLK_STAGE;
+                    umma::mbar_arrive_tx(&full[s], BLK_STAGE);
+                    umma::bulk_g2s(st, ahi, BLK_A, &full[s]);
+                    umma::bulk_g2s(st + BLK_A, ahi + (size_t)nrb64 * PIPE_IMG64_HALVES, BLK_A, &full[s]);
+                    umma::bulk_g2s(st + 2 * BLK_A, bhi, BLK_B, &full[s]);
+                    umma::bulk_g2s(st + 2 * BLK_A + BLK_B, bhi + (size_t)nrb64 * PIPE_IMG64_HALVES, BLK_B, &full[s]);
+                    last[s] = use;
+                }
+            }
+            // the copies complete whatever the other roles do: wait (bounded) for the last fill of
+            // each stage, so that none is in flight when the CTA leaves
+            for (int s = 0; s < BLK_STAGES; s++)
+                if (last[s] >= 0) umma::mbar_wait(&full[s], last[s] & 1, PIPE_WAIT_ITERS);
+        }
+    } else {
+        // ---- MMA issue (warp 1, one thread) ----
+        if (lane == 0) {
+            int it = 0, tt = 0;
+            constexpr uint32_t idesc = umma::idesc_f16(UM_M, 64);
+            constexpr uint32_t LBO = 128, SBO = 8 * 128;
+            for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+                const int task = t / nr;
+                if (!valid(task)) continue;
+                const int b = tt % BLK_ACC, ub = tt / BLK_ACC;
+                bool ok = ub == 0 || umma::mbar_wait(&tempty[b], (ub - 1) & 1, PIPE_WAIT_ITERS);
+                umma::fence_after();
+                const uint32_t acc = tmem + b * 64;
+                for (int ch = 0; ok && ch < nchunk; ch++, it++) {
+                    const int s = it % BLK_STAGES, use = it / BLK_STAGES;
+                    if (!umma::mbar_wait(&full[s], use & 1, PIPE_WAIT_ITERS)) { ok = false; break; }
+                    umma::fence_after();
+                    const uint32_t ah = umma::smem_u32(blk_sm + s * BLK_STAGE), al = ah + BLK_A, bh = al + BLK_A, bl = bh + BLK_B;
+                    for (int ks = 0; ks < 4; ks++) { // K = 16 halves: two core matrices
+                        const uint32_t o = ks * 256;
+                        umma::mma_f16(acc, umma::desc_kmajor(al + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc,
+                                      ch > 0 || ks > 0);
+                        umma::mma_f16(acc, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bl + o, LBO, SBO), idesc, 1);
+                        umma::mma_f16(acc, umma::desc_kmajor(ah + o, LBO, SBO), umma::desc_kmajor(bh + o, LBO, SBO), idesc, 1);
+                    }
+                    umma::commit(&empty[s]);
+                }
+                if (!ok) { atomicOr(status + task, ST_ERR_WAIT); break; }
+                umma::commit(&tfull[b]);
+                tt++;
+            }
+            // every MMA this thread issued completes before the CTA frees tensor memory
+            umma::commit(&drain);
+            umma::mbar_wait(&drain, 0, PIPE_WAIT_ITERS);
+        }
+    }
+    umma::fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        umma::fence_after();
+        umma::dealloc(tmem, BLK_ACC * 64);
     }
 }
 

@@ -178,6 +178,8 @@ void caps_integrate_plasma_free(integration_plasma_t *self);                    
 #define CAPS_ST_ERR_GRID  64  /* quadrature grid exceeded its node budget: result NaN */
 #define CAPS_ST_ERR_WAIT  128 /* a bounded wait for the tensor cores ran out: result NaN */
 #define CAPS_ST_ERR_HODLR 256 /* HODLR block rank over its limit (the batch call then factors it densely) */
+#define CAPS_ST_ERR_RANGE 512 /* mixed form: a factor entry |x| >= 4 (impossible for 1-M positive definite
+                                 with |M_ii| < 1), outside the range of its FP16 panel images: result NaN */
 
 /* log det(1-M) for n (xi_[i], m[i]) pairs of one geometry, all matrices
  * assembled and factored as one GPU batch (replaces n calls of caps_logdetD,
