@@ -417,33 +417,39 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
             if (!T.valid) continue;
             float *Sm = S + (size_t)T.task * sstride;
             const int b = tt & 1, ub = tt >> 1;
-            bool ok = true, waited = false;
-            for (int h = 0; h < (T.rb >= 0 ? 2 : 1) && ok; h++) {
-                const int R = (h ? T.rb : T.ra) + quad * 32 + lane;
-                for (int part = 0; part < 2; part++) {
-                    const int cb = T.col0 + part4 * 32 + part * 16;
-                    float c[16];
+            // parts p = 2 h + half: tile h (rows ra, then rb), this warp's columns 32 part4 + 16 half;
+            // the loads of part p + 1 go out before the stores of part p
+            const int np = T.rb >= 0 ? 4 : 2;
+            // row R of part p and its columns cb + j, j < jm (inside the matrix and R >= C)
+            auto row = [&](int p) { return ((p >> 1) ? T.rb : T.ra) + quad * 32 + lane; };
+            auto col = [&](int p) { return T.col0 + part4 * 32 + (p & 1) * 16; };
+            auto lim = [&](int R, int cb) { return R < n ? min(n - cb, R - cb + 1) : 0; };
+            auto load = [&](int p, float (&d)[16]) {
+                const int R = row(p), cb = col(p), jm = lim(R, cb);
+                const float *src = Sm + (size_t)cb * n + R;
 #pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        const int C = cb + j;
-                        c[j] = (R < n && C < n && R >= C) ? Sm[(size_t)C * n + R] : 0.0f;
-                    }
-                    if (!waited) {
-                        ok = umma::mbar_wait(&tfull[b], ub & 1, PIPE_WAIT_ITERS);
-                        umma::fence_after();
-                        waited = true;
-                        if (!ok) break;
-                    }
-                    float v[16];
-                    umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * 256 + h * 128 + part4 * 32 + part * 16, v);
-#pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        const int C = cb + j;
-                        if (R < n && C < n && R >= C) Sm[(size_t)C * n + R] = fmaf(v[j], -PIPE_IMG_UNSCALE2, c[j]);
-                    }
-                }
+                for (int j = 0; j < 16; j++, src += n) d[j] = j < jm ? *src : 0.0f;
+            };
+            float cc[16], cn[16];
+            load(0, cc);
+            if (!umma::mbar_wait(&tfull[b], ub & 1, PIPE_WAIT_ITERS)) {
+                atomicOr(status + T.task, ST_ERR_WAIT);
+                break;
             }
-            if (!ok) { atomicOr(status + T.task, ST_ERR_WAIT); break; }
+            umma::fence_after();
+#pragma unroll 1
+            for (int p = 0; p < np; p++) {
+                if (p + 1 < np) load(p + 1, cn);
+                float v[16];
+                umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * 256 + (p >> 1) * 128 + part4 * 32 + (p & 1) * 16, v);
+                const int R = row(p), cb = col(p), jm = lim(R, cb);
+                float *dst = Sm + (size_t)cb * n + R;
+#pragma unroll
+                for (int j = 0; j < 16; j++, dst += n)
+                    if (j < jm) *dst = fmaf(v[j], -PIPE_IMG_UNSCALE2, cc[j]);
+#pragma unroll
+                for (int j = 0; j < 16; j++) cc[j] = cn[j];
+            }
             umma::fence_before();
             mbar_arrive(&tempty[b]);
             tt++;
@@ -576,19 +582,33 @@ __global__ void __launch_bounds__(BLK_THREADS, 1) k_syrk_blk(int ntask, int n, i
     if (warp >= 2) {
         // ---- epilogue ----
         const int quad = warp & 3, part = (warp - 2) >> 2;
+        // the loads of the next tile go out before the wait for this one
+        // this thread's row R of tile t and its columns cb + j, j < jm (inside the block and R >= C)
+        const int cb = t0 + part * 16;
+        auto lim = [&](int R) { return R < n ? min(cend - cb, R - cb + 1) : 0; };
+        auto load = [&](int t, float (&d)[16]) {
+            const int task = t / nr, R = t0 + (t - task * nr) * UM_M + quad * 32 + lane, jm = lim(R);
+            const float *src = S + (size_t)task * sstride + (size_t)cb * n + R;
+#pragma unroll
+            for (int j = 0; j < 16; j++) d[j] = j < jm ? src[j * n] : 0.0f;
+        };
+        auto next = [&](int t) {
+            while (t < ntile && !valid(t / nr)) t += gridDim.x;
+            return t;
+        };
         int tt = 0;
-        for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
-            const int task = t / nr, row0 = t0 + (t - task * nr) * UM_M;
-            if (!valid(task)) continue;
-            float *Sm = S + (size_t)task * sstride;
-            const int b = tt % BLK_ACC, ub = tt / BLK_ACC;
-            const int R = row0 + quad * 32 + lane, cb = t0 + part * 16;
+        float cn[16];
+        int t = next(blockIdx.x);
+        if (t < ntile) load(t, cn);
+        while (t < ntile) {
             float c[16];
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-                const int C = cb + j;
-                c[j] = (R < n && C < cend && R >= C) ? Sm[(size_t)C * n + R] : 0.0f;
-            }
+            for (int j = 0; j < 16; j++) c[j] = cn[j];
+            const int tn = next(t + gridDim.x);
+            if (tn < ntile) load(tn, cn);
+            const int task = t / nr, R = t0 + (t - task * nr) * UM_M + quad * 32 + lane, jm = lim(R);
+            float *dst = S + (size_t)task * sstride + (size_t)cb * n + R;
+            const int b = tt % BLK_ACC, ub = tt / BLK_ACC;
             if (!umma::mbar_wait(&tfull[b], ub & 1, PIPE_WAIT_ITERS)) {
                 atomicOr(status + task, ST_ERR_WAIT);
                 break;
@@ -597,13 +617,12 @@ __global__ void __launch_bounds__(BLK_THREADS, 1) k_syrk_blk(int ntask, int n, i
             float v[16];
             umma::ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * 64 + part * 16, v);
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-                const int C = cb + j;
-                if (R < n && C < cend && R >= C) Sm[(size_t)C * n + R] = fmaf(v[j], -PIPE_IMG_UNSCALE2, c[j]);
-            }
+            for (int j = 0; j < 16; j++)
+                if (j < jm) dst[j * n] = fmaf(v[j], -PIPE_IMG_UNSCALE2, c[j]);
             umma::fence_before();
             mbar_arrive(&tempty[b]);
             tt++;
+            t = tn;
         }
     } else if (warp == 0) {
         // ---- producer: bulk copies of the images (one thread) ----
