@@ -47,6 +47,38 @@ __device__ __forceinline__ double block_sum256(double v, double *red8)
     return s;
 }
 
+// Sums of squares of FP32 entries without the FP64 pipe (a few per cent of the FP32 rate on
+// this GPU): x^2 = p + e exactly (p = fl(x x), e = fma(x, x, -p)), accumulated as a float-float
+// pair by Knuth's two-sum on the high parts with the low parts summed in FP32 (relative error
+// about 2^-48, as good as an FP64 sum of a few hundred terms).  The _rn intrinsics keep the
+// compiler from fusing the additions into FMAs, which the two-sum must not see.
+struct SqSum {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add2(float h2, float l2)
+    {
+        const float t = __fadd_rn(hi, h2), bp = __fsub_rn(t, hi);
+        lo = __fadd_rn(__fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(h2, bp)), __fadd_rn(lo, l2));
+        hi = t;
+    }
+    __device__ __forceinline__ void add_sq(float x)
+    {
+        const float p = __fmul_rn(x, x);
+        add2(p, fmaf(x, x, -p));
+    }
+};
+// SqSum over the 256 threads of a block: float-float within each warp (fixed butterfly), then
+// the eight warp sums in FP64 in warp order; the result is valid in thread 0
+__device__ __forceinline__ double block_sq256(SqSum q, double *red8)
+{
+    for (int o = 16; o > 0; o >>= 1) q.add2(__shfl_xor_sync(0xffffffffu, q.hi, o), __shfl_xor_sync(0xffffffffu, q.lo, o));
+    if ((threadIdx.x & 31) == 0) red8[threadIdx.x >> 5] = (double)q.hi + (double)q.lo;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < 8; w++) s += red8[w];
+    return s;
+}
+
 // S = A - I (lower triangle, FP32) for the tasks that need a factorisation
 __global__ void k_to_delta32(int ntask, int n, const double *A, size_t lda, size_t mstride, const int *status, float *S,
                              size_t sstride)
@@ -177,15 +209,15 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
         }
         __syncthreads();
     }
-    double sq = 0.0;
+    SqSum q;
     for (int e = tid; e < MB * MB; e += 256) {
         const int c = e / MB, r = e % MB;
         if (c < nb && r >= c && r < nb) {
             Sm[(size_t)c * n + r] = T[r][c];
-            sq = fma((double)T[r][c], (double)T[r][c], sq);
+            q.add_sq(T[r][c]);
         }
     }
-    sq = block_sum256(sq, red8);
+    const double sq = block_sq256(q, red8);
     if (tid == 0) fro[(size_t)task * fro_slots(n) + (size_t)(k0 / MB) * (fro_nbr(n) + 1)] = sq;
     // W = (I + Lam)^{-1} blockwise in 16 x 16 blocks: the four diagonal blocks by forward
     // substitution, one thread per column with the column in registers; then the blocks below,
@@ -308,7 +340,7 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
 #pragma unroll
             for (int j = 0; j < 4; j++) acc[i][j] = fmaf(av[i], wv[j], acc[i][j]);
     }
-    double sq = 0.0;
+    SqSum q;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         const int c = 4 * cg + j;
@@ -318,7 +350,7 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
             const int r = rg + 16 * i;
             if (r < rows) {
                 if (store_x) Sm[(size_t)(k0 + c) * n + r0 + r] = acc[i][j];
-                sq = fma((double)acc[i][j], (double)acc[i][j], sq);
+                q.add_sq(acc[i][j]);
             }
         }
     }
@@ -371,7 +403,7 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
         if (big) atomicOr(status + task, ST_ERR_RANGE);
     }
     __shared__ double red8[8];
-    sq = block_sum256(sq, red8);
+    const double sq = block_sq256(q, red8);
     if (threadIdx.x == 0) fro[(size_t)task * fro_slots(n) + (size_t)(k0 / MB) * (fro_nbr(n) + 1) + 1 + blockIdx.x] = sq;
 }
 
