@@ -66,16 +66,16 @@ struct SqSum {
         add2(p, fmaf(x, x, -p));
     }
 };
-// SqSum over the 256 threads of a block: float-float within each warp (fixed butterfly), then
-// the eight warp sums in FP64 in warp order; the result is valid in thread 0
-__device__ __forceinline__ double block_sq256(SqSum q, double *red8)
+// SqSum over the NW warps of a block: float-float within each warp (fixed butterfly), then
+// the warp sums in FP64 in warp order; the result is valid in thread 0
+template <int NW> __device__ __forceinline__ double block_sq(SqSum q, double *red)
 {
     for (int o = 16; o > 0; o >>= 1) q.add2(__shfl_xor_sync(0xffffffffu, q.hi, o), __shfl_xor_sync(0xffffffffu, q.lo, o));
-    if ((threadIdx.x & 31) == 0) red8[threadIdx.x >> 5] = (double)q.hi + (double)q.lo;
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)q.hi + (double)q.lo;
     __syncthreads();
     double s = 0.0;
     if (threadIdx.x == 0)
-        for (int w = 0; w < 8; w++) s += red8[w];
+        for (int w = 0; w < NW; w++) s += red[w];
     return s;
 }
 
@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
             q.add_sq(T[r][c]);
         }
     }
-    const double sq = block_sq256(q, red8);
+    const double sq = block_sq<8>(q, red8);
     if (tid == 0) fro[(size_t)task * fro_slots(n) + (size_t)(k0 / MB) * (fro_nbr(n) + 1)] = sq;
     // W = (I + Lam)^{-1} blockwise in 16 x 16 blocks: the four diagonal blocks by forward
     // substitution, one thread per column with the column in registers; then the blocks below,
@@ -275,11 +275,14 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
 
 // panel: X (I + Lam_kk)^T = S for the rows below the diagonal block, as X = S W^T with
 // W = (I + Lam_kk)^{-1} from k_potf2_w (I + Lam_kk is within a few per cent of I, so the
-// product is as accurate as the substitution).  64 rows per CTA of 256 threads; thread t
-// computes a 4 x 4 tile, rows t mod 16 + 16 i and columns 4 (t / 16) + j.  The rows are kept
-// in shared memory k-major with row r at position 4 (r mod 16) + r / 16 and W k-major, so
-// per k a thread reads its four rows and its four columns as one float4 each for 16 FMAs.
-constexpr int MT = 64;
+// product is as accurate as the substitution).  64 rows per CTA of 128 threads; thread t
+// computes rows t mod 16 + 16 i of the column groups g = t / 16 and 15 - g (columns 4 g + j
+// and 4 (15 - g) + j).  W is lower triangular (column c takes k <= c), so the pair needs
+// k < 4 g + 4 for both groups and k < 64 - 4 g for the second: 1088 FMAs for every thread, half
+// the FMAs and shared-memory reads of the full product, in the same order per column.  The
+// rows are kept in shared memory k-major with row r at position 4 (r mod 16) + r / 16 and W
+// k-major, so per k a thread reads its four rows and four columns of a group as one float4.
+constexpr int MT = 64, TRSM_THREADS = 128;
 // img != nullptr: rows at or below t2 (the first row of the trailing matrix of this 256-column
 // panel) also go to the panel's FP16 images for the whole-trailing-matrix update (layout of
 // syrk_pipe.cuh, nrb 128-row blocks per matrix); img64 != nullptr: every row goes to the FP16
@@ -290,7 +293,7 @@ constexpr int MT = 64;
 // are never stored.  store_x false: X is not written back to S (with both images, nothing
 // reads it there again: later steps read S only in their own columns, the final sums only
 // its diagonal).
-__global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, int *status,
+__global__ void __launch_bounds__(TRSM_THREADS) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, int *status,
                                                   const float *Winv, double *fro, __half *img, int t2, int nrb, __half *img64,
                                                   int blk64, bool store_x)
 {
@@ -304,106 +307,126 @@ __global__ void __launch_bounds__(256) k_trsm_inv(int ntask, int n, int k0, floa
     float *Sm = S + (size_t)task * sstride;
     const float *Wt = Winv + (size_t)task * MB * MB;
     const int rows = min(MT, n - r0);
+    constexpr int NT = TRSM_THREADS;
     {
-        float w[MB * MB / 256], x[MT * MB / 256];
+        float w[MB * MB / NT], x[MT * MB / NT];
 #pragma unroll
-        for (int u = 0; u < MB * MB / 256; u++) w[u] = __ldg(Wt + threadIdx.x + 256 * u);
+        for (int u = 0; u < MB * MB / NT; u++) w[u] = __ldg(Wt + threadIdx.x + NT * u);
 #pragma unroll
-        for (int u = 0; u < MT * MB / 256; u++) {
-            const int e = threadIdx.x + 256 * u, c = e / MT, r = e % MT;
+        for (int u = 0; u < MT * MB / NT; u++) {
+            const int e = threadIdx.x + NT * u, c = e / MT, r = e % MT;
             x[u] = (r < rows && c < nb) ? __ldg(Sm + (size_t)(k0 + c) * n + r0 + r) : 0.0f;
         }
 #pragma unroll
-        for (int u = 0; u < MB * MB / 256; u++) {
-            const int e = threadIdx.x + 256 * u; // W stored transposed: e = k MB + c
+        for (int u = 0; u < MB * MB / NT; u++) {
+            const int e = threadIdx.x + NT * u; // W stored transposed: e = k MB + c
             Wk[e / MB][e % MB] = w[u];
         }
 #pragma unroll
-        for (int u = 0; u < MT * MB / 256; u++) {
-            const int e = threadIdx.x + 256 * u, c = e / MT, r = e % MT;
+        for (int u = 0; u < MT * MB / NT; u++) {
+            const int e = threadIdx.x + NT * u, c = e / MT, r = e % MT;
             Xk[c][4 * (r & 15) + (r >> 4)] = x[u];
         }
     }
     __syncthreads();
-    const int rg = threadIdx.x & 15, cg = threadIdx.x >> 4;
-    float acc[4][4];
+    const int rg = threadIdx.x & 15, g = threadIdx.x >> 4, gh = 15 - g;
+    float acl[4][4], ach[4][4];
 #pragma unroll
     for (int i = 0; i < 4; i++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j] = 0.0f;
-    for (int k = 0; k < nb; k++) {
+        for (int j = 0; j < 4; j++) acl[i][j] = ach[i][j] = 0.0f;
+    const int k1 = min(nb, 4 * g + 4), k2 = min(nb, 4 * gh + 4);
+    for (int k = 0; k < k1; k++) {
         const float4 a = *reinterpret_cast<const float4 *>(&Xk[k][4 * rg]);
-        const float4 w = *reinterpret_cast<const float4 *>(&Wk[k][4 * cg]);
-        const float av[4] = {a.x, a.y, a.z, a.w}, wv[4] = {w.x, w.y, w.z, w.w};
+        const float4 wl = *reinterpret_cast<const float4 *>(&Wk[k][4 * g]);
+        const float4 wh = *reinterpret_cast<const float4 *>(&Wk[k][4 * gh]);
+        const float av[4] = {a.x, a.y, a.z, a.w}, lv[4] = {wl.x, wl.y, wl.z, wl.w}, hv[4] = {wh.x, wh.y, wh.z, wh.w};
 #pragma unroll
         for (int i = 0; i < 4; i++)
 #pragma unroll
-            for (int j = 0; j < 4; j++) acc[i][j] = fmaf(av[i], wv[j], acc[i][j]);
+            for (int j = 0; j < 4; j++) {
+                acl[i][j] = fmaf(av[i], lv[j], acl[i][j]);
+                ach[i][j] = fmaf(av[i], hv[j], ach[i][j]);
+            }
+    }
+    for (int k = k1; k < k2; k++) {
+        const float4 a = *reinterpret_cast<const float4 *>(&Xk[k][4 * rg]);
+        const float4 wh = *reinterpret_cast<const float4 *>(&Wk[k][4 * gh]);
+        const float av[4] = {a.x, a.y, a.z, a.w}, hv[4] = {wh.x, wh.y, wh.z, wh.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) ach[i][j] = fmaf(av[i], hv[j], ach[i][j]);
     }
     SqSum q;
+    bool big = false;
+    // the outputs of column group cg (columns 4 cg .. 4 cg + 3) from its accumulators
+    auto emit = [&](const float(&acc)[4][4], int cg) {
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-        const int c = 4 * cg + j;
-        if (c >= nb) continue;
+        for (int j = 0; j < 4; j++) {
+            const int c = 4 * cg + j;
+            if (c >= nb) continue;
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const int r = rg + 16 * i;
-            if (r < rows) {
-                if (store_x) Sm[(size_t)(k0 + c) * n + r0 + r] = acc[i][j];
-                q.add_sq(acc[i][j]);
-            }
-        }
-    }
-    if (img) {
-        // columns 4 cg .. 4 cg + 3 of this block are half of one 16-byte row of a core matrix
-        // (the two column groups of a warp fill it, its 16 rows two whole core matrices)
-        const int kk = k0 % (PIPE_IMG_CH * PIPE_IMG_TK) + 4 * cg; // column within the panel
-        const int ch = kk / PIPE_IMG_TK, kc = kk % PIPE_IMG_TK;
-        bool big = false;
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const int r = rg + 16 * i, R = r0 + r;
-            if (r < rows && R >= t2) {
-                const int rr = R - t2, rb = rr / UM_M, q = rr % UM_M;
-                __half *hi = img + (((size_t)task * nrb + rb) * PIPE_IMG_CH + ch) * 2 * PIPE_IMG_HALVES;
-                const int e = ((q / 8) * (PIPE_IMG_TK / 8) + kc / 8) * 64 + (q % 8) * 8 + kc % 8;
-                uint32_t h[4], l[4];
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    img_split16(acc[i][j], h[j], l[j]);
-                    big |= !(fabsf(acc[i][j]) < PIPE_IMG_XMAX);
+            for (int i = 0; i < 4; i++) {
+                const int r = rg + 16 * i;
+                if (r < rows) {
+                    if (store_x) Sm[(size_t)(k0 + c) * n + r0 + r] = acc[i][j];
+                    q.add_sq(acc[i][j]);
                 }
-                *reinterpret_cast<uint2 *>(hi + e) = make_uint2(h[0] | h[1] << 16, h[2] | h[3] << 16);
-                *reinterpret_cast<uint2 *>(hi + PIPE_IMG_HALVES + e) = make_uint2(l[0] | l[1] << 16, l[2] | l[3] << 16);
             }
         }
-        if (big) atomicOr(status + task, ST_ERR_RANGE);
-    }
-    if (img64) {
-        // this block's 64 rows are 64-row block blockIdx.x of the image (rows from k0 + 64);
-        // columns 4 cg .. 4 cg + 3 are half of one 16-byte row of a core matrix
-        const int nrb64 = pipe_img64_nrb(n);
-        __half *hi = img64 + (((size_t)blk64 * ntask + task) * 2 * nrb64 + blockIdx.x) * PIPE_IMG64_HALVES;
-        bool big = false;
+        if (img) {
+            // columns 4 cg .. 4 cg + 3 of this block are half of one 16-byte row of a core matrix
+            // (the two groups 2 w, 2 w + 1 or 14 - 2 w, 15 - 2 w of warp w fill it, its 16 rows
+            // two whole core matrices)
+            const int kk = k0 % (PIPE_IMG_CH * PIPE_IMG_TK) + 4 * cg; // column within the panel
+            const int ch = kk / PIPE_IMG_TK, kc = kk % PIPE_IMG_TK;
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const int r = rg + 16 * i;
-            if (r < rows) {
-                const int e = ((r / 8) * 8 + cg / 2) * 64 + (r % 8) * 8 + 4 * (cg % 2);
-                uint32_t h[4], l[4];
+            for (int i = 0; i < 4; i++) {
+                const int r = rg + 16 * i, R = r0 + r;
+                if (r < rows && R >= t2) {
+                    const int rr = R - t2, rb = rr / UM_M, qr = rr % UM_M;
+                    __half *hi = img + (((size_t)task * nrb + rb) * PIPE_IMG_CH + ch) * 2 * PIPE_IMG_HALVES;
+                    const int e = ((qr / 8) * (PIPE_IMG_TK / 8) + kc / 8) * 64 + (qr % 8) * 8 + kc % 8;
+                    uint32_t h[4], l[4];
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    img_split16(acc[i][j], h[j], l[j]);
-                    big |= !(fabsf(acc[i][j]) < PIPE_IMG_XMAX);
+                    for (int j = 0; j < 4; j++) {
+                        img_split16(acc[i][j], h[j], l[j]);
+                        big |= !(fabsf(acc[i][j]) < PIPE_IMG_XMAX);
+                    }
+                    *reinterpret_cast<uint2 *>(hi + e) = make_uint2(h[0] | h[1] << 16, h[2] | h[3] << 16);
+                    *reinterpret_cast<uint2 *>(hi + PIPE_IMG_HALVES + e) = make_uint2(l[0] | l[1] << 16, l[2] | l[3] << 16);
                 }
-                *reinterpret_cast<uint2 *>(hi + e) = make_uint2(h[0] | h[1] << 16, h[2] | h[3] << 16);
-                *reinterpret_cast<uint2 *>(hi + (size_t)nrb64 * PIPE_IMG64_HALVES + e) = make_uint2(l[0] | l[1] << 16, l[2] | l[3] << 16);
             }
         }
-        if (big) atomicOr(status + task, ST_ERR_RANGE);
-    }
-    __shared__ double red8[8];
-    const double sq = block_sq256(q, red8);
+        if (img64) {
+            // this block's 64 rows are 64-row block blockIdx.x of the image (rows from k0 + 64);
+            // columns 4 cg .. 4 cg + 3 are half of one 16-byte row of a core matrix
+            const int nrb64 = pipe_img64_nrb(n);
+            __half *hi = img64 + (((size_t)blk64 * ntask + task) * 2 * nrb64 + blockIdx.x) * PIPE_IMG64_HALVES;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int r = rg + 16 * i;
+                if (r < rows) {
+                    const int e = ((r / 8) * 8 + cg / 2) * 64 + (r % 8) * 8 + 4 * (cg % 2);
+                    uint32_t h[4], l[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        img_split16(acc[i][j], h[j], l[j]);
+                        big |= !(fabsf(acc[i][j]) < PIPE_IMG_XMAX);
+                    }
+                    *reinterpret_cast<uint2 *>(hi + e) = make_uint2(h[0] | h[1] << 16, h[2] | h[3] << 16);
+                    *reinterpret_cast<uint2 *>(hi + (size_t)nrb64 * PIPE_IMG64_HALVES + e) =
+                        make_uint2(l[0] | l[1] << 16, l[2] | l[3] << 16);
+                }
+            }
+        }
+    };
+    emit(acl, g);
+    emit(ach, gh);
+    if (big) atomicOr(status + task, ST_ERR_RANGE);
+    __shared__ double red4[NT / 32];
+    const double sq = block_sq<NT / 32>(q, red4);
     if (threadIdx.x == 0) fro[(size_t)task * fro_slots(n) + (size_t)(k0 / MB) * (fro_nbr(n) + 1) + 1 + blockIdx.x] = sq;
 }
 
@@ -757,7 +780,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         const bool im64 = images && blk < PIPE_IMG64_BLOCKS && k0 + MB < std::min(t2, n);
         dim3 gt((rest + MT - 1) / MT, ntask);
         if (tt.on) CK(cudaEventRecord(tt.next(), st));
-        k_trsm_inv<<<gt, 256, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part, im ? img : nullptr, t2,
+        k_trsm_inv<<<gt, TRSM_THREADS, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part, im ? img : nullptr, t2,
                                       im ? (n - t2 + UM_M - 1) / UM_M : 0, im64 ? img64 : nullptr, blk, !images);
         COUNT_LAUNCH(1);
         if (tt.on) { // the panel's rows below read; written: X (without images) or the split images
