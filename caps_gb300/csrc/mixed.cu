@@ -283,19 +283,15 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
 // rows are kept in shared memory k-major with row r at position 4 (r mod 16) + r / 16 and W
 // k-major, so per k a thread reads its four rows and four columns of a group as one float4.
 constexpr int MT = 64, TRSM_THREADS = 128;
-// img != nullptr: rows at or below t2 (the first row of the trailing matrix of this 256-column
-// panel) also go to the panel's FP16 images for the whole-trailing-matrix update (layout of
-// syrk_pipe.cuh, nrb 128-row blocks per matrix); img64 != nullptr: every row goes to the FP16
-// image of 64-column block blk64 of the panel for the left-looking updates of the later
-// blocks (layout of syrk_pipe.cuh).  An entry |x| >= 4, outside the images' range, marks the
-// matrix ST_ERR_RANGE.
-// Rows past n are left unwritten there; they only reach accumulator rows and columns that
-// are never stored.  store_x false: X is not written back to S (with both images, nothing
-// reads it there again: later steps read S only in their own columns, the final sums only
-// its diagonal).
+// img64 != nullptr: every row goes to the FP16 image of 64-column block blk64 of the 256-column
+// panel (layout of syrk_pipe.cuh), which the left-looking updates of the panel's later blocks
+// and the trailing update after the panel read.  An entry |x| >= 4, outside the images' range,
+// marks the matrix ST_ERR_RANGE.  Rows past n are left unwritten there; they only reach
+// accumulator rows and columns that are never stored.  store_x false: X is not written back
+// to S (with the images, nothing reads it there again: later steps read S only in their own
+// columns, the final sums only its diagonal).
 __global__ void __launch_bounds__(TRSM_THREADS) k_trsm_inv(int ntask, int n, int k0, float *S, size_t sstride, int *status,
-                                                  const float *Winv, double *fro, __half *img, int t2, int nrb, __half *img64,
-                                                  int blk64, bool store_x)
+                                                  const float *Winv, double *fro, __half *img64, int blk64, bool store_x)
 {
     const int task = blockIdx.y;
     if (task >= ntask || status[task] != ST_FACTOR) return;
@@ -375,33 +371,11 @@ __global__ void __launch_bounds__(TRSM_THREADS) k_trsm_inv(int ntask, int n, int
                 }
             }
         }
-        if (img) {
-            // columns 4 cg .. 4 cg + 3 of this block are half of one 16-byte row of a core matrix
-            // (the two groups 2 w, 2 w + 1 or 14 - 2 w, 15 - 2 w of warp w fill it, its 16 rows
-            // two whole core matrices)
-            const int kk = k0 % (PIPE_IMG_CH * PIPE_IMG_TK) + 4 * cg; // column within the panel
-            const int ch = kk / PIPE_IMG_TK, kc = kk % PIPE_IMG_TK;
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const int r = rg + 16 * i, R = r0 + r;
-                if (r < rows && R >= t2) {
-                    const int rr = R - t2, rb = rr / UM_M, qr = rr % UM_M;
-                    __half *hi = img + (((size_t)task * nrb + rb) * PIPE_IMG_CH + ch) * 2 * PIPE_IMG_HALVES;
-                    const int e = ((qr / 8) * (PIPE_IMG_TK / 8) + kc / 8) * 64 + (qr % 8) * 8 + kc % 8;
-                    uint32_t h[4], l[4];
-#pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        img_split16(acc[i][j], h[j], l[j]);
-                        big |= !(fabsf(acc[i][j]) < PIPE_IMG_XMAX);
-                    }
-                    *reinterpret_cast<uint2 *>(hi + e) = make_uint2(h[0] | h[1] << 16, h[2] | h[3] << 16);
-                    *reinterpret_cast<uint2 *>(hi + PIPE_IMG_HALVES + e) = make_uint2(l[0] | l[1] << 16, l[2] | l[3] << 16);
-                }
-            }
-        }
         if (img64) {
             // this block's 64 rows are 64-row block blockIdx.x of the image (rows from k0 + 64);
-            // columns 4 cg .. 4 cg + 3 are half of one 16-byte row of a core matrix
+            // columns 4 cg .. 4 cg + 3 are half of one 16-byte row of a core matrix (the groups
+            // 2 w, 2 w + 1 or 14 - 2 w, 15 - 2 w of warp w fill it, its 16 rows two whole core
+            // matrices)
             const int nrb64 = pipe_img64_nrb(n);
             __half *hi = img64 + (((size_t)blk64 * ntask + task) * 2 * nrb64 + blockIdx.x) * PIPE_IMG64_HALVES;
 #pragma unroll
@@ -678,7 +652,7 @@ static size_t mixed_img_offset(int ntask, int n)
 }
 size_t mixed_work_bytes(int ntask, int n)
 {
-    return mixed_img_offset(ntask, n) + (size_t)ntask * (pipe_img_bytes(n) + pipe_img64_bytes(n));
+    return mixed_img_offset(ntask, n) + (size_t)ntask * pipe_img64_bytes(n);
 }
 
 void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t mstride, int *status, float *S, size_t sstride,
@@ -689,8 +663,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     // panel images)
     float *Winv = (float *)work;
     double *part = (double *)((char *)work + (size_t)ntask * MB * MB * sizeof(float));
-    __half *img = (__half *)((char *)work + mixed_img_offset(ntask, n));
-    __half *img64 = (__half *)((char *)img + (size_t)ntask * pipe_img_bytes(n));
+    __half *img64 = (__half *)((char *)work + mixed_img_offset(ntask, n));
     CK(cudaMemsetAsync(part, 0, (size_t)ntask * fro_slots(n) * sizeof(double), st));
     // convert: A is the FP64 matrix 1 - M and S receives its delta form here; otherwise S
     // already holds it.  mdiag: M_ii in FP64, n per task (tr(A - I) = -tr M).
@@ -740,7 +713,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
             const int tw = ntask * pipe_tiles<128>(nr, 0);
             if (use_img && kw == PIPE_IMG_CH * PIPE_IMG_TK) // the panel solves left the panel's images: row-pair items
                 k_syrk_pair<<<std::min(ntask * pair_items(nr), nsm), PAIR_THREADS, PAIR_SMEM, st>>>(ntask, n, t0, S, sstride, status,
-                                                                                                  img);
+                                                                                                  img64);
             else
                 k_syrk_pipe<128, 32><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_WIDE, st>>>(ntask, n, k0, kw, t0, cmax, 0, S,
                                                                                               sstride, status);
@@ -759,8 +732,8 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         COUNT_LAUNCH(1);
     }
     // diagonal block k0 and the panel solve below it; false when nothing lies below.  With
-    // images, the solve also writes the FP16 images of the rows below the 256-column panel for
-    // its whole-trailing-matrix update, and of its own rows for the panel's later blocks.
+    // images, the solve writes the FP16 image of its 64 columns (every row below the diagonal
+    // block), which the panel's later blocks and the trailing update after the panel read.
     constexpr int PANEL = PIPE_IMG_CH * PIPE_IMG_TK; // outer panel width, 256
     auto factor_panel = [&](int k0, bool images) {
         KernelTimer &tp = g_kts[KT_POTF2], &tt = g_kts[KT_TRSM];
@@ -773,22 +746,17 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         }
         const int rest = n - k0 - MB;
         if (rest <= 0) return false;
-        const int t2 = k0 / PANEL * PANEL + PANEL;
-        const bool im = images && t2 < n;
-        // later blocks of this panel are updated with this one when columns remain before t2
-        const int blk = (k0 % PANEL) / MB;
-        const bool im64 = images && blk < PIPE_IMG64_BLOCKS && k0 + MB < std::min(t2, n);
+        const int blk = (k0 % PANEL) / MB; // 64-column block of the 256-column panel
         dim3 gt((rest + MT - 1) / MT, ntask);
         if (tt.on) CK(cudaEventRecord(tt.next(), st));
-        k_trsm_inv<<<gt, TRSM_THREADS, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part, im ? img : nullptr, t2,
-                                      im ? (n - t2 + UM_M - 1) / UM_M : 0, im64 ? img64 : nullptr, blk, !images);
+        k_trsm_inv<<<gt, TRSM_THREADS, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part, images ? img64 : nullptr, blk,
+                                                !images);
         COUNT_LAUNCH(1);
-        if (tt.on) { // the panel's rows below read; written: X (without images) or the split images
+        if (tt.on) { // the panel's rows below read; written: X (without images) or the FP16 image
             CK(cudaEventRecord(tt.next(), st));
             double w = 0;
             if (!images) w = 4.0 * rest * MB;
-            if (im) w += 4.0 * (n - t2) * MB;
-            if (im64) w += 4.0 * rest * MB;
+            if (images) w += 4.0 * rest * MB;
             tt.per_matrix_bytes.push_back(4.0 * rest * MB + w);
         }
         return true;
@@ -799,7 +767,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         // through the update once), then one K = OUTER trailing update, so the trailing
         // matrix passes through DRAM once per OUTER columns
         constexpr int OUTER = 4 * MB;
-        static_assert(OUTER == PANEL && OUTER / MB - 1 == PIPE_IMG64_BLOCKS, "outer panel = image panel");
+        static_assert(OUTER == PANEL && OUTER / MB == PIPE_IMG64_BLOCKS, "outer panel = image panel");
         bool more = true; // columns remain below the last factored panel
         for (int k0 = 0; k0 < n && more; k0 += OUTER) {
             for (int kj = k0; kj < k0 + OUTER; kj += MB) {

@@ -90,23 +90,31 @@ __device__ __forceinline__ void pipe_stage(const float *Sm, int n, int kc, int n
     }
 }
 
-// Panel images for the whole-trailing-matrix update (k_syrk_pair below, 64-column chunks):
-// the panel P = S[t0 .., k0 .. k0 + 256) scaled by 2^14, cut into 128-row blocks and
-// 64-column chunks, each chunk split into FP16 hi = fp16(2^14 x) and lo = fp16(2^14 x - hi)
-// and stored as the 16 KB image of a shared-memory slice (K-major core matrices of 8 rows x
-// 8 halves, 8-row groups 1024 B apart), hi and lo adjacent, so that one bulk copy brings both:
-// img[(((task nrb + rb) PIPE_IMG_CH + ch) 2 + part) PIPE_IMG_HALVES + e], nrb = ceil((n - t0) / 128),
-// e = ((q / 8) 8 + k / 8) 64 + (q mod 8) 8 + k mod 8 for row q and column k of the chunk.
-// The panel solves that produce P write them (k_trsm_inv in mixed.cu).
-// Range: P holds entries of a Cholesky factor of A = 1 - M, |x| <= sqrt(A_ii) < sqrt(2) for
-// |M_ii| < 1, so 2^14 x stays below the FP16 maximum 65504 (the writer flags |x| >= 4).
-// Entries from 2^-17 up have both halves normal: 22 significant bits, as many as the
-// split-TF32 pair; smaller ones keep an absolute resolution of 2^-38.  The products of two
+// Panel images, read by both image-fed updates (k_syrk_blk and k_syrk_pair below): 64-column
+// block b = 0 .. 3 of a 256-column panel (columns k0 + 64 b ..) scaled by 2^14, rows from
+// t1 = k0 + 64 (b + 1), each entry split into FP16 hi = fp16(2^14 x) and lo = fp16(2^14 x - hi),
+// cut into 64-row blocks of 8 KB in the shared-memory layout of the MMA operands (K-major core
+// matrices of 8 rows x 8 halves, 8-row groups 1024 B apart), all hi blocks of a matrix and then
+// all lo blocks, so that a 128-row slice is two consecutive blocks:
+// img[(((b ntask + task) 2 + part) pipe_img64_nrb(n) + rb) PIPE_IMG64_HALVES + e],
+// e = ((q / 8) 8 + k / 8) 64 + (q mod 8) 8 + k mod 8 for row q of the block and column k.
+// The left-looking update of block j reads chunk b < j from block b's image, the trailing
+// update after the panel (rows from t2 = k0 + 256) chunk b from 64-row block 3 - b + 2 rb.
+// The panel solves that produce the panel write them (k_trsm_inv in mixed.cu).
+// Range: the panel holds entries of a Cholesky factor of A = 1 - M, |x| <= sqrt(A_ii) <
+// sqrt(2) for |M_ii| < 1, so 2^14 x stays below the FP16 maximum 65504 (the writer flags
+// |x| >= 4).  Entries from 2^-17 up have both halves normal: 22 significant bits, as many as
+// a split-TF32 pair; smaller ones keep an absolute resolution of 2^-38.  The products of two
 // scaled entries are exact in the FP32 accumulator, which the update scales back by 2^-28.
-constexpr int PIPE_IMG_TK = 64, PIPE_IMG_CH = 4, PIPE_IMG_HALVES = UM_M * PIPE_IMG_TK, PIPE_IMG_BYTES = PIPE_IMG_HALVES * 2;
+constexpr int PIPE_IMG_TK = 64, PIPE_IMG_CH = 4;                        // chunk width, chunks per panel
 constexpr float PIPE_IMG_SCALE = 16384.0f, PIPE_IMG_UNSCALE2 = 1.0f / (16384.0f * 16384.0f), PIPE_IMG_XMAX = 4.0f;
+constexpr int PIPE_IMG64_HALVES = 64 * 64, PIPE_IMG64_BLOCKS = PIPE_IMG_CH;
+__host__ __device__ inline int pipe_img64_nrb(int n) { return 2 * ((n + UM_M - 1) / UM_M) + 2; }
 // bytes of image space per matrix of dimension n
-__host__ __device__ inline size_t pipe_img_bytes(int n) { return (size_t)((n + UM_M - 1) / UM_M) * PIPE_IMG_CH * 2 * PIPE_IMG_BYTES; }
+__host__ __device__ inline size_t pipe_img64_bytes(int n)
+{
+    return (size_t)PIPE_IMG64_BLOCKS * 2 * pipe_img64_nrb(n) * PIPE_IMG64_HALVES * 2;
+}
 // the FP16 pair of 2^14 x (bits of hi, lo)
 __device__ __forceinline__ void img_split16(float x, uint32_t &hi, uint32_t &lo)
 {
@@ -114,19 +122,6 @@ __device__ __forceinline__ void img_split16(float x, uint32_t &hi, uint32_t &lo)
     const __half h = __float2half_rn(s);
     hi = __half_as_ushort(h);
     lo = __half_as_ushort(__float2half_rn(s - __half2float(h)));
-}
-// Images for the left-looking updates inside a 256-column panel (k_syrk_blk below, 128 x 64
-// tiles, 64-column chunks), FP16 pairs of 2^14 x as above: 64-column block b = 0, 1, 2 of the
-// panel (columns k0 + 64 b ..), rows from t1 = k0 + 64 (b + 1), cut into 64-row blocks of 8 KB
-// (the core-matrix layout above), all hi blocks of a matrix and then all lo blocks, so that a
-// 128-row slice is two consecutive blocks:
-// img[(((b ntask + task) 2 + part) pipe_img64_nrb(n) + rb) PIPE_IMG64_HALVES + e].  The update
-// of block j reads chunk b < j from block b's image.
-constexpr int PIPE_IMG64_HALVES = 64 * 64, PIPE_IMG64_BLOCKS = 3;
-__host__ __device__ inline int pipe_img64_nrb(int n) { return 2 * ((n + UM_M - 1) / UM_M) + 2; }
-__host__ __device__ inline size_t pipe_img64_bytes(int n)
-{
-    return (size_t)PIPE_IMG64_BLOCKS * 2 * pipe_img64_nrb(n) * PIPE_IMG64_HALVES * 2;
 }
 
 struct PipeTile {
@@ -328,15 +323,15 @@ __global__ void __launch_bounds__(PIPE_THREADS, 1) k_syrk_pipe(int ntask, int n,
 // chunk for two tiles.  The diagonal tile (2q + 1, 2q + 1) and, for an odd number of row
 // blocks, the last row block's tiles are items of one tile.  Row pair q has 2q + 2 items
 // (columns 0 .. 2q paired, then the diagonal single), starting at item q (q + 1).  Roles:
-// warp 0 lane 0 fills PAIR_STAGES stages of 64 panel columns with one bulk copy per slice (hi
-// and lo adjacent, FP16 images of 2^14 P), warp 1 lane 0 issues the FP16 MMAs (hi hi + hi lo
-// + lo hi, FP32 accumulation) into one 128-column accumulator per tile of
-// the item (double-buffered: all 512 columns of tensor memory), warps 2..17 are the epilogue
+// warp 0 lane 0 fills PAIR_STAGES stages of 64 panel columns with two bulk copies per slice
+// (hi and lo of the FP16 panel images), warp 1 lane 0 issues the FP16 MMAs (hi hi + hi lo +
+// lo hi, FP32 accumulation) into one 128-column accumulator per tile of the item
+// (double-buffered: all 512 columns of tensor memory), warps 2..17 are the epilogue
 // (warp w reads tensor-memory lanes 32 (w mod 4); the four warps of a lane quadrant split the
 // columns).  Waits and failure handling as in k_syrk_pipe.
 constexpr int PAIR_STAGES = 2, PAIR_EPI_WARPS = 16;
 constexpr int PAIR_THREADS = (2 + PAIR_EPI_WARPS) * 32;                 // 576
-constexpr int PAIR_SLICE = PIPE_IMG_BYTES;                              // bytes of one hi or lo slice: 16 KB
+constexpr int PAIR_SLICE = UM_M * PIPE_IMG_TK * 2;                      // bytes of one hi or lo slice: 16 KB
 constexpr int PAIR_STAGE = 6 * PAIR_SLICE;                              // A0, A1, B (hi, lo each): 96 KB
 constexpr int PAIR_SMEM = PAIR_STAGES * PAIR_STAGE;                     // 192 KB
 
@@ -374,8 +369,9 @@ __device__ __forceinline__ PairTile pair_tile(int t, int ipt, int nr, int t0, co
     return T;
 }
 
-// S[t0.., t0..) -= P P^T over the PIPE_IMG_CH PIPE_IMG_TK = 256 panel columns of img (layout
-// above); grid = min(items, SMs), PAIR_THREADS threads, PAIR_SMEM bytes of dynamic shared memory
+// S[t0.., t0..) -= P P^T over the PIPE_IMG_CH PIPE_IMG_TK = 256 panel columns t0 - 256 .. t0 of the
+// panel images img (layout above); grid = min(items, SMs), PAIR_THREADS threads, PAIR_SMEM bytes
+// of dynamic shared memory
 __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n, int t0, float *S, size_t sstride, int *status,
                                                                const __half *img)
 {
@@ -404,8 +400,9 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
     __syncthreads();
     umma::fence_after();
     const uint32_t tmem = tslot;
-    auto slice = [&](int task, int rblock, int ch) { // hi slice of row block rblock, chunk ch; lo follows
-        return img + (((size_t)task * nr + rblock) * NCH + ch) * 2 * PIPE_IMG_HALVES;
+    const int nrb64 = pipe_img64_nrb(n);
+    auto slice = [&](int task, int rblock, int ch) { // hi slice of row block rblock, chunk ch (the lo slice is nrb64 blocks on)
+        return img + (((size_t)ch * ntask + task) * 2 * nrb64 + 3 - ch + 2 * rblock) * PIPE_IMG64_HALVES;
     };
 
     if (warp >= 2) {
@@ -473,9 +470,17 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
                     }
                     unsigned char *st = pair_sm + s * PAIR_STAGE;
                     umma::mbar_arrive_tx(&full[s], (bb >= 0 ? 6 : 4) * PA);
-                    umma::bulk_g2s(st, slice(T.task, ba, ch), 2 * PA, &full[s]);                       // A0 hi, lo
-                    if (bb >= 0) umma::bulk_g2s(st + 2 * PA, slice(T.task, bb, ch), 2 * PA, &full[s]); // A1 hi, lo
-                    umma::bulk_g2s(st + 4 * PA, slice(T.task, bc, ch), 2 * PA, &full[s]);              // B hi, lo
+                    const size_t lo = (size_t)nrb64 * PIPE_IMG64_HALVES;
+                    const __half *a0 = slice(T.task, ba, ch), *b0 = slice(T.task, bc, ch);
+                    umma::bulk_g2s(st, a0, PA, &full[s]); // A0 hi, lo
+                    umma::bulk_g2s(st + PA, a0 + lo, PA, &full[s]);
+                    if (bb >= 0) { // A1 hi, lo
+                        const __half *a1 = slice(T.task, bb, ch);
+                        umma::bulk_g2s(st + 2 * PA, a1, PA, &full[s]);
+                        umma::bulk_g2s(st + 3 * PA, a1 + lo, PA, &full[s]);
+                    }
+                    umma::bulk_g2s(st + 4 * PA, b0, PA, &full[s]); // B hi, lo
+                    umma::bulk_g2s(st + 5 * PA, b0 + lo, PA, &full[s]);
                     last[s] = use;
                 }
             }
