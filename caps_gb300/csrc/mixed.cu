@@ -146,26 +146,35 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
     for (int o = 0; o < nb; o += PB) {
         const int w = min(PB, nb - o);
         if (tid < 32) {
+            // every lane also keeps the sub-panel's future pivots dd[c] (pivot - 1), updated
+            // with the same fma and order as lane c's own diagonal entry: the shuffles of the
+            // update bring l_cj to every lane, so no pivot is broadcast, and the step's chain is
+            // one shuffle, an fma, an add, a reciprocal square root and a product
             const int i = tid;
-            float t[PB];
+            float t[PB], dd[PB];
 #pragma unroll
-            for (int k = 0; k < PB; k++) t[k] = (i < w && k <= i) ? T[o + i][o + k] : 0.0f;
+            for (int k = 0; k < PB; k++) {
+                t[k] = (i < w && k <= i) ? T[o + i][o + k] : 0.0f;
+                dd[k] = k < w ? T[o + k][o + k] : 0.0f;
+            }
 #pragma unroll
             for (int j = 0; j < PB; j++) {
                 if (j < w) { // uniform
-                const float d = __shfl_sync(0xffffffffu, t[j], j); // pivot - 1
+                const float d = dd[j]; // pivot - 1
                 const float one_d = 1.0f + d;
                 bad |= !(one_d > 0.0f);
-                const float lam = d / (sqrtf(fmaxf(one_d, 1e-30f)) + 1.0f);
-                const float inv = 1.0f / (1.0f + lam);
+                // inv = 1 / (1 + lam) = (1 + d)^(-1/2); lam = sqrt(1 + d) - 1 = d inv / (1 + inv)
+                // (no quotient: one with a tiny numerator, as d is at high l, is slow)
+                const float inv = __frsqrt_rn(fmaxf(one_d, 1e-30f));
                 if (i > j) t[j] *= inv;
-                else if (i == j) t[j] = lam;
+                else if (i == j) t[j] = d * inv * __frcp_rn(1.0f + inv);
                 if (i == 0) colj[o + j] = inv;
                 const float cj = t[j];
 #pragma unroll
                 for (int c = j + 1; c < PB; c++) {
                     const float v = __shfl_sync(0xffffffffu, cj, c); // column j of row c
                     if (i >= c && i < w) t[c] = fmaf(-cj, v, t[c]);
+                    dd[c] = fmaf(-v, v, dd[c]);
                 }
                 }
             }
@@ -227,7 +236,9 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
     constexpr int QB = 16;
     if (tid < MB) {
         const int o = (tid / QB) * QB, c = tid % QB;
-        float x[QB];
+        float x[QB], rdv[QB];
+#pragma unroll
+        for (int r = 0; r < QB; r++) rdv[r] = __frcp_rn(1.0f + T[o + r][o + r]); // off the chain below
 #pragma unroll
         for (int r = 0; r < QB; r++) {
             float a0 = 0.0f, a1 = 0.0f;
@@ -236,8 +247,7 @@ __global__ void __launch_bounds__(256) k_potf2_w(int ntask, int n, int k0, float
                 if (k & 1) a1 = fmaf(T[o + r][o + k], x[k], a1);
                 else a0 = fmaf(T[o + r][o + k], x[k], a0);
             }
-            const float d = 1.0f + T[o + r][o + r];
-            x[r] = r < c ? 0.0f : (r == c ? 1.0f / d : -(a0 + a1) / d);
+            x[r] = r < c ? 0.0f : (r == c ? rdv[r] : -(a0 + a1) * rdv[r]); // a product, not a quotient: see above
             W[o + r][o + c] = x[r];
         }
     }
