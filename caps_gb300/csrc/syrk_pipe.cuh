@@ -1,23 +1,27 @@
-// syrk_pipe.cuh -- persistent, warp-specialised form of the tcgen05 trailing update
-// (same arithmetic as k_syrk_umma: S_tile -= P_rows P_cols^T over panel columns k0 .. k0+kw,
-// split TF32 hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory).
+// syrk_pipe.cuh -- persistent, warp-specialised tcgen05 trailing updates of the mixed-form
+// Cholesky: S_tile -= P_rows P_cols^T over panel columns k0 .. k0+kw, three products
+// hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory.
 //
-// One CTA per SM walks a static list of 128 x TN tiles over all matrices of the batch
-// (tile t = blockIdx.x, blockIdx.x + gridDim.x, ...), with three roles that overlap
+// One CTA per SM walks a static list of tiles (or items of two tiles) over all matrices of
+// the batch (t = blockIdx.x, blockIdx.x + gridDim.x, ...), with three roles that overlap
 // across tiles instead of running one after another:
-//   * producers fill NS shared-memory stages with the hi/lo slices of a TK-column chunk of
-//     the two panel slices in the canonical K-major layout: either one thread of warp 0
-//     with four cp.async.bulk copies of images that the panel solves prepared (completion
-//     counted on the stage's "full" mbarrier by transaction bytes), or, without images, 16
-//     warps that load, split and store through registers and arrive on "full";
-//   * warp 16 (one thread) waits for a full stage, issues TK/8 k-steps x 3 MMAs into one
-//     of two TN-column tensor-memory accumulators, and commits to the stage's "empty"
-//     mbarrier (the slices may be overwritten once the MMAs have read them) and, after a
-//     tile's last chunk, to the accumulator's "full" mbarrier;
-//   * epilogue warps 17-24 (with images also warps 1-8) load the tile of S, wait for the
-//     accumulator, read it back with tcgen05.ld (warp w reads lanes 32 (w mod 4) .. +31 and
-//     its share of the columns), store S - acc and arrive on the accumulator's "empty"
-//     mbarrier.
+//   * producers fill shared-memory stages with the hi/lo slices of a chunk of panel columns
+//     in the canonical K-major layout (8-row x 16-byte core matrices);
+//   * one thread waits for a full stage, issues the chunk's MMAs into a tensor-memory
+//     accumulator, and commits to the stage's "empty" mbarrier (the slices may be
+//     overwritten once the MMAs have read them) and, after a tile's last chunk, to the
+//     accumulator's "full" mbarrier;
+//   * epilogue warps load the tile of S, wait for the accumulator, read it back with
+//     tcgen05.ld (warp w reads lanes 32 (w mod 4) .. +31 and its share of the columns), store
+//     S - acc and arrive on the accumulator's "empty" mbarrier.
+// Three kernels:
+//   * k_syrk_pair (whole trailing matrix) and k_syrk_blk (left-looking block updates inside a
+//     256-column panel) read FP16 panel images hi + lo of 2^14 x that the panel solves write:
+//     one thread fills each stage with cp.async.bulk copies (completion counted on the stage's
+//     "full" mbarrier by transaction bytes), kind::f16 MMAs;
+//   * k_syrk_pipe (the register-staged schedule) splits the panel itself: 16 producer warps
+//     load S, split each entry into TF32 hi and lo and store through registers; kind::tf32
+//     MMAs (warp 16), epilogue warps 17-24.
 // Every wait is bounded (PIPE_WAIT_ITERS polls of mbarrier.try_wait); a role that gives up
 // marks the tile's matrix with ST_ERR_WAIT and leaves its loop, the others then give up at
 // their next wait, the bulk-copy thread waits (bounded) for its last copies, the MMA thread
