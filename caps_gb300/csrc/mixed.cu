@@ -705,25 +705,31 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
         attr = true;
     }
-    // trailing update of S[t0.., t0..cmax) by the panel columns k0 .. k0 + kw - 1: the
-    // persistent pipelined kernel (one CTA per SM), or with CAPS_MIXED_NOPIPE=1 one CTA per tile
-    // ncb > 0: only the first ncb column blocks (the rest of the current outer panel)
-    auto syrk = [&](int k0, int kw, int t0, int cmax, int ncb) {
-        const int nr = (n - t0 + UM_M - 1) / UM_M, tpt = ncb > 0 ? nr * ncb : nr * (nr + 1);
+    // update of S[t0.., t0..cmax) by the panel columns k0 .. k0 + kw - 1: the persistent
+    // pipelined kernels (one CTA per SM), or with CAPS_MIXED_NOPIPE=1 one CTA per tile.  kind:
+    // UPD_BLOCK the 64 columns t0 .. t0 + 64 (left-looking, inside a half panel), UPD_MID the
+    // 256 columns t0 .. t0 + 256 (the first half of a panel onto the second half), UPD_TRAIL
+    // the whole trailing matrix
+    enum { UPD_BLOCK, UPD_MID, UPD_TRAIL };
+    auto syrk = [&](int k0, int kw, int t0, int cmax, int kind) {
+        const int nr = (n - t0 + UM_M - 1) / UM_M;
         if (g_kt.on) CK(cudaEventRecord(g_kt.next(), st));
         if (no_pipe)
-            k_syrk_umma<<<dim3(ncb == 1 ? nr : nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb == 1,
-                                                                                                 S, sstride, status);
-        else if (ncb > 0 && use_img) // one 64-column block from the FP16 images of the panel's earlier blocks
+            k_syrk_umma<<<dim3(kind == UPD_BLOCK ? nr : nr * (nr + 1), ntask), UM_THREADS, UM_SMEM, st>>>(
+                ntask, n, k0, kw, t0, cmax, kind == UPD_BLOCK, S, sstride, status);
+        else if (kind == UPD_BLOCK && use_img) // from the FP16 images of the half panel's earlier blocks
             k_syrk_blk<<<std::min(ntask * nr, nsm), BLK_THREADS, BLK_SMEM, st>>>(ntask, n, k0, t0, S, sstride, status, img64);
-        else if (ncb > 0) // the same from S: 128 x 64 tiles, 64-column chunks
-            k_syrk_pipe<64, 64><<<std::min(ntask * tpt, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb, S,
-                                                                                             sstride, status);
-        else { // the whole trailing matrix: 128 x 128 tiles (a third less staging per entry), 32-column chunks
+        else if (kind != UPD_TRAIL && use_img) // UPD_MID: row blocks against the two column blocks
+            k_syrk_pair<<<std::min(ntask * nr, nsm), PAIR_THREADS, PAIR_SMEM, st>>>(ntask, n, t0, kw, 1, S, sstride, status, img64);
+        else if (kind != UPD_TRAIL) { // the same from S: 128 x 64 tiles, 64-column chunks
+            const int ncb = (cmax - t0 + 63) / 64;
+            k_syrk_pipe<64, 64><<<std::min(ntask * nr * ncb, nsm), PIPE_THREADS, PIPE_SMEM, st>>>(ntask, n, k0, kw, t0, cmax, ncb, S,
+                                                                                                  sstride, status);
+        } else { // the whole trailing matrix: 128 x 128 tiles
             const int tw = ntask * pipe_tiles<128>(nr, 0);
             if (use_img && kw == PIPE_IMG_CH * PIPE_IMG_TK) // the panel solves left the panel's images: row-pair items
-                k_syrk_pair<<<std::min(ntask * pair_items(nr), nsm), PAIR_THREADS, PAIR_SMEM, st>>>(ntask, n, t0, S, sstride, status,
-                                                                                                  img64);
+                k_syrk_pair<<<std::min(ntask * pair_items(nr), nsm), PAIR_THREADS, PAIR_SMEM, st>>>(ntask, n, t0, kw, 0, S, sstride,
+                                                                                                  status, img64);
             else
                 k_syrk_pipe<128, 32><<<std::min(tw, nsm), PIPE_THREADS, PIPE_SMEM_WIDE, st>>>(ntask, n, k0, kw, t0, cmax, 0, S,
                                                                                               sstride, status);
@@ -744,7 +750,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
     // diagonal block k0 and the panel solve below it; false when nothing lies below.  With
     // images, the solve writes the FP16 image of its 64 columns (every row below the diagonal
     // block), which the panel's later blocks and the trailing update after the panel read.
-    constexpr int PANEL = PIPE_IMG_CH * PIPE_IMG_TK; // outer panel width, 256
+    constexpr int PANEL = PIPE_IMG_CH * PIPE_IMG_TK; // outer panel width, 512
     auto factor_panel = [&](int k0, bool images) {
         KernelTimer &tp = g_kts[KT_POTF2], &tt = g_kts[KT_TRSM];
         if (tp.on) CK(cudaEventRecord(tp.next(), st));
@@ -756,7 +762,7 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         }
         const int rest = n - k0 - MB;
         if (rest <= 0) return false;
-        const int blk = (k0 % PANEL) / MB; // 64-column block of the 256-column panel
+        const int blk = (k0 % PANEL) / MB; // 64-column block of the 512-column panel
         dim3 gt((rest + MT - 1) / MT, ntask);
         if (tt.on) CK(cudaEventRecord(tt.next(), st));
         k_trsm_inv<<<gt, TRSM_THREADS, 0, st>>>(ntask, n, k0, S, sstride, status, Winv, part, images ? img64 : nullptr, blk,
@@ -772,21 +778,26 @@ void launch_cholesky_mixed(int ntask, int n, const double *A, size_t lda, size_t
         return true;
     };
     if (tc && !legacy_mma) {
-        // two-level panels of OUTER columns: factor 64 columns at a time, each first updated
-        // with the panel's earlier blocks (left-looking, so every column block of S passes
-        // through the update once), then one K = OUTER trailing update, so the trailing
-        // matrix passes through DRAM once per OUTER columns
-        constexpr int OUTER = 4 * MB;
+        // panels of OUTER = 512 columns in two halves of 256: factor 64 columns at a time,
+        // each first updated with its half's earlier blocks (left-looking, so every column
+        // block of S passes through one such update); between the halves the first half is
+        // applied to the second half's 256 columns (all rows below), and after the panel one
+        // K = 512 update of the trailing matrix, which therefore passes through DRAM once per
+        // 512 columns
+        constexpr int OUTER = 8 * MB, HALF = OUTER / 2;
         static_assert(OUTER == PANEL && OUTER / MB == PIPE_IMG64_BLOCKS, "outer panel = image panel");
         bool more = true; // columns remain below the last factored panel
         for (int k0 = 0; k0 < n && more; k0 += OUTER) {
-            for (int kj = k0; kj < k0 + OUTER; kj += MB) {
-                if (kj > k0) syrk(k0, kj - k0, kj, std::min(kj + MB, n), 1);
-                if (!factor_panel(kj, use_img)) { more = false; break; }
+            for (int kh = k0; more && kh < k0 + OUTER; kh += HALF) {
+                if (kh > k0) syrk(k0, HALF, kh, std::min(kh + HALF, n), UPD_MID);
+                for (int kj = kh; kj < kh + HALF; kj += MB) {
+                    if (kj > kh) syrk(kh, kj - kh, kj, std::min(kj + MB, n), UPD_BLOCK);
+                    if (!factor_panel(kj, use_img)) { more = false; break; }
+                }
             }
             const int t2 = k0 + OUTER;
             if (!more || t2 >= n) break;
-            syrk(k0, OUTER, t2, n, 0);
+            syrk(k0, OUTER, t2, n, UPD_TRAIL);
         }
     } else {
         for (int k0 = 0; k0 < n; k0 += MB) {

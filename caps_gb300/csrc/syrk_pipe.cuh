@@ -95,22 +95,24 @@ __device__ __forceinline__ void pipe_stage(const float *Sm, int n, int kc, int n
 }
 
 // Panel images, read by both image-fed updates (k_syrk_blk and k_syrk_pair below): 64-column
-// block b = 0 .. 3 of a 256-column panel (columns k0 + 64 b ..) scaled by 2^14, rows from
+// block b = 0 .. 7 of a 512-column panel (columns k0 + 64 b ..) scaled by 2^14, rows from
 // t1 = k0 + 64 (b + 1), each entry split into FP16 hi = fp16(2^14 x) and lo = fp16(2^14 x - hi),
 // cut into 64-row blocks of 8 KB in the shared-memory layout of the MMA operands (K-major core
 // matrices of 8 rows x 8 halves, 8-row groups 1024 B apart), all hi blocks of a matrix and then
 // all lo blocks, so that a 128-row slice is two consecutive blocks:
 // img[(((b ntask + task) 2 + part) pipe_img64_nrb(n) + rb) PIPE_IMG64_HALVES + e],
 // e = ((q / 8) 8 + k / 8) 64 + (q mod 8) 8 + k mod 8 for row q of the block and column k.
-// The left-looking update of block j reads chunk b < j from block b's image, the trailing
-// update after the panel (rows from t2 = k0 + 256) chunk b from 64-row block 3 - b + 2 rb.
+// The left-looking update of block j reads the earlier blocks b of its 256-column half from
+// their images; the middle update (the first half applied to the second half's columns, rows
+// from k0 + 256) reads chunk b < 4 from 64-row block 3 - b + 2 rb, the trailing update after
+// the panel (rows from k0 + 512) chunk b from 64-row block 7 - b + 2 rb.
 // The panel solves that produce the panel write them (k_trsm_inv in mixed.cu).
 // Range: the panel holds entries of a Cholesky factor of A = 1 - M, |x| <= sqrt(A_ii) <
 // sqrt(2) for |M_ii| < 1, so 2^14 x stays below the FP16 maximum 65504 (the writer flags
 // |x| >= 4).  Entries from 2^-17 up have both halves normal: 22 significant bits, as many as
 // a split-TF32 pair; smaller ones keep an absolute resolution of 2^-38.  The products of two
 // scaled entries are exact in the FP32 accumulator, which the update scales back by 2^-28.
-constexpr int PIPE_IMG_TK = 64, PIPE_IMG_CH = 4;                        // chunk width, chunks per panel
+constexpr int PIPE_IMG_TK = 64, PIPE_IMG_CH = 8;                        // chunk width, chunks (blocks) per panel
 constexpr float PIPE_IMG_SCALE = 16384.0f, PIPE_IMG_UNSCALE2 = 1.0f / (16384.0f * 16384.0f), PIPE_IMG_XMAX = 4.0f;
 constexpr int PIPE_IMG64_HALVES = 64 * 64, PIPE_IMG64_BLOCKS = PIPE_IMG_CH;
 __host__ __device__ inline int pipe_img64_nrb(int n) { return 2 * ((n + UM_M - 1) / UM_M) + 2; }
@@ -372,21 +374,38 @@ __device__ __forceinline__ PairTile pair_tile(int t, int ipt, int nr, int t0, co
     T.valid = (status[T.task] & ~ST_ERR_WAIT) == ST_FACTOR;
     return T;
 }
-
-// S[t0.., t0..) -= P P^T over the PIPE_IMG_CH PIPE_IMG_TK = 256 panel columns t0 - 256 .. t0 of the
-// panel images img (layout above); grid = min(items, SMs), PAIR_THREADS threads, PAIR_SMEM bytes
-// of dynamic shared memory
-__global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n, int t0, float *S, size_t sstride, int *status,
-                                                               const __half *img)
+// the middle update's items: item t is row block t mod nr of matrix t / nr against the two
+// column blocks t0 .. t0 + 256 (ra = rb = the rows; rb < 0 when the second block lies past n)
+__device__ __forceinline__ PairTile mid_tile(int t, int nr, int n, int t0, const int *status)
 {
-    constexpr int PA = PAIR_SLICE, NCH = PIPE_IMG_CH;
+    PairTile T;
+    T.task = t / nr;
+    T.ra = t0 + (t - T.task * nr) * UM_M;
+    T.rb = t0 + UM_M < n ? T.ra : -1;
+    T.col0 = t0;
+    T.valid = (status[T.task] & ~ST_ERR_WAIT) == ST_FACTOR;
+    return T;
+}
+
+// mid = 0: S[t0.., t0..) -= P P^T over the kw panel columns t0 - kw .. t0 (the start of a panel,
+// so that chunk ch is image block ch); mid = 1: the same for columns t0 .. t0 + 256 only (the
+// middle update of a 512-column panel: the first half applied to the second half's columns),
+// items of one row block against the two column blocks, which share the row block's slice:
+// the stage holds the two column slices and the row slice, and the MMAs take the row slice
+// as A.  Grid = min(items, SMs), PAIR_THREADS threads, PAIR_SMEM bytes of dynamic shared memory.
+__global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n, int t0, int kw, int mid, float *S, size_t sstride,
+                                                               int *status, const __half *img)
+{
+    constexpr int PA = PAIR_SLICE;
+    const int NCH = kw / PIPE_IMG_TK;
     extern __shared__ __align__(1024) unsigned char pair_sm[];
     __shared__ uint64_t full[PAIR_STAGES], empty[PAIR_STAGES], tfull[2], tempty[2], drain;
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nr = (n - t0 + UM_M - 1) / UM_M;
-    const int ipt = pair_items(nr);
+    const int ipt = mid ? nr : pair_items(nr);
     const int nitem = ntask * ipt;
+    auto item = [&](int t) { return mid ? mid_tile(t, nr, n, t0, status) : pair_tile(t, ipt, nr, t0, status); };
 
     if (warp == 0) umma::alloc(&tslot, 512);
     if (tid == 0) {
@@ -406,7 +425,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
     const uint32_t tmem = tslot;
     const int nrb64 = pipe_img64_nrb(n);
     auto slice = [&](int task, int rblock, int ch) { // hi slice of row block rblock, chunk ch (the lo slice is nrb64 blocks on)
-        return img + (((size_t)ch * ntask + task) * 2 * nrb64 + 3 - ch + 2 * rblock) * PIPE_IMG64_HALVES;
+        return img + (((size_t)ch * ntask + task) * 2 * nrb64 + NCH - 1 - ch + 2 * rblock) * PIPE_IMG64_HALVES;
     };
 
     if (warp >= 2) {
@@ -414,16 +433,17 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
         const int quad = warp & 3, part4 = (warp - 2) >> 2; // four warps per lane quadrant, 32 columns each
         int tt = 0;
         for (int t = blockIdx.x; t < nitem; t += gridDim.x) {
-            const PairTile T = pair_tile(t, ipt, nr, t0, status);
+            const PairTile T = item(t);
             if (!T.valid) continue;
             float *Sm = S + (size_t)T.task * sstride;
             const int b = tt & 1, ub = tt >> 1;
-            // parts p = 2 h + half: tile h (rows ra, then rb), this warp's columns 32 part4 + 16 half;
-            // the loads of part p + 1 go out before the stores of part p
+            // parts p = 2 h + half: tile h (rows ra, then rb; in the middle update the column
+            // blocks col0, then col0 + 128), this warp's columns 32 part4 + 16 half; the loads of
+            // part p + 1 go out before the stores of part p
             const int np = T.rb >= 0 ? 4 : 2;
             // row R of part p and its columns cb + j, j < jm (inside the matrix and R >= C)
             auto row = [&](int p) { return ((p >> 1) ? T.rb : T.ra) + quad * 32 + lane; };
-            auto col = [&](int p) { return T.col0 + part4 * 32 + (p & 1) * 16; };
+            auto col = [&](int p) { return T.col0 + (mid ? (p >> 1) * UM_M : 0) + part4 * 32 + (p & 1) * 16; };
             auto lim = [&](int R, int cb) { return R < n ? min(n - cb, R - cb + 1) : 0; };
             auto load = [&](int p, float (&d)[16]) {
                 const int R = row(p), cb = col(p), jm = lim(R, cb);
@@ -462,9 +482,13 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
             for (int s = 0; s < PAIR_STAGES; s++) last[s] = -1;
             bool ok = true;
             for (int t = blockIdx.x; ok && t < nitem; t += gridDim.x) {
-                const PairTile T = pair_tile(t, ipt, nr, t0, status);
+                const PairTile T = item(t);
                 if (!T.valid) continue;
-                const int ba = (T.ra - t0) / UM_M, bc = (T.col0 - t0) / UM_M, bb = T.rb >= 0 ? (T.rb - t0) / UM_M : -1;
+                // image row blocks of the three slices: A0, A1 (the item's rows) and B (its
+                // columns); in the middle update the two column blocks and then the rows
+                const int br = (T.ra - t0) / UM_M;
+                const int s0 = mid ? 0 : br, s1 = mid ? 1 : (T.rb - t0) / UM_M, s2 = mid ? br : (T.col0 - t0) / UM_M;
+                const bool two = T.rb >= 0;
                 for (int ch = 0; ch < NCH; ch++, it++) {
                     const int s = it % PAIR_STAGES, use = it / PAIR_STAGES;
                     if (use > 0 && !umma::mbar_wait(&empty[s], (use - 1) & 1, PIPE_WAIT_ITERS)) {
@@ -473,13 +497,13 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
                         break;
                     }
                     unsigned char *st = pair_sm + s * PAIR_STAGE;
-                    umma::mbar_arrive_tx(&full[s], (bb >= 0 ? 6 : 4) * PA);
+                    umma::mbar_arrive_tx(&full[s], (two ? 6 : 4) * PA);
                     const size_t lo = (size_t)nrb64 * PIPE_IMG64_HALVES;
-                    const __half *a0 = slice(T.task, ba, ch), *b0 = slice(T.task, bc, ch);
+                    const __half *a0 = slice(T.task, s0, ch), *b0 = slice(T.task, s2, ch);
                     umma::bulk_g2s(st, a0, PA, &full[s]); // A0 hi, lo
                     umma::bulk_g2s(st + PA, a0 + lo, PA, &full[s]);
-                    if (bb >= 0) { // A1 hi, lo
-                        const __half *a1 = slice(T.task, bb, ch);
+                    if (two) { // A1 hi, lo
+                        const __half *a1 = slice(T.task, s1, ch);
                         umma::bulk_g2s(st + 2 * PA, a1, PA, &full[s]);
                         umma::bulk_g2s(st + 3 * PA, a1 + lo, PA, &full[s]);
                     }
@@ -500,7 +524,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
             constexpr uint32_t idesc = umma::idesc_f16(UM_M, UM_M);
             constexpr uint32_t LBO = 128, SBO = (PIPE_IMG_TK / 8) * 128;
             for (int t = blockIdx.x; t < nitem; t += gridDim.x) {
-                const PairTile T = pair_tile(t, ipt, nr, t0, status);
+                const PairTile T = item(t);
                 if (!T.valid) continue;
                 const int b = tt & 1, ub = tt >> 1, nh = T.rb >= 0 ? 2 : 1;
                 bool ok = ub == 0 || umma::mbar_wait(&tempty[b], (ub - 1) & 1, PIPE_WAIT_ITERS);
@@ -510,9 +534,11 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
                     if (!umma::mbar_wait(&full[s], use & 1, PIPE_WAIT_ITERS)) { ok = false; break; }
                     umma::fence_after();
                     const uint32_t base = umma::smem_u32(pair_sm + s * PAIR_STAGE);
-                    const uint32_t bh = base + 4 * PA, bl = bh + PA;
                     for (int h = 0; h < nh; h++) {
-                        const uint32_t ah = base + h * 2 * PA, al = ah + PA;
+                        // tile h: slot h against slot 2 (the shared slice); the middle update
+                        // takes the shared row slice as A
+                        const uint32_t sh = base + h * 2 * PA, sc = base + 4 * PA;
+                        const uint32_t ah = mid ? sc : sh, al = ah + PA, bh = mid ? sh : sc, bl = bh + PA;
                         const uint32_t acc = tmem + b * 256 + h * 128;
                         for (int ks = 0; ks < PIPE_IMG_TK / 16; ks++) { // K = 16 halves: two core matrices
                             const uint32_t o = ks * 256;
@@ -544,9 +570,9 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
 // ---------------------------------------------------------------------------
 // Left-looking block update from the FP16 images
 // ---------------------------------------------------------------------------
-// S[t0.., t0 .. t0 + 64) -= P P^T with P = columns k0 .. t0 of the current 256-column panel
-// (t0 - k0 = 64, 128 or 192: one 64-column chunk per earlier block of the panel, read from
-// that block's images), one 128 x 64 tile per row block.  Roles as in k_syrk_pair: warp 0 lane
+// S[t0.., t0 .. t0 + 64) -= P P^T with P = columns k0 .. t0 of the current 256-column half
+// of a panel (t0 - k0 = 64, 128 or 192: one 64-column chunk per earlier block of the half,
+// read from that block's images), one 128 x 64 tile per row block.  Roles as in k_syrk_pair: warp 0 lane
 // 0 fills BLK_STAGES stages of 48 KB with four bulk copies (A hi, A lo: two consecutive 64-row
 // image blocks of 8 KB each; B hi, B lo: one block each), warp 1 lane 0 issues the FP16 MMAs
 // into one of BLK_ACC 64-column accumulators, warps 2..17 are the epilogue (warp w reads lane
@@ -643,9 +669,10 @@ __global__ void __launch_bounds__(BLK_THREADS, 1) k_syrk_blk(int ntask, int n, i
                 const int task = t / nr, row0 = t0 + (t - task * nr) * UM_M;
                 if (!valid(task)) continue;
                 for (int ch = 0; ch < nchunk; ch++, it++) {
-                    // chunk ch is panel block ch, its image rows counted from k0 + 64 (ch + 1)
-                    const int t1 = k0 + 64 * (ch + 1);
-                    const __half *hi0 = img + ((size_t)ch * ntask + task) * 2 * nrb64 * PIPE_IMG64_HALVES;
+                    // chunk ch is the image of block k0 / 64 + ch of the panel, its rows counted
+                    // from k0 + 64 (ch + 1)
+                    const int t1 = k0 + 64 * (ch + 1), blk = (k0 % (PIPE_IMG_CH * PIPE_IMG_TK)) / 64 + ch;
+                    const __half *hi0 = img + ((size_t)blk * ntask + task) * 2 * nrb64 * PIPE_IMG64_HALVES;
                     const __half *ahi = hi0 + (size_t)((row0 - t1) / 64) * PIPE_IMG64_HALVES;
                     const __half *bhi = hi0 + (size_t)((t0 - t1) / 64) * PIPE_IMG64_HALVES;
                     const int s = it % BLK_STAGES, use = it / BLK_STAGES;
