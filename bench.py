@@ -204,10 +204,10 @@ def run_reference(args, dist, rank, world):
     print(json.dumps(line), flush=True)
 
 
-# DRAM bytes per algorithmic byte of the trailing update (k_syrk_pair and k_syrk_blk, all 32
-# update launches of the factorisation), from one ncu capture of 24 factored matrices of this
+# DRAM bytes per algorithmic byte of the updates (k_syrk_pair and k_syrk_blk, all 32 update
+# launches of the factorisation), from one ncu capture of 24 factored matrices of this
 # workload: below 1 because the FP16 panel images that the panel solves have just written are
-# partly still in L2 when the update reads them; nothing is read twice
+# partly still in L2 when the updates read them; nothing is read twice
 SYRK_DRAM_PER_ALGORITHMIC = 0.79
 
 
@@ -494,13 +494,14 @@ def main():
                       "peak_source": "measured live: DFMA-chain probe kernel (caps_gpu_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
                       "traffic": None} if args.precision == "fp64" else
                      {"bound": "hbm",
-                      "kernel": "tcgen05 trailing update of the FP32 delta-form Cholesky (256-column panels; panel as "
-                                "FP16 pairs hi + lo of 2^14 x, products hi hi + hi lo + lo hi accumulated in FP32 in "
-                                "TMEM; persistent and warp-specialised): k_syrk_pair for the whole trailing matrix "
-                                "(row-pair items sharing the column slice) and k_syrk_blk for the left-looking block "
-                                "updates, both fed by bulk copies of the panel images that the panel solves write; "
-                                "algorithmic bytes = target block read + written once (FP32) and the panel rows read "
-                                "once (4 bytes per entry), per factored matrix",
+                      "kernel": "tcgen05 updates of the FP32 delta-form Cholesky (512-column panels in two 256-column "
+                                "halves; panel as FP16 pairs hi + lo of 2^14 x, products hi hi + hi lo + lo hi accumulated "
+                                "in FP32 in TMEM; persistent and warp-specialised): k_syrk_pair for the K = 512 update of "
+                                "the whole trailing matrix (row-pair items sharing the column slice) and for the middle "
+                                "update of each panel (its first half onto the second half's 256 columns), k_syrk_blk for "
+                                "the left-looking block updates, all fed by bulk copies of the panel images that the panel "
+                                "solves write; algorithmic bytes = target block read + written once (FP32) and the panel "
+                                "rows read once (4 bytes per entry), per factored matrix",
                       "achieved": syrk_gbs, "peak": hbm_peak, "unit": "GB/s",
                       "frac": syrk_gbs / hbm_peak if syrk_gbs else None,
                       "traffic": syrk_bytes / syrk_n * SYRK_DRAM_PER_ALGORITHMIC if syrk_n else None,
@@ -508,9 +509,9 @@ def main():
                       "launches": syrk_n, "avg_launch_ms": syrk_ms / syrk_n if syrk_n else None,
                       "algorithmic_bytes_per_launch": syrk_bytes / syrk_n if syrk_n else None,
                       "traffic_source": "DRAM bytes per algorithmic byte over all 32 update launches of the factorisation "
-                                        "of 24 matrices of this workload in one ncu capture (whole-trailing-matrix updates "
-                                        "0.80, block updates 0.78: the images just written by the panel solves are partly "
-                                        "read from L2), times this run's algorithmic bytes per launch",
+                                        "of 24 matrices of this workload in one ncu capture (trailing updates 0.84, middle "
+                                        "updates 0.73, block updates 0.78: the images just written by the panel solves are "
+                                        "partly read from L2), times this run's algorithmic bytes per launch",
                       "fp32_accurate_tflops_factorisation": achieved,
                       "panel_kernels": panel_kernels or None,
                       "panel_kernels_note": "the panel solve is bytes-bound like the update (its rate against the same peak); "
