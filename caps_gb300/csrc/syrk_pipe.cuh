@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
                                                                int *status, const __half *img)
 {
     constexpr int PA = PAIR_SLICE;
-    const int NCH = kw / PIPE_IMG_TK;
+    const int nch = kw / PIPE_IMG_TK;
     extern __shared__ __align__(1024) unsigned char pair_sm[];
     __shared__ uint64_t full[PAIR_STAGES], empty[PAIR_STAGES], tfull[2], tempty[2], drain;
     __shared__ uint32_t tslot;
@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
     const uint32_t tmem = tslot;
     const int nrb64 = pipe_img64_nrb(n);
     auto slice = [&](int task, int rblock, int ch) { // hi slice of row block rblock, chunk ch (the lo slice is nrb64 blocks on)
-        return img + (((size_t)ch * ntask + task) * 2 * nrb64 + NCH - 1 - ch + 2 * rblock) * PIPE_IMG64_HALVES;
+        return img + (((size_t)ch * ntask + task) * 2 * nrb64 + nch - 1 - ch + 2 * rblock) * PIPE_IMG64_HALVES;
     };
 
     if (warp >= 2) {
@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
                 const int br = (T.ra - t0) / UM_M;
                 const int s0 = mid ? 0 : br, s1 = mid ? 1 : (T.rb - t0) / UM_M, s2 = mid ? br : (T.col0 - t0) / UM_M;
                 const bool two = T.rb >= 0;
-                for (int ch = 0; ch < NCH; ch++, it++) {
+                for (int ch = 0; ch < nch; ch++, it++) {
                     const int s = it % PAIR_STAGES, use = it / PAIR_STAGES;
                     if (use > 0 && !umma::mbar_wait(&empty[s], (use - 1) & 1, PIPE_WAIT_ITERS)) {
                         ok = false;
@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(PAIR_THREADS, 1) k_syrk_pair(int ntask, int n,
                 const int b = tt & 1, ub = tt >> 1, nh = T.rb >= 0 ? 2 : 1;
                 bool ok = ub == 0 || umma::mbar_wait(&tempty[b], (ub - 1) & 1, PIPE_WAIT_ITERS);
                 umma::fence_after();
-                for (int ch = 0; ok && ch < NCH; ch++, it++) {
+                for (int ch = 0; ok && ch < nch; ch++, it++) {
                     const int s = it % PAIR_STAGES, use = it / PAIR_STAGES;
                     if (!umma::mbar_wait(&full[s], use & 1, PIPE_WAIT_ITERS)) { ok = false; break; }
                     umma::fence_after();
