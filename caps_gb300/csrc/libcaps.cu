@@ -504,10 +504,11 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     const size_t per_task = dense_bytes + (size_t)2 * nu_stride * sizeof(sd)
                           + (size_t)nu_stride * sizeof(double2) + (size_t)3 * L * sizeof(sd) + (size_t)dim * 8
                           + (size_t)2 * 256 * nu_stride * 12  // partial sums, up to 256 warps
-                          + (size_t)(4 * (caps->ldim + 4096)) * sizeof(double4); // p tables
+                          + (size_t)(4 * (caps->ldim + 4096)) * sizeof(double4) // p tables
+                          + (mixed && !hodlr ? mixed_work_bytes(1, dim) : 0);   // diagonal-block inverses, panel images
     size_t budget = (size_t)(0.70 * (double)(freeb + g_eng.A.bytes + g_eng.I.bytes + g_eng.partM.bytes + g_eng.partE.bytes + g_eng.S32.bytes
                                              + g_eng.a12.bytes + g_eng.part.bytes + g_eng.B.bytes + g_eng.hwork.bytes
-                                             + g_eng.seed.bytes));
+                                             + g_eng.seed.bytes + g_eng.mwork.bytes));
     int chunk = (int)std::max<size_t>(1, std::min<size_t>(budget / per_task, 65535));
     chunk = std::min(chunk, n);
 
