@@ -318,11 +318,11 @@ void caps_gpu_work(long long *nmat, long long *nfactor, double *factor_flops);
 
 /* live timing of the mixed form's factorisation kernels: with caps_gpu_kernel_timing(1),
  * CUDA events on the library's stream bracket every launch; caps_gpu_kernel_stats returns
- * for the tcgen05 trailing update the summed device milliseconds, the algorithmic bytes
- * (trailing triangle read and written once plus the panel rows, per factored matrix) and
- * the launch count since the last enable; caps_gpu_kernel_stats_kind the same for kind 0
- * (trailing update), 1 (panel solve: the panel rows read, X or its split-TF32 images
- * written) or 2 (diagonal block: read, written, its inverse written).
+ * for the tcgen05 updates the summed device milliseconds, the algorithmic bytes (target
+ * block read and written once plus the panel rows, per factored matrix) and the launch
+ * count since the last enable; caps_gpu_kernel_stats_kind the same for kind 0 (updates),
+ * 1 (panel solve: the panel rows read, X or its FP16 image written) or 2 (diagonal block:
+ * read, written, its inverse written).
  * caps_gpu_kernel_timing(0) stops it. */
 void caps_gpu_kernel_timing(int enable);
 void caps_gpu_kernel_stats(double *ms, double *bytes, long long *launches);
