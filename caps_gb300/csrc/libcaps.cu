@@ -74,10 +74,27 @@ struct DevBuf {
     {
         if (need > bytes) {
             if (p) CK(cudaFree(p));
-            bytes = std::max(need, bytes + bytes / 4);
-            CK(cudaMalloc(&p, bytes));
+            p = nullptr;
+            // grow by a quarter at least (fewer reallocations as batches vary); where that
+            // does not fit, exactly what is needed
+            const size_t want = std::max(need, bytes + bytes / 4);
+            bytes = 0;
+            if (cudaMalloc(&p, want) == cudaSuccess) {
+                bytes = want;
+            } else {
+                (void)cudaGetLastError(); // an allocation failure is not sticky: clear it
+                p = nullptr;
+                CK(cudaMalloc(&p, need));
+                bytes = need;
+            }
         }
         return p;
+    }
+    void release()
+    {
+        if (p) CK(cudaFree(p));
+        p = nullptr;
+        bytes = 0;
     }
 };
 
@@ -94,6 +111,7 @@ struct Engine {
     double timings_cum[6] = {0, 0, 0, 0, 0, 0};
     static constexpr int NEV = 9;
     cudaEvent_t ev[NEV];
+    uint64_t shape = 0; // of the last batch (dimension, precision, path), see run_batch
     std::mutex mu;
     cudaStream_t stream() const { return user ? user : own; }
 };
@@ -481,9 +499,6 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     for (auto &T : tasks) nnu_max = std::max(nnu_max, T.nu_max - T.mu + 1);
     const int nu_stride = (nnu_max + 31) / 32 * 32;
 
-    // chunk size from free memory
-    size_t freeb = 0, totb = 0;
-    CK(cudaMemGetInfo(&freeb, &totb));
     // HODLR semantics: the HODLR path (elements on demand) where it applies; the FP64 form
     // takes it from CAPS_HODLR_AUTO_DIM on, the mixed form from CAPS_HODLR_AUTO_DIM_MIXED on
     const bool mixed = caps->precision == CAPS_PREC_MIXED;
@@ -496,6 +511,21 @@ static int run_batch(caps_t *caps, const double *xi_, const int *ms, int n, doub
     // ... and, where the window fits its shared-memory ring, M comes from the I recurrence seeded
     // by 4 L q-sums per matrix (sweep.cu) instead of the q-sums of every pair
     const bool sweep = ff_elem && sweep_fits(ldim);
+    // chunk size from free memory.  The budget counts the large work buffers held from earlier
+    // batches as free for this one: true while batches keep one shape, each buffer serving the
+    // same array again; when the shape (dimension, precision, path) changes they are released
+    // first, since a buffer the new path does not use would stay held beside the new ones
+    // (every batch ends synchronised with the device, so none is in use)
+    const uint64_t shape = ((uint64_t)dim << 16) | (uint64_t)mixed | (uint64_t)hodlr << 1 | (uint64_t)sweep << 2 |
+                           (uint64_t)ff_elem << 3 | (uint64_t)O.square << 4 | (uint64_t)O.M_out << 5 | (uint64_t)O.factor << 6;
+    if (g_eng.shape != shape) {
+        for (DevBuf *b : {&g_eng.A, &g_eng.I, &g_eng.partM, &g_eng.partE, &g_eng.S32, &g_eng.a12, &g_eng.part, &g_eng.B,
+                          &g_eng.hwork, &g_eng.seed, &g_eng.mwork})
+            b->release();
+        g_eng.shape = shape;
+    }
+    size_t freeb = 0, totb = 0;
+    CK(cudaMemGetInfo(&freeb, &totb));
     const size_t mat_bytes = O.square ? 16 : ff_elem ? 4 + 1 : (caps->precision == CAPS_PREC_MIXED ? 12 : 8);
     const size_t dense_bytes = hodlr ? hodlr_work_bytes(ldim, 1)
                              : sweep ? (size_t)dim * dim * 4 + seed_bytes(ldim, 1)
